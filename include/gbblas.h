@@ -1,0 +1,119 @@
+/*
+ * gbblas — GB300 (sm_103a) GEMM library behind jBLAS.jl's blocked matrix-multiply API.
+ *
+ * The C ABI below is the drop-in boundary: plain pointers, 64-bit sizes, no CUDA or
+ * torch types.  Every matrix pointer is a DEVICE pointer to column-major storage
+ * (the layout jBLAS's MMatrix uses, src/gemm.jl:3-11).  `stream` is a cudaStream_t
+ * passed as void* (NULL = the legacy default stream).  All calls are stream-ordered:
+ * they enqueue work and return; results are valid once the stream reaches that point.
+ * Every entry point returns GB_OK (0) or a negative gb_status_t; gb_status_string()
+ * gives a message.  Calls are thread-safe as long as concurrent calls use different
+ * streams or do not share output buffers.
+ *
+ * Reference interface each call replaces (paths relative to the jBLAS.jl tree):
+ *   gb_jmul_f64 / gb_jmul_f32   jmul!(D, A, X)                src/gemm.jl:244-348
+ *   gb_gemm_f64 / gb_gemm_f32   jmul! generalised to BLAS-3  src/gemm.jl:244 (D = A*X,
+ *                               alpha/beta and transposes are extensions; the kernel!
+ *                               pointer API src/kernels.jl:239 is its D += A*X form)
+ *   gb_gemm_grouped_f64/_f32    many independent kernel!/fastmul! products
+ *                               src/kernels.jl:202-208, 239 (one launch for all)
+ *   gb_gemm_adjoint_f32         no reference counterpart (the rrule of gemm!)
+ *   gb_plan_*                   blocking_structure / pick_kernel_size / BLASOptions
+ *                               src/memory_management.jl:78-177,
+ *                               src/kernel_structure.jl:76-99, src/blas_options.jl:2-7
+ */
+#ifndef GBBLAS_H
+#define GBBLAS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBBLAS_VERSION 100 /* 1.0.0 */
+
+typedef enum {
+  GB_OK = 0,
+  GB_ERR_INVALID_VALUE = -1,   /* a size, leading dimension, flag or pointer is invalid */
+  GB_ERR_UNSUPPORTED = -2,     /* valid request this GPU / build cannot serve */
+  GB_ERR_PIPELINE_TIMEOUT = -3,/* a bounded on-device wait expired; the kernel exited */
+  GB_ERR_CUDA = -4,            /* a CUDA runtime/driver call failed */
+  GB_ERR_ALLOC = -5,           /* device workspace allocation failed */
+  GB_ERR_NO_DEVICE = -6        /* no usable sm_103 device is current */
+} gb_status_t;
+
+/* Arithmetic mode of gb_gemm_f64. */
+typedef enum {
+  GB_MODE_NATIVE = 0,     /* FP64 FMA chain on the CUDA cores, jBLAS's per-element order */
+  GB_MODE_OZAKI_BF16 = 1, /* FP64-accurate emulation: BF16 slices on tcgen05, exact FP32 sums */
+  GB_MODE_OZAKI_INT8 = 2  /* INT8 slices: GB_ERR_UNSUPPORTED on sm_103a (no tcgen05 kind::i8) */
+} gb_mode_t;
+
+const char* gb_status_string(int status);
+int gb_version(void);
+
+/* Bounded-wait limit (nanoseconds) for every on-device pipeline wait; 0 restores the
+ * default (4 s).  A wait that expires makes the kernel exit and the call report
+ * GB_ERR_PIPELINE_TIMEOUT on a later gb_check_status(). */
+int gb_set_wait_limit_ns(uint64_t ns);
+
+/* Normwise tolerance the automatic Ozaki slice count must meet (slices = 0); 0 restores
+ * the default 2^-50. */
+int gb_set_ozaki_tolerance(double tol);
+
+/* Reads and clears the device-side status word written by timed-out waits
+ * (synchronises `stream`). */
+int gb_check_status(void* stream);
+
+/* ------------------------------------------------------------------ jmul! proper */
+/* D (M x P) = A (M x N) * X (N x P), contraction over N, leading dimensions M, N, M
+ * exactly as an MMatrix (src/gemm.jl:244).  Per element d = a1*x1; d = fma(ak, xk, d)
+ * for k = 2..N in order: results are bit-identical to jmul!'s arithmetic, and every
+ * element is written (jmul! leaves remainder tiles unwritten, src/gemm.jl:340-345). */
+int gb_jmul_f64(double* D, const double* A, const double* X, int64_t M, int64_t N, int64_t P,
+                void* stream);
+int gb_jmul_f32(float* D, const float* A, const float* X, int64_t M, int64_t N, int64_t P,
+                void* stream);
+
+/* ------------------------------------------------------------------ BLAS-3 GEMM */
+/* C = alpha*op(A)*op(B) + beta*C; op(X) = X (trans = 0) or X^T (trans = 1).
+ * op(A) is M x K, op(B) is K x N, C is M x N; lda >= rows of A as stored, etc.
+ * beta == 0: C is not read (NaN in C is overwritten).  alpha == 0 or K == 0:
+ * C = beta*C and A, B are not read.
+ * mode GB_MODE_NATIVE: per element acc = fma chain in k order (as jmul!), then
+ *   C = alpha*acc (beta == 0) or fma(alpha, acc, beta*C).
+ * mode GB_MODE_OZAKI_BF16: A and B are split into `slices` BF16 digit planes with
+ *   per-row / per-column power-of-two scaling (slices = 0 picks the count that meets
+ *   the library's default tolerance, 2^-50 normwise); slice products run on tcgen05
+ *   with exact FP32 accumulation and are recombined in FP64.  Rows of A or columns of
+ *   B holding Inf/NaN give NaN in the outputs they touch.
+ * err_bound_out (host pointer, may be NULL): for OZAKI, an a-priori bound on
+ *   ||C - C_exact||_F / (|alpha| ||A||_F ||B||_F) from the slicing truncation;
+ *   the call then synchronises `stream` to read the split statistics.  For NATIVE it
+ *   receives the standard bound K*u/(1-K*u) (u = 2^-53) of the same quantity. */
+int gb_gemm_f64(int transA, int transB, int64_t M, int64_t N, int64_t K, double alpha,
+                const double* A, int64_t lda, const double* B, int64_t ldb, double beta,
+                double* C, int64_t ldc, int mode, int slices, double* err_bound_out,
+                void* stream);
+int gb_gemm_f32(int transA, int transB, int64_t M, int64_t N, int64_t K, float alpha,
+                const float* A, int64_t lda, const float* B, int64_t ldb, float beta,
+                float* C, int64_t ldc, void* stream);
+
+/* Ozaki plan for a problem: slice count, bits per slice and the grouping of slice
+ * products that the tensor-core kernel would use (no GPU work). */
+typedef struct {
+  int32_t slices;        /* digit planes per operand */
+  int32_t bits;          /* bits per digit plane (|digit| <= 2^(bits-1)) */
+  int32_t k_chunk;       /* K elements per exact FP32 accumulation */
+  int32_t products;      /* slice-pair products per K chunk (p + q <= slices + 1) */
+  int32_t groups;        /* TMEM accumulation groups drained per output tile */
+  double  flops_tensor;  /* BF16 tensor flops the plan issues */
+} gb_ozaki_plan_t;
+int gb_plan_ozaki(int64_t M, int64_t N, int64_t K, int slices, gb_ozaki_plan_t* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBBLAS_H */

@@ -1,0 +1,429 @@
+// C-ABI entry points of libgbblas (declared in include/gbblas.h).
+//
+// Argument checking follows BLAS conventions (the reference has none: jmul! relies on
+// static sizes and @inbounds, src/gemm.jl:244,312).  Device workspace for the Ozaki
+// path is taken from the stream-ordered allocator (cudaMallocAsync / cudaFreeAsync on
+// the caller's stream), so concurrent calls on different streams never share scratch.
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <cudaTypedefs.h>
+
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "gb_common.cuh"
+#include "native_gemm.cuh"
+#include "ozaki.cuh"
+
+static thread_local char g_last_detail[256];
+
+int gb_set_cuda_error(cudaError_t e, const char* what) {
+  std::snprintf(g_last_detail, sizeof(g_last_detail), "%s: %s", what, cudaGetErrorString(e));
+  if (e == cudaErrorMemoryAllocation) return GB_ERR_ALLOC;
+  return GB_ERR_CUDA;
+}
+
+namespace gb {
+
+static std::atomic<uint64_t> g_wait_limit_ns{4000000000ull};
+static std::atomic<uint64_t> g_ozaki_tol_bits{0};
+
+struct DeviceInfo {
+  bool init = false;
+  int status_code = GB_OK;
+  int sms = 0;
+  DeviceStatus* status = nullptr;  // device-side status word
+};
+static std::mutex g_dev_mu;
+static std::vector<DeviceInfo> g_devs;
+
+// Per-device setup: architecture check, SM count, status word.
+static int device_info(DeviceInfo** out) {
+  int dev = 0;
+  GB_CUDA_TRY(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_dev_mu);
+  if (static_cast<int>(g_devs.size()) <= dev) g_devs.resize(dev + 1);
+  DeviceInfo& d = g_devs[dev];
+  if (!d.init) {
+    d.init = true;
+    int major = 0, minor = 0;
+    GB_CUDA_TRY(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev));
+    GB_CUDA_TRY(cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev));
+    GB_CUDA_TRY(cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev));
+    if (major != 10 || minor != 3) {
+      std::snprintf(g_last_detail, sizeof(g_last_detail),
+                    "device %d is sm_%d%d; this build carries sm_103a code only", dev, major, minor);
+      d.status_code = GB_ERR_NO_DEVICE;
+    } else {
+      cudaError_t e = cudaMalloc(&d.status, sizeof(DeviceStatus));
+      if (e == cudaSuccess) e = cudaMemset(d.status, 0, sizeof(DeviceStatus));
+      if (e != cudaSuccess) d.status_code = gb_set_cuda_error(e, "status word");
+    }
+  }
+  if (d.status_code != GB_OK) return d.status_code;
+  *out = &d;
+  return GB_OK;
+}
+
+// Device or managed memory only: a host pointer handed to a kernel would fault.
+static bool is_device_ptr(const void* p) {
+  if (p == nullptr) return false;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+static int check_gemm_args(int ta, int tb, int64_t M, int64_t N, int64_t K, int64_t lda, int64_t ldb,
+                           int64_t ldc, const void* A, const void* B, const void* C, bool need_ab) {
+  if ((ta != 0 && ta != 1) || (tb != 0 && tb != 1)) return GB_ERR_INVALID_VALUE;
+  if (M < 0 || N < 0 || K < 0) return GB_ERR_INVALID_VALUE;
+  const int64_t a_rows = ta ? K : M, b_rows = tb ? N : K;
+  if (lda < (a_rows > 1 ? a_rows : 1)) return GB_ERR_INVALID_VALUE;
+  if (ldb < (b_rows > 1 ? b_rows : 1)) return GB_ERR_INVALID_VALUE;
+  if (ldc < (M > 1 ? M : 1)) return GB_ERR_INVALID_VALUE;
+  if (M == 0 || N == 0) return GB_OK;
+  if (!is_device_ptr(C)) return GB_ERR_INVALID_VALUE;
+  if (need_ab && K > 0 && (!is_device_ptr(A) || !is_device_ptr(B))) return GB_ERR_INVALID_VALUE;
+  return GB_OK;
+}
+
+// ------------------------------------------------------------------ tensor maps
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
+int make_plane_tmap(CUtensorMap* map, const void* base, int64_t K, int64_t rows, int64_t slices,
+                    int64_t pitch, int box_rows) {
+  auto fn = encode_fn();
+  if (!fn) {
+    std::snprintf(g_last_detail, sizeof(g_last_detail), "cuTensorMapEncodeTiled unavailable");
+    return GB_ERR_CUDA;
+  }
+  cuuint64_t dims[3] = {static_cast<cuuint64_t>(K), static_cast<cuuint64_t>(rows),
+                        static_cast<cuuint64_t>(slices)};
+  cuuint64_t strides[2] = {static_cast<cuuint64_t>(pitch * 2),
+                           static_cast<cuuint64_t>(rows * pitch * 2)};
+  cuuint32_t box[3] = {64u, static_cast<cuuint32_t>(box_rows), 1u};
+  cuuint32_t estr[3] = {1u, 1u, 1u};
+  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides, box,
+                  estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    std::snprintf(g_last_detail, sizeof(g_last_detail), "cuTensorMapEncodeTiled failed (%d)",
+                  static_cast<int>(r));
+    return GB_ERR_CUDA;
+  }
+  return GB_OK;
+}
+
+// ------------------------------------------------------------------ Ozaki driver
+static double ozaki_tolerance() {
+  uint64_t b = g_ozaki_tol_bits.load();
+  if (b == 0) return std::ldexp(1.0, -50);
+  double t;
+  std::memcpy(&t, &b, sizeof(t));
+  return t;
+}
+
+// Host copy of the split statistics of both operands.
+struct HostStats {
+  std::vector<unsigned long long> amax_a, amax_b;
+  std::vector<double> sabs_a, sabs_b, ssq_a, ssq_b;
+};
+
+static int exp_of(unsigned long long bits) {
+  if (bits >= 0x7FF0000000000000ull) return INT32_MAX;
+  if (bits == 0) return 0;
+  double a;
+  std::memcpy(&a, &bits, sizeof(a));
+  return std::ilogb(a) + 1;
+}
+
+// A-priori normwise truncation bound ||C - C_exact||_F / (||A||_F ||B||_F) for s slices of
+// `bits` bits (see ozaki.cu): representation error of both operands plus the dropped
+// products (p + q > s + 1), plus the FP64 recombination rounding.
+static double ozaki_bound(const HostStats& h, int64_t K, int s, int bits, int steps) {
+  double e2a = 0, e2b = 0, na2 = 0, nb2 = 0, sa2 = 0, sb2 = 0;
+  for (size_t i = 0; i < h.amax_a.size(); ++i) {
+    const int e = exp_of(h.amax_a[i]);
+    if (e == INT32_MAX) return INFINITY;
+    e2a += std::ldexp(1.0, 2 * e);
+    na2 += h.ssq_a[i];
+    sa2 += h.sabs_a[i] * h.sabs_a[i];
+  }
+  for (size_t j = 0; j < h.amax_b.size(); ++j) {
+    const int e = exp_of(h.amax_b[j]);
+    if (e == INT32_MAX) return INFINITY;
+    e2b += std::ldexp(1.0, 2 * e);
+    nb2 += h.ssq_b[j];
+    sb2 += h.sabs_b[j] * h.sabs_b[j];
+  }
+  const double na = std::sqrt(na2), nb = std::sqrt(nb2);
+  if (na == 0.0 || nb == 0.0) return 0.0;
+  const double u2 = std::ldexp(1.0, -s * bits);
+  const double ea = std::sqrt(e2a), eb = std::sqrt(e2b);
+  const double cs = (s - 1) / (1.0 - std::ldexp(1.0, -bits));
+  const double trunc = u2 * (ea * std::sqrt(sb2) + eb * (std::sqrt(sa2) + K * u2 * ea) +
+                             static_cast<double>(K) * cs * ea * eb);
+  return trunc / (na * nb) + (steps + 2) * std::ldexp(1.0, -53);
+}
+
+static inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+static int ozaki_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int64_t K, double alpha,
+                      const double* A, int64_t lda, const double* B, int64_t ldb, double beta,
+                      double* C, int64_t ldc, int slices, double* err_bound_out, cudaStream_t s) {
+  if (slices < 0 || slices > OZ_MAX_SLICES) return GB_ERR_INVALID_VALUE;
+  if ((M + OZ_BM - 1) / OZ_BM * ((N + OZ_BN - 1) / OZ_BN) > 0x7FFFFFFF) return GB_ERR_UNSUPPORTED;
+  // op(A) rows i: X[i,k]; op(B) "rows" j: X[j,k] = op(B)[k,j]
+  const int64_t a_rs = ta ? lda : 1, a_ks = ta ? 1 : lda;
+  const int64_t b_rs = tb ? 1 : ldb, b_ks = tb ? ldb : 1;
+  const int64_t pitch = ((K + 63) / 64) * 64;
+
+  // statistics workspace
+  const size_t st_bytes = align256((M + N) * sizeof(unsigned long long)) + 2 * align256((M + N) * sizeof(double));
+  char* st_ws = nullptr;
+  GB_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&st_ws), st_bytes, s));
+  OzRowStats sa, sb;
+  sa.amax_bits = reinterpret_cast<unsigned long long*>(st_ws);
+  sb.amax_bits = sa.amax_bits + M;
+  sa.sum_abs = reinterpret_cast<double*>(st_ws + align256((M + N) * sizeof(unsigned long long)));
+  sb.sum_abs = sa.sum_abs + M;
+  sa.sum_sq = reinterpret_cast<double*>(st_ws + align256((M + N) * sizeof(unsigned long long)) +
+                                        align256((M + N) * sizeof(double)));
+  sb.sum_sq = sa.sum_sq + M;
+  int rc = oz_row_stats(A, M, K, a_rs, a_ks, sa, s);
+  if (!rc) rc = oz_row_stats(B, N, K, b_rs, b_ks, sb, s);
+  if (rc) {
+    cudaFreeAsync(st_ws, s);
+    return rc;
+  }
+
+  OzPlan plan;
+  int s_use = slices;
+  if (slices == 0 || err_bound_out) {
+    HostStats h;
+    h.amax_a.resize(M); h.amax_b.resize(N);
+    h.sabs_a.resize(M); h.sabs_b.resize(N);
+    h.ssq_a.resize(M); h.ssq_b.resize(N);
+    cudaMemcpyAsync(h.amax_a.data(), sa.amax_bits, M * 8, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(h.amax_b.data(), sb.amax_bits, N * 8, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(h.sabs_a.data(), sa.sum_abs, M * 8, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(h.sabs_b.data(), sb.sum_abs, N * 8, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(h.ssq_a.data(), sa.sum_sq, M * 8, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(h.ssq_b.data(), sb.sum_sq, N * 8, cudaMemcpyDeviceToHost, s);
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+      cudaFreeAsync(st_ws, s);
+      return gb_set_cuda_error(e, "ozaki statistics");
+    }
+    if (slices == 0) {
+      const double tol = ozaki_tolerance();
+      s_use = OZ_MAX_SLICES;
+      for (int cand = 1; cand <= OZ_MAX_SLICES; ++cand) {
+        OzPlan p;
+        if (oz_make_plan(M, N, K, cand, &p)) break;
+        if (ozaki_bound(h, K, cand, p.bits, p.groups * p.nchunks) <= tol) {
+          s_use = cand;
+          break;
+        }
+      }
+    }
+    rc = oz_make_plan(M, N, K, s_use, &plan);
+    if (rc) {
+      cudaFreeAsync(st_ws, s);
+      return rc;
+    }
+    if (err_bound_out) *err_bound_out = ozaki_bound(h, K, s_use, plan.bits, plan.groups * plan.nchunks);
+  } else {
+    rc = oz_make_plan(M, N, K, s_use, &plan);
+    if (rc) {
+      cudaFreeAsync(st_ws, s);
+      return rc;
+    }
+  }
+
+  const int grid = oz_grid_for(dev->sms, M, N);
+  const size_t pa_bytes = align256(static_cast<size_t>(s_use) * M * pitch * 2);
+  const size_t pb_bytes = align256(static_cast<size_t>(s_use) * N * pitch * 2);
+  const size_t ex_bytes = align256((M + N) * sizeof(int32_t));
+  const size_t tw_bytes = (plan.groups * plan.nchunks > 1)
+                              ? static_cast<size_t>(grid) * OZ_BM * OZ_BN * sizeof(double)
+                              : 0;
+  char* ws = nullptr;
+  cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&ws), pa_bytes + pb_bytes + ex_bytes + tw_bytes, s);
+  if (e != cudaSuccess) {
+    cudaFreeAsync(st_ws, s);
+    return gb_set_cuda_error(e, "ozaki workspace");
+  }
+  __nv_bfloat16* pa = reinterpret_cast<__nv_bfloat16*>(ws);
+  __nv_bfloat16* pb = reinterpret_cast<__nv_bfloat16*>(ws + pa_bytes);
+  int32_t* ea = reinterpret_cast<int32_t*>(ws + pa_bytes + pb_bytes);
+  int32_t* eb = ea + M;
+  double* tws = tw_bytes ? reinterpret_cast<double*>(ws + pa_bytes + pb_bytes + ex_bytes) : nullptr;
+
+  rc = oz_split(A, M, K, a_rs, a_ks, sa.amax_bits, s_use, plan.bits, pa, pitch, ea, s);
+  if (!rc) rc = oz_split(B, N, K, b_rs, b_ks, sb.amax_bits, s_use, plan.bits, pb, pitch, eb, s);
+  if (!rc) {
+    OzGemmArgs ga;
+    ga.planes_a = pa;
+    ga.planes_b = pb;
+    ga.pitch = pitch;
+    ga.slices = s_use;
+    ga.M = M;
+    ga.N = N;
+    ga.K = K;
+    ga.ea = ea;
+    ga.eb = eb;
+    ga.alpha = alpha;
+    ga.beta = beta;
+    ga.C = C;
+    ga.ldc = ldc;
+    ga.tws = tws;
+    ga.status = dev->status;
+    ga.wait_limit_ns = g_wait_limit_ns.load();
+    ga.grid = grid;
+    rc = oz_gemm_launch(ga, plan, s);
+  }
+  cudaFreeAsync(ws, s);
+  cudaFreeAsync(st_ws, s);
+  return rc;
+}
+
+}  // namespace gb
+
+using namespace gb;
+
+// ====================================================================== C ABI
+extern "C" {
+
+const char* gb_status_string(int status) {
+  switch (status) {
+    case GB_OK: return "ok";
+    case GB_ERR_INVALID_VALUE: return "invalid value (size, leading dimension, flag or pointer)";
+    case GB_ERR_UNSUPPORTED: return "unsupported on this device or build";
+    case GB_ERR_PIPELINE_TIMEOUT: return "on-device pipeline wait timed out; kernel exited";
+    case GB_ERR_CUDA: return g_last_detail[0] ? g_last_detail : "CUDA error";
+    case GB_ERR_ALLOC: return "device workspace allocation failed";
+    case GB_ERR_NO_DEVICE: return g_last_detail[0] ? g_last_detail : "no usable sm_103 device";
+    default: return "unknown status";
+  }
+}
+
+int gb_version(void) { return GBBLAS_VERSION; }
+
+int gb_set_wait_limit_ns(uint64_t ns) {
+  g_wait_limit_ns.store(ns == 0 ? 4000000000ull : ns);
+  return GB_OK;
+}
+
+int gb_set_ozaki_tolerance(double tol) {
+  if (!(tol >= 0.0)) return GB_ERR_INVALID_VALUE;
+  uint64_t b = 0;
+  if (tol > 0.0) std::memcpy(&b, &tol, sizeof(b));
+  g_ozaki_tol_bits.store(b);
+  return GB_OK;
+}
+
+int gb_check_status(void* stream) {
+  DeviceInfo* dev = nullptr;
+  int rc = device_info(&dev);
+  if (rc) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  DeviceStatus h;
+  GB_CUDA_TRY(cudaMemcpyAsync(&h, dev->status, sizeof(h), cudaMemcpyDeviceToHost, s));
+  GB_CUDA_TRY(cudaStreamSynchronize(s));
+  if (h.code != 0) {
+    std::snprintf(g_last_detail, sizeof(g_last_detail), "pipeline wait at site %d timed out in block %d",
+                  h.where, h.block);
+    GB_CUDA_TRY(cudaMemsetAsync(dev->status, 0, sizeof(DeviceStatus), s));
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    return h.code;
+  }
+  return GB_OK;
+}
+
+int gb_gemm_f64(int transA, int transB, int64_t M, int64_t N, int64_t K, double alpha, const double* A,
+                int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc, int mode,
+                int slices, double* err_bound_out, void* stream) {
+  if (mode != GB_MODE_NATIVE && mode != GB_MODE_OZAKI_BF16 && mode != GB_MODE_OZAKI_INT8)
+    return GB_ERR_INVALID_VALUE;
+  DeviceInfo* dev = nullptr;
+  int rc = device_info(&dev);
+  if (rc) return rc;
+  rc = check_gemm_args(transA, transB, M, N, K, lda, ldb, ldc, A, B, C, alpha != 0.0);
+  if (rc) return rc;
+  if (mode == GB_MODE_OZAKI_INT8) {
+    std::snprintf(g_last_detail, sizeof(g_last_detail),
+                  "tcgen05.mma kind::i8 is not available on sm_103a");
+    return GB_ERR_UNSUPPORTED;
+  }
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (M == 0 || N == 0) {
+    if (err_bound_out) *err_bound_out = 0.0;
+    return GB_OK;
+  }
+  if (mode == GB_MODE_NATIVE || alpha == 0.0 || K == 0) {
+    if (err_bound_out) {
+      const double ku = static_cast<double>(K) * std::ldexp(1.0, -53);
+      *err_bound_out = (alpha == 0.0 || K == 0) ? 0.0 : ku / (1.0 - ku);
+    }
+    return native_gemm_f64(transA, transB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, s);
+  }
+  return ozaki_gemm(dev, transA, transB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, slices,
+                    err_bound_out, s);
+}
+
+int gb_gemm_f32(int transA, int transB, int64_t M, int64_t N, int64_t K, float alpha, const float* A,
+                int64_t lda, const float* B, int64_t ldb, float beta, float* C, int64_t ldc, void* stream) {
+  DeviceInfo* dev = nullptr;
+  int rc = device_info(&dev);
+  if (rc) return rc;
+  rc = check_gemm_args(transA, transB, M, N, K, lda, ldb, ldc, A, B, C, alpha != 0.0f);
+  if (rc) return rc;
+  return native_gemm_f32(transA, transB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc,
+                         static_cast<cudaStream_t>(stream));
+}
+
+int gb_jmul_f64(double* D, const double* A, const double* X, int64_t M, int64_t N, int64_t P, void* stream) {
+  return gb_gemm_f64(0, 0, M, P, N, 1.0, A, M > 1 ? M : 1, X, N > 1 ? N : 1, 0.0, D, M > 1 ? M : 1,
+                     GB_MODE_NATIVE, 0, nullptr, stream);
+}
+
+int gb_jmul_f32(float* D, const float* A, const float* X, int64_t M, int64_t N, int64_t P, void* stream) {
+  return gb_gemm_f32(0, 0, M, P, N, 1.0f, A, M > 1 ? M : 1, X, N > 1 ? N : 1, 0.0f, D, M > 1 ? M : 1,
+                     stream);
+}
+
+int gb_plan_ozaki(int64_t M, int64_t N, int64_t K, int slices, gb_ozaki_plan_t* out) {
+  if (!out || M < 0 || N < 0 || K < 0) return GB_ERR_INVALID_VALUE;
+  OzPlan p;
+  int rc = oz_make_plan(M, N, K, slices, &p);
+  if (rc) return rc;
+  out->slices = p.slices;
+  out->bits = p.bits;
+  out->k_chunk = static_cast<int32_t>(p.k_chunk);
+  out->products = p.products;
+  out->groups = p.groups;
+  out->flops_tensor = p.flops_tensor;
+  return GB_OK;
+}
+
+}  // extern "C"

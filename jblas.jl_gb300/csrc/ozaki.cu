@@ -1,0 +1,594 @@
+// FP64-accurate GEMM by Ozaki-scheme splitting onto BF16 tcgen05 tensor cores.
+//
+// Method: Ozaki, Ogita, Oishi and Rump, "Error-free transformations of matrix
+// multiplication by using fast routines of matrix multiplication and its applications",
+// Numer. Algorithms 59 (2012), with the fixed-point (per-row / per-column power-of-two
+// scaled) digit splitting used by Mukunoki, Ozaki, Ogita and Imamura, "DGEMM using
+// Tensor Cores, and Its Accurate and Reproducible Versions", ISC 2020.
+//
+//   op(A)[i,k] = 2^ea_i * sum_p dA_p[i,k] * 2^(1 - p*b),   |dA_p| <= 2^(b-1), p = 1..s
+//   op(B)[k,j] = 2^eb_j * sum_q dB_q[k,j] * 2^(1 - q*b)
+//   C[i,j] ~= alpha * 2^(ea_i + eb_j) * sum_{p+q <= s+1} 2^(2 - (p+q)*b) * S_pq[i,j] + beta*C
+//   S_pq = dA_p * dB_q    (integer digits held exactly in BF16, products exact in FP32:
+//                          the planner keeps every partial sum an integer below 2^24)
+//
+// The digit planes are the GPU analogue of the packing buffers jBLAS never built
+// (src/memory_management.jl:78-177 plans cache blocks but nothing packs): K-major,
+// BF16, one plane per digit, read by TMA with the 128-byte swizzle.
+//
+// Slice-product kernel (one persistent CTA per SM, warp-specialised):
+//   warp 0      TMA producer: A/B digit tiles into a 4-stage shared-memory ring
+//               (the role of jBLAS's prefetch schedule, src/memory_management.jl:181-277)
+//   warp 1      allocates 512 TMEM columns; lane 0 issues tcgen05.mma 128x256x16 into a
+//               double-buffered FP32 accumulator (jBLAS's register tile, src/gemm.jl:318-333)
+//   warps 2-5   epilogue: tcgen05.ld each exact group sum, FP64 accumulation of the
+//               groups in a per-CTA tile buffer, final power-of-two rescale with alpha/beta
+//               (jBLAS's store_block, src/gemm.jl:3-11, here with the recombination fused)
+// Every mbarrier wait is bounded (gb_common.cuh); on expiry the CTA records
+// GB_ERR_PIPELINE_TIMEOUT, drains its in-flight copies and MMAs, frees TMEM and exits.
+#include <cuda_bf16.h>
+
+#include <cmath>
+
+#include "gb_common.cuh"
+#include "ozaki.cuh"
+
+namespace gb {
+
+// ============================================================== planner (host)
+
+int oz_bits_for(int64_t kc) {
+  int lg = 0;
+  while ((int64_t(1) << lg) < kc) ++lg;           // ceil(log2 kc)
+  int b = (26 - lg) / 2;                          // kc * 2^(2b-2) <= 2^24
+  if (b > 9) b = 9;                               // |digit| <= 256 is exact in BF16
+  return b;
+}
+
+int oz_make_plan(int64_t M, int64_t N, int64_t K, int slices, OzPlan* plan) {
+  if (slices < 1 || slices > OZ_MAX_SLICES) return GB_ERR_INVALID_VALUE;
+  OzPlan& P = *plan;
+  P.slices = slices;
+  // One exact chunk covers K up to 2^16 (b >= 5); longer K is cut into equal chunks.
+  int64_t kb_total = (K + OZ_BK - 1) / OZ_BK;
+  if (kb_total < 1) kb_total = 1;
+  int64_t nchunks = (K + 65535) / 65536;
+  if (nchunks < 1) nchunks = 1;
+  int64_t kb_chunk = (kb_total + nchunks - 1) / nchunks;
+  nchunks = (kb_total + kb_chunk - 1) / kb_chunk;
+  int64_t kc = kb_chunk * OZ_BK;
+  if (kc > K) kc = K < 1 ? 1 : K;
+  P.k_chunk = kc;
+  P.nchunks = static_cast<int>(nchunks);
+  P.bits = oz_bits_for(kc);
+  // pairs that can share one exact FP32 sum
+  const double per_pair = static_cast<double>(kc) * std::ldexp(1.0, 2 * P.bits - 2);
+  int share = static_cast<int>(std::floor(16777216.0 / per_pair));
+  if (share < 1) share = 1;
+  if (share > 8) share = 8;
+
+  OzSchedule& S = P.sched;
+  S.kb_total = static_cast<int32_t>(kb_total);
+  S.kb_chunk = static_cast<int32_t>(kb_chunk);
+  S.bits = P.bits;
+  int g = 0, np = 0;
+  for (int level = 2; level <= slices + 1; ++level) {
+    // pairs (p, q), p + q = level, 1 <= p, q <= slices, in increasing p
+    int in_group = 0;
+    for (int p = 1; p <= slices; ++p) {
+      const int q = level - p;
+      if (q < 1 || q > slices) continue;
+      if (in_group == 0) {
+        if (g >= OZ_MAX_GROUPS) return GB_ERR_UNSUPPORTED;
+        S.level[g] = static_cast<int8_t>(level);
+        S.npairs[g] = 0;
+        S.pair_off[g] = static_cast<int16_t>(np);
+        ++g;
+      }
+      if (np >= OZ_MAX_PAIRS) return GB_ERR_UNSUPPORTED;
+      S.pp[np] = static_cast<uint8_t>(p - 1);
+      S.pq[np] = static_cast<uint8_t>(q - 1);
+      ++np;
+      S.npairs[g - 1]++;
+      if (++in_group == share) in_group = 0;
+    }
+  }
+  S.ngroups = g;
+  P.groups = g;
+  P.products = np;
+  P.flops_tensor = 2.0 * static_cast<double>(M) * static_cast<double>(N) *
+                   static_cast<double>(kb_total * OZ_BK) * np;
+  return GB_OK;
+}
+
+// ============================================================== statistics kernels
+
+__device__ __forceinline__ unsigned long long abs_bits(double x) {
+  return static_cast<unsigned long long>(__double_as_longlong(x)) & 0x7FFFFFFFFFFFFFFFull;
+}
+
+// k contiguous (ks == 1): one warp per row.
+__global__ void stats_kc_kernel(const double* __restrict__ X, int64_t R, int64_t K, int64_t rs,
+                                OzRowStats st) {
+  const int lane = threadIdx.x & 31;
+  const int64_t r = static_cast<int64_t>(blockIdx.x) * (blockDim.x / 32) + (threadIdx.x >> 5);
+  if (r >= R) return;
+  const double* row = X + r * rs;
+  unsigned long long mx = 0;
+  double sa = 0.0, sq = 0.0;
+  for (int64_t k = lane; k < K; k += 32) {
+    const double x = row[k];
+    const unsigned long long b = abs_bits(x);
+    mx = b > mx ? b : mx;
+    sa += fabs(x);
+    sq = fma(x, x, sq);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long m2 = __shfl_xor_sync(0xffffffffu, mx, o);
+    mx = m2 > mx ? m2 : mx;
+    sa += __shfl_xor_sync(0xffffffffu, sa, o);
+    sq += __shfl_xor_sync(0xffffffffu, sq, o);
+  }
+  if (lane == 0) {
+    st.amax_bits[r] = mx;
+    st.sum_abs[r] = sa;
+    st.sum_sq[r] = sq;
+  }
+}
+
+// rows contiguous (rs == 1): 32 rows per block, 8 warps stride over k.
+__global__ void stats_rc_kernel(const double* __restrict__ X, int64_t R, int64_t K, int64_t ks,
+                                OzRowStats st) {
+  __shared__ unsigned long long smx[8][32];
+  __shared__ double ssa[8][32], ssq[8][32];
+  const int tr = threadIdx.x & 31, tk = threadIdx.x >> 5;
+  const int64_t r = static_cast<int64_t>(blockIdx.x) * 32 + tr;
+  unsigned long long mx = 0;
+  double sa = 0.0, sq = 0.0;
+  if (r < R) {
+    for (int64_t k = tk; k < K; k += 8) {
+      const double x = X[r + k * ks];
+      const unsigned long long b = abs_bits(x);
+      mx = b > mx ? b : mx;
+      sa += fabs(x);
+      sq = fma(x, x, sq);
+    }
+  }
+  smx[tk][tr] = mx;
+  ssa[tk][tr] = sa;
+  ssq[tk][tr] = sq;
+  __syncthreads();
+  if (tk == 0 && r < R) {
+    for (int w = 1; w < 8; ++w) {
+      mx = smx[w][tr] > mx ? smx[w][tr] : mx;
+      sa += ssa[w][tr];
+      sq += ssq[w][tr];
+    }
+    st.amax_bits[r] = mx;
+    st.sum_abs[r] = sa;
+    st.sum_sq[r] = sq;
+  }
+}
+
+int oz_row_stats(const double* X, int64_t R, int64_t K, int64_t rs, int64_t ks, OzRowStats st,
+                 cudaStream_t s) {
+  if (R <= 0) return GB_OK;
+  if (ks == 1) {
+    const int64_t blocks = (R + 7) / 8;
+    stats_kc_kernel<<<static_cast<unsigned>(blocks), 256, 0, s>>>(X, R, K, rs, st);
+  } else {
+    const int64_t blocks = (R + 31) / 32;
+    stats_rc_kernel<<<static_cast<unsigned>(blocks), 256, 0, s>>>(X, R, K, ks, st);
+  }
+  GB_CUDA_TRY(cudaGetLastError());
+  return GB_OK;
+}
+
+// ============================================================== split kernels
+
+constexpr int OZ_EXP_NONFINITE = 0x7FFFFFFF;
+
+__device__ __forceinline__ int row_exponent(unsigned long long amax_bits) {
+  if (amax_bits >= 0x7FF0000000000000ull) return OZ_EXP_NONFINITE;  // Inf or NaN in the row
+  if (amax_bits == 0) return 0;
+  return ilogb(__longlong_as_double(static_cast<long long>(amax_bits))) + 1;  // amax < 2^e
+}
+
+// k contiguous: one warp per row, lanes over k.
+__global__ void split_kc_kernel(const double* __restrict__ X, int64_t R, int64_t K, int64_t rs,
+                                const unsigned long long* __restrict__ amax_bits, int slices, int bits,
+                                __nv_bfloat16* __restrict__ planes, int64_t pitch,
+                                int32_t* __restrict__ exps) {
+  const int lane = threadIdx.x & 31;
+  const int64_t r = static_cast<int64_t>(blockIdx.x) * (blockDim.x / 32) + (threadIdx.x >> 5);
+  if (r >= R) return;
+  const int e = row_exponent(amax_bits[r]);
+  if (lane == 0) exps[r] = e;
+  const bool nonfinite = (e == OZ_EXP_NONFINITE);
+  const double step = pow2_normal(bits);
+  const double* row = X + r * rs;
+  const int64_t plane_stride = R * pitch;
+  __nv_bfloat16* out = planes + r * pitch;
+  for (int64_t k = lane; k < K; k += 32) {
+    double y = nonfinite ? 0.0 : scale_pow2(row[k], bits - 1 - e);
+    for (int p = 0; p < slices; ++p) {
+      const double d = rint(y);
+      y = (y - d) * step;
+      out[p * plane_stride + k] = __float2bfloat16_rn(static_cast<float>(d));
+    }
+  }
+}
+
+// rows contiguous: 32 rows x 64 k per block, transposed through shared memory so that
+// the K-major planes are written in 128-byte rows.
+__global__ void split_rc_kernel(const double* __restrict__ X, int64_t R, int64_t K, int64_t ks,
+                                const unsigned long long* __restrict__ amax_bits, int slices, int bits,
+                                __nv_bfloat16* __restrict__ planes, int64_t pitch,
+                                int32_t* __restrict__ exps) {
+  __shared__ __nv_bfloat16 tile[32][64 + 8];
+  const int tr = threadIdx.x & 31, tk = threadIdx.x >> 5;  // tk in [0, 8)
+  const int64_t r0 = static_cast<int64_t>(blockIdx.x) * 32;
+  const int64_t k0 = static_cast<int64_t>(blockIdx.y) * 64;
+  const int64_t r = r0 + tr;
+  int e = 0;
+  if (r < R) e = row_exponent(amax_bits[r]);
+  if (blockIdx.y == 0 && tk == 0 && r < R) exps[r] = e;
+  const bool nonfinite = (e == OZ_EXP_NONFINITE);
+  const double step = pow2_normal(bits);
+  double y[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const int64_t k = k0 + tk + 8 * j;
+    y[j] = (r < R && k < K && !nonfinite) ? scale_pow2(X[r + k * ks], bits - 1 - e) : 0.0;
+  }
+  const int64_t plane_stride = R * pitch;
+  for (int p = 0; p < slices; ++p) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const double d = rint(y[j]);
+      y[j] = (y[j] - d) * step;
+      tile[tr][tk + 8 * j] = __float2bfloat16_rn(static_cast<float>(d));
+    }
+    __syncthreads();
+    // 32 rows x 32 bf16 pairs: thread t writes pair (t % 32) of rows t/32, t/32 + 8, ...
+#pragma unroll
+    for (int rr = 0; rr < 4; ++rr) {
+      const int row_l = tk + 8 * rr;
+      const int64_t rg = r0 + row_l;
+      const int64_t kg = k0 + 2 * tr;
+      if (rg < R && kg < K) {
+        __nv_bfloat16* dst = planes + p * plane_stride + rg * pitch + kg;
+        if (kg + 1 < K) {
+          __nv_bfloat162 v;
+          v.x = tile[row_l][2 * tr];
+          v.y = tile[row_l][2 * tr + 1];
+          *reinterpret_cast<__nv_bfloat162*>(dst) = v;
+        } else {
+          dst[0] = tile[row_l][2 * tr];
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+int oz_split(const double* X, int64_t R, int64_t K, int64_t rs, int64_t ks,
+             const unsigned long long* amax_bits, int slices, int bits, __nv_bfloat16* planes,
+             int64_t pitch, int32_t* exps, cudaStream_t s) {
+  if (R <= 0) return GB_OK;
+  if (ks == 1) {
+    const int64_t blocks = (R + 7) / 8;
+    split_kc_kernel<<<static_cast<unsigned>(blocks), 256, 0, s>>>(X, R, K, rs, amax_bits, slices,
+                                                                   bits, planes, pitch, exps);
+  } else {
+    const int64_t gk = (K + 63) / 64;
+    if (gk > 65535) return GB_ERR_UNSUPPORTED;
+    dim3 grid(static_cast<unsigned>((R + 31) / 32), static_cast<unsigned>(gk < 1 ? 1 : gk));
+    split_rc_kernel<<<grid, 256, 0, s>>>(X, R, K, ks, amax_bits, slices, bits, planes, pitch, exps);
+  }
+  GB_CUDA_TRY(cudaGetLastError());
+  return GB_OK;
+}
+
+// ============================================================== slice-product kernel
+
+constexpr int OZ_THREADS = 192;                 // 6 warps
+constexpr int OZ_A_BYTES = OZ_BM * OZ_BK * 2;   // 16 KB
+constexpr int OZ_B_BYTES = OZ_BN * OZ_BK * 2;   // 32 KB
+constexpr int OZ_STAGE_BYTES = OZ_A_BYTES + OZ_B_BYTES;
+constexpr int OZ_TMEM_COLS = 512;               // two 128 x 256 FP32 accumulators
+constexpr int OZ_SMEM_BYTES = OZ_STAGES * OZ_STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+
+struct OzKernelParams {
+  int64_t M, N, K;
+  const int32_t* ea;
+  const int32_t* eb;
+  double alpha, beta;
+  double* C;
+  int64_t ldc;
+  double* tws;
+  DeviceStatus* status;
+  uint64_t wait_limit_ns;
+  int tiles_m, tiles_n;
+  int nchunks;
+};
+
+// Tile raster: bands of 16 row tiles, column tiles inside a band (keeps the concurrently
+// active A and B panels of one slice pair inside L2).
+__device__ __forceinline__ void tile_coords(int t, int tiles_m, int tiles_n, int& tm, int& tn) {
+  constexpr int GM = 16;
+  const int band = t / (GM * tiles_n);
+  const int in_band = t - band * GM * tiles_n;
+  const int band_rows = min(GM, tiles_m - band * GM);
+  tm = band * GM + in_band % band_rows;
+  tn = in_band / band_rows;
+}
+
+__global__ void __launch_bounds__(OZ_THREADS, 1)
+    oz_gemm_kernel(const __grid_constant__ CUtensorMap tmap_a, const __grid_constant__ CUtensorMap tmap_b,
+                   const __grid_constant__ OzSchedule sched, const OzKernelParams prm) {
+  extern __shared__ uint8_t smem_raw[];
+  // 1024-byte alignment for the 128-byte swizzle atoms
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + OZ_STAGES * OZ_STAGE_BYTES);
+  uint64_t* empty = full + OZ_STAGES;
+  uint64_t* tfull = empty + OZ_STAGES;
+  uint64_t* tempty = tfull + 2;
+  uint64_t* drain = tempty + 2;
+  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(drain + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_holder + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ntiles = prm.tiles_m * prm.tiles_n;
+  const int G = sched.ngroups;
+  const int nch = prm.nchunks;
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < OZ_STAGES; ++i) {
+      mbar_init(&full[i], 1);
+      mbar_init(&empty[i], 1);
+    }
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(&tfull[i], 1);
+      mbar_init(&tempty[i], 128);
+    }
+    mbar_init(drain, 1);
+    *abort_flag = 0;
+    fence_mbar_init();
+    tma_prefetch_desc(&tmap_a);
+    tma_prefetch_desc(&tmap_b);
+  }
+  if (warp == 1) {
+    tmem_alloc(tmem_holder, OZ_TMEM_COLS);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = *tmem_holder;
+
+  if (warp == 0) {
+    // ------------------------------------------------------------ TMA producer
+    if (lane == 0) {
+      int stage = 0;
+      uint32_t phase = 0;
+      int issued_parity[OZ_STAGES];
+      for (int i = 0; i < OZ_STAGES; ++i) issued_parity[i] = -1;
+      bool ok = true;
+      for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+        int tm, tn;
+        tile_coords(t, prm.tiles_m, prm.tiles_n, tm, tn);
+        const int m0 = tm * OZ_BM, n0 = tn * OZ_BN;
+        for (int g = 0; g < G && ok; ++g) {
+          for (int c = 0; c < nch && ok; ++c) {
+            const int kb0 = c * sched.kb_chunk;
+            const int kb1 = min(kb0 + sched.kb_chunk, sched.kb_total);
+            for (int i = 0; i < sched.npairs[g] && ok; ++i) {
+              const int pa = sched.pp[sched.pair_off[g] + i];
+              const int pb = sched.pq[sched.pair_off[g] + i];
+              for (int kb = kb0; kb < kb1; ++kb) {
+                if (!mbar_wait_bounded(&empty[stage], phase ^ 1, prm.wait_limit_ns, abort_flag,
+                                       prm.status, 1)) {
+                  ok = false;
+                  break;
+                }
+                uint8_t* sa = smem + stage * OZ_STAGE_BYTES;
+                uint8_t* sb = sa + OZ_A_BYTES;
+                mbar_arrive_expect_tx(&full[stage], OZ_STAGE_BYTES);
+                tma_load_3d(sa, &tmap_a, &full[stage], kb * OZ_BK, m0, pa);
+                tma_load_3d(sb, &tmap_b, &full[stage], kb * OZ_BK, n0, pb);
+                issued_parity[stage] = static_cast<int>(phase);
+                if (++stage == OZ_STAGES) { stage = 0; phase ^= 1; }
+              }
+            }
+          }
+        }
+      }
+      if (!ok) {
+        // let every copy this thread issued land before the CTA's shared memory goes away
+        for (int i = 0; i < OZ_STAGES; ++i)
+          if (issued_parity[i] >= 0) {
+            volatile int no_abort = 0;
+            mbar_wait_bounded(&full[i], static_cast<uint32_t>(issued_parity[i]), prm.wait_limit_ns,
+                              &no_abort, nullptr, 0);
+          }
+      }
+    }
+  } else if (warp == 1) {
+    // ------------------------------------------------------------ MMA issuer
+    if (lane == 0) {
+      constexpr uint32_t IDESC = idesc_bf16_f32(OZ_BM, OZ_BN);
+      int stage = 0;
+      uint32_t phase = 0;
+      int buf = 0;
+      uint32_t acc_phase = 0;
+      bool ok = true;
+      bool issued_any = false;
+      for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+        for (int g = 0; g < G && ok; ++g) {
+          for (int c = 0; c < nch && ok; ++c) {
+            const int kb0 = c * sched.kb_chunk;
+            const int kb1 = min(kb0 + sched.kb_chunk, sched.kb_total);
+            if (!mbar_wait_bounded(&tempty[buf], acc_phase ^ 1, prm.wait_limit_ns, abort_flag,
+                                   prm.status, 2)) {
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint32_t d_tmem = tmem_base + static_cast<uint32_t>(buf * OZ_BN);
+            uint32_t accumulate = 0;
+            for (int i = 0; i < sched.npairs[g] && ok; ++i) {
+              for (int kb = kb0; kb < kb1; ++kb) {
+                if (!mbar_wait_bounded(&full[stage], phase, prm.wait_limit_ns, abort_flag,
+                                       prm.status, 3)) {
+                  ok = false;
+                  break;
+                }
+                tc_fence_after();
+                const uint32_t sa = smem_u32(smem + stage * OZ_STAGE_BYTES);
+                const uint32_t sb = sa + OZ_A_BYTES;
+                const uint64_t adesc = smem_desc_sw128(sa);
+                const uint64_t bdesc = smem_desc_sw128(sb);
+#pragma unroll
+                for (int kk = 0; kk < OZ_BK / 16; ++kk) {
+                  // advance 16 BF16 = 32 bytes along K inside the swizzle atom
+                  tc_mma_f16(d_tmem, adesc + static_cast<uint64_t>(kk * 2),
+                             bdesc + static_cast<uint64_t>(kk * 2), IDESC, accumulate);
+                  accumulate = 1;
+                }
+                issued_any = true;
+                tc_commit(&empty[stage]);
+                if (++stage == OZ_STAGES) { stage = 0; phase ^= 1; }
+              }
+            }
+            if (!ok) break;
+            tc_commit(&tfull[buf]);
+            if (++buf == 2) { buf = 0; acc_phase ^= 1; }
+          }
+        }
+      }
+      if (!ok && issued_any) {
+        // wait for every MMA issued so far before TMEM is released
+        tc_commit(drain);
+        volatile int no_abort = 0;
+        mbar_wait_bounded(drain, 0, prm.wait_limit_ns, &no_abort, nullptr, 0);
+      }
+    }
+  } else {
+    // ------------------------------------------------------------ epilogue (warps 2..5)
+    const int q = warp & 3;                 // TMEM lane quadrant of this warp
+    const int row_l = q * 32 + lane;        // tile row owned by this thread
+    double* tws = prm.tws + static_cast<int64_t>(blockIdx.x) * (OZ_BM * OZ_BN);
+    int buf = 0;
+    uint32_t acc_phase = 0;
+    bool ok = true;
+    const double alpha = prm.alpha, beta = prm.beta;
+    for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+      int tm, tn;
+      tile_coords(t, prm.tiles_m, prm.tiles_n, tm, tn);
+      const int64_t row = static_cast<int64_t>(tm) * OZ_BM + row_l;
+      const int64_t n0 = static_cast<int64_t>(tn) * OZ_BN;
+      const bool row_ok = row < prm.M;
+      const int ea = row_ok ? prm.ea[row] : 0;
+      int step = 0;
+      const int nsteps = G * nch;
+      for (int g = 0; g < G && ok; ++g) {
+        const double w = pow2_normal(2 - sched.level[g] * sched.bits);
+        for (int c = 0; c < nch; ++c, ++step) {
+          // the whole warp agrees before the warp-collective tcgen05.ld
+          ok = __all_sync(0xffffffffu, mbar_wait_bounded(&tfull[buf], acc_phase, prm.wait_limit_ns,
+                                                         abort_flag, prm.status, 4));
+          if (!ok) break;
+          tc_fence_after();
+          const bool first = (step == 0), last = (step == nsteps - 1);
+          const uint32_t taddr = tmem_base + (static_cast<uint32_t>(q * 32) << 16) +
+                                 static_cast<uint32_t>(buf * OZ_BN);
+#pragma unroll 1
+          for (int cb = 0; cb < OZ_BN; cb += 32) {
+            uint32_t v[32];
+            tmem_ld_32x32b_x32(taddr + cb, v);
+            tc_wait_ld();
+            double* tcol = tws + static_cast<int64_t>(cb) * OZ_BM + row_l;
+            if (!last) {
+#pragma unroll
+              for (int j = 0; j < 32; ++j) {
+                const double s = static_cast<double>(__uint_as_float(v[j]));
+                double* tp = tcol + j * OZ_BM;
+                *tp = first ? s * w : fma(s, w, *tp);
+              }
+            } else {
+#pragma unroll
+              for (int j = 0; j < 32; ++j) {
+                const int64_t col = n0 + cb + j;
+                const double s = static_cast<double>(__uint_as_float(v[j]));
+                const double tot = first ? s * w : fma(s, w, tcol[j * OZ_BM]);
+                if (row_ok && col < prm.N) {
+                  const int eb = prm.eb[col];
+                  double val;
+                  if (ea == OZ_EXP_NONFINITE || eb == OZ_EXP_NONFINITE)
+                    val = __longlong_as_double(0x7FF8000000000000ll);
+                  else
+                    val = scale_pow2(tot, ea + eb);
+                  double* cp = prm.C + row + col * prm.ldc;
+                  *cp = (beta == 0.0) ? alpha * val : fma(alpha, val, beta * *cp);
+                }
+              }
+            }
+          }
+          tc_fence_before();
+          mbar_arrive(&tempty[buf]);
+          if (++buf == 2) { buf = 0; acc_phase ^= 1; }
+        }
+      }
+    }
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    __syncwarp();
+    tc_fence_after();
+    tmem_dealloc(tmem_base, OZ_TMEM_COLS);
+  }
+}
+
+int oz_gemm_launch(const OzGemmArgs& a, const OzPlan& plan, cudaStream_t s) {
+  CUtensorMap ta, tb;
+  int rc = make_plane_tmap(&ta, a.planes_a, a.K, a.M, a.slices, a.pitch, OZ_BM);
+  if (rc) return rc;
+  rc = make_plane_tmap(&tb, a.planes_b, a.K, a.N, a.slices, a.pitch, OZ_BN);
+  if (rc) return rc;
+  OzKernelParams prm;
+  prm.M = a.M;
+  prm.N = a.N;
+  prm.K = a.K;
+  prm.ea = a.ea;
+  prm.eb = a.eb;
+  prm.alpha = a.alpha;
+  prm.beta = a.beta;
+  prm.C = a.C;
+  prm.ldc = a.ldc;
+  prm.tws = a.tws;
+  prm.status = a.status;
+  prm.wait_limit_ns = a.wait_limit_ns;
+  prm.tiles_m = static_cast<int>((a.M + OZ_BM - 1) / OZ_BM);
+  prm.tiles_n = static_cast<int>((a.N + OZ_BN - 1) / OZ_BN);
+  prm.nchunks = plan.nchunks;
+  static bool attr_set = false;  // per process; the attribute is per function, not per device
+  if (!attr_set) {
+    GB_CUDA_TRY(cudaFuncSetAttribute(oz_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     OZ_SMEM_BYTES));
+    attr_set = true;
+  }
+  oz_gemm_kernel<<<a.grid, OZ_THREADS, OZ_SMEM_BYTES, s>>>(ta, tb, plan.sched, prm);
+  GB_CUDA_TRY(cudaGetLastError());
+  return GB_OK;
+}
+
+int oz_grid_for(int sms, int64_t M, int64_t N) {
+  const int64_t tiles = ((M + OZ_BM - 1) / OZ_BM) * ((N + OZ_BN - 1) / OZ_BN);
+  return static_cast<int>(tiles < sms ? tiles : sms);
+}
+
+}  // namespace gb

@@ -1,0 +1,94 @@
+// Ozaki-scheme FP64 emulation on BF16 tensor cores: planner structures and launchers.
+#pragma once
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gb_common.cuh"
+
+namespace gb {
+
+constexpr int OZ_MAX_SLICES = 20;
+constexpr int OZ_MAX_GROUPS = 256;
+constexpr int OZ_MAX_PAIRS = 256;
+
+// Tile of the slice-product kernel: 128 rows of C x 256 columns, K panels of 64 BF16.
+constexpr int OZ_BM = 128;
+constexpr int OZ_BN = 256;
+constexpr int OZ_BK = 64;
+constexpr int OZ_STAGES = 4;
+
+// Accumulation schedule of one output tile.  Group g sums the slice products
+// (pp[off+i], pq[off+i]), i < npairs[g], all of level p + q = level[g], over one K chunk
+// into a TMEM accumulator; the sum is an exact integer in FP32 by construction
+// (npairs * kc * 2^(2*bits-2) <= 2^24).  Groups run in order, each K chunk in order.
+struct OzSchedule {
+  int32_t ngroups;
+  int32_t kb_total;   // K panels of 64 over the whole K
+  int32_t kb_chunk;   // K panels per exact accumulation chunk
+  int32_t bits;       // bits per digit plane
+  int8_t level[OZ_MAX_GROUPS];
+  int8_t npairs[OZ_MAX_GROUPS];
+  int16_t pair_off[OZ_MAX_GROUPS];
+  uint8_t pp[OZ_MAX_PAIRS];
+  uint8_t pq[OZ_MAX_PAIRS];
+};
+
+// Host-side plan.
+struct OzPlan {
+  int slices;
+  int bits;
+  int64_t k_chunk;
+  int products;   // pairs with p + q <= slices + 1
+  int groups;     // TMEM groups per K chunk
+  int nchunks;
+  double flops_tensor;
+  OzSchedule sched;
+};
+
+// bits per digit plane for an exact FP32 sum of `kc` products of `pairs_per_group` pairs.
+int oz_bits_for(int64_t kc);
+// Builds the plan (schedule included) for a given slice count (1..OZ_MAX_SLICES).
+int oz_make_plan(int64_t M, int64_t N, int64_t K, int slices, OzPlan* plan);
+
+// Per-row statistics of op(X) (rows r < R, contraction index k < K):
+// amax bits of |x| (as uint64), sum |x|, sum x^2.
+struct OzRowStats {
+  unsigned long long* amax_bits;
+  double* sum_abs;
+  double* sum_sq;
+};
+
+int oz_row_stats(const double* X, int64_t R, int64_t K, int64_t rs, int64_t ks, OzRowStats st,
+                 cudaStream_t s);
+// Writes `slices` digit planes (BF16, [slice][row][pitch]) and per-row exponents.
+int oz_split(const double* X, int64_t R, int64_t K, int64_t rs, int64_t ks,
+             const unsigned long long* amax_bits, int slices, int bits, __nv_bfloat16* planes,
+             int64_t pitch, int32_t* exps, cudaStream_t s);
+
+struct OzGemmArgs {
+  const void* planes_a;   // [slices][M][pitch] bf16
+  const void* planes_b;   // [slices][N][pitch] bf16
+  int64_t pitch;          // elements per plane row (multiple of 64)
+  int slices;
+  int64_t M, N, K;
+  const int32_t* ea;      // row exponents of op(A)
+  const int32_t* eb;      // column exponents of op(B)
+  double alpha, beta;
+  double* C;
+  int64_t ldc;
+  double* tws;            // per-CTA FP64 tile accumulators (grid x 128 x 256)
+  DeviceStatus* status;
+  uint64_t wait_limit_ns;
+  int grid;
+};
+int oz_gemm_launch(const OzGemmArgs& a, const OzPlan& plan, cudaStream_t s);
+// Persistent grid size: one CTA per SM, at most one per output tile.
+int oz_grid_for(int sms, int64_t M, int64_t N);
+
+// Encodes a 3-D BF16 tensor map {K, rows, slices} with a 64 x box_rows x 1 box, 128-B swizzle.
+int make_plane_tmap(CUtensorMap* map, const void* base, int64_t K, int64_t rows, int64_t slices,
+                    int64_t pitch, int box_rows);
+
+}  // namespace gb

@@ -1,0 +1,12 @@
+"""gbblas: GB300 (sm_103a) GEMM behind jBLAS.jl's jmul!/gemm! interface.
+
+Everything here calls the C ABI of libgbblas.so (include/gbblas.h); there is no CPU or
+PyTorch fallback for any computation.
+"""
+from ._lib import GBError, LIB_PATH, MODE_NATIVE, MODE_OZAKI_BF16, MODE_OZAKI_INT8, lib
+from .api import (DimensionMismatch, check_device_status, gemm, gemm_, gemm_raw, jmul_,
+                  ozaki_plan, set_ozaki_tolerance, set_wait_limit_ns)
+
+__all__ = ["GBError", "DimensionMismatch", "LIB_PATH", "MODE_NATIVE", "MODE_OZAKI_BF16",
+           "MODE_OZAKI_INT8", "lib", "gemm", "gemm_", "gemm_raw", "jmul_", "ozaki_plan",
+           "set_ozaki_tolerance", "set_wait_limit_ns", "check_device_status"]

@@ -1,0 +1,86 @@
+"""ctypes binding of libgbblas.so (the C ABI declared in include/gbblas.h).
+
+The library is built in-tree by ``build_lib.py``; if it is missing this module raises
+instead of falling back to any CPU or PyTorch computation.
+"""
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(os.path.dirname(_HERE), "lib", "libgbblas.so")
+
+GB_OK = 0
+GB_ERR_INVALID_VALUE = -1
+GB_ERR_UNSUPPORTED = -2
+GB_ERR_PIPELINE_TIMEOUT = -3
+GB_ERR_CUDA = -4
+GB_ERR_ALLOC = -5
+GB_ERR_NO_DEVICE = -6
+
+MODE_NATIVE = 0
+MODE_OZAKI_BF16 = 1
+MODE_OZAKI_INT8 = 2
+
+c_i64 = ctypes.c_int64
+c_int = ctypes.c_int
+c_vp = ctypes.c_void_p
+c_double = ctypes.c_double
+c_float = ctypes.c_float
+
+
+class OzakiPlan(ctypes.Structure):
+    _fields_ = [("slices", ctypes.c_int32), ("bits", ctypes.c_int32), ("k_chunk", ctypes.c_int32),
+                ("products", ctypes.c_int32), ("groups", ctypes.c_int32),
+                ("flops_tensor", ctypes.c_double)]
+
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "gb_status_string": (ctypes.c_char_p, [c_int]),
+    "gb_version": (c_int, []),
+    "gb_set_wait_limit_ns": (c_int, [ctypes.c_uint64]),
+    "gb_set_ozaki_tolerance": (c_int, [c_double]),
+    "gb_check_status": (c_int, [c_vp]),
+    "gb_jmul_f64": (c_int, [c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, c_vp]),
+    "gb_jmul_f32": (c_int, [c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, c_vp]),
+    "gb_gemm_f64": (c_int, [c_int, c_int, c_i64, c_i64, c_i64, c_double, c_vp, c_i64, c_vp, c_i64,
+                            c_double, c_vp, c_i64, c_int, c_int, ctypes.POINTER(c_double), c_vp]),
+    "gb_gemm_f32": (c_int, [c_int, c_int, c_i64, c_i64, c_i64, c_float, c_vp, c_i64, c_vp, c_i64,
+                            c_float, c_vp, c_i64, c_vp]),
+    "gb_plan_ozaki": (c_int, [c_i64, c_i64, c_i64, c_int, ctypes.POINTER(OzakiPlan)]),
+}
+
+_lib = None
+
+
+def lib():
+    """The loaded library (ctypes.CDLL); raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libgbblas.so not built (%s); run __graft_entry__.build() or "
+                               "python jblas.jl_gb300/build_lib.py" % LIB_PATH)
+        l = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(l, name, None)
+            if fn is None:
+                continue
+            fn.restype = res
+            fn.argtypes = args
+        _lib = l
+    return _lib
+
+
+class GBError(RuntimeError):
+    """A gbblas call returned a non-zero status."""
+
+    def __init__(self, status, where=""):
+        self.status = status
+        msg = lib().gb_status_string(status).decode()
+        super().__init__("%s%s (status %d)" % (where + ": " if where else "", msg, status))
+
+
+def check(status, where=""):
+    if status != GB_OK:
+        raise GBError(status, where)
+    return status

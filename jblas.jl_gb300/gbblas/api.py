@@ -1,0 +1,145 @@
+"""Host-side mirror of jBLAS's matrix-multiply interface over the gbblas C ABI.
+
+Reference interface (paths relative to the jBLAS.jl tree):
+  jmul!(D, A, X)  src/gemm.jl:244-348   D (M x P) = A (M x N) * X (N x P), returns D
+  kernel!(pD, pA, pX, Kernel{...})       src/kernels.jl:239 (pointer form, D += A*X)
+
+``jmul_`` keeps jmul!'s argument order, meaning (the reference's N is the contraction
+dimension) and in-place contract: D is overwritten and returned.  ``gemm_`` is the
+BLAS-3 generalisation (alpha, beta, transposes, FP64 mode).  Matrices are CUDA torch
+tensors; column-major storage (stride (1, ld)) is used as is, row-major storage is
+read as the transpose of a column-major matrix, so no copy is made for either.
+Shape errors raise ``DimensionMismatch`` (jmul!'s sizes are type parameters, so the
+reference reports them as a method error at compile time); library errors raise
+``GBError`` with the status string.
+"""
+import ctypes
+
+import torch
+
+from . import _lib
+from ._lib import GBError, check
+
+
+class DimensionMismatch(ValueError):
+    """Operand shapes do not conform (Julia's DimensionMismatch)."""
+
+
+def _stream_ptr(t):
+    return ctypes.c_void_p(torch.cuda.current_stream(t.device).cuda_stream)
+
+
+def _storage(X, name, allow_copy):
+    """(tensor, ld, trans) with X == (trans ? S^T : S) for column-major S of leading dim ld."""
+    if X.dim() != 2:
+        raise DimensionMismatch("%s must be a matrix, got %d dims" % (name, X.dim()))
+    if not X.is_cuda:
+        raise ValueError("%s must be a CUDA tensor (device memory)" % name)
+    r, c = X.shape
+    s0, s1 = X.stride()
+    if (s0 == 1 or r <= 1) and (c <= 1 or s1 >= max(1, r)):
+        return X, (s1 if c > 1 else max(1, r)), 0
+    if (s1 == 1 or c <= 1) and (r <= 1 or s0 >= max(1, c)):
+        return X, (s0 if r > 1 else max(1, c)), 1
+    if not allow_copy:
+        raise ValueError("%s must have unit stride in one dimension" % name)
+    Y = X.t().contiguous().t()
+    return Y, max(1, r), 0
+
+
+def _dtype_of(*ts):
+    dt = ts[0].dtype
+    for t in ts[1:]:
+        if t.dtype != dt:
+            raise TypeError("all operands must share one dtype, got %s and %s" % (dt, t.dtype))
+    if dt not in (torch.float64, torch.float32):
+        raise TypeError("gbblas computes in float64 or float32, got %s" % dt)
+    return dt
+
+
+def gemm_raw(transA, transB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, *, dtype,
+             mode=_lib.MODE_NATIVE, slices=0, want_bound=False, stream=None):
+    """Direct C-ABI call on device pointers (ints).  Returns the error bound or None."""
+    L = _lib.lib()
+    st = ctypes.c_void_p(stream)
+    if dtype == torch.float64:
+        bound = ctypes.c_double(0.0)
+        rc = L.gb_gemm_f64(int(transA), int(transB), M, N, K, float(alpha), ctypes.c_void_p(A), lda,
+                           ctypes.c_void_p(B), ldb, float(beta), ctypes.c_void_p(C), ldc, int(mode),
+                           int(slices), ctypes.byref(bound) if want_bound else None, st)
+        check(rc, "gb_gemm_f64")
+        return bound.value if want_bound else None
+    if mode != _lib.MODE_NATIVE:
+        raise ValueError("Ozaki modes emulate float64; float32 runs natively")
+    rc = L.gb_gemm_f32(int(transA), int(transB), M, N, K, float(alpha), ctypes.c_void_p(A), lda,
+                       ctypes.c_void_p(B), ldb, float(beta), ctypes.c_void_p(C), ldc, st)
+    check(rc, "gb_gemm_f32")
+    return None
+
+
+_MODES = {"native": _lib.MODE_NATIVE, "ozaki": _lib.MODE_OZAKI_BF16,
+          "ozaki_bf16": _lib.MODE_OZAKI_BF16, "ozaki_int8": _lib.MODE_OZAKI_INT8}
+
+
+def gemm_(C, A, B, alpha=1.0, beta=0.0, *, mode="native", slices=0, return_bound=False):
+    """C = alpha * A @ B + beta * C in place; A (M x K), B (K x N), C (M x N).
+
+    mode "native": the jmul! FMA chain (bit-identical to the oracle); "ozaki": FP64
+    emulation on BF16 tensor cores (float64 only; slices = 0 picks the count for the
+    library tolerance).  With return_bound the a-priori normwise error bound is
+    returned alongside C.
+    """
+    dt = _dtype_of(C, A, B)
+    M, K = A.shape
+    K2, N = B.shape
+    if K2 != K or tuple(C.shape) != (M, N):
+        raise DimensionMismatch("A is %dx%d, B is %dx%d, C is %dx%d" % (M, K, K2, N, *C.shape))
+    md = _MODES[mode] if isinstance(mode, str) else int(mode)
+    Cs, ldc, tc = _storage(C, "C", allow_copy=False)
+    As, lda, ta = _storage(A, "A", allow_copy=True)
+    Bs, ldb, tb = _storage(B, "B", allow_copy=True)
+    stream = torch.cuda.current_stream(C.device).cuda_stream
+    if tc == 0:
+        bound = gemm_raw(ta, tb, M, N, K, alpha, As.data_ptr(), lda, Bs.data_ptr(), ldb, beta,
+                         Cs.data_ptr(), ldc, dtype=dt, mode=md, slices=slices,
+                         want_bound=return_bound, stream=stream)
+    else:
+        # C stored row-major: C^T (N x M, column-major) = B^T A^T
+        bound = gemm_raw(1 - tb, 1 - ta, N, M, K, alpha, Bs.data_ptr(), ldb, As.data_ptr(), lda,
+                         beta, Cs.data_ptr(), ldc, dtype=dt, mode=md, slices=slices,
+                         want_bound=return_bound, stream=stream)
+    return (C, bound) if return_bound else C
+
+
+def jmul_(D, A, X):
+    """jmul!(D, A, X): D = A * X with jBLAS's per-element FMA order (src/gemm.jl:244)."""
+    return gemm_(D, A, X, 1.0, 0.0, mode="native")
+
+
+def gemm(A, B, *, mode="native", slices=0):
+    """Allocating form: returns A @ B as a new column-major tensor."""
+    dt = _dtype_of(A, B)
+    C = torch.empty((B.shape[1], A.shape[0]), dtype=dt, device=A.device).t()
+    return gemm_(C, A, B, 1.0, 0.0, mode=mode, slices=slices)
+
+
+def ozaki_plan(M, N, K, slices):
+    """The slice/bit/grouping plan the Ozaki kernel uses for this shape (no GPU work)."""
+    p = _lib.OzakiPlan()
+    check(_lib.lib().gb_plan_ozaki(M, N, K, slices, ctypes.byref(p)), "gb_plan_ozaki")
+    return {"slices": p.slices, "bits": p.bits, "k_chunk": p.k_chunk, "products": p.products,
+            "groups": p.groups, "flops_tensor": p.flops_tensor}
+
+
+def set_ozaki_tolerance(tol):
+    check(_lib.lib().gb_set_ozaki_tolerance(float(tol)), "gb_set_ozaki_tolerance")
+
+
+def set_wait_limit_ns(ns):
+    check(_lib.lib().gb_set_wait_limit_ns(int(ns)), "gb_set_wait_limit_ns")
+
+
+def check_device_status(stream=None):
+    """Raises GBError if a kernel recorded a pipeline timeout since the last check."""
+    s = ctypes.c_void_p(stream if stream is not None else torch.cuda.current_stream().cuda_stream)
+    check(_lib.lib().gb_check_status(s), "gb_check_status")

@@ -1,0 +1,311 @@
+"""CPU oracle for the jBLAS blocked-GEMM hot path — TEST INFRASTRUCTURE ONLY.
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU baseline arm may import
+this module, and only as the checker or the timed CPU reference; the GPU product path
+never calls it.
+
+Parity status: UNPINNED by the reference's own tests (jBLAS.jl's test/runtests.jl has
+no assertions, seeds or stored outputs, and the package cannot run without Julia).  The
+restatements here are pinned against each other instead:
+  * ``gemm`` / ``jmul``      C restatement of jmul!'s FMA chain (jmul_oracle.c), checked
+                             bit-exactly against ``chain_exact`` and the committed
+                             fixtures of tests/golden/ (made by make_golden.py);
+  * ``chain_exact``          pure-Python restatement with exact rationals: each step
+                             rounds a*b + d exactly once (CPython's int/int true division
+                             is correctly rounded), following src/gemm.jl:76-89,154-168;
+  * ``dot2_entries``         compensated dot products (Ogita-Rump-Oishi Dot2) for
+                             near-exact values at sampled entries of large products;
+  * ``ozaki_*``              numpy restatement of the Ozaki splitting and recombination
+                             the GPU kernel performs, operation for operation.
+"""
+import ctypes
+import math
+import os
+import sys
+from fractions import Fraction
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+if HERE not in sys.path:
+    sys.path.insert(0, HERE)
+import build_oracle  # noqa: E402
+
+_lib = None
+c_i64 = ctypes.c_int64
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="F_CONTIGUOUS")
+_vp = ctypes.c_void_p
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = build_oracle.build()
+        L = ctypes.CDLL(path)
+        L.or_gemm_f64.argtypes = [ctypes.c_int, ctypes.c_int, c_i64, c_i64, c_i64, ctypes.c_double, _vp,
+                                  c_i64, _vp, c_i64, ctypes.c_double, _vp, c_i64, ctypes.c_int]
+        L.or_gemm_f32.argtypes = [ctypes.c_int, ctypes.c_int, c_i64, c_i64, c_i64, ctypes.c_float, _vp,
+                                  c_i64, _vp, c_i64, ctypes.c_float, _vp, c_i64, ctypes.c_int]
+        for nm in ("or_jmul_tiled_f64", "or_jmul_tiled_f32"):
+            getattr(L, nm).argtypes = [c_i64, c_i64, c_i64, _vp, c_i64, _vp, c_i64, _vp, c_i64,
+                                       ctypes.c_int]
+        L.or_dot2_entries.argtypes = [ctypes.c_int, ctypes.c_int, c_i64, _vp, c_i64, _vp, c_i64, c_i64,
+                                      _vp, _vp, _vp, _vp, _vp, ctypes.c_int]
+        L.or_fma_array.argtypes = [c_i64, _vp, _vp, _vp, _vp]
+        L.or_chain_entries_f64.argtypes = [ctypes.c_int, ctypes.c_int, c_i64, ctypes.c_double, _vp, c_i64,
+                                           _vp, c_i64, ctypes.c_double, _vp, c_i64, c_i64, _vp, _vp, _vp,
+                                           ctypes.c_int]
+        L.or_chain_entries_f32.argtypes = [ctypes.c_int, ctypes.c_int, c_i64, ctypes.c_float, _vp, c_i64,
+                                           _vp, c_i64, ctypes.c_float, _vp, c_i64, c_i64, _vp, _vp, _vp,
+                                           ctypes.c_int]
+        L.or_num_threads.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(_vp)
+
+
+def _colmajor(X, dtype):
+    """(array, ld) for a 2-D array stored column-major (copying if needed)."""
+    X = np.asarray(X)
+    if X.dtype != dtype:
+        X = X.astype(dtype)
+    if not X.flags.f_contiguous:
+        X = np.asfortranarray(X)
+    return X, max(1, X.shape[0])
+
+
+def num_threads():
+    return lib().or_num_threads()
+
+
+def gemm(A, B, C=None, alpha=1.0, beta=0.0, trans_a=False, trans_b=False, dtype=np.float64,
+         nthreads=None):
+    """alpha*op(A)*op(B) + beta*C with jmul!'s element order; returns a new F-ordered array.
+
+    A, B are the STORED matrices (op applied by the flags), as in BLAS."""
+    A, lda = _colmajor(A, dtype)
+    B, ldb = _colmajor(B, dtype)
+    M = A.shape[1] if trans_a else A.shape[0]
+    K = A.shape[0] if trans_a else A.shape[1]
+    N = B.shape[0] if trans_b else B.shape[1]
+    out = np.zeros((M, N), dtype=dtype, order="F") if C is None else np.array(C, dtype=dtype, order="F")
+    nt = nthreads or num_threads()
+    fn = lib().or_gemm_f64 if dtype == np.float64 else lib().or_gemm_f32
+    fn(int(trans_a), int(trans_b), M, N, K, alpha, _ptr(A), lda, _ptr(B), ldb, beta, _ptr(out),
+       max(1, M), nt)
+    return out
+
+
+def jmul(A, X, dtype=np.float64):
+    """jmul!(D, A, X) restated: D = A * X (src/gemm.jl:244)."""
+    return gemm(A, X, dtype=dtype)
+
+
+def jmul_tiled(A, B, nthreads=1, dtype=np.float64, out=None):
+    """The timed CPU baseline: jmul!'s register-tiled loop nest (same results as jmul)."""
+    A, lda = _colmajor(A, dtype)
+    B, ldb = _colmajor(B, dtype)
+    M, K = A.shape
+    N = B.shape[1]
+    if out is None:
+        out = np.empty((M, N), dtype=dtype, order="F")
+    fn = lib().or_jmul_tiled_f64 if dtype == np.float64 else lib().or_jmul_tiled_f32
+    fn(M, N, K, _ptr(A), lda, _ptr(B), ldb, _ptr(out), max(1, M), int(nthreads))
+    return out
+
+
+def chain_entries(A, B, rows, cols, C=None, alpha=1.0, beta=0.0, trans_a=False, trans_b=False,
+                  dtype=np.float64, nthreads=None):
+    """jmul!'s exact per-element result (with alpha/beta) at sampled (rows[s], cols[s])."""
+    A, lda = _colmajor(A, dtype)
+    B, ldb = _colmajor(B, dtype)
+    K = A.shape[0] if trans_a else A.shape[1]
+    rows = np.ascontiguousarray(rows, dtype=np.int64)
+    cols = np.ascontiguousarray(cols, dtype=np.int64)
+    if C is None:
+        C0, ldc = np.zeros((1, 1), dtype=dtype, order="F"), 1
+    else:
+        C0, ldc = _colmajor(C, dtype)
+    out = np.empty(rows.size, dtype=dtype)
+    fn = lib().or_chain_entries_f64 if dtype == np.float64 else lib().or_chain_entries_f32
+    fn(int(trans_a), int(trans_b), K, alpha, _ptr(A), lda, _ptr(B), ldb, beta, _ptr(C0), ldc, rows.size,
+       _ptr(rows), _ptr(cols), _ptr(out), nthreads or num_threads())
+    return out
+
+
+def dot2_entries(A, B, rows, cols, trans_a=False, trans_b=False, nthreads=None):
+    """Near-exact (hi, lo, sum|a||b|) of (op(A) op(B))[rows[s], cols[s]] via Dot2."""
+    A, lda = _colmajor(A, np.float64)
+    B, ldb = _colmajor(B, np.float64)
+    K = A.shape[0] if trans_a else A.shape[1]
+    rows = np.ascontiguousarray(rows, dtype=np.int64)
+    cols = np.ascontiguousarray(cols, dtype=np.int64)
+    n = rows.size
+    hi = np.empty(n)
+    lo = np.empty(n)
+    ab = np.empty(n)
+    lib().or_dot2_entries(int(trans_a), int(trans_b), K, _ptr(A), lda, _ptr(B), ldb, n, _ptr(rows),
+                          _ptr(cols), _ptr(hi), _ptr(lo), _ptr(ab), nthreads or num_threads())
+    return hi, lo, ab
+
+
+def fma(a, b, c):
+    """Elementwise fused multiply-add with one rounding (float64 arrays)."""
+    a, b, c = (np.ascontiguousarray(np.broadcast_to(x, np.broadcast(a, b, c).shape), dtype=np.float64)
+               for x in (a, b, c))
+    out = np.empty_like(a)
+    lib().or_fma_array(a.size, _ptr(a), _ptr(b), _ptr(c), _ptr(out))
+    return out
+
+
+# ------------------------------------------------------------------ exact restatement
+
+def _round_to_float(q: Fraction, bits: int) -> float:
+    """Round a rational to the nearest binary float with `bits` significand bits
+    (ties to even), IEEE range of float64 (bits=53) or float32 (bits=24)."""
+    if q == 0:
+        return 0.0
+    if bits == 53:
+        return q.numerator / q.denominator  # correctly rounded in CPython
+    emin, emax = -126, 127
+    sign = -1.0 if q < 0 else 1.0
+    a = abs(q)
+    e = a.numerator.bit_length() - a.denominator.bit_length()
+    if Fraction(2) ** e > a:
+        e -= 1
+    e = max(e, emin)
+    scale = Fraction(2) ** (bits - 1 - e)
+    m = a * scale
+    n = m.numerator // m.denominator
+    rem = m - n
+    if rem > Fraction(1, 2) or (rem == Fraction(1, 2) and n % 2 == 1):
+        n += 1
+    v = Fraction(n) / scale
+    if v >= Fraction(2) ** (emax + 1):
+        return sign * math.inf
+    return sign * float(v)
+
+
+def chain_exact(A, X, bits=53):
+    """D = A*X with each step d = round(a*x + d) evaluated exactly (pure Python, slow).
+
+    d = a1*x1 (rounded), then d = fma(ak, xk, d) for k = 2..K (src/gemm.jl:76-89,154-168).
+    Signed zeros follow IEEE: round(-0) keeps the sign of an exact zero sum as fma does."""
+    A = np.asarray(A, dtype=np.float64)
+    X = np.asarray(X, dtype=np.float64)
+    M, K = A.shape
+    P = X.shape[1]
+    D = np.zeros((M, P), dtype=np.float64, order="F")
+    for j in range(P):
+        for i in range(M):
+            if K == 0:
+                D[i, j] = 0.0
+                continue
+            d = _round_to_float(Fraction(A[i, 0]) * Fraction(X[0, j]), bits)
+            if d == 0.0:
+                d = math.copysign(0.0, A[i, 0]) * math.copysign(1.0, X[0, j])
+            for k in range(1, K):
+                exact = Fraction(A[i, k]) * Fraction(X[k, j]) + Fraction(d)
+                r = _round_to_float(exact, bits)
+                if r == 0.0:
+                    prod_sign = math.copysign(1.0, A[i, k]) * math.copysign(1.0, X[k, j])
+                    if exact == 0 and prod_sign < 0 and math.copysign(1.0, d) < 0:
+                        r = -0.0  # (-0) + (-0) = -0; any other exact zero sum is +0
+                    elif exact == 0:
+                        r = 0.0
+                    else:
+                        r = math.copysign(0.0, float(exact))
+                d = r
+            D[i, j] = d
+    return D
+
+
+# ------------------------------------------------------------------ Ozaki restatement
+
+def ozaki_bits_for(kc):
+    lg = 0
+    while (1 << lg) < kc:
+        lg += 1
+    return min(9, (26 - lg) // 2)
+
+
+def ozaki_plan(K, slices):
+    """Same plan as the GPU planner: bits, K chunks of 64-wide panels, groups of pairs."""
+    kb_total = max(1, (K + 63) // 64)
+    nchunks = max(1, (K + 65535) // 65536)
+    kb_chunk = (kb_total + nchunks - 1) // nchunks
+    nchunks = (kb_total + kb_chunk - 1) // kb_chunk
+    kc = kb_chunk * 64
+    if kc > K:
+        kc = max(1, K)
+    bits = ozaki_bits_for(kc)
+    share = max(1, min(8, int(math.floor(16777216.0 / (kc * 2.0 ** (2 * bits - 2))))))
+    groups = []
+    for level in range(2, slices + 2):
+        cur = None
+        for p in range(1, slices + 1):
+            q = level - p
+            if q < 1 or q > slices:
+                continue
+            if cur is None or len(cur[1]) == share:
+                cur = (level, [])
+                groups.append(cur)
+            cur[1].append((p - 1, q - 1))
+    return {"bits": bits, "kb_chunk": kb_chunk, "kb_total": kb_total, "nchunks": nchunks,
+            "k_chunk": kc, "groups": groups,
+            "products": sum(len(g[1]) for g in groups)}
+
+
+def ozaki_split(X, slices, bits):
+    """Digits (slices, R, K) and exponents (R,) of the rows of X (R x K float64)."""
+    X = np.asarray(X, dtype=np.float64)
+    R, K = X.shape
+    absx = np.abs(X)
+    nonfinite = ~np.isfinite(X).all(axis=1) if K else np.zeros(R, bool)
+    amax = absx.max(axis=1) if K else np.zeros(R)
+    _, ex = np.frexp(np.where(nonfinite, 1.0, amax))
+    e = np.where(amax == 0, 0, ex).astype(np.int64)
+    e = np.where(nonfinite, 2**31 - 1, e)
+    y = np.ldexp(np.where(nonfinite[:, None], 0.0, X), (bits - 1 - np.where(nonfinite, 0, e))[:, None])
+    digits = np.empty((slices, R, K))
+    for p in range(slices):
+        d = np.rint(y)
+        y = (y - d) * 2.0 ** bits
+        digits[p] = d
+    return digits, e
+
+
+def ozaki_gemm(A, B, C=None, alpha=1.0, beta=0.0, slices=8):
+    """The GPU Ozaki result restated in numpy (A: M x K, B: K x N logical operands)."""
+    A = np.asarray(A, dtype=np.float64)
+    B = np.asarray(B, dtype=np.float64)
+    M, K = A.shape
+    N = B.shape[1]
+    plan = ozaki_plan(K, slices)
+    bits = plan["bits"]
+    dA, ea = ozaki_split(A, slices, bits)
+    dB, eb = ozaki_split(B.T, slices, bits)
+    steps = len(plan["groups"]) * plan["nchunks"]
+    T = None
+    kc = plan["kb_chunk"] * 64
+    for level, pairs in plan["groups"]:
+        w = 2.0 ** (2 - level * bits)
+        for c in range(plan["nchunks"]):
+            k0, k1 = c * kc, min(K, (c + 1) * kc)
+            S = np.zeros((M, N))
+            for p, q in pairs:
+                S += dA[p][:, k0:k1] @ dB[q][:, k0:k1].T   # exact: integers below 2^53
+            T = S * w if T is None else T + S * w           # fma(S, w, T) with S*w exact
+    del steps
+    bad = (ea[:, None] == 2**31 - 1) | (eb[None, :] == 2**31 - 1)
+    E = np.where(bad, 0, ea[:, None] + eb[None, :])
+    val = np.ldexp(T, E.astype(np.int64))
+    val = np.where(bad, np.nan, val)
+    if beta == 0.0:
+        out = alpha * val
+    else:
+        out = fma(np.full_like(val, alpha), val, beta * np.asarray(C, dtype=np.float64))
+    return np.asfortranarray(out)

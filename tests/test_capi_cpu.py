@@ -1,0 +1,70 @@
+"""The C-ABI library loads and exports its header's symbols; host-only calls (no GPU work)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+import gbblas
+from gbblas import _lib
+import oracle
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "gbblas.h")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(gb_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_loads():
+    assert os.path.exists(gbblas.LIB_PATH)
+    assert gbblas.lib().gb_version() == 100
+
+
+def test_every_declared_symbol_is_exported():
+    names = declared_functions()
+    assert "gb_gemm_f64" in names and "gb_jmul_f64" in names
+    L = gbblas.lib()
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_every_declared_symbol_has_a_python_signature():
+    assert set(declared_functions()) <= set(_lib.SIGNATURES)
+
+
+def test_status_strings():
+    L = gbblas.lib()
+    for code in range(0, -7, -1):
+        assert L.gb_status_string(code)
+    assert b"unknown" in L.gb_status_string(-99)
+
+
+@pytest.mark.parametrize("K", [1, 63, 64, 256, 1000, 4096, 8192, 16384, 70000])
+@pytest.mark.parametrize("slices", [1, 3, 8, 12])
+def test_ozaki_plan_matches_restatement(K, slices):
+    got = gbblas.ozaki_plan(512, 384, K, slices)
+    ref = oracle.ozaki_plan(K, slices)
+    assert got["bits"] == ref["bits"]
+    assert got["k_chunk"] == ref["k_chunk"]
+    assert got["products"] == ref["products"]
+    assert got["groups"] == len(ref["groups"])
+    assert got["flops_tensor"] == 2.0 * 512 * 384 * ref["kb_total"] * 64 * ref["products"]
+
+
+def test_ozaki_plan_rejects_bad_slices():
+    L = gbblas.lib()
+    p = _lib.OzakiPlan()
+    assert L.gb_plan_ozaki(8, 8, 8, 0, ctypes.byref(p)) == _lib.GB_ERR_INVALID_VALUE
+    assert L.gb_plan_ozaki(8, 8, 8, 21, ctypes.byref(p)) == _lib.GB_ERR_INVALID_VALUE
+    assert L.gb_plan_ozaki(-1, 8, 8, 3, ctypes.byref(p)) == _lib.GB_ERR_INVALID_VALUE
+
+
+def test_setters():
+    L = gbblas.lib()
+    assert L.gb_set_wait_limit_ns(0) == 0
+    assert L.gb_set_ozaki_tolerance(-1.0) == _lib.GB_ERR_INVALID_VALUE
+    assert L.gb_set_ozaki_tolerance(0.0) == 0

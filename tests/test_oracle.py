@@ -1,0 +1,125 @@
+"""CPU checks of the oracle itself: golden fixtures, restatements against each other."""
+import glob
+import os
+from fractions import Fraction
+
+import numpy as np
+import pytest
+
+import oracle
+
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+
+
+def test_golden_fixtures_present():
+    assert len(GOLDEN) >= 10
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
+def test_c_oracle_matches_golden_bit_exact(path):
+    z = np.load(path)
+    A, X, D = z["A"], z["X"], z["D"]
+    got = oracle.jmul(A, X, dtype=D.dtype.type)
+    assert got.dtype == D.dtype
+    np.testing.assert_array_equal(got.view(np.uint64 if D.dtype == np.float64 else np.uint32),
+                                  np.asfortranarray(D).view(np.uint64 if D.dtype == np.float64 else np.uint32))
+
+
+def test_exact_chain_reproduces_a_fixture():
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "f64_13x12x12_uniform.npz"))
+    D = oracle.chain_exact(z["A"], z["X"])
+    np.testing.assert_array_equal(D, z["D"])
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("shape", [(1, 1, 1), (7, 5, 3), (41, 17, 13), (64, 64, 64), (130, 70, 33)])
+@pytest.mark.parametrize("nthreads", [1, 4])
+def test_tiled_baseline_equals_chain(dtype, shape, nthreads):
+    M, K, N = shape
+    g = np.random.default_rng(5)
+    A = np.asfortranarray(g.uniform(-1, 1, (M, K)).astype(dtype))
+    B = np.asfortranarray(g.uniform(-1, 1, (K, N)).astype(dtype))
+    ref = oracle.gemm(A, B, dtype=dtype)
+    got = oracle.jmul_tiled(A, B, nthreads=nthreads, dtype=dtype)
+    np.testing.assert_array_equal(got, ref)
+
+
+def test_chain_entries_equals_full_oracle():
+    g = np.random.default_rng(6)
+    A = np.asfortranarray(g.uniform(-1, 1, (33, 20)))
+    B = np.asfortranarray(g.uniform(-1, 1, (25, 20)))   # stored N x K: op(B) = B^T
+    C = np.asfortranarray(g.uniform(-1, 1, (33, 25)))
+    full = oracle.gemm(A, B, C=C, alpha=1.5, beta=0.5, trans_b=True)
+    rows = g.integers(0, 33, 50)
+    cols = g.integers(0, 25, 50)
+    got = oracle.chain_entries(A, B, rows, cols, C=C, alpha=1.5, beta=0.5, trans_b=True)
+    np.testing.assert_array_equal(got, full[rows, cols])
+
+
+def test_alpha_beta_semantics():
+    A = np.asfortranarray(np.ones((3, 2)))
+    B = np.asfortranarray(np.ones((2, 4)))
+    C = np.asfortranarray(np.full((3, 4), np.nan))
+    out = oracle.gemm(A, B, C=C, alpha=2.0, beta=0.0)   # beta == 0: C is not read
+    assert np.all(out == 4.0)
+    C2 = np.asfortranarray(np.full((3, 4), 3.0))
+    A2 = np.asfortranarray(np.full((3, 2), np.nan))
+    out = oracle.gemm(A2, B, C=C2, alpha=0.0, beta=2.0)  # alpha == 0: A, B are not read
+    assert np.all(out == 6.0)
+    out = oracle.gemm(np.zeros((3, 0), order="F"), np.zeros((0, 4), order="F"), C=C2, alpha=1.0, beta=0.5)
+    assert np.all(out == 1.5)
+
+
+def test_dot2_is_near_exact():
+    g = np.random.default_rng(7)
+    K = 300
+    A = np.asfortranarray(g.standard_normal((4, K)) * np.ldexp(1.0, g.integers(-20, 20, (4, K))))
+    B = np.asfortranarray(g.standard_normal((K, 3)))
+    rows = np.array([0, 1, 2, 3])
+    cols = np.array([0, 1, 2, 0])
+    hi, lo, ab = oracle.dot2_entries(A, B, rows, cols)
+    for s in range(4):
+        exact = sum(Fraction(A[rows[s], k]) * Fraction(B[k, cols[s]]) for k in range(K))
+        err = abs(Fraction(hi[s]) + Fraction(lo[s]) - exact)
+        assert float(err) <= 4 * 2.0 ** -104 * ab[s] + 2.0 ** -1000
+
+
+def test_ozaki_split_reconstructs():
+    g = np.random.default_rng(8)
+    X = g.standard_normal((20, 50)) * np.ldexp(1.0, g.integers(-8, 9, (20, 50)))
+    X[3] = 0.0
+    for bits in (5, 6, 7, 9):
+        for s in (1, 3, 8):
+            d, e = oracle.ozaki_split(X, s, bits)
+            assert np.all(np.abs(d) <= 2 ** (bits - 1))
+            assert np.all(d == np.rint(d))
+            w = 2.0 ** (1 - bits * np.arange(1, s + 1))
+            rec = np.ldexp(np.tensordot(w, d, axes=1), e[:, None])
+            err = np.abs(rec - X)
+            assert np.all(err <= np.ldexp(1.0, e - s * bits)[:, None] * (1 + 1e-12))
+
+
+def test_ozaki_restatement_error_within_truncation():
+    g = np.random.default_rng(9)
+    M, K, N = 12, 200, 9
+    A = g.uniform(-1, 1, (M, K))
+    B = g.uniform(-1, 1, (K, N))
+    exact = oracle.gemm(A, B)
+    prev = None
+    for s in (2, 4, 6, 8):
+        got = oracle.ozaki_gemm(A, B, slices=s)
+        err = np.linalg.norm(got - exact) / (np.linalg.norm(A) * np.linalg.norm(B))
+        if prev is not None:
+            assert err <= prev * 1.01 + 1e-17
+        prev = err
+    assert prev < 1e-15
+
+
+def test_ozaki_plan_grouping_respects_exactness():
+    for K in (1, 64, 1000, 4096, 8192, 16384, 100000):
+        for s in (1, 5, 9, 14):
+            p = oracle.ozaki_plan(K, s)
+            assert p["products"] == sum(1 for a in range(1, s + 1) for b in range(1, s + 1) if a + b <= s + 1)
+            for level, pairs in p["groups"]:
+                assert all(a + b + 2 == level for a, b in pairs)
+                assert len(pairs) * p["k_chunk"] * 2.0 ** (2 * p["bits"] - 2) <= 2.0 ** 24
