@@ -67,6 +67,28 @@ int gb_set_ozaki_tolerance(double tol);
  * (synchronises `stream`). */
 int gb_check_status(void* stream);
 
+/* ------------------------------------------------------------------ tracing */
+/* Kernel kinds counted and timed by the tracing layer. */
+typedef enum {
+  GB_KERNEL_OZAKI_STATS = 0,
+  GB_KERNEL_OZAKI_SPLIT = 1,
+  GB_KERNEL_OZAKI_SLICE_MMA = 2,
+  GB_KERNEL_NATIVE_GEMM = 3,
+  GB_KERNEL_SCALE_C = 4,
+  GB_KERNEL_GROUPED_GEMM = 5,
+  GB_KERNEL_ADJOINT_SPLIT = 6,
+  GB_KERNEL_ADJOINT_MMA = 7,
+  GB_KERNEL_KINDS = 16
+} gb_kernel_kind_t;
+const char* gb_kernel_kind_name(int kind);
+/* Launches of each kernel kind since the library was loaded (counts[0..n)). */
+int gb_launch_counts(long long* counts, int n);
+/* Between start and stop, every launch is bracketed by CUDA events on its stream; stop
+ * synchronises those events and returns the summed milliseconds and launch count of
+ * each kind (ms[0..n), launches[0..n); either may be NULL). */
+int gb_profile_start(void);
+int gb_profile_stop(double* ms, long long* launches, int n);
+
 /* ------------------------------------------------------------------ jmul! proper */
 /* D (M x P) = A (M x N) * X (N x P), contraction over N, leading dimensions M, N, M
  * exactly as an MMatrix (src/gemm.jl:244).  Per element d = a1*x1; d = fma(ak, xk, d)
@@ -112,6 +134,9 @@ typedef struct {
   double  flops_tensor;  /* BF16 tensor flops the plan issues */
 } gb_ozaki_plan_t;
 int gb_plan_ozaki(int64_t M, int64_t N, int64_t K, int slices, gb_ozaki_plan_t* out);
+/* The plan of the most recent OZAKI gb_gemm_f64 call made by the calling thread (zeroes
+ * before the first), e.g. the slice count an automatic call picked. */
+int gb_last_ozaki_plan(gb_ozaki_plan_t* out);
 
 #ifdef __cplusplus
 }

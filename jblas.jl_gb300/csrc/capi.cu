@@ -20,6 +20,7 @@
 #include "ozaki.cuh"
 
 static thread_local char g_last_detail[256];
+static thread_local gb_ozaki_plan_t g_last_plan;
 
 int gb_set_cuda_error(cudaError_t e, const char* what) {
   std::snprintf(g_last_detail, sizeof(g_last_detail), "%s: %s", what, cudaGetErrorString(e));
@@ -156,33 +157,80 @@ static int exp_of(unsigned long long bits) {
   return std::ilogb(a) + 1;
 }
 
-// A-priori normwise truncation bound ||C - C_exact||_F / (||A||_F ||B||_F) for s slices of
-// `bits` bits (see ozaki.cu): representation error of both operands plus the dropped
-// products (p + q > s + 1), plus the FP64 recombination rounding.
-static double ozaki_bound(const HostStats& h, int64_t K, int s, int bits, int steps) {
+// A-priori normwise bound ||C - C_exact||_F / (||A||_F ||B||_F) for a plan (alpha = 1,
+// beta = 0), from the split statistics (row/column exponents e, f; sums of |.|; norms):
+//   truncation  both operands cut after s digits, plus the dropped products p + q > s + 1
+//   recombination  FP64 sum of the exact group results, smallest level first: each drain
+//               rounds once, so a term is charged once per later partial sum
+//   final       the power-of-two rescale is exact, the alpha product rounds once
+// Norm inequalities used: ||diag(x) Y diag(z)||_F <= ||x||_2 ||z||_2 max|Y| style bounds on
+// the integer digit products (|S| <= npairs * kc * 2^(2b-2)).
+// Norms of the split statistics, gathered once per call.  All exponent sums are taken
+// relative to 2^(emax_a + emax_b) so that extreme magnitudes neither overflow nor vanish.
+struct BoundStats {
+  bool nonfinite = false;
+  double na = 0, nb = 0, EA = 0, EB = 0, SA = 0, SB = 0;  // scaled by 2^-ref_a, 2^-ref_b
+};
+
+static BoundStats bound_stats(const HostStats& h) {
+  BoundStats r;
+  int ref_a = -1100, ref_b = -1100;
+  for (auto bits : h.amax_a) {
+    const int e = exp_of(bits);
+    if (e == INT32_MAX) r.nonfinite = true; else if (bits && e > ref_a) ref_a = e;
+  }
+  for (auto bits : h.amax_b) {
+    const int e = exp_of(bits);
+    if (e == INT32_MAX) r.nonfinite = true; else if (bits && e > ref_b) ref_b = e;
+  }
+  if (r.nonfinite) return r;
   double e2a = 0, e2b = 0, na2 = 0, nb2 = 0, sa2 = 0, sb2 = 0;
   for (size_t i = 0; i < h.amax_a.size(); ++i) {
-    const int e = exp_of(h.amax_a[i]);
-    if (e == INT32_MAX) return INFINITY;
-    e2a += std::ldexp(1.0, 2 * e);
-    na2 += h.ssq_a[i];
-    sa2 += h.sabs_a[i] * h.sabs_a[i];
+    if (!h.amax_a[i]) continue;
+    e2a += std::ldexp(1.0, 2 * (exp_of(h.amax_a[i]) - ref_a));
+    const double sa = std::ldexp(h.sabs_a[i], -ref_a);
+    sa2 += sa * sa;
+    na2 += std::ldexp(h.ssq_a[i], -2 * ref_a);
   }
   for (size_t j = 0; j < h.amax_b.size(); ++j) {
-    const int e = exp_of(h.amax_b[j]);
-    if (e == INT32_MAX) return INFINITY;
-    e2b += std::ldexp(1.0, 2 * e);
-    nb2 += h.ssq_b[j];
-    sb2 += h.sabs_b[j] * h.sabs_b[j];
+    if (!h.amax_b[j]) continue;
+    e2b += std::ldexp(1.0, 2 * (exp_of(h.amax_b[j]) - ref_b));
+    const double sb = std::ldexp(h.sabs_b[j], -ref_b);
+    sb2 += sb * sb;
+    nb2 += std::ldexp(h.ssq_b[j], -2 * ref_b);
   }
-  const double na = std::sqrt(na2), nb = std::sqrt(nb2);
+  r.na = std::sqrt(na2); r.nb = std::sqrt(nb2);
+  r.EA = std::sqrt(e2a); r.EB = std::sqrt(e2b);
+  r.SA = std::sqrt(sa2); r.SB = std::sqrt(sb2);
+  return r;
+}
+
+static double ozaki_bound(const BoundStats& st, int64_t K, const OzPlan& plan) {
+  if (st.nonfinite) return INFINITY;
+  const double na = st.na, nb = st.nb;
   if (na == 0.0 || nb == 0.0) return 0.0;
-  const double u2 = std::ldexp(1.0, -s * bits);
-  const double ea = std::sqrt(e2a), eb = std::sqrt(e2b);
-  const double cs = (s - 1) / (1.0 - std::ldexp(1.0, -bits));
-  const double trunc = u2 * (ea * std::sqrt(sb2) + eb * (std::sqrt(sa2) + K * u2 * ea) +
-                             static_cast<double>(K) * cs * ea * eb);
-  return trunc / (na * nb) + (steps + 2) * std::ldexp(1.0, -53);
+  const double EA = st.EA, EB = st.EB, SA = st.SA, SB = st.SB;
+  const int s = plan.slices, b = plan.bits;
+  const double Kd = static_cast<double>(K);
+  const double u = std::ldexp(1.0, -53);
+  const double us = std::ldexp(1.0, -s * b);
+  const double cs = (s - 1) / (1.0 - std::ldexp(1.0, -b));
+  const double trunc = us * (EA * SB + EB * (SA + Kd * us * EA)) + Kd * us * cs * EA * EB;
+  // leading (level-2) group: |digit_1 * w_1| <= |x| + 2^-b
+  const double top = na * nb + std::ldexp(1.0, -b) * (EA * SB + EB * SA) + Kd * std::ldexp(1.0, -2 * b) * EA * EB;
+  const int G = plan.sched.ngroups, nch = plan.nchunks;
+  const double Kp = static_cast<double>(plan.k_chunk) * nch;
+  const double D = static_cast<double>(G) * nch;
+  double lower = 0.0;
+  for (int g = 0; g < G; ++g) {
+    const int level = plan.sched.level[g];
+    if (level == 2) continue;
+    const double coef = D - static_cast<double>(g) * nch;
+    lower += coef * plan.sched.npairs[g] * Kp * std::ldexp(1.0, -(level - 2) * b);
+  }
+  const double recomb = u * (nch * top + lower * EA * EB);
+  const double fin = u * top;
+  return 1.01 * (trunc + recomb + fin) / (na * nb);
 }
 
 static inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
@@ -234,13 +282,14 @@ static int ozaki_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int
       cudaFreeAsync(st_ws, s);
       return gb_set_cuda_error(e, "ozaki statistics");
     }
+    const BoundStats bst = bound_stats(h);
     if (slices == 0) {
       const double tol = ozaki_tolerance();
       s_use = OZ_MAX_SLICES;
       for (int cand = 1; cand <= OZ_MAX_SLICES; ++cand) {
         OzPlan p;
         if (oz_make_plan(M, N, K, cand, &p)) break;
-        if (ozaki_bound(h, K, cand, p.bits, p.groups * p.nchunks) <= tol) {
+        if (ozaki_bound(bst, K, p) <= tol) {
           s_use = cand;
           break;
         }
@@ -251,7 +300,7 @@ static int ozaki_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int
       cudaFreeAsync(st_ws, s);
       return rc;
     }
-    if (err_bound_out) *err_bound_out = ozaki_bound(h, K, s_use, plan.bits, plan.groups * plan.nchunks);
+    if (err_bound_out) *err_bound_out = ozaki_bound(bst, K, plan);
   } else {
     rc = oz_make_plan(M, N, K, s_use, &plan);
     if (rc) {
@@ -260,6 +309,12 @@ static int ozaki_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int
     }
   }
 
+  g_last_plan.slices = plan.slices;
+  g_last_plan.bits = plan.bits;
+  g_last_plan.k_chunk = static_cast<int32_t>(plan.k_chunk);
+  g_last_plan.products = plan.products;
+  g_last_plan.groups = plan.groups;
+  g_last_plan.flops_tensor = plan.flops_tensor;
   const int grid = oz_grid_for(dev->sms, M, N);
   const size_t pa_bytes = align256(static_cast<size_t>(s_use) * M * pitch * 2);
   const size_t pb_bytes = align256(static_cast<size_t>(s_use) * N * pitch * 2);
@@ -410,6 +465,12 @@ int gb_jmul_f64(double* D, const double* A, const double* X, int64_t M, int64_t 
 int gb_jmul_f32(float* D, const float* A, const float* X, int64_t M, int64_t N, int64_t P, void* stream) {
   return gb_gemm_f32(0, 0, M, P, N, 1.0f, A, M > 1 ? M : 1, X, N > 1 ? N : 1, 0.0f, D, M > 1 ? M : 1,
                      stream);
+}
+
+int gb_last_ozaki_plan(gb_ozaki_plan_t* out) {
+  if (!out) return GB_ERR_INVALID_VALUE;
+  *out = g_last_plan;
+  return GB_OK;
 }
 
 int gb_plan_ozaki(int64_t M, int64_t N, int64_t K, int slices, gb_ozaki_plan_t* out) {

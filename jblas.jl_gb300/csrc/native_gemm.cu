@@ -13,6 +13,7 @@
 // padding, which would turn -0 into +0 and Inf*0 into NaN).
 #include "gb_common.cuh"
 #include "native_gemm.cuh"
+#include "profile.cuh"
 
 namespace gb {
 
@@ -170,7 +171,8 @@ static int launch_scale(int64_t M, int64_t N, T beta, T* C, int64_t ldc, cudaStr
   int64_t blocks = (total + 255) / 256;
   if (blocks > 152 * 16) blocks = 152 * 16;
   if (blocks < 1) blocks = 1;
-  scale_c_kernel<T><<<static_cast<unsigned>(blocks), 256, 0, s>>>(M, N, beta, C, ldc);
+  GB_LAUNCH(GB_KERNEL_SCALE_C, s,
+            scale_c_kernel<T><<<static_cast<unsigned>(blocks), 256, 0, s>>>(M, N, beta, C, ldc));
   GB_CUDA_TRY(cudaGetLastError());
   return GB_OK;
 }
@@ -183,9 +185,10 @@ static int launch_simt(int ta, int tb, int64_t M, int64_t N, int64_t K, T alpha,
   if (gx > 0x7FFFFFFF || gy > 65535) return GB_ERR_UNSUPPORTED;
   dim3 grid(static_cast<unsigned>(gx), static_cast<unsigned>(gy));
   constexpr int NT = (BM / TM) * (BN / TN);
-#define GB_SIMT_CASE(TA_, TB_)                                                      \
-  simt_gemm_kernel<T, BM, BN, BK, TM, TN, TA_, TB_><<<grid, NT, 0, s>>>(M, N, K, alpha, A, \
-                                                                       lda, B, ldb, beta, C, ldc)
+#define GB_SIMT_CASE(TA_, TB_)                                                                   \
+  GB_LAUNCH(GB_KERNEL_NATIVE_GEMM, s,                                                            \
+            (simt_gemm_kernel<T, BM, BN, BK, TM, TN, TA_, TB_><<<grid, NT, 0, s>>>(M, N, K, alpha, A, \
+                                                                                  lda, B, ldb, beta, C, ldc)))
   if (!ta && !tb) GB_SIMT_CASE(false, false);
   else if (!ta && tb) GB_SIMT_CASE(false, true);
   else if (ta && !tb) GB_SIMT_CASE(true, false);

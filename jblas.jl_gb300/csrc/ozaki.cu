@@ -32,6 +32,7 @@
 
 #include "gb_common.cuh"
 #include "ozaki.cuh"
+#include "profile.cuh"
 
 namespace gb {
 
@@ -71,8 +72,11 @@ int oz_make_plan(int64_t M, int64_t N, int64_t K, int slices, OzPlan* plan) {
   S.kb_total = static_cast<int32_t>(kb_total);
   S.kb_chunk = static_cast<int32_t>(kb_chunk);
   S.bits = P.bits;
+  // Levels from the smallest contribution (slices + 1) up to the leading one (2): the FP64
+  // recombination then adds small terms first, so its rounding error stays near one ulp of
+  // the result instead of growing with the number of groups.
   int g = 0, np = 0;
-  for (int level = 2; level <= slices + 1; ++level) {
+  for (int level = slices + 1; level >= 2; --level) {
     // pairs (p, q), p + q = level, 1 <= p, q <= slices, in increasing p
     int in_group = 0;
     for (int p = 1; p <= slices; ++p) {
@@ -176,10 +180,12 @@ int oz_row_stats(const double* X, int64_t R, int64_t K, int64_t rs, int64_t ks, 
   if (R <= 0) return GB_OK;
   if (ks == 1) {
     const int64_t blocks = (R + 7) / 8;
-    stats_kc_kernel<<<static_cast<unsigned>(blocks), 256, 0, s>>>(X, R, K, rs, st);
+    GB_LAUNCH(GB_KERNEL_OZAKI_STATS, s,
+              stats_kc_kernel<<<static_cast<unsigned>(blocks), 256, 0, s>>>(X, R, K, rs, st));
   } else {
     const int64_t blocks = (R + 31) / 32;
-    stats_rc_kernel<<<static_cast<unsigned>(blocks), 256, 0, s>>>(X, R, K, ks, st);
+    GB_LAUNCH(GB_KERNEL_OZAKI_STATS, s,
+              stats_rc_kernel<<<static_cast<unsigned>(blocks), 256, 0, s>>>(X, R, K, ks, st));
   }
   GB_CUDA_TRY(cudaGetLastError());
   return GB_OK;
@@ -279,13 +285,15 @@ int oz_split(const double* X, int64_t R, int64_t K, int64_t rs, int64_t ks,
   if (R <= 0) return GB_OK;
   if (ks == 1) {
     const int64_t blocks = (R + 7) / 8;
-    split_kc_kernel<<<static_cast<unsigned>(blocks), 256, 0, s>>>(X, R, K, rs, amax_bits, slices,
-                                                                   bits, planes, pitch, exps);
+    GB_LAUNCH(GB_KERNEL_OZAKI_SPLIT, s,
+              split_kc_kernel<<<static_cast<unsigned>(blocks), 256, 0, s>>>(X, R, K, rs, amax_bits, slices,
+                                                                             bits, planes, pitch, exps));
   } else {
     const int64_t gk = (K + 63) / 64;
     if (gk > 65535) return GB_ERR_UNSUPPORTED;
     dim3 grid(static_cast<unsigned>((R + 31) / 32), static_cast<unsigned>(gk < 1 ? 1 : gk));
-    split_rc_kernel<<<grid, 256, 0, s>>>(X, R, K, ks, amax_bits, slices, bits, planes, pitch, exps);
+    GB_LAUNCH(GB_KERNEL_OZAKI_SPLIT, s,
+              split_rc_kernel<<<grid, 256, 0, s>>>(X, R, K, ks, amax_bits, slices, bits, planes, pitch, exps));
   }
   GB_CUDA_TRY(cudaGetLastError());
   return GB_OK;
@@ -581,7 +589,8 @@ int oz_gemm_launch(const OzGemmArgs& a, const OzPlan& plan, cudaStream_t s) {
                                      OZ_SMEM_BYTES));
     attr_set = true;
   }
-  oz_gemm_kernel<<<a.grid, OZ_THREADS, OZ_SMEM_BYTES, s>>>(ta, tb, plan.sched, prm);
+  GB_LAUNCH(GB_KERNEL_OZAKI_SLICE_MMA, s,
+            oz_gemm_kernel<<<a.grid, OZ_THREADS, OZ_SMEM_BYTES, s>>>(ta, tb, plan.sched, prm));
   GB_CUDA_TRY(cudaGetLastError());
   return GB_OK;
 }

@@ -48,7 +48,14 @@ SIGNATURES = {
     "gb_gemm_f32": (c_int, [c_int, c_int, c_i64, c_i64, c_i64, c_float, c_vp, c_i64, c_vp, c_i64,
                             c_float, c_vp, c_i64, c_vp]),
     "gb_plan_ozaki": (c_int, [c_i64, c_i64, c_i64, c_int, ctypes.POINTER(OzakiPlan)]),
+    "gb_last_ozaki_plan": (c_int, [ctypes.POINTER(OzakiPlan)]),
+    "gb_kernel_kind_name": (ctypes.c_char_p, [c_int]),
+    "gb_launch_counts": (c_int, [ctypes.POINTER(ctypes.c_longlong), c_int]),
+    "gb_profile_start": (c_int, []),
+    "gb_profile_stop": (c_int, [ctypes.POINTER(c_double), ctypes.POINTER(ctypes.c_longlong), c_int]),
 }
+
+KERNEL_KINDS = 16
 
 _lib = None
 

@@ -131,6 +131,14 @@ def ozaki_plan(M, N, K, slices):
             "groups": p.groups, "flops_tensor": p.flops_tensor}
 
 
+def last_ozaki_plan():
+    """Plan of this thread's most recent Ozaki call (the slice count an automatic call chose)."""
+    p = _lib.OzakiPlan()
+    check(_lib.lib().gb_last_ozaki_plan(ctypes.byref(p)), "gb_last_ozaki_plan")
+    return {"slices": p.slices, "bits": p.bits, "k_chunk": p.k_chunk, "products": p.products,
+            "groups": p.groups, "flops_tensor": p.flops_tensor}
+
+
 def set_ozaki_tolerance(tol):
     check(_lib.lib().gb_set_ozaki_tolerance(float(tol)), "gb_set_ozaki_tolerance")
 
@@ -143,3 +151,37 @@ def check_device_status(stream=None):
     """Raises GBError if a kernel recorded a pipeline timeout since the last check."""
     s = ctypes.c_void_p(stream if stream is not None else torch.cuda.current_stream().cuda_stream)
     check(_lib.lib().gb_check_status(s), "gb_check_status")
+
+
+def launch_counts():
+    """{kernel kind name: launches since load} from the library's always-on counters."""
+    L = _lib.lib()
+    arr = (ctypes.c_longlong * _lib.KERNEL_KINDS)()
+    check(L.gb_launch_counts(arr, _lib.KERNEL_KINDS), "gb_launch_counts")
+    return {L.gb_kernel_kind_name(i).decode(): arr[i] for i in range(_lib.KERNEL_KINDS) if arr[i]}
+
+
+class profile:
+    """Context manager: CUDA-event times of every library kernel launched inside it.
+
+    with gbblas.profile() as p: ...
+    p.ms[name], p.launches[name]   summed device milliseconds and launch counts per kind
+    """
+
+    def __enter__(self):
+        check(_lib.lib().gb_profile_start(), "gb_profile_start")
+        self.ms, self.launches = {}, {}
+        return self
+
+    def __exit__(self, *exc):
+        L = _lib.lib()
+        n = _lib.KERNEL_KINDS
+        ms = (ctypes.c_double * n)()
+        ln = (ctypes.c_longlong * n)()
+        check(L.gb_profile_stop(ms, ln, n), "gb_profile_stop")
+        for i in range(n):
+            if ln[i]:
+                name = L.gb_kernel_kind_name(i).decode()
+                self.ms[name] = ms[i]
+                self.launches[name] = ln[i]
+        return False

@@ -244,7 +244,7 @@ def ozaki_plan(K, slices):
     bits = ozaki_bits_for(kc)
     share = max(1, min(8, int(math.floor(16777216.0 / (kc * 2.0 ** (2 * bits - 2))))))
     groups = []
-    for level in range(2, slices + 2):
+    for level in range(slices + 1, 1, -1):   # smallest contributions first
         cur = None
         for p in range(1, slices + 1):
             q = level - p

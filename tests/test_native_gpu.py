@@ -115,7 +115,7 @@ def test_nan_inf_propagation_matches_oracle(cuda):
     A[10, 2] = np.nan
     B[4, 9] = -np.inf
     ref = oracle.jmul(A, B)
-    D = torch.empty((40, 20), dtype=torch.float64, device=cuda).t()
+    D = torch.empty((20, 40), dtype=torch.float64, device=cuda).t()
     gbblas.jmul_(D, to_dev(A), to_dev(B))
     torch.cuda.synchronize()
     assert_bit_equal(to_host(D), ref)
