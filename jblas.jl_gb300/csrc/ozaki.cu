@@ -62,6 +62,8 @@ int oz_make_plan(int64_t M, int64_t N, int64_t K, int slices, OzPlan* plan) {
   P.k_chunk = kc;
   P.nchunks = static_cast<int>(nchunks);
   P.bits = oz_bits_for(kc);
+  // the split builds x * 2^(slices*bits - 1 - e) in at most 128-bit integers
+  if (slices * P.bits > 126) return GB_ERR_UNSUPPORTED;
   // pairs that can share one exact FP32 sum
   const double per_pair = static_cast<double>(kc) * std::ldexp(1.0, 2 * P.bits - 2);
   int share = static_cast<int>(std::floor(16777216.0 / per_pair));
@@ -201,99 +203,165 @@ __device__ __forceinline__ int row_exponent(unsigned long long amax_bits) {
   return ilogb(__longlong_as_double(static_cast<long long>(amax_bits))) + 1;  // amax < 2^e
 }
 
-// k contiguous: one warp per row, lanes over k.
-__global__ void split_kc_kernel(const double* __restrict__ X, int64_t R, int64_t K, int64_t rs,
-                                const unsigned long long* __restrict__ amax_bits, int slices, int bits,
-                                __nv_bfloat16* __restrict__ planes, int64_t pitch,
-                                int32_t* __restrict__ exps) {
-  const int lane = threadIdx.x & 31;
-  const int64_t r = static_cast<int64_t>(blockIdx.x) * (blockDim.x / 32) + (threadIdx.x >> 5);
-  if (r >= R) return;
-  const int e = row_exponent(amax_bits[r]);
-  if (lane == 0) exps[r] = e;
-  const bool nonfinite = (e == OZ_EXP_NONFINITE);
-  const double step = pow2_normal(bits);
-  const double* row = X + r * rs;
-  const int64_t plane_stride = R * pitch;
-  __nv_bfloat16* out = planes + r * pitch;
-  for (int64_t k = lane; k < K; k += 32) {
-    double y = nonfinite ? 0.0 : scale_pow2(row[k], bits - 1 - e);
-    for (int p = 0; p < slices; ++p) {
-      const double d = rint(y);
-      y = (y - d) * step;
-      out[p * plane_stride + k] = __float2bfloat16_rn(static_cast<float>(d));
+// Digit extraction in integer arithmetic (GB300's FP64 pipe is ~1/64 of FP32, so the
+// split never touches it).  For a row with exponent e (amax < 2^e) and SB = slices*bits:
+//   Y = round-half-away(x * 2^(SB-1-e))          an integer, |Y| <= 2^(SB-1)
+//   digits d_s..d_2 = balanced base-2^b digits of Y, in [-2^(b-1), 2^(b-1));  d_1 the rest
+//   so x * 2^-e = sum_p d_p 2^(1 - p*b) + delta,  |delta| <= 2^-SB,  |d_1| <= 2^(b-1).
+// Y is built from the IEEE fields of x (m * 2^(ex-52)) with shifts only.  Word = uint64_t
+// for SB <= 62, unsigned __int128 beyond.
+template <typename Word>
+__device__ __forceinline__ Word fixed_point(double x, int e, int SB) {
+  const unsigned long long bits = static_cast<unsigned long long>(__double_as_longlong(x));
+  const int biased = static_cast<int>((bits >> 52) & 0x7FF);
+  unsigned long long m = bits & 0x000FFFFFFFFFFFFFull;
+  int ex = -1022;
+  if (biased) {
+    m |= 0x0010000000000000ull;
+    ex = biased - 1023;
+  }
+  Word mag = 0;
+  if (m) {
+    const int sh = ex - 53 + SB - e;   // v = m * 2^sh
+    if (sh >= 0) {
+      mag = static_cast<Word>(m) << sh;
+    } else {
+      const int t = -sh;
+      if (t < 64) mag = static_cast<Word>((m + (1ull << (t - 1))) >> t);
+    }
+  }
+  return (bits >> 63) ? static_cast<Word>(0) - mag : mag;
+}
+
+// Signed arithmetic shift of a two's-complement word.
+template <typename Word>
+__device__ __forceinline__ Word sar(Word y, int b);
+template <>
+__device__ __forceinline__ uint64_t sar<uint64_t>(uint64_t y, int b) {
+  return static_cast<uint64_t>(static_cast<int64_t>(y) >> b);
+}
+template <>
+__device__ __forceinline__ unsigned __int128 sar<unsigned __int128>(unsigned __int128 y, int b) {
+  return static_cast<unsigned __int128>(static_cast<__int128>(y) >> b);
+}
+
+// Exact BF16 of a small integer |d| <= 2^22 without a conversion instruction:
+// float(d) = bits(1.5*2^23 + d) - 1.5*2^23, then the upper half of the float is the BF16.
+__device__ __forceinline__ uint32_t bf16_bits_of_int(int d) {
+  const float f = __int_as_float(0x4B400000 + d) - 12582912.0f;
+  return __float_as_uint(f) >> 16;
+}
+
+// 16 consecutive k of one row -> `slices` planes of 16 BF16 digits (two 16-byte stores each).
+template <typename Word>
+__device__ __forceinline__ void split_16(const double (&x)[16], int e, int slices, int bits,
+                                         __nv_bfloat16* out0, int64_t plane_stride, int nvalid) {
+  const int SB = slices * bits;
+  const int H = 1 << (bits - 1);
+  const Word MASK = (static_cast<Word>(1) << bits) - 1;
+  Word y[16];
+  const bool nonfinite = (e == 0x7FFFFFFF);
+#pragma unroll
+  for (int j = 0; j < 16; ++j) y[j] = nonfinite ? static_cast<Word>(0) : fixed_point<Word>(x[j], e, SB);
+  // least significant digit first
+  for (int p = slices - 1; p >= 0; --p) {
+    uint32_t packed[8];
+#pragma unroll
+    for (int j = 0; j < 16; j += 2) {
+      int d0, d1;
+      if (p > 0) {
+        d0 = static_cast<int>(static_cast<int64_t>((y[j] + H) & MASK)) - H;
+        d1 = static_cast<int>(static_cast<int64_t>((y[j + 1] + H) & MASK)) - H;
+        y[j] = sar<Word>(y[j] - static_cast<Word>(static_cast<int64_t>(d0)), bits);
+        y[j + 1] = sar<Word>(y[j + 1] - static_cast<Word>(static_cast<int64_t>(d1)), bits);
+      } else {
+        d0 = static_cast<int>(static_cast<int64_t>(y[j]));
+        d1 = static_cast<int>(static_cast<int64_t>(y[j + 1]));
+      }
+      packed[j / 2] = bf16_bits_of_int(d0) | (bf16_bits_of_int(d1) << 16);
+    }
+    __nv_bfloat16* dst = out0 + p * plane_stride;
+    if (nvalid == 16) {
+      uint4* d4 = reinterpret_cast<uint4*>(dst);
+      d4[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+      d4[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+    } else {
+      unsigned short* d2 = reinterpret_cast<unsigned short*>(dst);
+      for (int j = 0; j < nvalid; ++j) d2[j] = static_cast<unsigned short>(packed[j / 2] >> (16 * (j & 1)));
     }
   }
 }
 
-// rows contiguous: 32 rows x 64 k per block, transposed through shared memory so that
-// the K-major planes are written in 128-byte rows.
-__global__ void split_rc_kernel(const double* __restrict__ X, int64_t R, int64_t K, int64_t ks,
-                                const unsigned long long* __restrict__ amax_bits, int slices, int bits,
-                                __nv_bfloat16* __restrict__ planes, int64_t pitch,
-                                int32_t* __restrict__ exps) {
-  __shared__ __nv_bfloat16 tile[32][64 + 8];
-  const int tr = threadIdx.x & 31, tk = threadIdx.x >> 5;  // tk in [0, 8)
-  const int64_t r0 = static_cast<int64_t>(blockIdx.x) * 32;
-  const int64_t k0 = static_cast<int64_t>(blockIdx.y) * 64;
-  const int64_t r = r0 + tr;
-  int e = 0;
-  if (r < R) e = row_exponent(amax_bits[r]);
-  if (blockIdx.y == 0 && tk == 0 && r < R) exps[r] = e;
-  const bool nonfinite = (e == OZ_EXP_NONFINITE);
-  const double step = pow2_normal(bits);
-  double y[8];
-#pragma unroll
-  for (int j = 0; j < 8; ++j) {
-    const int64_t k = k0 + tk + 8 * j;
-    y[j] = (r < R && k < K && !nonfinite) ? scale_pow2(X[r + k * ks], bits - 1 - e) : 0.0;
+// One thread = one row r and 16 consecutive k.  RC (rows contiguous, rs == 1): threads of a
+// block run along r, so every load instruction reads consecutive rows; otherwise (k
+// contiguous) threads run along k.  Stores are 32 contiguous bytes per plane per thread.
+template <bool RC, typename Word>
+__global__ void __launch_bounds__(256) split_kernel(const double* __restrict__ X, int64_t R, int64_t K,
+                                                    int64_t rs, int64_t ks,
+                                                    const unsigned long long* __restrict__ amax_bits,
+                                                    int slices, int bits, __nv_bfloat16* __restrict__ planes,
+                                                    int64_t pitch, int32_t* __restrict__ exps) {
+  int64_t r, kc;
+  if (RC) {
+    r = static_cast<int64_t>(blockIdx.x) * 256 + threadIdx.x;
+    kc = blockIdx.y;
+  } else {
+    kc = static_cast<int64_t>(blockIdx.x) * 256 + threadIdx.x;
+    r = blockIdx.y;
   }
+  const int64_t k0 = kc * 16;
+  if (r >= R || k0 >= K) return;
+  const int e = row_exponent(amax_bits[r]);
+  if (k0 == 0) exps[r] = e;
+  const int nvalid = static_cast<int>(K - k0 < 16 ? K - k0 : 16);
+  double x[16];
+  const double* src = X + r * rs + k0 * ks;
+#pragma unroll
+  for (int j = 0; j < 16; ++j) x[j] = (j < nvalid) ? src[j * ks] : 0.0;
+  __nv_bfloat16* out0 = planes + r * pitch + k0;
   const int64_t plane_stride = R * pitch;
-  for (int p = 0; p < slices; ++p) {
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      const double d = rint(y[j]);
-      y[j] = (y[j] - d) * step;
-      tile[tr][tk + 8 * j] = __float2bfloat16_rn(static_cast<float>(d));
-    }
-    __syncthreads();
-    // 32 rows x 32 bf16 pairs: thread t writes pair (t % 32) of rows t/32, t/32 + 8, ...
-#pragma unroll
-    for (int rr = 0; rr < 4; ++rr) {
-      const int row_l = tk + 8 * rr;
-      const int64_t rg = r0 + row_l;
-      const int64_t kg = k0 + 2 * tr;
-      if (rg < R && kg < K) {
-        __nv_bfloat16* dst = planes + p * plane_stride + rg * pitch + kg;
-        if (kg + 1 < K) {
-          __nv_bfloat162 v;
-          v.x = tile[row_l][2 * tr];
-          v.y = tile[row_l][2 * tr + 1];
-          *reinterpret_cast<__nv_bfloat162*>(dst) = v;
-        } else {
-          dst[0] = tile[row_l][2 * tr];
-        }
-      }
-    }
-    __syncthreads();
-  }
+  split_16<Word>(x, e, slices, bits, out0, plane_stride, nvalid);
 }
 
 int oz_split(const double* X, int64_t R, int64_t K, int64_t rs, int64_t ks,
              const unsigned long long* amax_bits, int slices, int bits, __nv_bfloat16* planes,
              int64_t pitch, int32_t* exps, cudaStream_t s) {
-  if (R <= 0) return GB_OK;
-  if (ks == 1) {
-    const int64_t blocks = (R + 7) / 8;
-    GB_LAUNCH(GB_KERNEL_OZAKI_SPLIT, s,
-              split_kc_kernel<<<static_cast<unsigned>(blocks), 256, 0, s>>>(X, R, K, rs, amax_bits, slices,
-                                                                             bits, planes, pitch, exps));
+  if (R <= 0 || K <= 0) return GB_OK;
+  const int64_t kchunks = (K + 15) / 16;
+  const bool wide = slices * bits > 62;
+  if (rs == 1 && R > 1) {
+    const int64_t gx = (R + 255) / 256;
+    if (kchunks > 65535) return GB_ERR_UNSUPPORTED;
+    dim3 grid(static_cast<unsigned>(gx), static_cast<unsigned>(kchunks));
+    if (wide)
+      GB_LAUNCH(GB_KERNEL_OZAKI_SPLIT, s,
+                (split_kernel<true, unsigned __int128><<<grid, 256, 0, s>>>(X, R, K, rs, ks, amax_bits, slices,
+                                                                             bits, planes, pitch, exps)));
+    else
+      GB_LAUNCH(GB_KERNEL_OZAKI_SPLIT, s,
+                (split_kernel<true, uint64_t><<<grid, 256, 0, s>>>(X, R, K, rs, ks, amax_bits, slices, bits,
+                                                                    planes, pitch, exps)));
   } else {
-    const int64_t gk = (K + 63) / 64;
-    if (gk > 65535) return GB_ERR_UNSUPPORTED;
-    dim3 grid(static_cast<unsigned>((R + 31) / 32), static_cast<unsigned>(gk < 1 ? 1 : gk));
-    GB_LAUNCH(GB_KERNEL_OZAKI_SPLIT, s,
-              split_rc_kernel<<<grid, 256, 0, s>>>(X, R, K, ks, amax_bits, slices, bits, planes, pitch, exps));
+    const int64_t gx = (kchunks + 255) / 256;
+    if (R > 65535) {
+      // rows beyond the grid's y range: launch in row bands
+      for (int64_t r0 = 0; r0 < R; r0 += 65535) {
+        const int64_t rb = (R - r0 < 65535) ? R - r0 : 65535;
+        int rc = oz_split(X + r0 * rs, rb, K, rs, ks, amax_bits + r0, slices, bits, planes + r0 * pitch,
+                          pitch, exps + r0, s);
+        if (rc) return rc;
+      }
+      return GB_OK;
+    }
+    dim3 grid(static_cast<unsigned>(gx), static_cast<unsigned>(R));
+    if (wide)
+      GB_LAUNCH(GB_KERNEL_OZAKI_SPLIT, s,
+                (split_kernel<false, unsigned __int128><<<grid, 256, 0, s>>>(X, R, K, rs, ks, amax_bits, slices,
+                                                                              bits, planes, pitch, exps)));
+    else
+      GB_LAUNCH(GB_KERNEL_OZAKI_SPLIT, s,
+                (split_kernel<false, uint64_t><<<grid, 256, 0, s>>>(X, R, K, rs, ks, amax_bits, slices, bits,
+                                                                     planes, pitch, exps)));
   }
   GB_CUDA_TRY(cudaGetLastError());
   return GB_OK;

@@ -260,21 +260,41 @@ def ozaki_plan(K, slices):
 
 
 def ozaki_split(X, slices, bits):
-    """Digits (slices, R, K) and exponents (R,) of the rows of X (R x K float64)."""
+    """Digits (slices, R, K) and exponents (R,) of the rows of X (R x K float64).
+
+    Row exponent e: max|x| < 2^e.  Y = round-half-away(x * 2^(s*b - 1 - e)) is an integer;
+    the digits are its balanced base-2^b expansion from the least significant end
+    (d_s..d_2 in [-2^(b-1), 2^(b-1)), d_1 the remaining top part), so that
+    x * 2^-e = sum_p d_p 2^(1 - p*b) + delta with |delta| <= 2^-(s*b)."""
     X = np.asarray(X, dtype=np.float64)
     R, K = X.shape
-    absx = np.abs(X)
     nonfinite = ~np.isfinite(X).all(axis=1) if K else np.zeros(R, bool)
-    amax = absx.max(axis=1) if K else np.zeros(R)
+    amax = np.abs(X).max(axis=1) if K else np.zeros(R)
     _, ex = np.frexp(np.where(nonfinite, 1.0, amax))
     e = np.where(amax == 0, 0, ex).astype(np.int64)
+    e_safe = np.where(nonfinite, 0, e)
     e = np.where(nonfinite, 2**31 - 1, e)
-    y = np.ldexp(np.where(nonfinite[:, None], 0.0, X), (bits - 1 - np.where(nonfinite, 0, e))[:, None])
+    SB = slices * bits
+    H, MASK = 1 << (bits - 1), (1 << bits) - 1
+    v = np.ldexp(np.where(nonfinite[:, None], 0.0, X), (SB - 1 - e_safe)[:, None].astype(np.int32))
+    mag = np.abs(v)
+    fl = np.floor(mag)
+    ymag = fl + (mag - fl >= 0.5)
     digits = np.empty((slices, R, K))
-    for p in range(slices):
-        d = np.rint(y)
-        y = (y - d) * 2.0 ** bits
-        digits[p] = d
+    if SB <= 62:
+        Y = (np.sign(v) * ymag).astype(np.int64)
+        for p in range(slices - 1, 0, -1):
+            d = ((Y + H) & MASK) - H
+            Y = (Y - d) >> bits
+            digits[p] = d
+        digits[0] = Y
+    else:
+        Y = np.array([[int(a) for a in row] for row in (np.sign(v) * ymag)], dtype=object).reshape(R, K)
+        for p in range(slices - 1, 0, -1):
+            d = ((Y + H) & MASK) - H
+            Y = (Y - d) >> bits
+            digits[p] = d.astype(np.float64)
+        digits[0] = Y.astype(np.float64)
     return digits, e
 
 

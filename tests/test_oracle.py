@@ -89,9 +89,10 @@ def test_ozaki_split_reconstructs():
     X = g.standard_normal((20, 50)) * np.ldexp(1.0, g.integers(-8, 9, (20, 50)))
     X[3] = 0.0
     for bits in (5, 6, 7, 9):
-        for s in (1, 3, 8):
+        for s in (1, 3, 8, 12):
             d, e = oracle.ozaki_split(X, s, bits)
             assert np.all(np.abs(d) <= 2 ** (bits - 1))
+            assert np.all(d[1:] < 2 ** (bits - 1))
             assert np.all(d == np.rint(d))
             w = 2.0 ** (1 - bits * np.arange(1, s + 1))
             rec = np.ldexp(np.tensordot(w, d, axes=1), e[:, None])
