@@ -555,7 +555,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     // ------------------------------------------------------------ epilogue (warps 2..5)
     const int q = warp & 3;                 // TMEM lane quadrant of this warp
     const int row_l = q * 32 + lane;        // tile row owned by this thread
-    double* tws = prm.tws + static_cast<int64_t>(blockIdx.x) * (OZ_BM * OZ_BN);
+    double* __restrict__ tws = prm.tws + static_cast<int64_t>(blockIdx.x) * (OZ_BM * OZ_BN);
     int buf = 0;
     uint32_t acc_phase = 0;
     bool ok = true;
@@ -585,29 +585,42 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
             uint32_t v[32];
             tmem_ld_32x32b_x32(taddr + cb, v);
             tc_wait_ld();
-            double* tcol = tws + static_cast<int64_t>(cb) * OZ_BM + row_l;
+            double* __restrict__ tcol = tws + static_cast<int64_t>(cb) * OZ_BM + row_l;
+            // all loads of the chunk are issued before any store (no aliasing chain)
+            double t[32];
+            if (!first) {
+#pragma unroll
+              for (int j = 0; j < 32; ++j) t[j] = tcol[j * OZ_BM];
+            }
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+              const double sj = static_cast<double>(__uint_as_float(v[j]));
+              t[j] = first ? sj * w : fma(sj, w, t[j]);
+            }
             if (!last) {
 #pragma unroll
-              for (int j = 0; j < 32; ++j) {
-                const double s = static_cast<double>(__uint_as_float(v[j]));
-                double* tp = tcol + j * OZ_BM;
-                *tp = first ? s * w : fma(s, w, *tp);
-              }
+              for (int j = 0; j < 32; ++j) tcol[j * OZ_BM] = t[j];
             } else {
+              const int64_t colb = n0 + cb;
+              int ebj[32];
 #pragma unroll
-              for (int j = 0; j < 32; ++j) {
-                const int64_t col = n0 + cb + j;
-                const double s = static_cast<double>(__uint_as_float(v[j]));
-                const double tot = first ? s * w : fma(s, w, tcol[j * OZ_BM]);
-                if (row_ok && col < prm.N) {
-                  const int eb = prm.eb[col];
+              for (int j = 0; j < 32; ++j) ebj[j] = (colb + j < prm.N) ? __ldg(prm.eb + colb + j) : 0;
+              if (row_ok) {
+                double* __restrict__ crow = prm.C + row + colb * prm.ldc;
+                double c0[32];
+                if (beta != 0.0) {
+#pragma unroll
+                  for (int j = 0; j < 32; ++j) c0[j] = (colb + j < prm.N) ? crow[j * prm.ldc] : 0.0;
+                }
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                  if (colb + j >= prm.N) continue;
                   double val;
-                  if (ea == OZ_EXP_NONFINITE || eb == OZ_EXP_NONFINITE)
+                  if (ea == OZ_EXP_NONFINITE || ebj[j] == OZ_EXP_NONFINITE)
                     val = __longlong_as_double(0x7FF8000000000000ll);
                   else
-                    val = scale_pow2(tot, ea + eb);
-                  double* cp = prm.C + row + col * prm.ldc;
-                  *cp = (beta == 0.0) ? alpha * val : fma(alpha, val, beta * *cp);
+                    val = scale_pow2(t[j], ea + ebj[j]);
+                  crow[j * prm.ldc] = (beta == 0.0) ? alpha * val : fma(alpha, val, beta * c0[j]);
                 }
               }
             }
