@@ -63,6 +63,10 @@ int gb_set_wait_limit_ns(uint64_t ns);
  * the default 2^-50. */
 int gb_set_ozaki_tolerance(double tol);
 
+/* Returns the current device's cached workspace memory to the driver (synchronises the
+ * device).  Workspace is otherwise kept between calls. */
+int gb_release_workspace(void);
+
 /* Reads and clears the device-side status word written by timed-out waits
  * (synchronises `stream`). */
 int gb_check_status(void* stream);

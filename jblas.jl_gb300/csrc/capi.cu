@@ -38,6 +38,7 @@ struct DeviceInfo {
   int status_code = GB_OK;
   int sms = 0;
   DeviceStatus* status = nullptr;  // device-side status word
+  cudaMemPool_t pool = nullptr;    // workspace pool, memory kept across calls
 };
 static std::mutex g_dev_mu;
 static std::vector<DeviceInfo> g_devs;
@@ -62,7 +63,22 @@ static int device_info(DeviceInfo** out) {
     } else {
       cudaError_t e = cudaMalloc(&d.status, sizeof(DeviceStatus));
       if (e == cudaSuccess) e = cudaMemset(d.status, 0, sizeof(DeviceStatus));
-      if (e != cudaSuccess) d.status_code = gb_set_cuda_error(e, "status word");
+      if (e == cudaSuccess) {
+        // A library-owned stream-ordered pool that keeps its memory: the Ozaki workspace
+        // (digit planes, GB-sized at large shapes) is reused call after call instead of
+        // being unmapped at every synchronisation.
+        cudaMemPoolProps props;
+        std::memset(&props, 0, sizeof(props));
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        e = cudaMemPoolCreate(&d.pool, &props);
+        if (e == cudaSuccess) {
+          uint64_t keep = UINT64_MAX;
+          e = cudaMemPoolSetAttribute(d.pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+      }
+      if (e != cudaSuccess) d.status_code = gb_set_cuda_error(e, "device setup");
     }
   }
   if (d.status_code != GB_OK) return d.status_code;
@@ -248,7 +264,7 @@ static int ozaki_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int
   // statistics workspace
   const size_t st_bytes = align256((M + N) * sizeof(unsigned long long)) + 2 * align256((M + N) * sizeof(double));
   char* st_ws = nullptr;
-  GB_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&st_ws), st_bytes, s));
+  GB_CUDA_TRY(cudaMallocFromPoolAsync(reinterpret_cast<void**>(&st_ws), st_bytes, dev->pool, s));
   OzRowStats sa, sb;
   sa.amax_bits = reinterpret_cast<unsigned long long*>(st_ws);
   sb.amax_bits = sa.amax_bits + M;
@@ -323,7 +339,8 @@ static int ozaki_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int
                               ? static_cast<size_t>(grid) * OZ_BM * OZ_BN * sizeof(double)
                               : 0;
   char* ws = nullptr;
-  cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&ws), pa_bytes + pb_bytes + ex_bytes + tw_bytes, s);
+  cudaError_t e = cudaMallocFromPoolAsync(reinterpret_cast<void**>(&ws), pa_bytes + pb_bytes + ex_bytes + tw_bytes,
+                                          dev->pool, s);
   if (e != cudaSuccess) {
     cudaFreeAsync(st_ws, s);
     return gb_set_cuda_error(e, "ozaki workspace");
@@ -394,6 +411,15 @@ int gb_set_ozaki_tolerance(double tol) {
   uint64_t b = 0;
   if (tol > 0.0) std::memcpy(&b, &tol, sizeof(b));
   g_ozaki_tol_bits.store(b);
+  return GB_OK;
+}
+
+int gb_release_workspace(void) {
+  DeviceInfo* dev = nullptr;
+  int rc = device_info(&dev);
+  if (rc) return rc;
+  GB_CUDA_TRY(cudaDeviceSynchronize());
+  GB_CUDA_TRY(cudaMemPoolTrimTo(dev->pool, 0));
   return GB_OK;
 }
 
