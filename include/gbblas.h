@@ -127,6 +127,62 @@ int gb_gemm_f32(int transA, int transB, int64_t M, int64_t N, int64_t K, float a
                 const float* A, int64_t lda, const float* B, int64_t ldb, float beta,
                 float* C, int64_t ldc, void* stream);
 
+/* ------------------------------------------------------------------ grouped GEMM */
+/* One independent product C = alpha*A*B + beta*C (column-major, no transposes, device
+ * pointers; alpha == 0: A, B not read; beta == 0: C not read). */
+typedef struct {
+  int64_t m, n, k;
+  int64_t lda, ldb, ldc;
+  const void* A;
+  const void* B;
+  void* C;
+  double alpha, beta;   /* used as float by the f32 entry point */
+} gb_problem_t;
+
+/* Tile configuration per size class.  Classes by max(m, n): <=16, <=32, <=64, <=128,
+ * <=256, >256.  Configurations (rows x cols of a C tile, 256 threads each):
+ *   0: 16x16  1: 32x32  2: 64x32  3: 64x64  4: 128x64 (f32 only)  5: 128x128 (f32 only)
+ * This replaces jBLAS's fixed BLASOptions(m_k, p_k) (src/blas_options.jl:2-7). */
+#define GB_GROUPED_CLASSES 6
+#define GB_GROUPED_CONFIGS 6
+typedef struct {
+  int32_t config[GB_GROUPED_CLASSES];
+} gb_grouped_tuning_t;
+
+int gb_grouped_default_tuning(int dtype_bytes, gb_grouped_tuning_t* out);
+/* Device workspace a grouped call over `count` problems needs (prefix sums of tiles). */
+size_t gb_grouped_workspace_size(int count);
+/* All `count` products (table `problems` in DEVICE memory) in one persistent launch after
+ * a prologue that counts tiles per problem.  tuning NULL = defaults.  workspace NULL =
+ * taken from the library's pool; a caller-provided workspace (>= gb_grouped_workspace_size)
+ * makes the call allocation-free, e.g. for CUDA-graph capture.  Per element the result
+ * equals jmul!'s FMA chain (with the alpha/beta extension of gb_gemm_*).  The table's
+ * sizes and pointers are trusted (device memory is not inspected on the host).
+ * Reference: many fastmul!/kernel! products, src/kernels.jl:202-208, 239. */
+int gb_gemm_grouped_f64(const gb_problem_t* problems, int count, const gb_grouped_tuning_t* tuning,
+                        void* workspace, size_t workspace_bytes, void* stream);
+int gb_gemm_grouped_f32(const gb_problem_t* problems, int count, const gb_grouped_tuning_t* tuning,
+                        void* workspace, size_t workspace_bytes, void* stream);
+/* Autotuner: times every configuration per size class on the given problems (HOST copy
+ * of the table; their C buffers are left untouched, results go to scratch) with `reps`
+ * timed repetitions and writes the fastest configuration per class; class_ms (may be
+ * NULL) receives the best time per class in ms.  Synchronises `stream`.
+ * Reference: pick_kernel_size / blocking_structure, src/kernel_structure.jl:76-99,
+ * src/memory_management.jl:78-177. */
+int gb_autotune_grouped(int dtype_bytes, const gb_problem_t* host_problems, int count, int reps,
+                        gb_grouped_tuning_t* out, float* class_ms, void* stream);
+
+/* ------------------------------------------------------------------ adjoint */
+/* Pullback of C = A*B (A M x K, B K x N, column-major FP32): given dC (M x N),
+ *   dA = dC * B^T  (M x K)   and   dB = A^T * dC  (K x N)
+ * in one tensor-core launch.  No reference counterpart: it is the rrule of jBLAS's
+ * jmul!/gemm! (src/gemm.jl:244).  Products use the 3xBF16 split (x = hi + lo, the
+ * lo*lo term dropped) with FP32 accumulation: per element |error| <= about
+ * 2^-15 (|dC||B|^T)_ik plus FP32 summation error.  dC is read from memory once. */
+int gb_gemm_adjoint_f32(int64_t M, int64_t N, int64_t K, const float* A, int64_t lda, const float* B,
+                        int64_t ldb, const float* dC, int64_t lddc, float* dA, int64_t ldda, float* dB,
+                        int64_t lddb, void* stream);
+
 /* Ozaki plan for a problem: slice count, bits per slice and the grouping of slice
  * products that the tensor-core kernel would use (no GPU work). */
 typedef struct {

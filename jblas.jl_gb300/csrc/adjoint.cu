@@ -1,0 +1,203 @@
+// Adjoint of gemm!: dA = dC * B^T and dB = A^T * dC in ONE tcgen05 launch (FP32 in/out).
+//
+// No reference counterpart: this is the pullback a ChainRulesCore rrule for jBLAS's
+// jmul!/gemm! (src/gemm.jl:244) returns.  Products use the 3xBF16 split: every FP32 value
+// x is held as hi = bf16(x), lo = bf16(x - hi), and
+//   x*y ~= hi_x*hi_y + hi_x*lo_y + lo_x*hi_y      (lo_x*lo_y, below 2^-16 |xy|, is dropped)
+// accumulated in FP32 in TMEM: three plane pairs of one group of the slice-product engine.
+//
+// Operand planes (K-major BF16, two planes each: hi, lo):
+//   dA = dC * B^T   left  dC as [p][i][j]   (transposed from column-major dC)
+//                   right B  as [p][k][j]   (transposed from column-major B)
+//   dB = A^T * dC   left  A  as [p][k][i]   (A's columns are already contiguous in i)
+//                   right dC as [p][j][i]   (dC's columns are already contiguous in i)
+// dC is read from memory once: one kernel writes both of its plane layouts.
+#include <cuda_bf16.h>
+
+#include <cstring>
+
+#include "gb_common.cuh"
+#include "profile.cuh"
+#include "tc_gemm.cuh"
+
+namespace gb {
+
+__device__ __forceinline__ void split_hi_lo(float x, uint32_t& hi_bits, uint32_t& lo_bits) {
+  const __nv_bfloat16 hi = __float2bfloat16_rn(x);
+  const float r = x - __bfloat162float(hi);
+  const __nv_bfloat16 lo = __float2bfloat16_rn(r);
+  hi_bits = static_cast<uint32_t>(__bfloat16_as_ushort(hi));
+  lo_bits = static_cast<uint32_t>(__bfloat16_as_ushort(lo));
+}
+
+// One thread = one row r of X (R x Kd view, element (r, k) at X[r*rs + k*ks]) and 16
+// consecutive k.  Writes planes[0] (hi) and planes[1] (lo), [plane][r][pitch], 32 bytes
+// per plane per thread.  RC: rows contiguous (threads along r); otherwise threads along k.
+// DUAL (rows contiguous only): also writes the transposed layout [plane][k][pitch2] + r,
+// so a matrix needed in both orientations is read once.
+template <bool RC, bool DUAL>
+__global__ void __launch_bounds__(256) split3_kernel(const float* __restrict__ X, int64_t R, int64_t Kd,
+                                                     int64_t rs, int64_t ks, __nv_bfloat16* __restrict__ planes,
+                                                     int64_t pitch, __nv_bfloat16* __restrict__ planes_t,
+                                                     int64_t pitch_t) {
+  int64_t r, kc;
+  if (RC) {
+    r = static_cast<int64_t>(blockIdx.x) * 256 + threadIdx.x;
+    kc = blockIdx.y;
+  } else {
+    kc = static_cast<int64_t>(blockIdx.x) * 256 + threadIdx.x;
+    r = blockIdx.y;
+  }
+  const int64_t k0 = kc * 16;
+  if (r >= R || k0 >= Kd) return;
+  const int nvalid = static_cast<int>(Kd - k0 < 16 ? Kd - k0 : 16);
+  const float* src = X + r * rs + k0 * ks;
+  uint32_t hp[8], lp[8];
+#pragma unroll
+  for (int j = 0; j < 16; j += 2) {
+    uint32_t h0, l0, h1, l1;
+    const float x0 = (j < nvalid) ? src[j * ks] : 0.0f;
+    const float x1 = (j + 1 < nvalid) ? src[(j + 1) * ks] : 0.0f;
+    split_hi_lo(x0, h0, l0);
+    split_hi_lo(x1, h1, l1);
+    hp[j / 2] = h0 | (h1 << 16);
+    lp[j / 2] = l0 | (l1 << 16);
+    if (DUAL) {
+      // transposed layout: row k, column r (consecutive threads: consecutive r)
+      const int64_t plane_t = Kd * pitch_t;
+      unsigned short* t = reinterpret_cast<unsigned short*>(planes_t);
+      if (j < nvalid) {
+        t[(k0 + j) * pitch_t + r] = static_cast<unsigned short>(h0);
+        t[plane_t + (k0 + j) * pitch_t + r] = static_cast<unsigned short>(l0);
+      }
+      if (j + 1 < nvalid) {
+        t[(k0 + j + 1) * pitch_t + r] = static_cast<unsigned short>(h1);
+        t[plane_t + (k0 + j + 1) * pitch_t + r] = static_cast<unsigned short>(l1);
+      }
+    }
+  }
+  const int64_t plane = R * pitch;
+  __nv_bfloat16* dst = planes + r * pitch + k0;
+  if (nvalid == 16) {
+    uint4* h4 = reinterpret_cast<uint4*>(dst);
+    uint4* l4 = reinterpret_cast<uint4*>(dst + plane);
+    h4[0] = make_uint4(hp[0], hp[1], hp[2], hp[3]);
+    h4[1] = make_uint4(hp[4], hp[5], hp[6], hp[7]);
+    l4[0] = make_uint4(lp[0], lp[1], lp[2], lp[3]);
+    l4[1] = make_uint4(lp[4], lp[5], lp[6], lp[7]);
+  } else {
+    unsigned short* d2 = reinterpret_cast<unsigned short*>(dst);
+    for (int j = 0; j < nvalid; ++j) {
+      d2[j] = static_cast<unsigned short>(hp[j / 2] >> (16 * (j & 1)));
+      d2[plane + j] = static_cast<unsigned short>(lp[j / 2] >> (16 * (j & 1)));
+    }
+  }
+}
+
+static int split3(const float* X, int64_t R, int64_t Kd, int64_t rs, int64_t ks, __nv_bfloat16* planes,
+                  int64_t pitch, __nv_bfloat16* planes_t, int64_t pitch_t, cudaStream_t s) {
+  if (R <= 0 || Kd <= 0) return GB_OK;
+  const int64_t kchunks = (Kd + 15) / 16;
+  if (rs == 1 || planes_t) {
+    if (kchunks > 65535) return GB_ERR_UNSUPPORTED;
+    dim3 grid(static_cast<unsigned>((R + 255) / 256), static_cast<unsigned>(kchunks));
+    if (planes_t)
+      GB_LAUNCH(GB_KERNEL_ADJOINT_SPLIT, s,
+                (split3_kernel<true, true><<<grid, 256, 0, s>>>(X, R, Kd, rs, ks, planes, pitch, planes_t, pitch_t)));
+    else
+      GB_LAUNCH(GB_KERNEL_ADJOINT_SPLIT, s,
+                (split3_kernel<true, false><<<grid, 256, 0, s>>>(X, R, Kd, rs, ks, planes, pitch, nullptr, 0)));
+  } else {
+    if (R > 65535) return GB_ERR_UNSUPPORTED;
+    dim3 grid(static_cast<unsigned>((kchunks + 255) / 256), static_cast<unsigned>(R));
+    GB_LAUNCH(GB_KERNEL_ADJOINT_SPLIT, s,
+              (split3_kernel<false, false><<<grid, 256, 0, s>>>(X, R, Kd, rs, ks, planes, pitch, nullptr, 0)));
+  }
+  GB_CUDA_TRY(cudaGetLastError());
+  return GB_OK;
+}
+
+static inline int64_t pitch64(int64_t k) { return ((k + 63) / 64) * 64; }
+static inline size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Schedule of the 3xBF16 product: one group, pairs (hi,hi), (hi,lo), (lo,hi).
+static void split3_schedule(SliceSchedule& S, int kb_chunk) {
+  std::memset(&S, 0, sizeof(S));
+  S.ngroups = 1;
+  S.kb_chunk = kb_chunk;
+  S.bits = 0;
+  S.level[0] = 0;
+  S.npairs[0] = 3;
+  S.pair_off[0] = 0;
+  S.pp[0] = 0; S.pq[0] = 0;
+  S.pp[1] = 0; S.pq[1] = 1;
+  S.pp[2] = 1; S.pq[2] = 0;
+}
+
+// Workspace layout for an adjoint of A (M x K), B (K x N), dC (M x N).
+size_t adjoint_workspace_bytes(int64_t M, int64_t N, int64_t K) {
+  const int64_t pN = pitch64(N), pM = pitch64(M);
+  return al256(2 * static_cast<size_t>(M) * pN * 2) + al256(2 * static_cast<size_t>(K) * pN * 2) +
+         al256(2 * static_cast<size_t>(K) * pM * 2) + al256(2 * static_cast<size_t>(N) * pM * 2);
+}
+
+int adjoint_f32(int64_t M, int64_t N, int64_t K, const float* A, int64_t lda, const float* B, int64_t ldb,
+                const float* dC, int64_t lddc, float* dA, int64_t ldda, float* dB, int64_t lddb, void* ws,
+                int sms, DeviceStatus* status, uint64_t wait_limit_ns, cudaStream_t s) {
+  const int64_t pN = pitch64(N), pM = pitch64(M);
+  char* w = static_cast<char*>(ws);
+  __nv_bfloat16* P1 = reinterpret_cast<__nv_bfloat16*>(w);                      // dC [p][i][j]
+  w += al256(2 * static_cast<size_t>(M) * pN * 2);
+  __nv_bfloat16* P2 = reinterpret_cast<__nv_bfloat16*>(w);                      // B  [p][k][j]
+  w += al256(2 * static_cast<size_t>(K) * pN * 2);
+  __nv_bfloat16* P3 = reinterpret_cast<__nv_bfloat16*>(w);                      // A  [p][k][i]
+  w += al256(2 * static_cast<size_t>(K) * pM * 2);
+  __nv_bfloat16* P4 = reinterpret_cast<__nv_bfloat16*>(w);                      // dC [p][j][i]
+
+  // dC (M x N, column-major): rows i contiguous -> [p][i][j] and, from the same read, [p][j][i]
+  int rc = split3(dC, M, N, 1, lddc, P1, pN, P4, pM, s);
+  // B (K x N): rows k contiguous -> [p][k][j]
+  if (!rc) rc = split3(B, K, N, 1, ldb, P2, pN, nullptr, 0, s);
+  // A^T rows k (contraction over i, contiguous in memory) -> [p][k][i]
+  if (!rc) rc = split3(A, K, M, lda, 1, P3, pM, nullptr, 0, s);
+  if (rc) return rc;
+
+  CUtensorMap ta0, tb0, ta1, tb1;
+  rc = make_plane_tmap(&ta0, P1, N, M, 2, pN, TC_BM);
+  if (!rc) rc = make_plane_tmap(&tb0, P2, N, K, 2, pN, TC_BN);
+  if (!rc) rc = make_plane_tmap(&ta1, P3, M, K, 2, pM, TC_BM);
+  if (!rc) rc = make_plane_tmap(&tb1, P4, M, N, 2, pM, TC_BN);
+  if (rc) return rc;
+
+  TcParams prm;
+  std::memset(&prm, 0, sizeof(prm));
+  TcProblem& P = prm.prob[0];   // dA (M x K), contraction N
+  P.M = M; P.N = K; P.K = N;
+  P.tiles_m = static_cast<int32_t>((M + TC_BM - 1) / TC_BM);
+  P.tiles_n = static_cast<int32_t>((K + TC_BN - 1) / TC_BN);
+  P.tile_begin = 0;
+  P.kb_total = static_cast<int32_t>((N + TC_BK - 1) / TC_BK);
+  P.nchunks = 1;
+  P.C = dA; P.ldc = ldda;
+  P.alpha = 1.0; P.beta = 0.0;
+  TcProblem& Q = prm.prob[1];   // dB (K x N), contraction M
+  Q.M = K; Q.N = N; Q.K = M;
+  Q.tiles_m = static_cast<int32_t>((K + TC_BM - 1) / TC_BM);
+  Q.tiles_n = static_cast<int32_t>((N + TC_BN - 1) / TC_BN);
+  Q.tile_begin = P.tiles_m * P.tiles_n;
+  Q.kb_total = static_cast<int32_t>((M + TC_BK - 1) / TC_BK);
+  Q.nchunks = 1;
+  Q.C = dB; Q.ldc = lddb;
+  Q.alpha = 1.0; Q.beta = 0.0;
+  prm.nprob = 2;
+  prm.total_tiles = Q.tile_begin + Q.tiles_m * Q.tiles_n;
+  prm.tws = nullptr;
+  prm.status = status;
+  prm.wait_limit_ns = wait_limit_ns;
+  SliceSchedule sched;
+  split3_schedule(sched, P.kb_total > Q.kb_total ? P.kb_total : Q.kb_total);
+  const int grid = prm.total_tiles < sms ? prm.total_tiles : sms;
+  return tc_gemm_launch(TC_EPI_F32, ta0, tb0, &ta1, &tb1, sched, prm, grid, GB_KERNEL_ADJOINT_MMA, s);
+}
+
+}  // namespace gb

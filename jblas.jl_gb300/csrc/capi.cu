@@ -16,8 +16,16 @@
 #include <vector>
 
 #include "gb_common.cuh"
+#include "grouped.cuh"
 #include "native_gemm.cuh"
 #include "ozaki.cuh"
+
+namespace gb {
+size_t adjoint_workspace_bytes(int64_t M, int64_t N, int64_t K);
+int adjoint_f32(int64_t M, int64_t N, int64_t K, const float* A, int64_t lda, const float* B, int64_t ldb,
+                const float* dC, int64_t lddc, float* dA, int64_t ldda, float* dB, int64_t lddb, void* ws,
+                int sms, DeviceStatus* status, uint64_t wait_limit_ns, cudaStream_t s);
+}  // namespace gb
 
 static thread_local char g_last_detail[256];
 static thread_local gb_ozaki_plan_t g_last_plan;
@@ -255,7 +263,7 @@ static int ozaki_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int
                       const double* A, int64_t lda, const double* B, int64_t ldb, double beta,
                       double* C, int64_t ldc, int slices, double* err_bound_out, cudaStream_t s) {
   if (slices < 0 || slices > OZ_MAX_SLICES) return GB_ERR_INVALID_VALUE;
-  if ((M + OZ_BM - 1) / OZ_BM * ((N + OZ_BN - 1) / OZ_BN) > 0x7FFFFFFF) return GB_ERR_UNSUPPORTED;
+  if ((M + TC_BM - 1) / TC_BM * ((N + TC_BN - 1) / TC_BN) > 0x7FFFFFFF) return GB_ERR_UNSUPPORTED;
   // op(A) rows i: X[i,k]; op(B) "rows" j: X[j,k] = op(B)[k,j]
   const int64_t a_rs = ta ? lda : 1, a_ks = ta ? 1 : lda;
   const int64_t b_rs = tb ? 1 : ldb, b_ks = tb ? ldb : 1;
@@ -336,7 +344,7 @@ static int ozaki_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int
   const size_t pb_bytes = align256(static_cast<size_t>(s_use) * N * pitch * 2);
   const size_t ex_bytes = align256((M + N) * sizeof(int32_t));
   const size_t tw_bytes = (plan.groups * plan.nchunks > 1)
-                              ? static_cast<size_t>(grid) * OZ_BM * OZ_BN * sizeof(double)
+                              ? static_cast<size_t>(grid) * TC_BM * TC_BN * sizeof(double)
                               : 0;
   char* ws = nullptr;
   cudaError_t e = cudaMallocFromPoolAsync(reinterpret_cast<void**>(&ws), pa_bytes + pb_bytes + ex_bytes + tw_bytes,
@@ -481,6 +489,89 @@ int gb_gemm_f32(int transA, int transB, int64_t M, int64_t N, int64_t K, float a
   if (rc) return rc;
   return native_gemm_f32(transA, transB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc,
                          static_cast<cudaStream_t>(stream));
+}
+
+int gb_gemm_adjoint_f32(int64_t M, int64_t N, int64_t K, const float* A, int64_t lda, const float* B,
+                        int64_t ldb, const float* dC, int64_t lddc, float* dA, int64_t ldda, float* dB,
+                        int64_t lddb, void* stream) {
+  DeviceInfo* dev = nullptr;
+  int rc = device_info(&dev);
+  if (rc) return rc;
+  if (M < 0 || N < 0 || K < 0) return GB_ERR_INVALID_VALUE;
+  auto ld_ok = [](int64_t ld, int64_t rows) { return ld >= (rows > 1 ? rows : 1); };
+  if (!ld_ok(lda, M) || !ld_ok(ldb, K) || !ld_ok(lddc, M) || !ld_ok(ldda, M) || !ld_ok(lddb, K))
+    return GB_ERR_INVALID_VALUE;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const bool need_da = M > 0 && K > 0, need_db = K > 0 && N > 0;
+  if ((need_da && !is_device_ptr(dA)) || (need_db && !is_device_ptr(dB))) return GB_ERR_INVALID_VALUE;
+  if (M == 0 || N == 0 || K == 0) {
+    // an empty contraction gives zero gradients
+    if (need_da) GB_CUDA_TRY(cudaMemset2DAsync(dA, ldda * sizeof(float), 0, M * sizeof(float), K, s));
+    if (need_db) GB_CUDA_TRY(cudaMemset2DAsync(dB, lddb * sizeof(float), 0, K * sizeof(float), N, s));
+    return GB_OK;
+  }
+  if (!is_device_ptr(A) || !is_device_ptr(B) || !is_device_ptr(dC)) return GB_ERR_INVALID_VALUE;
+  if (static_cast<int64_t>(tc_tiles(M, K)) + tc_tiles(K, N) > 0x7FFFFFFF) return GB_ERR_UNSUPPORTED;
+  void* ws = nullptr;
+  GB_CUDA_TRY(cudaMallocFromPoolAsync(&ws, adjoint_workspace_bytes(M, N, K), dev->pool, s));
+  rc = adjoint_f32(M, N, K, A, lda, B, ldb, dC, lddc, dA, ldda, dB, lddb, ws, dev->sms, dev->status,
+                   g_wait_limit_ns.load(), s);
+  cudaFreeAsync(ws, s);
+  return rc;
+}
+
+int gb_grouped_default_tuning(int dtype_bytes, gb_grouped_tuning_t* out) {
+  if (!out || (dtype_bytes != 4 && dtype_bytes != 8)) return GB_ERR_INVALID_VALUE;
+  *out = grouped_default_tuning(dtype_bytes);
+  return GB_OK;
+}
+
+size_t gb_grouped_workspace_size(int count) { return count < 0 ? 0 : grouped_workspace_bytes(count); }
+
+static int grouped_call(int dtype_bytes, const gb_problem_t* problems, int count, const gb_grouped_tuning_t* tuning,
+                        void* workspace, size_t workspace_bytes, void* stream) {
+  DeviceInfo* dev = nullptr;
+  int rc = device_info(&dev);
+  if (rc) return rc;
+  if (count < 0) return GB_ERR_INVALID_VALUE;
+  if (count == 0) return GB_OK;
+  if (!is_device_ptr(problems)) return GB_ERR_INVALID_VALUE;
+  const gb_grouped_tuning_t t = tuning ? *tuning : grouped_default_tuning(dtype_bytes);
+  rc = grouped_validate_tuning(dtype_bytes, t);
+  if (rc) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const size_t need = grouped_workspace_bytes(count);
+  void* ws = workspace;
+  if (ws) {
+    if (workspace_bytes < need || !is_device_ptr(ws) || (reinterpret_cast<uintptr_t>(ws) & 7))
+      return GB_ERR_INVALID_VALUE;
+  } else {
+    GB_CUDA_TRY(cudaMallocFromPoolAsync(&ws, need, dev->pool, s));
+  }
+  rc = grouped_launch(dtype_bytes, problems, count, t, static_cast<long long*>(ws), dev->sms, s);
+  if (!workspace) cudaFreeAsync(ws, s);
+  return rc;
+}
+
+int gb_gemm_grouped_f64(const gb_problem_t* problems, int count, const gb_grouped_tuning_t* tuning,
+                        void* workspace, size_t workspace_bytes, void* stream) {
+  return grouped_call(8, problems, count, tuning, workspace, workspace_bytes, stream);
+}
+
+int gb_gemm_grouped_f32(const gb_problem_t* problems, int count, const gb_grouped_tuning_t* tuning,
+                        void* workspace, size_t workspace_bytes, void* stream) {
+  return grouped_call(4, problems, count, tuning, workspace, workspace_bytes, stream);
+}
+
+int gb_autotune_grouped(int dtype_bytes, const gb_problem_t* host_problems, int count, int reps,
+                        gb_grouped_tuning_t* out, float* class_ms, void* stream) {
+  if (!out || count < 0 || (count > 0 && !host_problems) || (dtype_bytes != 4 && dtype_bytes != 8))
+    return GB_ERR_INVALID_VALUE;
+  DeviceInfo* dev = nullptr;
+  int rc = device_info(&dev);
+  if (rc) return rc;
+  return grouped_autotune(dtype_bytes, host_problems, count, dev->sms, dev->pool, reps < 1 ? 1 : reps, out,
+                          class_ms, static_cast<cudaStream_t>(stream));
 }
 
 int gb_jmul_f64(double* D, const double* A, const double* X, int64_t M, int64_t N, int64_t P, void* stream) {

@@ -1,0 +1,316 @@
+// Grouped GEMM: thousands of independent, uneven C_i = alpha_i A_i B_i + beta_i C_i in one
+// persistent launch (FP64 or FP32, CUDA cores, jmul!'s per-element FMA order).
+//
+// jBLAS multiplies small static matrices one call at a time (fastmul!/kernel!,
+// src/kernels.jl:202-208, 239) with a tile size fixed at code-generation time
+// (pick_kernel_size, src/kernel_structure.jl:76-99; BLASOptions, src/blas_options.jl:2-7).
+// Here one launch walks every tile of every problem:
+//   1. a prologue kernel classifies each problem by max(m, n) into a size class, takes
+//      that class's tile configuration from the tuning table (chosen by the autotuner,
+//      gb_autotune_grouped), counts its tiles and writes the exclusive prefix sum;
+//   2. the persistent kernel (grid = SMs x resident CTAs) strides over the global tile
+//      index, finds its problem by binary search in the prefix sums and runs that
+//      configuration's tile routine.
+// Both kernels read only device memory, so a call can be captured in a CUDA graph.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "gb_common.cuh"
+#include "grouped.cuh"
+#include "profile.cuh"
+
+namespace gb {
+
+struct TileCfg {
+  int bm, bn, bk, tm, tn;
+};
+// Every configuration runs on 256 threads: (bm / tm) * (bn / tn) == 256.
+__host__ __device__ constexpr TileCfg tile_cfg(int c) {
+  return c == 0 ? TileCfg{16, 16, 16, 1, 1}
+       : c == 1 ? TileCfg{32, 32, 16, 2, 2}
+       : c == 2 ? TileCfg{64, 32, 16, 4, 2}
+       : c == 3 ? TileCfg{64, 64, 16, 4, 4}
+       : c == 4 ? TileCfg{128, 64, 8, 8, 4}
+                : TileCfg{128, 128, 8, 8, 8};
+}
+
+__host__ __device__ inline int size_class(int64_t m, int64_t n) {
+  const int64_t d = m > n ? m : n;
+  return d <= 16 ? 0 : d <= 32 ? 1 : d <= 64 ? 2 : d <= 128 ? 3 : d <= 256 ? 4 : 5;
+}
+
+template <typename T>
+__device__ __forceinline__ T fmad(T a, T b, T c);
+template <>
+__device__ __forceinline__ double fmad<double>(double a, double b, double c) { return fma(a, b, c); }
+template <>
+__device__ __forceinline__ float fmad<float>(float a, float b, float c) { return fmaf(a, b, c); }
+
+constexpr int GROUPED_THREADS = 256;
+constexpr int GROUPED_SMEM = 2 * 16 * 64 * 8;  // largest As + Bs of any configuration (bytes)
+
+// One BM x BN tile of problem `p` (column-major, no transposes).  Per element the FMA chain
+// runs k = 0..K-1 in order from -0.0 (equal to jmul!'s a1*x1 first step, bit for bit).
+template <typename T, int BM, int BN, int BK, int TM, int TN>
+__device__ __forceinline__ void grouped_tile(const gb_problem_t& p, int tm, int tn, unsigned char* smem) {
+  static_assert((BM / TM) * (BN / TN) == GROUPED_THREADS, "configuration must use 256 threads");
+  T* As = reinterpret_cast<T*>(smem);   // [BK][BM]
+  T* Bs = As + BK * BM;                 // [BK][BN]
+  const int tid = threadIdx.x;
+  const int tx = tid % (BN / TN), ty = tid / (BN / TN);
+  const int64_t M = p.m, N = p.n, K = p.k;
+  const int64_t m0 = static_cast<int64_t>(tm) * BM, n0 = static_cast<int64_t>(tn) * BN;
+  const T* __restrict__ A = static_cast<const T*>(p.A);
+  const T* __restrict__ B = static_cast<const T*>(p.B);
+  T acc[TM][TN];
+#pragma unroll
+  for (int i = 0; i < TM; ++i)
+#pragma unroll
+    for (int j = 0; j < TN; ++j) acc[i][j] = T(-0.0);
+
+  const int64_t Kc = (p.alpha == 0.0) ? 0 : K;   // alpha == 0: A and B are not read
+  for (int64_t k0 = 0; k0 < Kc; k0 += BK) {
+    const int kc = static_cast<int>(K - k0 < BK ? K - k0 : BK);
+#pragma unroll
+    for (int e = tid; e < BM * BK; e += GROUPED_THREADS) {
+      const int ml = e % BM, kl = e / BM;
+      const int64_t m = m0 + ml, k = k0 + kl;
+      As[kl * BM + ml] = (m < M && k < K) ? A[m + k * p.lda] : T(0);
+    }
+#pragma unroll
+    for (int e = tid; e < BK * BN; e += GROUPED_THREADS) {
+      const int kl = e % BK, nl = e / BK;
+      const int64_t n = n0 + nl, k = k0 + kl;
+      Bs[kl * BN + nl] = (n < N && k < K) ? B[k + n * p.ldb] : T(0);
+    }
+    __syncthreads();
+    for (int kk = 0; kk < kc; ++kk) {
+      T a[TM], b[TN];
+#pragma unroll
+      for (int i = 0; i < TM; ++i) a[i] = As[kk * BM + ty + i * (BM / TM)];
+#pragma unroll
+      for (int j = 0; j < TN; ++j) b[j] = Bs[kk * BN + tx + j * (BN / TN)];
+#pragma unroll
+      for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) acc[i][j] = fmad<T>(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+  const T alpha = static_cast<T>(p.alpha), beta = static_cast<T>(p.beta);
+  T* __restrict__ C = static_cast<T*>(p.C);
+#pragma unroll
+  for (int i = 0; i < TM; ++i) {
+    const int64_t m = m0 + ty + i * (BM / TM);
+    if (m >= M) continue;
+#pragma unroll
+    for (int j = 0; j < TN; ++j) {
+      const int64_t n = n0 + tx + j * (BN / TN);
+      if (n >= N) continue;
+      T* c = &C[m + n * p.ldc];
+      if (alpha == T(0)) *c = (beta == T(0)) ? T(0) : beta * *c;   // A, B not read
+      else *c = (beta == T(0)) ? alpha * acc[i][j] : fmad<T>(alpha, acc[i][j], beta * *c);
+    }
+  }
+}
+
+// Prologue: tiles per problem under the tuning table, exclusive prefix sum into
+// offsets[0..count]; one block, each thread scans a contiguous chunk.
+__global__ void __launch_bounds__(1024) grouped_prefix_kernel(const gb_problem_t* __restrict__ probs, int count,
+                                                              gb_grouped_tuning_t tuning,
+                                                              long long* __restrict__ offsets) {
+  __shared__ long long part[1024];
+  const int t = threadIdx.x;
+  const int per = (count + 1023) / 1024;
+  const int b = t * per, e = min(count, b + per);
+  long long sum = 0;
+  for (int i = b; i < e; ++i) {
+    const gb_problem_t& p = probs[i];
+    const TileCfg c = tile_cfg(tuning.config[size_class(p.m, p.n)]);
+    const long long tiles = (p.m <= 0 || p.n <= 0) ? 0 : ((p.m + c.bm - 1) / c.bm) * ((p.n + c.bn - 1) / c.bn);
+    sum += tiles;
+  }
+  part[t] = sum;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {   // inclusive Hillis-Steele scan of the parts
+    const long long v = (t >= off) ? part[t - off] : 0;
+    __syncthreads();
+    part[t] += v;
+    __syncthreads();
+  }
+  long long run = (t == 0) ? 0 : part[t - 1];
+  for (int i = b; i < e; ++i) {
+    offsets[i] = run;
+    const gb_problem_t& p = probs[i];
+    const TileCfg c = tile_cfg(tuning.config[size_class(p.m, p.n)]);
+    run += (p.m <= 0 || p.n <= 0) ? 0 : ((p.m + c.bm - 1) / c.bm) * ((p.n + c.bn - 1) / c.bn);
+  }
+  if (t == 1023) offsets[count] = part[1023];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(GROUPED_THREADS) grouped_gemm_kernel(const gb_problem_t* __restrict__ probs,
+                                                                       int count, gb_grouped_tuning_t tuning,
+                                                                       const long long* __restrict__ offsets) {
+  __shared__ __align__(16) unsigned char smem[GROUPED_SMEM];
+  const long long total = offsets[count];
+  for (long long w = blockIdx.x; w < total; w += gridDim.x) {
+    // problem index: last p with offsets[p] <= w (problems with no tiles share offsets)
+    int lo = 0, hi = count - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (offsets[mid] <= w) lo = mid; else hi = mid - 1;
+    }
+    const gb_problem_t p = probs[lo];
+    const int cfg = tuning.config[size_class(p.m, p.n)];
+    const TileCfg c = tile_cfg(cfg);
+    const long long local = w - offsets[lo];
+    const int tiles_m = static_cast<int>((p.m + c.bm - 1) / c.bm);
+    const int tm = static_cast<int>(local % tiles_m), tn = static_cast<int>(local / tiles_m);
+    if (sizeof(T) == 8) {
+      // FP64 runs at the DFMA rate whatever the tile: the small configurations keep the
+      // register count (and so the resident CTAs per SM) low.
+      switch (cfg) {
+        case 0: grouped_tile<T, 16, 16, 16, 1, 1>(p, tm, tn, smem); break;
+        case 1: grouped_tile<T, 32, 32, 16, 2, 2>(p, tm, tn, smem); break;
+        case 2: grouped_tile<T, 64, 32, 16, 4, 2>(p, tm, tn, smem); break;
+        default: grouped_tile<T, 64, 64, 16, 4, 4>(p, tm, tn, smem); break;
+      }
+    } else {
+      switch (cfg) {
+        case 0: grouped_tile<T, 16, 16, 16, 1, 1>(p, tm, tn, smem); break;
+        case 1: grouped_tile<T, 32, 32, 16, 2, 2>(p, tm, tn, smem); break;
+        case 2: grouped_tile<T, 64, 32, 16, 4, 2>(p, tm, tn, smem); break;
+        case 3: grouped_tile<T, 64, 64, 16, 4, 4>(p, tm, tn, smem); break;
+        case 4: grouped_tile<T, 128, 64, 8, 8, 4>(p, tm, tn, smem); break;
+        default: grouped_tile<T, 128, 128, 8, 8, 8>(p, tm, tn, smem); break;
+      }
+    }
+  }
+}
+
+gb_grouped_tuning_t grouped_default_tuning(int dtype_bytes) {
+  gb_grouped_tuning_t t;
+  std::memset(&t, 0, sizeof(t));
+  // classes: <=16, <=32, <=64, <=128, <=256, >256
+  const int f64[GB_GROUPED_CLASSES] = {0, 1, 2, 3, 3, 3};
+  const int f32[GB_GROUPED_CLASSES] = {0, 1, 3, 3, 4, 5};
+  for (int c = 0; c < GB_GROUPED_CLASSES; ++c) t.config[c] = dtype_bytes == 8 ? f64[c] : f32[c];
+  return t;
+}
+
+int grouped_configs(int dtype_bytes) { return dtype_bytes == 8 ? 4 : GB_GROUPED_CONFIGS; }
+
+int grouped_validate_tuning(int dtype_bytes, const gb_grouped_tuning_t& t) {
+  for (int c = 0; c < GB_GROUPED_CLASSES; ++c)
+    if (t.config[c] < 0 || t.config[c] >= grouped_configs(dtype_bytes)) return GB_ERR_INVALID_VALUE;
+  return GB_OK;
+}
+
+template <typename T>
+static int grid_for(int sms) {
+  static int per_sm = 0;
+  if (!per_sm) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, grouped_gemm_kernel<T>, GROUPED_THREADS, 0) !=
+            cudaSuccess ||
+        per_sm < 1)
+      per_sm = 1;
+  }
+  return sms * per_sm;
+}
+
+int grouped_launch(int dtype_bytes, const gb_problem_t* d_probs, int count, const gb_grouped_tuning_t& tuning,
+                   long long* d_offsets, int sms, cudaStream_t s) {
+  if (count <= 0) return GB_OK;
+  GB_LAUNCH(GB_KERNEL_GROUPED_GEMM, s,
+            (grouped_prefix_kernel<<<1, 1024, 0, s>>>(d_probs, count, tuning, d_offsets)));
+  if (dtype_bytes == 8) {
+    const int grid = grid_for<double>(sms);
+    GB_LAUNCH(GB_KERNEL_GROUPED_GEMM, s,
+              (grouped_gemm_kernel<double><<<grid, GROUPED_THREADS, 0, s>>>(d_probs, count, tuning, d_offsets)));
+  } else {
+    const int grid = grid_for<float>(sms);
+    GB_LAUNCH(GB_KERNEL_GROUPED_GEMM, s,
+              (grouped_gemm_kernel<float><<<grid, GROUPED_THREADS, 0, s>>>(d_probs, count, tuning, d_offsets)));
+  }
+  GB_CUDA_TRY(cudaGetLastError());
+  return GB_OK;
+}
+
+size_t grouped_workspace_bytes(int count) {
+  return (static_cast<size_t>(count) + 1) * sizeof(long long);
+}
+
+// Autotuner: for every size class present, time each configuration on that class's
+// problems alone (C redirected to scratch, beta = 0, so the caller's C is untouched) and
+// keep the fastest.  Replaces BLASOptions' fixed block sizes (src/blas_options.jl:2-7).
+int grouped_autotune(int dtype_bytes, const gb_problem_t* h_probs, int count, int sms, cudaMemPool_t pool,
+                     int reps, gb_grouped_tuning_t* out, float* class_ms, cudaStream_t s) {
+  gb_grouped_tuning_t best = grouped_default_tuning(dtype_bytes);
+  std::vector<std::vector<gb_problem_t>> by_class(GB_GROUPED_CLASSES);
+  size_t max_c = 1;
+  for (int i = 0; i < count; ++i) {
+    const gb_problem_t& p = h_probs[i];
+    if (p.m <= 0 || p.n <= 0) continue;
+    by_class[size_class(p.m, p.n)].push_back(p);
+    max_c = std::max(max_c, static_cast<size_t>(p.m * p.n));
+  }
+  void* scratch = nullptr;
+  gb_problem_t* d_sub = nullptr;
+  long long* d_off = nullptr;
+  GB_CUDA_TRY(cudaMallocFromPoolAsync(&scratch, max_c * dtype_bytes, pool, s));
+  GB_CUDA_TRY(cudaMallocFromPoolAsync(reinterpret_cast<void**>(&d_sub), sizeof(gb_problem_t) * (count + 1), pool, s));
+  GB_CUDA_TRY(cudaMallocFromPoolAsync(reinterpret_cast<void**>(&d_off), sizeof(long long) * (count + 1), pool, s));
+  cudaEvent_t e0, e1;
+  GB_CUDA_TRY(cudaEventCreate(&e0));
+  GB_CUDA_TRY(cudaEventCreate(&e1));
+  int rc = GB_OK;
+  for (int c = 0; c < GB_GROUPED_CLASSES && rc == GB_OK; ++c) {
+    if (class_ms) class_ms[c] = 0.f;
+    auto& v = by_class[c];
+    if (v.empty()) continue;
+    for (auto& p : v) {
+      p.C = scratch;
+      p.ldc = p.m;
+      p.beta = 0.0;
+    }
+    if (cudaMemcpyAsync(d_sub, v.data(), v.size() * sizeof(gb_problem_t), cudaMemcpyHostToDevice, s) != cudaSuccess) {
+      rc = GB_ERR_CUDA;
+      break;
+    }
+    float best_ms = 1e30f;
+    for (int cfg = 0; cfg < grouped_configs(dtype_bytes); ++cfg) {
+      gb_grouped_tuning_t t = best;
+      t.config[c] = cfg;
+      rc = grouped_launch(dtype_bytes, d_sub, static_cast<int>(v.size()), t, d_off, sms, s);   // warm-up
+      if (rc) break;
+      cudaEventRecord(e0, s);
+      for (int r = 0; r < reps; ++r) grouped_launch(dtype_bytes, d_sub, static_cast<int>(v.size()), t, d_off, sms, s);
+      cudaEventRecord(e1, s);
+      if (cudaEventSynchronize(e1) != cudaSuccess) {
+        rc = GB_ERR_CUDA;
+        break;
+      }
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      ms /= reps;
+      if (ms < best_ms) {
+        best_ms = ms;
+        best.config[c] = cfg;
+      }
+    }
+    if (class_ms) class_ms[c] = best_ms;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFreeAsync(scratch, s);
+  cudaFreeAsync(d_sub, s);
+  cudaFreeAsync(d_off, s);
+  if (rc == GB_OK) *out = best;
+  return rc;
+}
+
+}  // namespace gb

@@ -29,10 +29,12 @@
 #include <cuda_bf16.h>
 
 #include <cmath>
+#include <cstring>
 
 #include "gb_common.cuh"
 #include "ozaki.cuh"
 #include "profile.cuh"
+#include "tc_gemm.cuh"
 
 namespace gb {
 
@@ -51,13 +53,13 @@ int oz_make_plan(int64_t M, int64_t N, int64_t K, int slices, OzPlan* plan) {
   OzPlan& P = *plan;
   P.slices = slices;
   // One exact chunk covers K up to 2^16 (b >= 5); longer K is cut into equal chunks.
-  int64_t kb_total = (K + OZ_BK - 1) / OZ_BK;
+  int64_t kb_total = (K + TC_BK - 1) / TC_BK;
   if (kb_total < 1) kb_total = 1;
   int64_t nchunks = (K + 65535) / 65536;
   if (nchunks < 1) nchunks = 1;
   int64_t kb_chunk = (kb_total + nchunks - 1) / nchunks;
   nchunks = (kb_total + kb_chunk - 1) / kb_chunk;
-  int64_t kc = kb_chunk * OZ_BK;
+  int64_t kc = kb_chunk * TC_BK;
   if (kc > K) kc = K < 1 ? 1 : K;
   P.k_chunk = kc;
   P.nchunks = static_cast<int>(nchunks);
@@ -70,8 +72,9 @@ int oz_make_plan(int64_t M, int64_t N, int64_t K, int slices, OzPlan* plan) {
   if (share < 1) share = 1;
   if (share > 8) share = 8;
 
-  OzSchedule& S = P.sched;
-  S.kb_total = static_cast<int32_t>(kb_total);
+  SliceSchedule& S = P.sched;
+  std::memset(&S, 0, sizeof(S));
+  P.kb_total = static_cast<int32_t>(kb_total);
   S.kb_chunk = static_cast<int32_t>(kb_chunk);
   S.bits = P.bits;
   // Levels from the smallest contribution (slices + 1) up to the leading one (2): the FP64
@@ -85,13 +88,13 @@ int oz_make_plan(int64_t M, int64_t N, int64_t K, int slices, OzPlan* plan) {
       const int q = level - p;
       if (q < 1 || q > slices) continue;
       if (in_group == 0) {
-        if (g >= OZ_MAX_GROUPS) return GB_ERR_UNSUPPORTED;
+        if (g >= TC_MAX_GROUPS) return GB_ERR_UNSUPPORTED;
         S.level[g] = static_cast<int8_t>(level);
         S.npairs[g] = 0;
         S.pair_off[g] = static_cast<int16_t>(np);
         ++g;
       }
-      if (np >= OZ_MAX_PAIRS) return GB_ERR_UNSUPPORTED;
+      if (np >= TC_MAX_PAIRS) return GB_ERR_UNSUPPORTED;
       S.pp[np] = static_cast<uint8_t>(p - 1);
       S.pq[np] = static_cast<uint8_t>(q - 1);
       ++np;
@@ -103,7 +106,7 @@ int oz_make_plan(int64_t M, int64_t N, int64_t K, int slices, OzPlan* plan) {
   P.groups = g;
   P.products = np;
   P.flops_tensor = 2.0 * static_cast<double>(M) * static_cast<double>(N) *
-                   static_cast<double>(kb_total * OZ_BK) * np;
+                   static_cast<double>(kb_total * TC_BK) * np;
   return GB_OK;
 }
 
@@ -367,317 +370,42 @@ int oz_split(const double* X, int64_t R, int64_t K, int64_t rs, int64_t ks,
   return GB_OK;
 }
 
-// ============================================================== slice-product kernel
-
-constexpr int OZ_THREADS = 192;                 // 6 warps
-constexpr int OZ_A_BYTES = OZ_BM * OZ_BK * 2;   // 16 KB
-constexpr int OZ_B_BYTES = OZ_BN * OZ_BK * 2;   // 32 KB
-constexpr int OZ_STAGE_BYTES = OZ_A_BYTES + OZ_B_BYTES;
-constexpr int OZ_TMEM_COLS = 512;               // two 128 x 256 FP32 accumulators
-constexpr int OZ_SMEM_BYTES = OZ_STAGES * OZ_STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
-
-struct OzKernelParams {
-  int64_t M, N, K;
-  const int32_t* ea;
-  const int32_t* eb;
-  double alpha, beta;
-  double* C;
-  int64_t ldc;
-  double* tws;
-  DeviceStatus* status;
-  uint64_t wait_limit_ns;
-  int tiles_m, tiles_n;
-  int nchunks;
-};
-
-// Tile raster: bands of 16 row tiles, column tiles inside a band (keeps the concurrently
-// active A and B panels of one slice pair inside L2).
-__device__ __forceinline__ void tile_coords(int t, int tiles_m, int tiles_n, int& tm, int& tn) {
-  constexpr int GM = 16;
-  const int band = t / (GM * tiles_n);
-  const int in_band = t - band * GM * tiles_n;
-  const int band_rows = min(GM, tiles_m - band * GM);
-  tm = band * GM + in_band % band_rows;
-  tn = in_band / band_rows;
-}
-
-__global__ void __launch_bounds__(OZ_THREADS, 1)
-    oz_gemm_kernel(const __grid_constant__ CUtensorMap tmap_a, const __grid_constant__ CUtensorMap tmap_b,
-                   const __grid_constant__ OzSchedule sched, const OzKernelParams prm) {
-  extern __shared__ uint8_t smem_raw[];
-  // 1024-byte alignment for the 128-byte swizzle atoms
-  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + OZ_STAGES * OZ_STAGE_BYTES);
-  uint64_t* empty = full + OZ_STAGES;
-  uint64_t* tfull = empty + OZ_STAGES;
-  uint64_t* tempty = tfull + 2;
-  uint64_t* drain = tempty + 2;
-  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(drain + 1);
-  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_holder + 1);
-
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int ntiles = prm.tiles_m * prm.tiles_n;
-  const int G = sched.ngroups;
-  const int nch = prm.nchunks;
-
-  if (threadIdx.x == 0) {
-    for (int i = 0; i < OZ_STAGES; ++i) {
-      mbar_init(&full[i], 1);
-      mbar_init(&empty[i], 1);
-    }
-    for (int i = 0; i < 2; ++i) {
-      mbar_init(&tfull[i], 1);
-      mbar_init(&tempty[i], 128);
-    }
-    mbar_init(drain, 1);
-    *abort_flag = 0;
-    fence_mbar_init();
-    tma_prefetch_desc(&tmap_a);
-    tma_prefetch_desc(&tmap_b);
-  }
-  if (warp == 1) {
-    tmem_alloc(tmem_holder, OZ_TMEM_COLS);
-    tmem_relinquish();
-  }
-  tc_fence_before();
-  __syncthreads();
-  tc_fence_after();
-  const uint32_t tmem_base = *tmem_holder;
-
-  if (warp == 0) {
-    // ------------------------------------------------------------ TMA producer
-    if (lane == 0) {
-      int stage = 0;
-      uint32_t phase = 0;
-      int issued_parity[OZ_STAGES];
-      for (int i = 0; i < OZ_STAGES; ++i) issued_parity[i] = -1;
-      bool ok = true;
-      for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-        int tm, tn;
-        tile_coords(t, prm.tiles_m, prm.tiles_n, tm, tn);
-        const int m0 = tm * OZ_BM, n0 = tn * OZ_BN;
-        for (int g = 0; g < G && ok; ++g) {
-          for (int c = 0; c < nch && ok; ++c) {
-            const int kb0 = c * sched.kb_chunk;
-            const int kb1 = min(kb0 + sched.kb_chunk, sched.kb_total);
-            for (int i = 0; i < sched.npairs[g] && ok; ++i) {
-              const int pa = sched.pp[sched.pair_off[g] + i];
-              const int pb = sched.pq[sched.pair_off[g] + i];
-              for (int kb = kb0; kb < kb1; ++kb) {
-                if (!mbar_wait_bounded(&empty[stage], phase ^ 1, prm.wait_limit_ns, abort_flag,
-                                       prm.status, 1)) {
-                  ok = false;
-                  break;
-                }
-                uint8_t* sa = smem + stage * OZ_STAGE_BYTES;
-                uint8_t* sb = sa + OZ_A_BYTES;
-                mbar_arrive_expect_tx(&full[stage], OZ_STAGE_BYTES);
-                tma_load_3d(sa, &tmap_a, &full[stage], kb * OZ_BK, m0, pa);
-                tma_load_3d(sb, &tmap_b, &full[stage], kb * OZ_BK, n0, pb);
-                issued_parity[stage] = static_cast<int>(phase);
-                if (++stage == OZ_STAGES) { stage = 0; phase ^= 1; }
-              }
-            }
-          }
-        }
-      }
-      if (!ok) {
-        // let every copy this thread issued land before the CTA's shared memory goes away
-        for (int i = 0; i < OZ_STAGES; ++i)
-          if (issued_parity[i] >= 0) {
-            volatile int no_abort = 0;
-            mbar_wait_bounded(&full[i], static_cast<uint32_t>(issued_parity[i]), prm.wait_limit_ns,
-                              &no_abort, nullptr, 0);
-          }
-      }
-    }
-  } else if (warp == 1) {
-    // ------------------------------------------------------------ MMA issuer
-    if (lane == 0) {
-      constexpr uint32_t IDESC = idesc_bf16_f32(OZ_BM, OZ_BN);
-      int stage = 0;
-      uint32_t phase = 0;
-      int buf = 0;
-      uint32_t acc_phase = 0;
-      bool ok = true;
-      bool issued_any = false;
-      for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-        for (int g = 0; g < G && ok; ++g) {
-          for (int c = 0; c < nch && ok; ++c) {
-            const int kb0 = c * sched.kb_chunk;
-            const int kb1 = min(kb0 + sched.kb_chunk, sched.kb_total);
-            if (!mbar_wait_bounded(&tempty[buf], acc_phase ^ 1, prm.wait_limit_ns, abort_flag,
-                                   prm.status, 2)) {
-              ok = false;
-              break;
-            }
-            tc_fence_after();
-            const uint32_t d_tmem = tmem_base + static_cast<uint32_t>(buf * OZ_BN);
-            uint32_t accumulate = 0;
-            for (int i = 0; i < sched.npairs[g] && ok; ++i) {
-              for (int kb = kb0; kb < kb1; ++kb) {
-                if (!mbar_wait_bounded(&full[stage], phase, prm.wait_limit_ns, abort_flag,
-                                       prm.status, 3)) {
-                  ok = false;
-                  break;
-                }
-                tc_fence_after();
-                const uint32_t sa = smem_u32(smem + stage * OZ_STAGE_BYTES);
-                const uint32_t sb = sa + OZ_A_BYTES;
-                const uint64_t adesc = smem_desc_sw128(sa);
-                const uint64_t bdesc = smem_desc_sw128(sb);
-#pragma unroll
-                for (int kk = 0; kk < OZ_BK / 16; ++kk) {
-                  // advance 16 BF16 = 32 bytes along K inside the swizzle atom
-                  tc_mma_f16(d_tmem, adesc + static_cast<uint64_t>(kk * 2),
-                             bdesc + static_cast<uint64_t>(kk * 2), IDESC, accumulate);
-                  accumulate = 1;
-                }
-                issued_any = true;
-                tc_commit(&empty[stage]);
-                if (++stage == OZ_STAGES) { stage = 0; phase ^= 1; }
-              }
-            }
-            if (!ok) break;
-            tc_commit(&tfull[buf]);
-            if (++buf == 2) { buf = 0; acc_phase ^= 1; }
-          }
-        }
-      }
-      if (!ok && issued_any) {
-        // wait for every MMA issued so far before TMEM is released
-        tc_commit(drain);
-        volatile int no_abort = 0;
-        mbar_wait_bounded(drain, 0, prm.wait_limit_ns, &no_abort, nullptr, 0);
-      }
-    }
-  } else {
-    // ------------------------------------------------------------ epilogue (warps 2..5)
-    const int q = warp & 3;                 // TMEM lane quadrant of this warp
-    const int row_l = q * 32 + lane;        // tile row owned by this thread
-    double* __restrict__ tws = prm.tws + static_cast<int64_t>(blockIdx.x) * (OZ_BM * OZ_BN);
-    int buf = 0;
-    uint32_t acc_phase = 0;
-    bool ok = true;
-    const double alpha = prm.alpha, beta = prm.beta;
-    for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-      int tm, tn;
-      tile_coords(t, prm.tiles_m, prm.tiles_n, tm, tn);
-      const int64_t row = static_cast<int64_t>(tm) * OZ_BM + row_l;
-      const int64_t n0 = static_cast<int64_t>(tn) * OZ_BN;
-      const bool row_ok = row < prm.M;
-      const int ea = row_ok ? prm.ea[row] : 0;
-      int step = 0;
-      const int nsteps = G * nch;
-      for (int g = 0; g < G && ok; ++g) {
-        const double w = pow2_normal(2 - sched.level[g] * sched.bits);
-        for (int c = 0; c < nch; ++c, ++step) {
-          // the whole warp agrees before the warp-collective tcgen05.ld
-          ok = __all_sync(0xffffffffu, mbar_wait_bounded(&tfull[buf], acc_phase, prm.wait_limit_ns,
-                                                         abort_flag, prm.status, 4));
-          if (!ok) break;
-          tc_fence_after();
-          const bool first = (step == 0), last = (step == nsteps - 1);
-          const uint32_t taddr = tmem_base + (static_cast<uint32_t>(q * 32) << 16) +
-                                 static_cast<uint32_t>(buf * OZ_BN);
-#pragma unroll 1
-          for (int cb = 0; cb < OZ_BN; cb += 32) {
-            uint32_t v[32];
-            tmem_ld_32x32b_x32(taddr + cb, v);
-            tc_wait_ld();
-            double* __restrict__ tcol = tws + static_cast<int64_t>(cb) * OZ_BM + row_l;
-            // all loads of the chunk are issued before any store (no aliasing chain)
-            double t[32];
-            if (!first) {
-#pragma unroll
-              for (int j = 0; j < 32; ++j) t[j] = tcol[j * OZ_BM];
-            }
-#pragma unroll
-            for (int j = 0; j < 32; ++j) {
-              const double sj = static_cast<double>(__uint_as_float(v[j]));
-              t[j] = first ? sj * w : fma(sj, w, t[j]);
-            }
-            if (!last) {
-#pragma unroll
-              for (int j = 0; j < 32; ++j) tcol[j * OZ_BM] = t[j];
-            } else {
-              const int64_t colb = n0 + cb;
-              int ebj[32];
-#pragma unroll
-              for (int j = 0; j < 32; ++j) ebj[j] = (colb + j < prm.N) ? __ldg(prm.eb + colb + j) : 0;
-              if (row_ok) {
-                double* __restrict__ crow = prm.C + row + colb * prm.ldc;
-                double c0[32];
-                if (beta != 0.0) {
-#pragma unroll
-                  for (int j = 0; j < 32; ++j) c0[j] = (colb + j < prm.N) ? crow[j * prm.ldc] : 0.0;
-                }
-#pragma unroll
-                for (int j = 0; j < 32; ++j) {
-                  if (colb + j >= prm.N) continue;
-                  double val;
-                  if (ea == OZ_EXP_NONFINITE || ebj[j] == OZ_EXP_NONFINITE)
-                    val = __longlong_as_double(0x7FF8000000000000ll);
-                  else
-                    val = scale_pow2(t[j], ea + ebj[j]);
-                  crow[j * prm.ldc] = (beta == 0.0) ? alpha * val : fma(alpha, val, beta * c0[j]);
-                }
-              }
-            }
-          }
-          tc_fence_before();
-          mbar_arrive(&tempty[buf]);
-          if (++buf == 2) { buf = 0; acc_phase ^= 1; }
-        }
-      }
-    }
-  }
-
-  tc_fence_before();
-  __syncthreads();
-  if (warp == 1) {
-    __syncwarp();
-    tc_fence_after();
-    tmem_dealloc(tmem_base, OZ_TMEM_COLS);
-  }
-}
+// ============================================================== slice products
 
 int oz_gemm_launch(const OzGemmArgs& a, const OzPlan& plan, cudaStream_t s) {
   CUtensorMap ta, tb;
-  int rc = make_plane_tmap(&ta, a.planes_a, a.K, a.M, a.slices, a.pitch, OZ_BM);
+  int rc = make_plane_tmap(&ta, a.planes_a, a.K, a.M, a.slices, a.pitch, TC_BM);
   if (rc) return rc;
-  rc = make_plane_tmap(&tb, a.planes_b, a.K, a.N, a.slices, a.pitch, OZ_BN);
+  rc = make_plane_tmap(&tb, a.planes_b, a.K, a.N, a.slices, a.pitch, TC_BN);
   if (rc) return rc;
-  OzKernelParams prm;
-  prm.M = a.M;
-  prm.N = a.N;
-  prm.K = a.K;
-  prm.ea = a.ea;
-  prm.eb = a.eb;
-  prm.alpha = a.alpha;
-  prm.beta = a.beta;
-  prm.C = a.C;
-  prm.ldc = a.ldc;
+  TcParams prm;
+  std::memset(&prm, 0, sizeof(prm));
+  TcProblem& P = prm.prob[0];
+  P.M = a.M;
+  P.N = a.N;
+  P.K = a.K;
+  P.tiles_m = static_cast<int32_t>((a.M + TC_BM - 1) / TC_BM);
+  P.tiles_n = static_cast<int32_t>((a.N + TC_BN - 1) / TC_BN);
+  P.tile_begin = 0;
+  P.kb_total = plan.kb_total;
+  P.nchunks = plan.nchunks;
+  P.C = a.C;
+  P.ldc = a.ldc;
+  P.alpha = a.alpha;
+  P.beta = a.beta;
+  P.ea = a.ea;
+  P.eb = a.eb;
+  prm.nprob = 1;
+  prm.total_tiles = P.tiles_m * P.tiles_n;
   prm.tws = a.tws;
   prm.status = a.status;
   prm.wait_limit_ns = a.wait_limit_ns;
-  prm.tiles_m = static_cast<int>((a.M + OZ_BM - 1) / OZ_BM);
-  prm.tiles_n = static_cast<int>((a.N + OZ_BN - 1) / OZ_BN);
-  prm.nchunks = plan.nchunks;
-  static bool attr_set = false;  // per process; the attribute is per function, not per device
-  if (!attr_set) {
-    GB_CUDA_TRY(cudaFuncSetAttribute(oz_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     OZ_SMEM_BYTES));
-    attr_set = true;
-  }
-  GB_LAUNCH(GB_KERNEL_OZAKI_SLICE_MMA, s,
-            oz_gemm_kernel<<<a.grid, OZ_THREADS, OZ_SMEM_BYTES, s>>>(ta, tb, plan.sched, prm));
-  GB_CUDA_TRY(cudaGetLastError());
-  return GB_OK;
+  return tc_gemm_launch(TC_EPI_OZAKI_F64, ta, tb, nullptr, nullptr, plan.sched, prm, a.grid,
+                        GB_KERNEL_OZAKI_SLICE_MMA, s);
 }
 
 int oz_grid_for(int sms, int64_t M, int64_t N) {
-  const int64_t tiles = ((M + OZ_BM - 1) / OZ_BM) * ((N + OZ_BN - 1) / OZ_BN);
+  const int64_t tiles = tc_tiles(M, N);
   return static_cast<int>(tiles < sms ? tiles : sms);
 }
 

@@ -6,45 +6,23 @@
 #include <stdint.h>
 
 #include "gb_common.cuh"
+#include "tc_gemm.cuh"
 
 namespace gb {
 
 constexpr int OZ_MAX_SLICES = 20;
-constexpr int OZ_MAX_GROUPS = 256;
-constexpr int OZ_MAX_PAIRS = 256;
 
-// Tile of the slice-product kernel: 128 rows of C x 256 columns, K panels of 64 BF16.
-constexpr int OZ_BM = 128;
-constexpr int OZ_BN = 256;
-constexpr int OZ_BK = 64;
-constexpr int OZ_STAGES = 4;
-
-// Accumulation schedule of one output tile.  Group g sums the slice products
-// (pp[off+i], pq[off+i]), i < npairs[g], all of level p + q = level[g], over one K chunk
-// into a TMEM accumulator; the sum is an exact integer in FP32 by construction
-// (npairs * kc * 2^(2*bits-2) <= 2^24).  Groups run in order, each K chunk in order.
-struct OzSchedule {
-  int32_t ngroups;
-  int32_t kb_total;   // K panels of 64 over the whole K
-  int32_t kb_chunk;   // K panels per exact accumulation chunk
-  int32_t bits;       // bits per digit plane
-  int8_t level[OZ_MAX_GROUPS];
-  int8_t npairs[OZ_MAX_GROUPS];
-  int16_t pair_off[OZ_MAX_GROUPS];
-  uint8_t pp[OZ_MAX_PAIRS];
-  uint8_t pq[OZ_MAX_PAIRS];
-};
-
-// Host-side plan.
+// Host-side plan of one Ozaki product.
 struct OzPlan {
   int slices;
   int bits;
   int64_t k_chunk;
+  int32_t kb_total;
   int products;   // pairs with p + q <= slices + 1
   int groups;     // TMEM groups per K chunk
   int nchunks;
   double flops_tensor;
-  OzSchedule sched;
+  SliceSchedule sched;
 };
 
 // bits per digit plane for an exact FP32 sum of `kc` products of `pairs_per_group` pairs.
@@ -78,7 +56,7 @@ struct OzGemmArgs {
   double alpha, beta;
   double* C;
   int64_t ldc;
-  double* tws;            // per-CTA FP64 tile accumulators (grid x 128 x 256)
+  double* tws;            // per-CTA FP64 tile buffers (grid x 128 x 256)
   DeviceStatus* status;
   uint64_t wait_limit_ns;
   int grid;
@@ -87,8 +65,5 @@ int oz_gemm_launch(const OzGemmArgs& a, const OzPlan& plan, cudaStream_t s);
 // Persistent grid size: one CTA per SM, at most one per output tile.
 int oz_grid_for(int sms, int64_t M, int64_t N);
 
-// Encodes a 3-D BF16 tensor map {K, rows, slices} with a 64 x box_rows x 1 box, 128-B swizzle.
-int make_plane_tmap(CUtensorMap* map, const void* base, int64_t K, int64_t rows, int64_t slices,
-                    int64_t pitch, int box_rows);
 
 }  // namespace gb

@@ -34,6 +34,32 @@ class OzakiPlan(ctypes.Structure):
                 ("flops_tensor", ctypes.c_double)]
 
 
+GROUPED_CLASSES = 6
+
+
+class Problem(ctypes.Structure):
+    """gb_problem_t: one product of a grouped call."""
+    _fields_ = [("m", ctypes.c_int64), ("n", ctypes.c_int64), ("k", ctypes.c_int64),
+                ("lda", ctypes.c_int64), ("ldb", ctypes.c_int64), ("ldc", ctypes.c_int64),
+                ("A", ctypes.c_void_p), ("B", ctypes.c_void_p), ("C", ctypes.c_void_p),
+                ("alpha", ctypes.c_double), ("beta", ctypes.c_double)]
+
+
+class Tuning(ctypes.Structure):
+    """gb_grouped_tuning_t: tile configuration per size class."""
+    _fields_ = [("config", ctypes.c_int32 * GROUPED_CLASSES)]
+
+    def as_list(self):
+        return list(self.config)
+
+    @classmethod
+    def from_list(cls, cfg):
+        t = cls()
+        for i, c in enumerate(cfg):
+            t.config[i] = int(c)
+        return t
+
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "gb_status_string": (ctypes.c_char_p, [c_int]),
@@ -49,8 +75,16 @@ SIGNATURES = {
     "gb_gemm_f32": (c_int, [c_int, c_int, c_i64, c_i64, c_i64, c_float, c_vp, c_i64, c_vp, c_i64,
                             c_float, c_vp, c_i64, c_vp]),
     "gb_plan_ozaki": (c_int, [c_i64, c_i64, c_i64, c_int, ctypes.POINTER(OzakiPlan)]),
+    "gb_gemm_adjoint_f32": (c_int, [c_i64, c_i64, c_i64, c_vp, c_i64, c_vp, c_i64, c_vp, c_i64, c_vp, c_i64,
+                                    c_vp, c_i64, c_vp]),
     "gb_last_ozaki_plan": (c_int, [ctypes.POINTER(OzakiPlan)]),
     "gb_kernel_kind_name": (ctypes.c_char_p, [c_int]),
+    "gb_grouped_default_tuning": (c_int, [c_int, ctypes.POINTER(Tuning)]),
+    "gb_grouped_workspace_size": (ctypes.c_size_t, [c_int]),
+    "gb_gemm_grouped_f64": (c_int, [c_vp, c_int, ctypes.POINTER(Tuning), c_vp, ctypes.c_size_t, c_vp]),
+    "gb_gemm_grouped_f32": (c_int, [c_vp, c_int, ctypes.POINTER(Tuning), c_vp, ctypes.c_size_t, c_vp]),
+    "gb_autotune_grouped": (c_int, [c_int, ctypes.POINTER(Problem), c_int, c_int, ctypes.POINTER(Tuning),
+                                    ctypes.POINTER(ctypes.c_float), c_vp]),
     "gb_launch_counts": (c_int, [ctypes.POINTER(ctypes.c_longlong), c_int]),
     "gb_profile_start": (c_int, []),
     "gb_profile_stop": (c_int, [ctypes.POINTER(c_double), ctypes.POINTER(ctypes.c_longlong), c_int]),

@@ -185,3 +185,76 @@ class profile:
                 self.ms[name] = ms[i]
                 self.launches[name] = ln[i]
         return False
+
+
+def gemm_adjoint_(dA, dB, A, B, dC):
+    """dA = dC @ B^T and dB = A^T @ dC in one tensor-core launch (float32, 3xBF16 split).
+
+    The pullback of C = A @ B (the rrule of jBLAS's jmul!/gemm!).  Inputs may be any
+    2-D float32 CUDA tensors (copied to column-major if needed); dA and dB must be
+    column-major and are overwritten."""
+    for t in (dA, dB, A, B, dC):
+        if t.dtype != torch.float32:
+            raise TypeError("the adjoint kernel computes in float32")
+    M, K = A.shape
+    K2, N = B.shape
+    if K2 != K or tuple(dC.shape) != (M, N) or tuple(dA.shape) != (M, K) or tuple(dB.shape) != (K, N):
+        raise DimensionMismatch("A %s, B %s, dC %s, dA %s, dB %s" % (tuple(A.shape), tuple(B.shape),
+                                tuple(dC.shape), tuple(dA.shape), tuple(dB.shape)))
+
+    def colmajor(X, name, out=False):
+        S, ld, tr = _storage(X, name, allow_copy=not out)
+        if tr:
+            if out:
+                raise ValueError("%s must be column-major (stride (1, ld))" % name)
+            S = X.t().contiguous().t()
+            ld = max(1, X.shape[0])
+        return S, ld
+
+    As, lda = colmajor(A, "A")
+    Bs, ldb = colmajor(B, "B")
+    Cs, ldc = colmajor(dC, "dC")
+    dAs, ldda = colmajor(dA, "dA", out=True)
+    dBs, lddb = colmajor(dB, "dB", out=True)
+    st = ctypes.c_void_p(torch.cuda.current_stream(A.device).cuda_stream)
+    rc = _lib.lib().gb_gemm_adjoint_f32(M, N, K, ctypes.c_void_p(As.data_ptr()), lda,
+                                        ctypes.c_void_p(Bs.data_ptr()), ldb, ctypes.c_void_p(Cs.data_ptr()),
+                                        ldc, ctypes.c_void_p(dAs.data_ptr()), ldda,
+                                        ctypes.c_void_p(dBs.data_ptr()), lddb, st)
+    check(rc, "gb_gemm_adjoint_f32")
+    return dA, dB
+
+
+def _empty_colmajor(rows, cols, like):
+    return torch.empty((cols, rows), dtype=like.dtype, device=like.device).t()
+
+
+class GemmFunction(torch.autograd.Function):
+    """C = A @ B with the gbblas kernels forward and backward.
+
+    The PyTorch counterpart of registering an rrule for gemm!: forward is the native
+    jmul! chain (float32) or the Ozaki path (float64); backward is the fused adjoint
+    kernel (float32) or two Ozaki products (float64)."""
+
+    @staticmethod
+    def forward(ctx, A, B):
+        ctx.save_for_backward(A, B)
+        C = _empty_colmajor(A.shape[0], B.shape[1], A)
+        return gemm_(C, A, B, mode="native" if A.dtype == torch.float32 else "ozaki")
+
+    @staticmethod
+    def backward(ctx, dC):
+        A, B = ctx.saved_tensors
+        dA = _empty_colmajor(A.shape[0], A.shape[1], A)
+        dB = _empty_colmajor(B.shape[0], B.shape[1], B)
+        if A.dtype == torch.float32:
+            gemm_adjoint_(dA, dB, A, B, dC.to(torch.float32))
+        else:
+            gemm_(dA, dC, B.t(), mode="ozaki")
+            gemm_(dB, A.t(), dC, mode="ozaki")
+        return dA, dB
+
+
+def gemm_autograd(A, B):
+    """Differentiable A @ B through GemmFunction."""
+    return GemmFunction.apply(A, B)
