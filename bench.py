@@ -48,6 +48,9 @@ def parse_args():
     p.add_argument("--no-native", action="store_true", help="skip the native FP64 comparison")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU sample")
+    p.add_argument("--workload", choices=["ozaki", "native", "grouped", "adjoint"], default="ozaki",
+                   help="ozaki: the headline (default); native: FP64/FP32 sweep; grouped: 4096 uneven "
+                        "problems; adjoint: fused dA/dB")
     return p.parse_args()
 
 
@@ -195,6 +198,156 @@ def reference_arm(args, rank, world):
     return 0
 
 
+def _event_ms(fn, steps, stream):
+    import torch
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def _side_line(args, metric, value, unit, ms, config, extra):
+    line = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "data": "synthetic", "config": config}
+    line.update(extra)
+    print(json.dumps(line), flush=True)
+
+
+def workload_native(args):
+    """Config-2 sweep: native FP64 / FP32 GEMM, alpha = 1.5, beta = 0.5, uniform[-1, 1)."""
+    import torch
+    import gbblas
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev)
+    shapes = [(n, n, n) for n in (1024, 2048, 4096, 8192, 16384)] + [(16384, 64, 16384), (64, 16384, 16384)]
+    rows = []
+    for dt in (torch.float64, torch.float32):
+        for (M, N, K) in shapes:
+            if dt == torch.float64 and M * N * K > 8192 ** 3 and args.steps > 1:
+                steps = 1
+            else:
+                steps = args.steps
+            A = torch.rand((K, M), dtype=dt, device=dev).t() * 2 - 1
+            B = torch.rand((N, K), dtype=dt, device=dev).t() * 2 - 1
+            C = torch.rand((N, M), dtype=dt, device=dev).t() * 2 - 1
+            A, B, C = (x.t().contiguous().t() for x in (A, B, C))
+            gbblas.gemm_(C, A, B, 1.5, 0.5)
+            torch.cuda.synchronize()
+            ms = _event_ms(lambda: gbblas.gemm_(C, A, B, 1.5, 0.5), steps, stream)
+            rows.append({"dtype": str(dt).replace("torch.", ""), "M": M, "N": N, "K": K, "ms": ms,
+                         "tflops": 2.0 * M * N * K / (ms * 1e-3) / 1e12})
+            del A, B, C
+    f64 = [r for r in rows if r["dtype"] == "float64" and r["M"] == r["N"] == r["K"] == 8192][0]
+    _side_line(args, "native FP64 GEMM TFLOP/s (CUDA cores, jmul! FMA order)", f64["tflops"], "TFLOP/s",
+               f64["ms"], {"workload": "native_gemm_sweep", "alpha": 1.5, "beta": 0.5,
+                           "headline_shape": "f64 8192^3"},
+               {"dtype": "f64", "sweep": rows,
+                "roofline": {"bound": "fp64_pipe", "achieved": f64["tflops"], "peak": 1.25, "unit": "TFLOP/s",
+                             "frac": f64["tflops"] / 1.25, "peak_source": "nominal GB300 FP64 (not in the measured "
+                                                                           "peaks file)"}})
+    return 0
+
+
+def workload_grouped(args):
+    """Config 4: 4096 problems, m, n, k log-uniform in [8, 512], one persistent grouped launch in a
+    CUDA graph with autotuned tiles, against a loop of plain per-problem launches."""
+    import torch
+    import gbblas
+    from gbblas import grouped, workloads
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev)
+    sizes = [tuple(int(x) for x in r) for r in workloads.grouped_sizes(4096)]
+    out = {}
+    for dt in (torch.float64, torch.float32):
+        As, Bs, Cs = [], [], []
+        for m, n, k in sizes:
+            As.append((torch.rand((k, m), dtype=dt, device=dev) * 2 - 1).t())
+            Bs.append((torch.rand((n, k), dtype=dt, device=dev) * 2 - 1).t())
+            Cs.append(torch.empty((n, m), dtype=dt, device=dev).t())
+        plan = grouped.GroupedGemm(As, Bs, Cs)
+        flops = plan.flops()
+        default_ms = _event_ms(plan.run, max(1, args.steps), stream)
+        cache = os.path.join(ROOT, "gpurun_out", "grouped_tuning.json")
+        tuning, class_ms = grouped.autotune(plan, reps=3, cache=cache)
+        plan.tuning = tuning
+        graph = plan.capture()
+        for _ in range(args.warmup):
+            graph.replay()
+        torch.cuda.synchronize()
+        graph_ms = _event_ms(graph.replay, args.steps, stream)
+
+        def loop():
+            for A, B, C in zip(As, Bs, Cs):
+                gbblas.gemm_(C, A, B)
+        loop()
+        torch.cuda.synchronize()
+        loop_ms = _event_ms(loop, 1, stream)            # eager: 4096 C-ABI calls from the host
+        g2 = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g2):
+            loop()                                      # the same 4096 launches, replayed as a graph
+        g2.replay()
+        torch.cuda.synchronize()
+        loop_graph_ms = _event_ms(g2.replay, args.steps, stream)
+        out[str(dt).replace("torch.", "")] = {
+            "flops": flops, "graph_ms": graph_ms, "graph_tflops": flops / (graph_ms * 1e-3) / 1e12,
+            "default_tuning_ms": default_ms, "loop_ms": loop_ms, "loop_graph_ms": loop_graph_ms,
+            "loop_graph_tflops": flops / (loop_graph_ms * 1e-3) / 1e12,
+            "speedup_vs_loop_graph": loop_graph_ms / graph_ms, "tuning": tuning.as_list(),
+            "class_ms": class_ms}
+        del g2
+        del As, Bs, Cs, plan, graph
+    f64 = out["float64"]
+    _side_line(args, "grouped FP64 GEMM TFLOP/s, 4096 uneven problems, one persistent launch in a CUDA graph",
+               f64["graph_tflops"], "TFLOP/s", f64["graph_ms"],
+               {"workload": "grouped_4096_loguniform_8_512", "count": 4096, "alpha": 1.0, "beta": 0.0},
+               {"dtype": "f64", "results": out,
+                "roofline": {"bound": "fp64_pipe", "achieved": f64["graph_tflops"], "peak": 1.25, "unit": "TFLOP/s",
+                             "frac": f64["graph_tflops"] / 1.25, "peak_source": "nominal GB300 FP64"},
+                "gpu_launches": 2 * args.steps})
+    return 0
+
+
+def workload_adjoint(args):
+    """Config 5: loss = sum(W .* (A*B)), A 4096x2048, B 2048x4096, W 4096x4096 N(0,1) float32:
+    dA = W B^T and dB = A^T W in one launch (3xBF16 split, FP32 accumulation)."""
+    import torch
+    import gbblas
+    from gbblas import workloads
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev)
+    M, K, N = 4096, 2048, 4096
+
+    def dev_cm(x):
+        return torch.from_numpy(np.ascontiguousarray(x.T)).to(dev).t()
+    A = dev_cm(workloads.normal(M, K, stream=51))
+    B = dev_cm(workloads.normal(K, N, stream=52))
+    W = dev_cm(workloads.normal(M, N, stream=53))
+    dA = torch.empty((K, M), dtype=torch.float32, device=dev).t()
+    dB = torch.empty((N, K), dtype=torch.float32, device=dev).t()
+    for _ in range(args.warmup):
+        gbblas.gemm_adjoint_(dA, dB, A, B, W)
+    torch.cuda.synchronize()
+    with gbblas.profile() as prof:
+        ms = _event_ms(lambda: gbblas.gemm_adjoint_(dA, dB, A, B, W), args.steps, stream)
+    useful = 2 * 2.0 * M * N * K
+    tensor = 3 * useful
+    mma_ms = prof.ms.get("adjoint_mma", float("nan")) / max(1, prof.launches.get("adjoint_mma", 1))
+    peaks, src = load_peaks()
+    achieved = tensor / (mma_ms * 1e-3) / 1e12
+    _side_line(args, "adjoint dA = dC*B^T and dB = A^T*dC (one launch) TFLOP/s", useful / (ms * 1e-3) / 1e12,
+               "TFLOP/s", ms, {"workload": "adjoint_4096x2048x4096_f32", "M": M, "K": K, "N": N,
+                                "split": "3xBF16, FP32 accumulation"},
+               {"dtype": "f32", "kernel_ms_per_step": {k: v / args.steps for k, v in prof.ms.items()},
+                "roofline": {"bound": "tensor", "achieved": achieved, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
+                             "frac": achieved / peaks["bf16_tflops"], "peak_source": "%s bf16_tflops" % src,
+                             "work": "BF16 tensor flops = 3 products x 2 outputs x 2*M*N*K"}})
+    return 0
+
+
 def main():
     args = parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -202,6 +355,11 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         return reference_arm(args, rank, world)
+    if args.workload != "ozaki":
+        import __graft_entry__  # noqa: F401  (path setup only)
+        if rank != 0:
+            return 0
+        return {"native": workload_native, "grouped": workload_grouped, "adjoint": workload_adjoint}[args.workload](args)
 
     import torch
     import gbblas

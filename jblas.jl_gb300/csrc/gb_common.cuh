@@ -82,7 +82,7 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
   uint32_t spins = 0;
   while (true) {
     if (mbar_try_wait(bar, parity)) return true;
-    if ((++spins & 255u) == 0) {
+    if ((++spins & 15u) == 0) {
       if (*abort) return false;
       if (globaltimer_ns() - t0 > limit_ns) {
         report_error(st, GB_ERR_PIPELINE_TIMEOUT, where);

@@ -23,6 +23,9 @@ constexpr int TC_STAGE_BYTES = TC_A_BYTES + TC_B_BYTES;
 constexpr int TC_TMEM_COLS = 512;               // two 128 x 256 FP32 accumulators
 constexpr int TC_SMEM_BYTES = TC_STAGES * TC_STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
 constexpr int EXP_NONFINITE = 0x7FFFFFFF;
+// Cleanup waits after an abort (copies and MMAs already in flight) use their own limit,
+// independent of the caller's, so that TMEM and shared memory are never released early.
+constexpr uint64_t TC_CLEANUP_WAIT_NS = 2000000000ull;
 
 // Tile raster: bands of 16 row tiles, column tiles inside a band (keeps the concurrently
 // active A and B panels of one plane pair inside L2).
@@ -133,7 +136,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         for (int i = 0; i < TC_STAGES; ++i)
           if (issued_parity[i] >= 0) {
             volatile int no_abort = 0;
-            mbar_wait_bounded(&full[i], static_cast<uint32_t>(issued_parity[i]), prm.wait_limit_ns,
+            mbar_wait_bounded(&full[i], static_cast<uint32_t>(issued_parity[i]), TC_CLEANUP_WAIT_NS,
                               &no_abort, nullptr, 0);
           }
       }
@@ -196,7 +199,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         // wait for every MMA issued so far before TMEM is released
         tc_commit(drain);
         volatile int no_abort = 0;
-        mbar_wait_bounded(drain, 0, prm.wait_limit_ns, &no_abort, nullptr, 0);
+        mbar_wait_bounded(drain, 0, TC_CLEANUP_WAIT_NS, &no_abort, nullptr, 0);
       }
     }
   } else {
