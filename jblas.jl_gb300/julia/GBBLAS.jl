@@ -1,0 +1,144 @@
+"""
+    GBBLAS
+
+Julia front end of libgbblas (the GB300 GEMM behind jBLAS.jl's `jmul!`).  A thin `ccall`
+layer over the C ABI in `include/gbblas.h`:
+
+    jmul!(D, A, X)                 D = A * X, jBLAS's per-element FMA order (src/gemm.jl:244)
+    gemm!(C, A, B)                 the same call spelled as in the task (`jmul!` semantics)
+    gemm!(C, A, B, α, β; mode, slices)   BLAS-3 form; mode = :native | :ozaki
+    gemm_adjoint!(dA, dB, A, B, dC)      dA = dC*B', dB = A'*dC in one launch (Float32)
+    ChainRulesCore.rrule(::typeof(gemm), A, B)   pullback through gemm_adjoint!
+
+Matrices are device arrays (anything with `pointer` to CUDA device memory and a column-
+major layout, e.g. CUDA.jl's `CuArray`); `stream` defaults to the task-local stream of
+CUDA.jl when that package is loaded, else the legacy default stream (C_NULL).
+"""
+module GBBLAS
+
+const libgbblas = get(ENV, "GBBLAS_LIB", joinpath(@__DIR__, "..", "lib", "libgbblas.so"))
+
+const GB_OK = Cint(0)
+const MODE = Dict(:native => Cint(0), :ozaki => Cint(1), :ozaki_bf16 => Cint(1), :ozaki_int8 => Cint(2))
+
+struct GBError <: Exception
+    status::Cint
+end
+Base.showerror(io::IO, e::GBError) =
+    print(io, "gbblas: ", unsafe_string(ccall((:gb_status_string, libgbblas), Cstring, (Cint,), e.status)),
+          " (status ", e.status, ")")
+
+check(st::Cint) = st == GB_OK ? nothing : throw(GBError(st))
+
+# Stream handle: CUDA.jl's current stream if the package is present, otherwise NULL.
+current_stream() = isdefined(Main, :CUDA) ? Base.unsafe_convert(Ptr{Cvoid}, Main.CUDA.stream().handle) : C_NULL
+
+ld(X::AbstractMatrix) = max(1, stride(X, 2))
+
+"""
+    jmul!(D, A, X) -> D
+
+`D = A * X` for `A` (M×N), `X` (N×P), the reference's argument order and naming (N is the
+contraction dimension).  Results equal jBLAS's FMA chain bit for bit, every element
+written.
+"""
+function jmul!(D::AbstractMatrix{Float64}, A::AbstractMatrix{Float64}, X::AbstractMatrix{Float64})
+    M, N = size(A); P = size(X, 2)
+    size(X, 1) == N && size(D) == (M, P) || throw(DimensionMismatch("jmul!: $(size(D)) = $(size(A)) * $(size(X))"))
+    check(ccall((:gb_gemm_f64, libgbblas), Cint,
+                (Cint, Cint, Int64, Int64, Int64, Cdouble, Ptr{Cdouble}, Int64, Ptr{Cdouble}, Int64, Cdouble,
+                 Ptr{Cdouble}, Int64, Cint, Cint, Ptr{Cdouble}, Ptr{Cvoid}),
+                0, 0, M, P, N, 1.0, pointer(A), ld(A), pointer(X), ld(X), 0.0, pointer(D), ld(D),
+                MODE[:native], 0, C_NULL, current_stream()))
+    D
+end
+function jmul!(D::AbstractMatrix{Float32}, A::AbstractMatrix{Float32}, X::AbstractMatrix{Float32})
+    M, N = size(A); P = size(X, 2)
+    size(X, 1) == N && size(D) == (M, P) || throw(DimensionMismatch("jmul!: $(size(D)) = $(size(A)) * $(size(X))"))
+    check(ccall((:gb_gemm_f32, libgbblas), Cint,
+                (Cint, Cint, Int64, Int64, Int64, Cfloat, Ptr{Cfloat}, Int64, Ptr{Cfloat}, Int64, Cfloat,
+                 Ptr{Cfloat}, Int64, Ptr{Cvoid}),
+                0, 0, M, P, N, 1f0, pointer(A), ld(A), pointer(X), ld(X), 0f0, pointer(D), ld(D),
+                current_stream()))
+    D
+end
+
+"""
+    gemm!(C, A, B) -> C                      same as jmul!(C, A, B)
+    gemm!(C, A, B, α, β; mode=:native, slices=0) -> C
+
+`C = α A B + β C`.  `mode = :ozaki` (Float64) emulates FP64 on the BF16 tensor cores with
+`slices` digit planes (0 = the library picks the count for its normwise tolerance).
+"""
+gemm!(C, A, B) = jmul!(C, A, B)
+function gemm!(C::AbstractMatrix{Float64}, A::AbstractMatrix{Float64}, B::AbstractMatrix{Float64}, α::Real, β::Real;
+               mode::Symbol = :native, slices::Integer = 0)
+    M, K = size(A); N = size(B, 2)
+    size(B, 1) == K && size(C) == (M, N) || throw(DimensionMismatch("gemm!"))
+    check(ccall((:gb_gemm_f64, libgbblas), Cint,
+                (Cint, Cint, Int64, Int64, Int64, Cdouble, Ptr{Cdouble}, Int64, Ptr{Cdouble}, Int64, Cdouble,
+                 Ptr{Cdouble}, Int64, Cint, Cint, Ptr{Cdouble}, Ptr{Cvoid}),
+                0, 0, M, N, K, α, pointer(A), ld(A), pointer(B), ld(B), β, pointer(C), ld(C),
+                MODE[mode], slices, C_NULL, current_stream()))
+    C
+end
+function gemm!(C::AbstractMatrix{Float32}, A::AbstractMatrix{Float32}, B::AbstractMatrix{Float32}, α::Real, β::Real)
+    M, K = size(A); N = size(B, 2)
+    size(B, 1) == K && size(C) == (M, N) || throw(DimensionMismatch("gemm!"))
+    check(ccall((:gb_gemm_f32, libgbblas), Cint,
+                (Cint, Cint, Int64, Int64, Int64, Cfloat, Ptr{Cfloat}, Int64, Ptr{Cfloat}, Int64, Cfloat,
+                 Ptr{Cfloat}, Int64, Ptr{Cvoid}),
+                0, 0, M, N, K, α, pointer(A), ld(A), pointer(B), ld(B), β, pointer(C), ld(C), current_stream()))
+    C
+end
+
+"""
+    gemm_adjoint!(dA, dB, A, B, dC) -> (dA, dB)
+
+`dA = dC * B'` and `dB = A' * dC` (Float32) in one tensor-core launch, 3xBF16 split with
+FP32 accumulation.
+"""
+function gemm_adjoint!(dA::AbstractMatrix{Float32}, dB::AbstractMatrix{Float32}, A::AbstractMatrix{Float32},
+                       B::AbstractMatrix{Float32}, dC::AbstractMatrix{Float32})
+    M, K = size(A); N = size(B, 2)
+    check(ccall((:gb_gemm_adjoint_f32, libgbblas), Cint,
+                (Int64, Int64, Int64, Ptr{Cfloat}, Int64, Ptr{Cfloat}, Int64, Ptr{Cfloat}, Int64, Ptr{Cfloat}, Int64,
+                 Ptr{Cfloat}, Int64, Ptr{Cvoid}),
+                M, N, K, pointer(A), ld(A), pointer(B), ld(B), pointer(dC), ld(dC), pointer(dA), ld(dA),
+                pointer(dB), ld(dB), current_stream()))
+    dA, dB
+end
+
+"""
+    gemm(A, B)
+
+Allocating product for use with automatic differentiation: the `rrule` below returns
+the pullback computed by `gemm_adjoint!` (Float32) or two Ozaki products (Float64).
+"""
+gemm(A::AbstractMatrix, B::AbstractMatrix) = jmul!(similar(A, size(A, 1), size(B, 2)), A, B)
+
+# ChainRulesCore is optional: the rrule is defined when the package is available.
+if Base.find_package("ChainRulesCore") !== nothing
+    import ChainRulesCore
+    function ChainRulesCore.rrule(::typeof(gemm), A::AbstractMatrix{Float32}, B::AbstractMatrix{Float32})
+        C = gemm(A, B)
+        function gemm_pullback(ΔC)
+            dC = convert(typeof(C), ChainRulesCore.unthunk(ΔC))
+            dA, dB = gemm_adjoint!(similar(A), similar(B), A, B, dC)
+            return ChainRulesCore.NoTangent(), dA, dB
+        end
+        return C, gemm_pullback
+    end
+    function ChainRulesCore.rrule(::typeof(gemm), A::AbstractMatrix{Float64}, B::AbstractMatrix{Float64})
+        C = gemm(A, B)
+        function gemm_pullback(ΔC)
+            dC = convert(typeof(C), ChainRulesCore.unthunk(ΔC))
+            dA = gemm!(similar(A), dC, permutedims(B), 1.0, 0.0; mode = :ozaki)
+            dB = gemm!(similar(B), permutedims(A), dC, 1.0, 0.0; mode = :ozaki)
+            return ChainRulesCore.NoTangent(), dA, dB
+        end
+        return C, gemm_pullback
+    end
+end
+
+end # module
