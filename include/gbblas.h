@@ -163,6 +163,21 @@ int gb_gemm_grouped_f64(const gb_problem_t* problems, int count, const gb_groupe
                         void* workspace, size_t workspace_bytes, void* stream);
 int gb_gemm_grouped_f32(const gb_problem_t* problems, int count, const gb_grouped_tuning_t* tuning,
                         void* workspace, size_t workspace_bytes, void* stream);
+/* Allocation-free grouped FP64 GEMM.  No counterpart in the reference (jBLAS never
+ * allocates because it only multiplies static-size arrays on the CPU).  For callers that
+ * cannot allocate device memory when they multiply: code issuing work while a CUDA graph
+ * capture in global mode is open (cudaMalloc is illegal there), threads that must not
+ * block on the implicit device synchronisation of cudaMalloc/cudaFree, and hosts whose
+ * device memory is entirely owned by another runtime.  The tile prefix sums live in a
+ * file-scope device array of GB_GROUPED_NOALLOC_MAX + 1 int64 (512 KiB), which every GPU
+ * that loads the library keeps until the process exits.  count above the maximum gives
+ * GB_ERR_INVALID_VALUE.  The first call on a device looks the array's device address up
+ * (cudaGetSymbolAddress, no allocation); make that first call before any stream capture.
+ * Every call shares the one array: calls that overlap on the GPU (other streams, other
+ * threads) race and must be serialised by the caller.  Results equal gb_gemm_grouped_f64's. */
+#define GB_GROUPED_NOALLOC_MAX 65536
+int gb_gemm_grouped_f64_noalloc(const gb_problem_t* problems, int count, const gb_grouped_tuning_t* tuning,
+                                void* stream);
 /* Autotuner: times every configuration per size class on the given problems (HOST copy
  * of the table; their C buffers are left untouched, results go to scratch) with `reps`
  * timed repetitions and writes the fastest configuration per class; class_ms (may be

@@ -563,6 +563,11 @@ int gb_gemm_grouped_f32(const gb_problem_t* problems, int count, const gb_groupe
   return grouped_call(4, problems, count, tuning, workspace, workspace_bytes, stream);
 }
 
+int gb_gemm_grouped_f64_noalloc(const gb_problem_t* problems, int count, const gb_grouped_tuning_t* tuning,
+                                void* stream) {
+  return grouped_f64_noalloc(problems, count, tuning, static_cast<cudaStream_t>(stream));
+}
+
 int gb_autotune_grouped(int dtype_bytes, const gb_problem_t* host_problems, int count, int reps,
                         gb_grouped_tuning_t* out, float* class_ms, void* stream) {
   if (!out || count < 0 || (count > 0 && !host_problems) || (dtype_bytes != 4 && dtype_bytes != 8))

@@ -16,6 +16,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "gb_common.cuh"
@@ -311,6 +312,73 @@ int grouped_autotune(int dtype_bytes, const gb_problem_t* h_probs, int count, in
   cudaFreeAsync(d_off, s);
   if (rc == GB_OK) *out = best;
   return rc;
+}
+
+}  // namespace gb
+
+// ============================================================ allocation-free variant
+//
+// For callers that cannot allocate device memory at call time (see gbblas.h): the tile
+// prefix sums live in a fixed file-scope device array instead of pool or caller memory.
+// Every GPU that loads the library holds this array until the process exits.
+namespace gb {
+
+constexpr int GROUPED_NOALLOC_MAX = GB_GROUPED_NOALLOC_MAX;
+constexpr int NOALLOC_MAX_DEVICES = 64;
+
+static __device__ __align__(256) long long g_noalloc_offsets[GROUPED_NOALLOC_MAX + 1];
+
+// Device address of g_noalloc_offsets per device.  In host code the symbol names a host
+// stand-in, so the address is looked up once per device (with that device current) and
+// reused; the lookup neither allocates nor launches.
+static std::mutex g_noalloc_mu;
+static long long* g_noalloc_ptr[NOALLOC_MAX_DEVICES];
+static int g_noalloc_sms[NOALLOC_MAX_DEVICES];
+
+static int noalloc_setup(long long** ptr, int* sms) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return gb_set_cuda_error(e, "cudaGetDevice");
+  if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return GB_ERR_UNSUPPORTED;
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    int major = 0, minor = 0, n = 0;
+    e = cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return gb_set_cuda_error(e, "device attributes");
+    if (major != 10 || minor != 3) return GB_ERR_NO_DEVICE;
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_offsets);
+    if (e != cudaSuccess) return gb_set_cuda_error(e, "cudaGetSymbolAddress(g_noalloc_offsets)");
+    g_noalloc_sms[dev] = n;
+    g_noalloc_ptr[dev] = static_cast<long long*>(p);
+  }
+  *ptr = g_noalloc_ptr[dev];
+  *sms = g_noalloc_sms[dev];
+  return GB_OK;
+}
+
+int grouped_f64_noalloc(const gb_problem_t* d_probs, int count, const gb_grouped_tuning_t* tuning, cudaStream_t s) {
+  if (count < 0 || count > GROUPED_NOALLOC_MAX) return GB_ERR_INVALID_VALUE;
+  long long* offsets = nullptr;
+  int sms = 0;
+  int rc = noalloc_setup(&offsets, &sms);
+  if (rc) return rc;
+  if (count == 0) return GB_OK;
+  const gb_grouped_tuning_t t = tuning ? *tuning : grouped_default_tuning(8);
+  rc = grouped_validate_tuning(8, t);
+  if (rc) return rc;
+  // The prologue rewrites offsets[0..count] on every call, so nothing needs clearing.
+  // Launched directly (not through the tracing layer, which creates CUDA events while
+  // profiling is on).
+  grouped_prefix_kernel<<<1, 1024, 0, s>>>(d_probs, count, t, offsets);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return gb_set_cuda_error(e, "grouped prologue launch");
+  grouped_gemm_kernel<double><<<grid_for<double>(sms), GROUPED_THREADS, 0, s>>>(d_probs, count, t, offsets);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return gb_set_cuda_error(e, "grouped launch");
+  return GB_OK;
 }
 
 }  // namespace gb

@@ -14,4 +14,5 @@ int grouped_launch(int dtype_bytes, const gb_problem_t* d_probs, int count, cons
                    long long* d_offsets, int sms, cudaStream_t s);
 int grouped_autotune(int dtype_bytes, const gb_problem_t* h_probs, int count, int sms, cudaMemPool_t pool,
                      int reps, gb_grouped_tuning_t* out, float* class_ms, cudaStream_t s);
+int grouped_f64_noalloc(const gb_problem_t* d_probs, int count, const gb_grouped_tuning_t* tuning, cudaStream_t s);
 }  // namespace gb

@@ -83,6 +83,7 @@ SIGNATURES = {
     "gb_grouped_workspace_size": (ctypes.c_size_t, [c_int]),
     "gb_gemm_grouped_f64": (c_int, [c_vp, c_int, ctypes.POINTER(Tuning), c_vp, ctypes.c_size_t, c_vp]),
     "gb_gemm_grouped_f32": (c_int, [c_vp, c_int, ctypes.POINTER(Tuning), c_vp, ctypes.c_size_t, c_vp]),
+    "gb_gemm_grouped_f64_noalloc": (c_int, [c_vp, c_int, ctypes.POINTER(Tuning), c_vp]),
     "gb_autotune_grouped": (c_int, [c_int, ctypes.POINTER(Problem), c_int, c_int, ctypes.POINTER(Tuning),
                                     ctypes.POINTER(ctypes.c_float), c_vp]),
     "gb_launch_counts": (c_int, [ctypes.POINTER(ctypes.c_longlong), c_int]),
