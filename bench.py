@@ -44,6 +44,7 @@ def parse_args():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["gbblas", "reference"], default="gbblas")
     p.add_argument("--size", type=int, default=8192)
+    p.add_argument("--mnk", type=str, default=None, help="M,N,K override of --size (profiling cases)")
     p.add_argument("--slices", type=int, default=0, help="0 = automatic (library tolerance)")
     p.add_argument("--no-native", action="store_true", help="skip the native FP64 comparison")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
@@ -387,6 +388,8 @@ def main():
 
     n = args.size
     M = N = K = n
+    if args.mnk:
+        M, N, K = (int(x) for x in args.mnk.split(","))
     flops = 2.0 * M * N * K
     A_h = np.asfortranarray(workloads.ozaki_matrix(M, K, per="row", stream=1 + 2 * rank))
     B_h = np.asfortranarray(workloads.ozaki_matrix(K, N, per="col", stream=2 + 2 * rank))
@@ -457,7 +460,7 @@ def main():
         timed_s = ms_step * args.steps / 1e3
         peak_key = "bf16_tflops_sustained" if timed_s >= 1.0 else "bf16_tflops"
         achieved = plan["flops_tensor"] / (mma_ms * 1e-3) / 1e12
-        traffic = committed_traffic("%d" % n)
+        traffic = committed_traffic("%d" % n) if not args.mnk else None
 
         # ------------------------------------------------------------ accuracy and native
         import oracle
@@ -490,7 +493,8 @@ def main():
             "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "ozaki_fp64_gemm_%d^3" % n, "M": M, "N": N, "K": K,
+            "config": {"workload": ("ozaki_fp64_gemm_%d^3" % n) if not args.mnk else
+                       "ozaki_fp64_gemm_%dx%dx%d" % (M, N, K), "M": M, "N": N, "K": K,
                        "distribution": "sign*U[1,2)*2^(e_line+e_elem), e_line in [-30,30] per row/col, "
                                        "e_elem in [-8,8]",
                        "slices": plan["slices"], "bits": plan["bits"], "slice_products": plan["products"],
