@@ -308,18 +308,32 @@ static int ozaki_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int
     }
     const BoundStats bst = bound_stats(h);
     if (slices == 0) {
+      // Cheapest plan (slices, K chunking -> digit width) whose bound meets the tolerance.
       const double tol = ozaki_tolerance();
-      s_use = OZ_MAX_SLICES;
-      for (int cand = 1; cand <= OZ_MAX_SLICES; ++cand) {
-        OzPlan p;
-        if (oz_make_plan(M, N, K, cand, &p)) break;
-        if (ozaki_bound(bst, K, p) <= tol) {
-          s_use = cand;
-          break;
+      double best_cost = 0.0;
+      bool found = false;
+      for (int chunks = 1; chunks <= 8; chunks *= 2) {
+        for (int cand = 1; cand <= OZ_MAX_SLICES; ++cand) {
+          OzPlan p;
+          if (oz_make_plan_chunks(M, N, K, cand, chunks, &p)) break;
+          if (ozaki_bound(bst, K, p) > tol) continue;
+          const double c = oz_plan_cost(p);
+          if (!found || c < best_cost) {
+            best_cost = c;
+            plan = p;
+            found = true;
+          }
+          break;   // more slices only cost more at this chunking
         }
       }
+      if (!found) {   // tolerance out of reach: the most slices the split supports
+        rc = GB_ERR_UNSUPPORTED;
+        for (int cand = OZ_MAX_SLICES; cand >= 1 && rc; --cand) rc = oz_make_plan(M, N, K, cand, &plan);
+      }
+      s_use = plan.slices;
+    } else {
+      rc = oz_make_plan(M, N, K, s_use, &plan);
     }
-    rc = oz_make_plan(M, N, K, s_use, &plan);
     if (rc) {
       cudaFreeAsync(st_ws, s);
       return rc;

@@ -49,13 +49,20 @@ int oz_bits_for(int64_t kc) {
 }
 
 int oz_make_plan(int64_t M, int64_t N, int64_t K, int slices, OzPlan* plan) {
-  if (slices < 1 || slices > OZ_MAX_SLICES) return GB_ERR_INVALID_VALUE;
+  return oz_make_plan_chunks(M, N, K, slices, 1, plan);
+}
+
+int oz_make_plan_chunks(int64_t M, int64_t N, int64_t K, int slices, int min_chunks, OzPlan* plan) {
+  if (slices < 1 || slices > OZ_MAX_SLICES || min_chunks < 1) return GB_ERR_INVALID_VALUE;
   OzPlan& P = *plan;
   P.slices = slices;
-  // One exact chunk covers K up to 2^16 (b >= 5); longer K is cut into equal chunks.
+  // One exact chunk covers K up to 2^16 (b >= 5); longer K, or a requested split into
+  // min_chunks (shorter chunks allow wider digits), gives equal chunks of whole K panels.
   int64_t kb_total = (K + TC_BK - 1) / TC_BK;
   if (kb_total < 1) kb_total = 1;
   int64_t nchunks = (K + 65535) / 65536;
+  if (nchunks < min_chunks) nchunks = min_chunks;
+  if (nchunks > kb_total) nchunks = kb_total;
   if (nchunks < 1) nchunks = 1;
   int64_t kb_chunk = (kb_total + nchunks - 1) / nchunks;
   nchunks = (kb_total + kb_chunk - 1) / kb_chunk;
@@ -409,4 +416,16 @@ int oz_grid_for(int sms, int64_t M, int64_t N) {
   return static_cast<int>(tiles < sms ? tiles : sms);
 }
 
+}  // namespace gb
+
+namespace gb {
+// Relative cost of a plan for one 128 x 256 output tile: tensor work (products x K panels)
+// and FP64 drains (one per group and K chunk; a drain of a 128 x 256 FP32 group costs about
+// as much as DRAIN_PANELS K panels of MMA) overlap, so the larger dominates.
+double oz_plan_cost(const OzPlan& p) {
+  constexpr double DRAIN_PANELS = 40.0;
+  const double mma = static_cast<double>(p.products) * p.kb_total;
+  const double drain = static_cast<double>(p.groups) * p.nchunks * DRAIN_PANELS;
+  return (mma > drain ? mma : drain) + 0.1 * (mma < drain ? mma : drain);
+}
 }  // namespace gb

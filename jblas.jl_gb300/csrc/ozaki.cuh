@@ -29,6 +29,10 @@ struct OzPlan {
 int oz_bits_for(int64_t kc);
 // Builds the plan (schedule included) for a given slice count (1..OZ_MAX_SLICES).
 int oz_make_plan(int64_t M, int64_t N, int64_t K, int slices, OzPlan* plan);
+// Same, with K cut into at least `min_chunks` exact accumulation chunks (wider digits).
+int oz_make_plan_chunks(int64_t M, int64_t N, int64_t K, int slices, int min_chunks, OzPlan* plan);
+// Relative per-tile cost of a plan (tensor work vs FP64 drains), for choosing among plans.
+double oz_plan_cost(const OzPlan& p);
 
 // Per-row statistics of op(X) (rows r < R, contraction index k < K):
 // amax bits of |x| (as uint64), sum |x|, sum x^2.

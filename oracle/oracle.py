@@ -232,10 +232,14 @@ def ozaki_bits_for(kc):
     return min(9, (26 - lg) // 2)
 
 
-def ozaki_plan(K, slices):
-    """Same plan as the GPU planner: bits, K chunks of 64-wide panels, groups of pairs."""
+def ozaki_plan(K, slices, min_chunks=1):
+    """Same plan as the GPU planner: bits, K chunks of 64-wide panels, groups of pairs.
+
+    min_chunks > 1 cuts K into at least that many exact chunks (wider digits), as the
+    automatic slice choice may do."""
     kb_total = max(1, (K + 63) // 64)
-    nchunks = max(1, (K + 65535) // 65536)
+    nchunks = max(1, (K + 65535) // 65536, min_chunks)
+    nchunks = min(nchunks, kb_total)
     kb_chunk = (kb_total + nchunks - 1) // nchunks
     nchunks = (kb_total + kb_chunk - 1) // kb_chunk
     kc = kb_chunk * 64
@@ -298,13 +302,20 @@ def ozaki_split(X, slices, bits):
     return digits, e
 
 
-def ozaki_gemm(A, B, C=None, alpha=1.0, beta=0.0, slices=8):
+def chunks_for(K, k_chunk):
+    """min_chunks that reproduces a plan's K chunk (as reported by the library)."""
+    kb_total = max(1, (K + 63) // 64)
+    kb_chunk = max(1, (k_chunk + 63) // 64)
+    return max(1, (kb_total + kb_chunk - 1) // kb_chunk)
+
+
+def ozaki_gemm(A, B, C=None, alpha=1.0, beta=0.0, slices=8, min_chunks=1):
     """The GPU Ozaki result restated in numpy (A: M x K, B: K x N logical operands)."""
     A = np.asarray(A, dtype=np.float64)
     B = np.asarray(B, dtype=np.float64)
     M, K = A.shape
     N = B.shape[1]
-    plan = ozaki_plan(K, slices)
+    plan = ozaki_plan(K, slices, min_chunks)
     bits = plan["bits"]
     dA, ea = ozaki_split(A, slices, bits)
     dB, eb = ozaki_split(B.T, slices, bits)

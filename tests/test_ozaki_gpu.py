@@ -66,6 +66,20 @@ def test_transposes_and_alpha_beta(cuda, trans):
     assert_bit_equal(got, ref)
 
 
+@pytest.mark.parametrize("shape", [(300, 8192, 260), (256, 4096, 512), (130, 1000, 70)])
+def test_auto_plan_bit_exact(cuda, shape):
+    """slices = 0: the library picks slices and K chunking; the result equals the restatement
+    of the plan it reports."""
+    M, K, N = shape
+    A = np.asfortranarray(workloads.ozaki_matrix(M, K, per="row", stream=61))
+    B = np.asfortranarray(workloads.ozaki_matrix(K, N, per="col", stream=62))
+    got, bound = _run(A, B, slices=0, want_bound=True)
+    plan = gbblas.last_ozaki_plan()
+    assert bound <= 2.0 ** -50
+    ref = oracle.ozaki_gemm(A, B, slices=plan["slices"], min_chunks=oracle.chunks_for(K, plan["k_chunk"]))
+    assert_bit_equal(got, ref)
+
+
 def test_chunked_k(cuda):
     """K > 65536 takes two exact accumulation chunks per slice pair."""
     M, K, N = 64, 70000, 40
@@ -149,3 +163,24 @@ def test_int8_mode_unsupported(cuda):
     with pytest.raises(gbblas.GBError) as e:
         gbblas.gemm_(d, d, d, mode="ozaki_int8")
     assert e.value.status == gbblas._lib.GB_ERR_UNSUPPORTED
+
+
+def test_config3_8192_accuracy_beats_native(cuda):
+    """Config 3 at full size: M = N = K = 8192, sign*U[1,2)*2^(e_line + e_elem) inputs, slices
+    chosen by the library; normwise error (4096 Dot2-sampled entries) below the bound and
+    below the native FP64 kernel's on the same inputs."""
+    n = 8192
+    A = np.asfortranarray(workloads.ozaki_matrix(n, n, per="row", stream=1))
+    B = np.asfortranarray(workloads.ozaki_matrix(n, n, per="col", stream=2))
+    Ad, Bd = to_dev(A), to_dev(B)
+    C = torch.empty((n, n), dtype=torch.float64, device=cuda).t()
+    _, bound = gbblas.gemm_(C, Ad, Bd, mode="ozaki", return_bound=True)
+    oz = to_host(C)
+    gbblas.gemm_(C, Ad, Bd, mode="native")
+    nat = to_host(C)
+    g = np.random.default_rng(12345)
+    rows, cols = g.integers(0, n, 4096), g.integers(0, n, 4096)
+    e_oz = _normwise_err(oz, A, B, rows, cols)
+    e_nat = _normwise_err(nat, A, B, rows, cols)
+    assert e_oz <= bound <= 2.0 ** -50
+    assert e_oz <= e_nat, (e_oz, e_nat)
