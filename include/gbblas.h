@@ -63,6 +63,12 @@ int gb_set_wait_limit_ns(uint64_t ns);
  * the default 2^-50. */
 int gb_set_ozaki_tolerance(double tol);
 
+/* K chunking used by OZAKI calls with an explicit slice count: K is cut into at least
+ * `min_chunks` exact accumulation chunks (shorter chunks allow wider digits, at the cost
+ * of more accumulator drains); 0 or 1 restores the default (one chunk up to K = 65536).
+ * slices = 0 ignores it and chooses slices and chunking together. */
+int gb_set_ozaki_min_chunks(int min_chunks);
+
 /* Returns the current device's cached workspace memory to the driver (synchronises the
  * device).  Workspace is otherwise kept between calls. */
 int gb_release_workspace(void);

@@ -40,6 +40,7 @@ namespace gb {
 
 static std::atomic<uint64_t> g_wait_limit_ns{4000000000ull};
 static std::atomic<uint64_t> g_ozaki_tol_bits{0};
+static std::atomic<int> g_ozaki_min_chunks{1};
 
 struct DeviceInfo {
   bool init = false;
@@ -332,7 +333,7 @@ static int ozaki_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int
       }
       s_use = plan.slices;
     } else {
-      rc = oz_make_plan(M, N, K, s_use, &plan);
+      rc = oz_make_plan_chunks(M, N, K, s_use, g_ozaki_min_chunks.load(), &plan);
     }
     if (rc) {
       cudaFreeAsync(st_ws, s);
@@ -340,7 +341,7 @@ static int ozaki_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int
     }
     if (err_bound_out) *err_bound_out = ozaki_bound(bst, K, plan);
   } else {
-    rc = oz_make_plan(M, N, K, s_use, &plan);
+    rc = oz_make_plan_chunks(M, N, K, s_use, g_ozaki_min_chunks.load(), &plan);
     if (rc) {
       cudaFreeAsync(st_ws, s);
       return rc;
@@ -442,6 +443,12 @@ int gb_release_workspace(void) {
   if (rc) return rc;
   GB_CUDA_TRY(cudaDeviceSynchronize());
   GB_CUDA_TRY(cudaMemPoolTrimTo(dev->pool, 0));
+  return GB_OK;
+}
+
+int gb_set_ozaki_min_chunks(int min_chunks) {
+  if (min_chunks < 0 || min_chunks > 64) return GB_ERR_INVALID_VALUE;
+  g_ozaki_min_chunks.store(min_chunks == 0 ? 1 : min_chunks);
   return GB_OK;
 }
 

@@ -38,6 +38,17 @@ __device__ __forceinline__ void tile_coords(int t, int tiles_m, int tiles_n, int
   tn = in_band / band_rows;
 }
 
+// S * 2^wexp as a double, for an FP32 value S holding an integer (|S| <= 2^24) and
+// wbias = (896 + wexp) << 23: the FP32 exponent is rebased to FP64 (bias 127 -> 1023) and
+// shifted by wexp in integer arithmetic, so no FP32->FP64 conversion runs on the FP64 pipe.
+// Exact for every such S; +-0 keeps its sign.
+__device__ __forceinline__ double exact_int_f32_times_pow2(uint32_t u, unsigned long long wbias) {
+  const unsigned long long sign = static_cast<unsigned long long>(u & 0x80000000u) << 32;
+  const uint32_t mag = u & 0x7FFFFFFFu;
+  const unsigned long long body = mag ? ((static_cast<unsigned long long>(mag) + wbias) << 29) : 0ull;
+  return __longlong_as_double(static_cast<long long>(sign | body));
+}
+
 __device__ __forceinline__ int problem_of(const TcParams& prm, int t) {
   return (prm.nprob == 2 && t >= prm.prob[1].tile_begin) ? 1 : 0;
 }
@@ -224,7 +235,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       int step = 0;
       const int nsteps = G * P.nchunks;
       for (int g = 0; g < G && ok; ++g) {
-        const double w = pow2_normal(2 - sched.level[g] * sched.bits);
+        // group weight 2^wexp folded into the exponent of each exact integer group sum
+        const int wexp = 2 - sched.level[g] * sched.bits;
+        const unsigned long long wbias = static_cast<unsigned long long>(896 + wexp) << 23;
         for (int c = 0; c < P.nchunks; ++c, ++step) {
           // the whole warp agrees before the warp-collective tcgen05.ld
           ok = __all_sync(0xffffffffu, mbar_wait_bounded(&tfull[buf], acc_phase, prm.wait_limit_ns,
@@ -267,8 +280,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             }
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
-              const double sj = static_cast<double>(__uint_as_float(v[j]));
-              tv[j] = first ? sj * w : fma(sj, w, tv[j]);
+              const double sw = exact_int_f32_times_pow2(v[j], wbias);
+              tv[j] = first ? sw : tv[j] + sw;   // == fma(S, 2^wexp, T): S * 2^wexp is exact
             }
             if (!last) {
 #pragma unroll

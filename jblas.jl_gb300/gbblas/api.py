@@ -143,6 +143,11 @@ def set_ozaki_tolerance(tol):
     check(_lib.lib().gb_set_ozaki_tolerance(float(tol)), "gb_set_ozaki_tolerance")
 
 
+def set_ozaki_min_chunks(n):
+    """K chunking for explicit-slice Ozaki calls (wider digits for n > 1); 0/1 = default."""
+    check(_lib.lib().gb_set_ozaki_min_chunks(int(n)), "gb_set_ozaki_min_chunks")
+
+
 def set_wait_limit_ns(ns):
     check(_lib.lib().gb_set_wait_limit_ns(int(ns)), "gb_set_wait_limit_ns")
 
