@@ -4,7 +4,8 @@
 //               of jBLAS's prefetch schedule, src/memory_management.jl:181-277)
 //   warp 1      allocates 512 TMEM columns; lane 0 issues tcgen05.mma 128x256x16 into a
 //               double-buffered FP32 accumulator (jBLAS's register tile, src/gemm.jl:318-333)
-//   warps 2-5   epilogue: tcgen05.ld of each finished group sum, then the fused store
+//   warps 2-9   epilogue: tcgen05.ld of each finished group sum, then the fused store; two
+//               warps per TMEM lane quadrant, each draining half of the 256 columns
 //               (jBLAS's store_block, src/gemm.jl:3-11, with recombination / alpha / beta)
 // Every mbarrier wait is bounded; on expiry the CTA records GB_ERR_PIPELINE_TIMEOUT, waits
 // (bounded) for its in-flight copies and MMAs, frees TMEM and exits.
@@ -16,7 +17,8 @@
 
 namespace gb {
 
-constexpr int TC_THREADS = 192;                 // 6 warps
+constexpr int TC_THREADS = 320;                 // 10 warps
+constexpr int TC_EPI_THREADS = 256;             // warps 2..9
 constexpr int TC_A_BYTES = TC_BM * TC_BK * 2;   // 16 KB
 constexpr int TC_B_BYTES = TC_BN * TC_BK * 2;   // 32 KB
 constexpr int TC_STAGE_BYTES = TC_A_BYTES + TC_B_BYTES;
@@ -80,7 +82,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
     for (int i = 0; i < 2; ++i) {
       mbar_init(&tfull[i], 1);
-      mbar_init(&tempty[i], 128);
+      mbar_init(&tempty[i], TC_EPI_THREADS);
     }
     mbar_init(drain, 1);
     *abort_flag = 0;
@@ -217,6 +219,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     // ------------------------------------------------------------ epilogue (warps 2..5)
     const int q = warp & 3;                 // TMEM lane quadrant of this warp
     const int row_l = q * 32 + lane;        // tile row owned by this thread
+    const int col0 = ((warp - 2) >> 2) * (TC_BN / 2);   // this warp's half of the columns
     int buf = 0;
     uint32_t acc_phase = 0;
     bool ok = true;
@@ -248,7 +251,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           const uint32_t taddr = tmem_base + (static_cast<uint32_t>(q * 32) << 16) +
                                  static_cast<uint32_t>(buf * TC_BN);
 #pragma unroll 1
-          for (int cb = 0; cb < TC_BN; cb += 32) {
+          for (int cb = col0; cb < col0 + TC_BN / 2; cb += 32) {
             uint32_t v[32];
             tmem_ld_32x32b_x32(taddr + cb, v);
             tc_wait_ld();
