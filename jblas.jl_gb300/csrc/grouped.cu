@@ -43,6 +43,14 @@ __host__ __device__ inline int size_class(int64_t m, int64_t n) {
   return d <= 16 ? 0 : d <= 32 ? 1 : d <= 64 ? 2 : d <= 128 ? 3 : d <= 256 ? 4 : 5;
 }
 
+// tuning.config[cls] without a dynamically indexed (local-memory) array
+__device__ __forceinline__ int config_of(const gb_grouped_tuning_t& t, int cls) {
+  int v = t.config[0];
+#pragma unroll
+  for (int c = 1; c < GB_GROUPED_CLASSES; ++c) v = (cls == c) ? t.config[c] : v;
+  return v;
+}
+
 template <typename T>
 __device__ __forceinline__ T fmad(T a, T b, T c);
 template <>
@@ -130,7 +138,7 @@ __global__ void __launch_bounds__(1024) grouped_prefix_kernel(const gb_problem_t
   long long sum = 0;
   for (int i = b; i < e; ++i) {
     const gb_problem_t& p = probs[i];
-    const TileCfg c = tile_cfg(tuning.config[size_class(p.m, p.n)]);
+    const TileCfg c = tile_cfg(config_of(tuning, size_class(p.m, p.n)));
     const long long tiles = (p.m <= 0 || p.n <= 0) ? 0 : ((p.m + c.bm - 1) / c.bm) * ((p.n + c.bn - 1) / c.bn);
     sum += tiles;
   }
@@ -146,7 +154,7 @@ __global__ void __launch_bounds__(1024) grouped_prefix_kernel(const gb_problem_t
   for (int i = b; i < e; ++i) {
     offsets[i] = run;
     const gb_problem_t& p = probs[i];
-    const TileCfg c = tile_cfg(tuning.config[size_class(p.m, p.n)]);
+    const TileCfg c = tile_cfg(config_of(tuning, size_class(p.m, p.n)));
     run += (p.m <= 0 || p.n <= 0) ? 0 : ((p.m + c.bm - 1) / c.bm) * ((p.n + c.bn - 1) / c.bn);
   }
   if (t == 1023) offsets[count] = part[1023];
@@ -166,7 +174,7 @@ __global__ void __launch_bounds__(GROUPED_THREADS) grouped_gemm_kernel(const gb_
       if (offsets[mid] <= w) lo = mid; else hi = mid - 1;
     }
     const gb_problem_t p = probs[lo];
-    const int cfg = tuning.config[size_class(p.m, p.n)];
+    const int cfg = config_of(tuning, size_class(p.m, p.n));
     const TileCfg c = tile_cfg(cfg);
     const long long local = w - offsets[lo];
     const int tiles_m = static_cast<int>((p.m + c.bm - 1) / c.bm);

@@ -220,6 +220,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int q = warp & 3;                 // TMEM lane quadrant of this warp
     const int row_l = q * 32 + lane;        // tile row owned by this thread
     const int col0 = ((warp - 2) >> 2) * (TC_BN / 2);   // this warp's half of the columns
+    // the per-CTA FP64 tile buffer is re-read at every drain while digit planes stream
+    // through L2: keep it resident
+    const uint64_t keep = l2_policy_evict_last();
     int buf = 0;
     uint32_t acc_phase = 0;
     bool ok = true;
@@ -279,7 +282,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             double tv[32];
             if (!first) {
 #pragma unroll
-              for (int j = 0; j < 32; ++j) tv[j] = tcol[j * TC_BM];
+              for (int j = 0; j < 32; ++j) tv[j] = ld_f64_hint(tcol + j * TC_BM, keep);
             }
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
@@ -288,7 +291,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             }
             if (!last) {
 #pragma unroll
-              for (int j = 0; j < 32; ++j) tcol[j * TC_BM] = tv[j];
+              for (int j = 0; j < 32; ++j) st_f64_hint(tcol + j * TC_BM, tv[j], keep);
             } else if (row_ok) {
               double* __restrict__ crow = static_cast<double*>(P.C) + row + colb * P.ldc;
 #pragma unroll
