@@ -63,6 +63,11 @@ int gb_set_wait_limit_ns(uint64_t ns);
  * the default 2^-50. */
 int gb_set_ozaki_tolerance(double tol);
 
+/* Tensor-core engine for the Ozaki and adjoint products: 0 = automatic (CTA pairs),
+ * 1 = one CTA per 128 x 256 tile, 2 = CTA pairs on 256 x 256 tiles (tcgen05 cta_group::2,
+ * half of B per SM).  Ozaki results are identical under both engines. */
+int gb_set_tc_engine(int engine);
+
 /* K chunking used by OZAKI calls with an explicit slice count: K is cut into at least
  * `min_chunks` exact accumulation chunks (shorter chunks allow wider digits, at the cost
  * of more accumulator drains); 0 or 1 restores the default (one chunk up to K = 65536).

@@ -169,12 +169,14 @@ int adjoint_f32(int64_t M, int64_t N, int64_t K, const float* A, int64_t lda, co
   if (!rc) rc = make_plane_tmap(&tb1, P4, M, N, 2, pM, TC_BN);
   if (rc) return rc;
 
+  const bool pair = tc_use_pair();
+  const int64_t tbm = pair ? 256 : TC_BM, tbn = pair ? 256 : TC_BN;
   TcParams prm;
   std::memset(&prm, 0, sizeof(prm));
   TcProblem& P = prm.prob[0];   // dA (M x K), contraction N
   P.M = M; P.N = K; P.K = N;
-  P.tiles_m = static_cast<int32_t>((M + TC_BM - 1) / TC_BM);
-  P.tiles_n = static_cast<int32_t>((K + TC_BN - 1) / TC_BN);
+  P.tiles_m = static_cast<int32_t>((M + tbm - 1) / tbm);
+  P.tiles_n = static_cast<int32_t>((K + tbn - 1) / tbn);
   P.tile_begin = 0;
   P.kb_total = static_cast<int32_t>((N + TC_BK - 1) / TC_BK);
   P.nchunks = 1;
@@ -182,8 +184,8 @@ int adjoint_f32(int64_t M, int64_t N, int64_t K, const float* A, int64_t lda, co
   P.alpha = 1.0; P.beta = 0.0;
   TcProblem& Q = prm.prob[1];   // dB (K x N), contraction M
   Q.M = K; Q.N = N; Q.K = M;
-  Q.tiles_m = static_cast<int32_t>((K + TC_BM - 1) / TC_BM);
-  Q.tiles_n = static_cast<int32_t>((N + TC_BN - 1) / TC_BN);
+  Q.tiles_m = static_cast<int32_t>((K + tbm - 1) / tbm);
+  Q.tiles_n = static_cast<int32_t>((N + tbn - 1) / tbn);
   Q.tile_begin = P.tiles_m * P.tiles_n;
   Q.kb_total = static_cast<int32_t>((M + TC_BK - 1) / TC_BK);
   Q.nchunks = 1;
@@ -196,6 +198,15 @@ int adjoint_f32(int64_t M, int64_t N, int64_t K, const float* A, int64_t lda, co
   prm.wait_limit_ns = wait_limit_ns;
   SliceSchedule sched;
   split3_schedule(sched, P.kb_total > Q.kb_total ? P.kb_total : Q.kb_total);
+  if (pair) {
+    CUtensorMap tb0h, tb1h;   // 128-row B boxes: each CTA of a pair loads half of the B tile
+    rc = make_plane_tmap(&tb0h, P2, N, K, 2, pN, 128);
+    if (!rc) rc = make_plane_tmap(&tb1h, P4, M, N, 2, pM, 128);
+    if (rc) return rc;
+    const int64_t ctas = 2 * static_cast<int64_t>(prm.total_tiles), cap = sms & ~1;
+    return tc_gemm_pair_launch(TC_EPI_F32, ta0, tb0h, &ta1, &tb1h, sched, prm,
+                               static_cast<int>(ctas < cap ? ctas : cap), GB_KERNEL_ADJOINT_MMA, s);
+  }
   const int grid = prm.total_tiles < sms ? prm.total_tiles : sms;
   return tc_gemm_launch(TC_EPI_F32, ta0, tb0, &ta1, &tb1, sched, prm, grid, GB_KERNEL_ADJOINT_MMA, s);
 }

@@ -19,6 +19,7 @@
 #include "grouped.cuh"
 #include "native_gemm.cuh"
 #include "ozaki.cuh"
+#include "tc_gemm.cuh"
 
 namespace gb {
 size_t adjoint_workspace_bytes(int64_t M, int64_t N, int64_t K);
@@ -443,6 +444,12 @@ int gb_release_workspace(void) {
   if (rc) return rc;
   GB_CUDA_TRY(cudaDeviceSynchronize());
   GB_CUDA_TRY(cudaMemPoolTrimTo(dev->pool, 0));
+  return GB_OK;
+}
+
+int gb_set_tc_engine(int engine) {
+  if (engine < 0 || engine > 2) return GB_ERR_INVALID_VALUE;
+  tc_set_engine(engine);
   return GB_OK;
 }
 

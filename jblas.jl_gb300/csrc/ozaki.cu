@@ -385,14 +385,15 @@ int oz_gemm_launch(const OzGemmArgs& a, const OzPlan& plan, cudaStream_t s) {
   if (rc) return rc;
   rc = make_plane_tmap(&tb, a.planes_b, a.K, a.N, a.slices, a.pitch, TC_BN);
   if (rc) return rc;
+  const bool pair = tc_use_pair();
   TcParams prm;
   std::memset(&prm, 0, sizeof(prm));
   TcProblem& P = prm.prob[0];
   P.M = a.M;
   P.N = a.N;
   P.K = a.K;
-  P.tiles_m = static_cast<int32_t>((a.M + TC_BM - 1) / TC_BM);
-  P.tiles_n = static_cast<int32_t>((a.N + TC_BN - 1) / TC_BN);
+  P.tiles_m = static_cast<int32_t>(pair ? (a.M + 255) / 256 : (a.M + TC_BM - 1) / TC_BM);
+  P.tiles_n = static_cast<int32_t>(pair ? (a.N + 255) / 256 : (a.N + TC_BN - 1) / TC_BN);
   P.tile_begin = 0;
   P.kb_total = plan.kb_total;
   P.nchunks = plan.nchunks;
@@ -407,11 +408,23 @@ int oz_gemm_launch(const OzGemmArgs& a, const OzPlan& plan, cudaStream_t s) {
   prm.tws = a.tws;
   prm.status = a.status;
   prm.wait_limit_ns = a.wait_limit_ns;
+  if (pair) {
+    CUtensorMap tb2;   // B boxes of 128 rows: each CTA of a pair loads half of a 256-row tile
+    rc = make_plane_tmap(&tb2, a.planes_b, a.K, a.N, a.slices, a.pitch, 128);
+    if (rc) return rc;
+    return tc_gemm_pair_launch(TC_EPI_OZAKI_F64, ta, tb2, nullptr, nullptr, plan.sched, prm, a.grid,
+                               GB_KERNEL_OZAKI_SLICE_MMA, s);
+  }
   return tc_gemm_launch(TC_EPI_OZAKI_F64, ta, tb, nullptr, nullptr, plan.sched, prm, a.grid,
                         GB_KERNEL_OZAKI_SLICE_MMA, s);
 }
 
 int oz_grid_for(int sms, int64_t M, int64_t N) {
+  if (tc_use_pair()) {
+    const int64_t ctas = 2 * static_cast<int64_t>(tc_pair_tiles(M, N));
+    const int64_t cap = sms & ~1;
+    return static_cast<int>(ctas < cap ? ctas : cap);
+  }
   const int64_t tiles = tc_tiles(M, N);
   return static_cast<int>(tiles < sms ? tiles : sms);
 }

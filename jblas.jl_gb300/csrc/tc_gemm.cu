@@ -11,6 +11,8 @@
 // (bounded) for its in-flight copies and MMAs, frees TMEM and exits.
 #include <cuda_bf16.h>
 
+#include <atomic>
+
 #include "gb_common.cuh"
 #include "profile.cuh"
 #include "tc_gemm.cuh"
@@ -334,6 +336,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     tmem_dealloc(tmem_base, TC_TMEM_COLS);
   }
 }
+
+static std::atomic<int> g_tc_engine{0};
+int tc_engine_setting() { return g_tc_engine.load(std::memory_order_relaxed); }
+void tc_set_engine(int e) { g_tc_engine.store(e); }
 
 int tc_gemm_launch(int epi, const CUtensorMap& ta0, const CUtensorMap& tb0, const CUtensorMap* ta1,
                    const CUtensorMap* tb1, const SliceSchedule& sched, const TcParams& prm, int grid,

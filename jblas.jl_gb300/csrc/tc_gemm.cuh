@@ -67,10 +67,25 @@ int tc_gemm_launch(int epi, const CUtensorMap& ta0, const CUtensorMap& tb0, cons
                    const CUtensorMap* tb1, const SliceSchedule& sched, const TcParams& prm, int grid,
                    int kernel_kind, cudaStream_t s);
 
+// CTA-pair form (tc_gemm2.cu): 256 x 256 tiles on two SMs; TcProblem tile counts and
+// tile_begin are in 256 x 256 units, grid is even.
+int tc_gemm_pair_launch(int epi, const CUtensorMap& ta0, const CUtensorMap& tb0, const CUtensorMap* ta1,
+                        const CUtensorMap* tb1, const SliceSchedule& sched, const TcParams& prm, int grid,
+                        int kernel_kind, cudaStream_t s);
+
+// Engine selection: 0 = automatic (CTA pairs), 1 = single-CTA 128 x 256 tiles, 2 = CTA pairs.
+int tc_engine_setting();
+void tc_set_engine(int e);
+inline bool tc_use_pair() { return tc_engine_setting() != 1; }
+
 // 3-D BF16 tensor map {K, rows, planes} over [planes][rows][pitch], box 64 x box_rows x 1,
 // 128-byte swizzle (defined in capi.cu).
 int make_plane_tmap(CUtensorMap* map, const void* base, int64_t K, int64_t rows, int64_t slices,
                     int64_t pitch, int box_rows);
+
+inline int tc_pair_tiles(int64_t M, int64_t N) {
+  return static_cast<int>(((M + 255) / 256) * ((N + 255) / 256));
+}
 
 inline int tc_tiles(int64_t M, int64_t N) {
   return static_cast<int>(((M + TC_BM - 1) / TC_BM) * ((N + TC_BN - 1) / TC_BN));

@@ -67,6 +67,7 @@ SIGNATURES = {
     "gb_set_wait_limit_ns": (c_int, [ctypes.c_uint64]),
     "gb_set_ozaki_tolerance": (c_int, [c_double]),
     "gb_set_ozaki_min_chunks": (c_int, [c_int]),
+    "gb_set_tc_engine": (c_int, [c_int]),
     "gb_check_status": (c_int, [c_vp]),
     "gb_release_workspace": (c_int, []),
     "gb_jmul_f64": (c_int, [c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, c_vp]),

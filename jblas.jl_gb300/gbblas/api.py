@@ -148,6 +148,11 @@ def set_ozaki_min_chunks(n):
     check(_lib.lib().gb_set_ozaki_min_chunks(int(n)), "gb_set_ozaki_min_chunks")
 
 
+def set_tc_engine(engine):
+    """Tensor-core engine: 0 automatic, 1 single-CTA 128x256 tiles, 2 CTA pairs (256x256)."""
+    check(_lib.lib().gb_set_tc_engine(int(engine)), "gb_set_tc_engine")
+
+
 def set_wait_limit_ns(ns):
     check(_lib.lib().gb_set_wait_limit_ns(int(ns)), "gb_set_wait_limit_ns")
 
