@@ -217,7 +217,6 @@ typedef struct {
   int32_t k_chunk;       /* K elements per exact FP32 accumulation */
   int32_t products;      /* slice-pair products per K chunk (p + q <= slices + 1) */
   int32_t groups;        /* TMEM accumulation groups drained per output tile */
-  int32_t frac_bits;     /* fractional bits of the int64 fixed-point recombination */
   double  flops_tensor;  /* BF16 tensor flops the plan issues */
 } gb_ozaki_plan_t;
 int gb_plan_ozaki(int64_t M, int64_t N, int64_t K, int slices, gb_ozaki_plan_t* out);

@@ -244,13 +244,17 @@ static double ozaki_bound(const BoundStats& st, int64_t K, const OzPlan& plan) {
   const double trunc = us * (EA * SB + EB * (SA + Kd * us * EA)) + Kd * us * cs * EA * EB;
   // leading (level-2) group: |digit_1 * w_1| <= |x| + 2^-b
   const double top = na * nb + std::ldexp(1.0, -b) * (EA * SB + EB * SA) + Kd * std::ldexp(1.0, -2 * b) * EA * EB;
-  // int64 fixed-point recombination: contributions below 2^-F are rounded once each
-  // (half a unit), and the accumulator is converted to FP64 once (one rounding).
-  const int G = plan.sched.ngroups, nch = plan.nchunks, F = plan.sched.frac_bits;
-  double lossy = 0.0;
-  for (int g = 0; g < G; ++g)
-    if (2 - plan.sched.level[g] * b + F < 0) lossy += nch;
-  const double recomb = u * top + lossy * std::ldexp(1.0, -F - 1) * EA * EB;
+  const int G = plan.sched.ngroups, nch = plan.nchunks;
+  const double Kp = static_cast<double>(plan.k_chunk) * nch;
+  const double D = static_cast<double>(G) * nch;
+  double lower = 0.0;
+  for (int g = 0; g < G; ++g) {
+    const int level = plan.sched.level[g];
+    if (level == 2) continue;
+    const double coef = D - static_cast<double>(g) * nch;
+    lower += coef * plan.sched.npairs[g] * Kp * std::ldexp(1.0, -(level - 2) * b);
+  }
+  const double recomb = u * (nch * top + lower * EA * EB);
   const double fin = u * top;
   return 1.01 * (trunc + recomb + fin) / (na * nb);
 }
@@ -350,14 +354,13 @@ static int ozaki_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int
   g_last_plan.k_chunk = static_cast<int32_t>(plan.k_chunk);
   g_last_plan.products = plan.products;
   g_last_plan.groups = plan.groups;
-  g_last_plan.frac_bits = plan.sched.frac_bits;
   g_last_plan.flops_tensor = plan.flops_tensor;
   const int grid = oz_grid_for(dev->sms, M, N);
   const size_t pa_bytes = align256(static_cast<size_t>(s_use) * M * pitch * 2);
   const size_t pb_bytes = align256(static_cast<size_t>(s_use) * N * pitch * 2);
   const size_t ex_bytes = align256((M + N) * sizeof(int32_t));
   const size_t tw_bytes = (plan.groups * plan.nchunks > 1)
-                              ? static_cast<size_t>(grid) * TC_BM * TC_BN * sizeof(long long)
+                              ? static_cast<size_t>(grid) * TC_BM * TC_BN * sizeof(double)
                               : 0;
   char* ws = nullptr;
   cudaError_t e = cudaMallocFromPoolAsync(reinterpret_cast<void**>(&ws), pa_bytes + pb_bytes + ex_bytes + tw_bytes,
@@ -370,7 +373,7 @@ static int ozaki_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int
   __nv_bfloat16* pb = reinterpret_cast<__nv_bfloat16*>(ws + pa_bytes);
   int32_t* ea = reinterpret_cast<int32_t*>(ws + pa_bytes + pb_bytes);
   int32_t* eb = ea + M;
-  long long* tws = tw_bytes ? reinterpret_cast<long long*>(ws + pa_bytes + pb_bytes + ex_bytes) : nullptr;
+  double* tws = tw_bytes ? reinterpret_cast<double*>(ws + pa_bytes + pb_bytes + ex_bytes) : nullptr;
 
   rc = oz_split(A, M, K, a_rs, a_ks, sa.amax_bits, s_use, plan.bits, pa, pitch, ea, s);
   if (!rc) rc = oz_split(B, N, K, b_rs, b_ks, sb.amax_bits, s_use, plan.bits, pb, pitch, eb, s);
@@ -630,7 +633,6 @@ int gb_plan_ozaki(int64_t M, int64_t N, int64_t K, int slices, gb_ozaki_plan_t* 
   out->k_chunk = static_cast<int32_t>(p.k_chunk);
   out->products = p.products;
   out->groups = p.groups;
-  out->frac_bits = p.sched.frac_bits;
   out->flops_tensor = p.flops_tensor;
   return GB_OK;
 }

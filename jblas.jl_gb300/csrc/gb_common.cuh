@@ -263,25 +263,6 @@ __device__ __forceinline__ void st_f64_hint(double* p, double v, uint64_t pol) {
   asm volatile("st.global.L2::cache_hint.f64 [%0], %1, %2;" ::"l"(p), "d"(v), "l"(pol) : "memory");
 }
 
-__device__ __forceinline__ long long ld_s64_hint(const long long* p, uint64_t pol) {
-  long long v;
-  asm volatile("ld.global.L2::cache_hint.s64 %0, [%1], %2;" : "=l"(v) : "l"(p), "l"(pol));
-  return v;
-}
-__device__ __forceinline__ void st_s64_hint(long long* p, long long v, uint64_t pol) {
-  asm volatile("st.global.L2::cache_hint.s64 [%0], %1, %2;" ::"l"(p), "l"(v), "l"(pol) : "memory");
-}
-
-// Fixed-point contribution of an exact integer group sum held in an FP32 value:
-// S * 2^sh as int64, exact for sh >= 0; for sh < 0 rounded half up, (S + 2^(-sh-1)) >> -sh;
-// 0 when the shift leaves nothing (-sh >= 62).
-__device__ __forceinline__ long long fixed_contrib(uint32_t u, int sh) {
-  const long long v = static_cast<long long>(__float2int_rn(__uint_as_float(u)));
-  if (sh >= 0) return v << sh;
-  if (sh <= -62) return 0;
-  return (v + (1ll << (-sh - 1))) >> (-sh);
-}
-
 // 2^e as a double for e in the normal range [-1022, 1023] (exact construction).
 __device__ __forceinline__ double pow2_normal(int e) {
   return __hiloint2double((e + 1023) << 20, 0);

@@ -112,16 +112,6 @@ int oz_make_plan_chunks(int64_t M, int64_t N, int64_t K, int slices, int min_chu
   S.ngroups = g;
   P.groups = g;
   P.products = np;
-  // Fixed point of the tile accumulator: |T| <= K' * R with K' = kb_total * 64 and
-  // R = sum_g npairs_g 2^(-(level_g - 2) b) <= 1 + ceil((products - 1) / 2^b); F leaves
-  // |T| * 2^F below 2^62 (integer arithmetic only, so host and restatement agree).
-  {
-    const int64_t r = 1 + ((np - 1) + (int64_t(1) << P.bits) - 1) / (int64_t(1) << P.bits);
-    uint64_t tmax = static_cast<uint64_t>(kb_total) * 64u * static_cast<uint64_t>(r);
-    int len = 0;
-    while (tmax) { ++len; tmax >>= 1; }
-    S.frac_bits = 62 - len;
-  }
   P.flops_tensor = 2.0 * static_cast<double>(M) * static_cast<double>(N) *
                    static_cast<double>(kb_total * TC_BK) * np;
   return GB_OK;
@@ -442,12 +432,11 @@ int oz_grid_for(int sms, int64_t M, int64_t N) {
 }  // namespace gb
 
 namespace gb {
-// Relative cost of a plan for one output tile: tensor work (products x K panels) and FP64
-// drains (one per group and K chunk) overlap, so the larger dominates.  DRAIN_PANELS is the
-// measured cost of draining one 128 x 256 group into the FP64 tile buffer, in units of one
-// 64-wide K panel of MMA work (GB300: ~29 us per drain vs ~0.35 us per panel).
+// Relative cost of a plan for one 128 x 256 output tile: tensor work (products x K panels)
+// and FP64 drains (one per group and K chunk; a drain of a 128 x 256 FP32 group costs about
+// as much as DRAIN_PANELS K panels of MMA) overlap, so the larger dominates.
 double oz_plan_cost(const OzPlan& p) {
-  constexpr double DRAIN_PANELS = 80.0;
+  constexpr double DRAIN_PANELS = 40.0;
   const double mma = static_cast<double>(p.products) * p.kb_total;
   const double drain = static_cast<double>(p.groups) * p.nchunks * DRAIN_PANELS;
   return (mma > drain ? mma : drain) + 0.1 * (mma < drain ? mma : drain);

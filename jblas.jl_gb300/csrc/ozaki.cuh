@@ -60,7 +60,7 @@ struct OzGemmArgs {
   double alpha, beta;
   double* C;
   int64_t ldc;
-  long long* tws;         // per-CTA int64 fixed-point tile buffers (grid x 128 x 256)
+  double* tws;            // per-CTA FP64 tile buffers (grid x 128 x 256)
   DeviceStatus* status;
   uint64_t wait_limit_ns;
   int grid;

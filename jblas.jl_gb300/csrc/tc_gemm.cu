@@ -42,6 +42,17 @@ __device__ __forceinline__ void tile_coords(int t, int tiles_m, int tiles_n, int
   tn = in_band / band_rows;
 }
 
+// S * 2^wexp as a double, for an FP32 value S holding an integer (|S| <= 2^24) and
+// wbias = (896 + wexp) << 23: the FP32 exponent is rebased to FP64 (bias 127 -> 1023) and
+// shifted by wexp in integer arithmetic, so no FP32->FP64 conversion runs on the FP64 pipe.
+// Exact for every such S; +-0 keeps its sign.
+__device__ __forceinline__ double exact_int_f32_times_pow2(uint32_t u, unsigned long long wbias) {
+  const unsigned long long sign = static_cast<unsigned long long>(u & 0x80000000u) << 32;
+  const uint32_t mag = u & 0x7FFFFFFFu;
+  const unsigned long long body = mag ? ((static_cast<unsigned long long>(mag) + wbias) << 29) : 0ull;
+  return __longlong_as_double(static_cast<long long>(sign | body));
+}
+
 __device__ __forceinline__ int problem_of(const TcParams& prm, int t) {
   return (prm.nprob == 2 && t >= prm.prob[1].tile_begin) ? 1 : 0;
 }
@@ -228,12 +239,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       const double alpha = P.alpha, beta = P.beta;
       int ea = 0;
       if (EPI == TC_EPI_OZAKI_F64) ea = row_ok ? P.ea[row] : 0;
-      long long* __restrict__ tws = prm.tws + static_cast<int64_t>(blockIdx.x) * (TC_BM * TC_BN);
+      double* __restrict__ tws = prm.tws + static_cast<int64_t>(blockIdx.x) * (TC_BM * TC_BN);
       int step = 0;
       const int nsteps = G * P.nchunks;
       for (int g = 0; g < G && ok; ++g) {
-        // group weight 2^(2 - level*bits) in the F-fractional-bit fixed point of the tile buffer
-        const int sh = 2 - sched.level[g] * sched.bits + sched.frac_bits;
+        // group weight 2^wexp folded into the exponent of each exact integer group sum
+        const int wexp = 2 - sched.level[g] * sched.bits;
+        const unsigned long long wbias = static_cast<unsigned long long>(896 + wexp) << 23;
         for (int c = 0; c < P.nchunks; ++c, ++step) {
           // the whole warp agrees before the warp-collective tcgen05.ld
           ok = __all_sync(0xffffffffu, mbar_wait_bounded(&tfull[buf], acc_phase, prm.wait_limit_ns,
@@ -267,22 +279,21 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
               }
               continue;
             }
-            long long* __restrict__ tcol = tws + static_cast<int64_t>(cb) * TC_BM + row_l;
+            double* __restrict__ tcol = tws + static_cast<int64_t>(cb) * TC_BM + row_l;
             // all loads of the chunk are issued before any store (no aliasing chain)
-            // int64 fixed point: every exact group sum enters once, integer adds only
-            long long tv[32];
+            double tv[32];
             if (!first) {
 #pragma unroll
-              for (int j = 0; j < 32; ++j) tv[j] = ld_s64_hint(tcol + j * TC_BM, keep);
+              for (int j = 0; j < 32; ++j) tv[j] = ld_f64_hint(tcol + j * TC_BM, keep);
             }
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
-              const long long c = fixed_contrib(v[j], sh);
-              tv[j] = first ? c : tv[j] + c;
+              const double sw = exact_int_f32_times_pow2(v[j], wbias);
+              tv[j] = first ? sw : tv[j] + sw;   // == fma(S, 2^wexp, T): S * 2^wexp is exact
             }
             if (!last) {
 #pragma unroll
-              for (int j = 0; j < 32; ++j) st_s64_hint(tcol + j * TC_BM, tv[j], keep);
+              for (int j = 0; j < 32; ++j) st_f64_hint(tcol + j * TC_BM, tv[j], keep);
             } else if (row_ok) {
               double* __restrict__ crow = static_cast<double*>(P.C) + row + colb * P.ldc;
 #pragma unroll
@@ -303,7 +314,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                   if (ea == EXP_NONFINITE || ebj[j] == EXP_NONFINITE)
                     val = __longlong_as_double(0x7FF8000000000000ll);
                   else
-                    val = scale_pow2(__ll2double_rn(tv[j8 + j]), ea + ebj[j] - sched.frac_bits);
+                    val = scale_pow2(tv[j8 + j], ea + ebj[j]);
                   crow[(j8 + j) * P.ldc] = (beta == 0.0) ? alpha * val : fma(alpha, val, beta * c0[j]);
                 }
               }

@@ -31,7 +31,7 @@ struct SliceSchedule {
   int32_t ngroups;
   int32_t kb_chunk;   // K panels of 64 per exact accumulation chunk
   int32_t bits;       // bits per digit plane (Ozaki weights 2^(2 - level*bits))
-  int32_t frac_bits;  // Ozaki: fractional bits F of the int64 fixed-point tile accumulator
+  int32_t pad;
   int8_t level[TC_MAX_GROUPS];
   int8_t npairs[TC_MAX_GROUPS];
   int16_t pair_off[TC_MAX_GROUPS];
@@ -57,7 +57,7 @@ struct TcParams {
   TcProblem prob[2];
   int32_t nprob;
   int32_t total_tiles;
-  long long* tws;       // per-CTA int64 fixed-point tile buffers (Ozaki, more than one drain)
+  double* tws;          // per-CTA FP64 tile buffers (Ozaki, more than one drain per tile)
   DeviceStatus* status;
   uint64_t wait_limit_ns;
 };

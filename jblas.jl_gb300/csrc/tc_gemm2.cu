@@ -42,6 +42,13 @@ __device__ __forceinline__ void p2_tile_coords(int t, int tiles_m, int tiles_n, 
   tn = in_band / band_rows;
 }
 
+__device__ __forceinline__ double p2_exact_int_f32_times_pow2(uint32_t u, unsigned long long wbias) {
+  const unsigned long long sign = static_cast<unsigned long long>(u & 0x80000000u) << 32;
+  const uint32_t mag = u & 0x7FFFFFFFu;
+  const unsigned long long body = mag ? ((static_cast<unsigned long long>(mag) + wbias) << 29) : 0ull;
+  return __longlong_as_double(static_cast<long long>(sign | body));
+}
+
 // TcProblem fields are reused with pair tiles: tiles_m = ceil(M / 256), tiles_n = ceil(N / 256),
 // tile_begin in pair-tile units.
 __device__ __forceinline__ int p2_problem_of(const TcParams& prm, int t) {
@@ -234,12 +241,12 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(P2_THREADS, 1)
       const double alpha = P.alpha, beta = P.beta;
       int ea = 0;
       if (EPI == TC_EPI_OZAKI_F64) ea = row_ok ? P.ea[row] : 0;
-      long long* __restrict__ tws = prm.tws + static_cast<int64_t>(blockIdx.x) * (TC_BM * TC_BN);
+      double* __restrict__ tws = prm.tws + static_cast<int64_t>(blockIdx.x) * (TC_BM * TC_BN);
       int step = 0;
       const int nsteps = G * P.nchunks;
       for (int g = 0; g < G && ok; ++g) {
-        // group weight 2^(2 - level*bits) in the F-fractional-bit fixed point of the tile buffer
-        const int sh = 2 - sched.level[g] * sched.bits + sched.frac_bits;
+        const int wexp = 2 - sched.level[g] * sched.bits;
+        const unsigned long long wbias = static_cast<unsigned long long>(896 + wexp) << 23;
         for (int c = 0; c < P.nchunks; ++c, ++step) {
           ok = __all_sync(0xffffffffu,
                           mbar_wait_bounded(&tfull[buf], acc_phase, prm.wait_limit_ns, abort_flag, prm.status, 4));
@@ -271,21 +278,20 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(P2_THREADS, 1)
               }
               continue;
             }
-            long long* __restrict__ tcol = tws + static_cast<int64_t>(cb) * TC_BM + row_l;
-            // int64 fixed point: every exact group sum enters once, integer adds only
-            long long tv[32];
+            double* __restrict__ tcol = tws + static_cast<int64_t>(cb) * TC_BM + row_l;
+            double tv[32];
             if (!first) {
 #pragma unroll
-              for (int j = 0; j < 32; ++j) tv[j] = ld_s64_hint(tcol + j * TC_BM, keep);
+              for (int j = 0; j < 32; ++j) tv[j] = ld_f64_hint(tcol + j * TC_BM, keep);
             }
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
-              const long long c = fixed_contrib(v[j], sh);
-              tv[j] = first ? c : tv[j] + c;
+              const double sw = p2_exact_int_f32_times_pow2(v[j], wbias);
+              tv[j] = first ? sw : tv[j] + sw;
             }
             if (!last) {
 #pragma unroll
-              for (int j = 0; j < 32; ++j) st_s64_hint(tcol + j * TC_BM, tv[j], keep);
+              for (int j = 0; j < 32; ++j) st_f64_hint(tcol + j * TC_BM, tv[j], keep);
             } else if (row_ok) {
               double* __restrict__ crow = static_cast<double*>(P.C) + row + colb * P.ldc;
 #pragma unroll
@@ -305,7 +311,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(P2_THREADS, 1)
                   if (ea == P2_EXP_NONFINITE || ebj[j] == P2_EXP_NONFINITE)
                     val = __longlong_as_double(0x7FF8000000000000ll);
                   else
-                    val = scale_pow2(__ll2double_rn(tv[j8 + j]), ea + ebj[j] - sched.frac_bits);
+                    val = scale_pow2(tv[j8 + j], ea + ebj[j]);
                   crow[(j8 + j) * P.ldc] = (beta == 0.0) ? alpha * val : fma(alpha, val, beta * c0[j]);
                 }
               }

@@ -30,7 +30,7 @@ c_float = ctypes.c_float
 
 class OzakiPlan(ctypes.Structure):
     _fields_ = [("slices", ctypes.c_int32), ("bits", ctypes.c_int32), ("k_chunk", ctypes.c_int32),
-                ("products", ctypes.c_int32), ("groups", ctypes.c_int32), ("frac_bits", ctypes.c_int32),
+                ("products", ctypes.c_int32), ("groups", ctypes.c_int32),
                 ("flops_tensor", ctypes.c_double)]
 
 

@@ -128,7 +128,7 @@ def ozaki_plan(M, N, K, slices):
     p = _lib.OzakiPlan()
     check(_lib.lib().gb_plan_ozaki(M, N, K, slices, ctypes.byref(p)), "gb_plan_ozaki")
     return {"slices": p.slices, "bits": p.bits, "k_chunk": p.k_chunk, "products": p.products,
-            "groups": p.groups, "frac_bits": p.frac_bits, "flops_tensor": p.flops_tensor}
+            "groups": p.groups, "flops_tensor": p.flops_tensor}
 
 
 def last_ozaki_plan():
@@ -136,7 +136,7 @@ def last_ozaki_plan():
     p = _lib.OzakiPlan()
     check(_lib.lib().gb_last_ozaki_plan(ctypes.byref(p)), "gb_last_ozaki_plan")
     return {"slices": p.slices, "bits": p.bits, "k_chunk": p.k_chunk, "products": p.products,
-            "groups": p.groups, "frac_bits": p.frac_bits, "flops_tensor": p.flops_tensor}
+            "groups": p.groups, "flops_tensor": p.flops_tensor}
 
 
 def set_ozaki_tolerance(tol):

@@ -258,12 +258,9 @@ def ozaki_plan(K, slices, min_chunks=1):
                 cur = (level, [])
                 groups.append(cur)
             cur[1].append((p - 1, q - 1))
-    products = sum(len(g[1]) for g in groups)
-    # fixed point of the tile accumulator: |T| <= kb_total * 64 * (1 + ceil((products - 1) / 2^b))
-    r = 1 + ((products - 1) + (1 << bits) - 1) // (1 << bits)
-    frac_bits = 62 - (kb_total * 64 * r).bit_length()
     return {"bits": bits, "kb_chunk": kb_chunk, "kb_total": kb_total, "nchunks": nchunks,
-            "k_chunk": kc, "groups": groups, "products": products, "frac_bits": frac_bits}
+            "k_chunk": kc, "groups": groups,
+            "products": sum(len(g[1]) for g in groups)}
 
 
 def ozaki_split(X, slices, bits):
@@ -322,24 +319,21 @@ def ozaki_gemm(A, B, C=None, alpha=1.0, beta=0.0, slices=8, min_chunks=1):
     bits = plan["bits"]
     dA, ea = ozaki_split(A, slices, bits)
     dB, eb = ozaki_split(B.T, slices, bits)
-    F = plan["frac_bits"]
-    T = np.zeros((M, N), dtype=np.int64)
+    steps = len(plan["groups"]) * plan["nchunks"]
+    T = None
     kc = plan["kb_chunk"] * 64
     for level, pairs in plan["groups"]:
-        sh = 2 - level * bits + F                            # weight 2^(2 - level*b) in 2^-F units
+        w = 2.0 ** (2 - level * bits)
         for c in range(plan["nchunks"]):
             k0, k1 = c * kc, min(K, (c + 1) * kc)
             S = np.zeros((M, N))
             for p, q in pairs:
                 S += dA[p][:, k0:k1] @ dB[q][:, k0:k1].T   # exact: integers below 2^53
-            Si = S.astype(np.int64)
-            if sh >= 0:
-                T += Si << sh
-            elif sh > -62:
-                T += (Si + (1 << (-sh - 1))) >> (-sh)      # rounded half up, once per group
+            T = S * w if T is None else T + S * w           # fma(S, w, T) with S*w exact
+    del steps
     bad = (ea[:, None] == 2**31 - 1) | (eb[None, :] == 2**31 - 1)
-    E = np.where(bad, 0, ea[:, None] + eb[None, :] - F)
-    val = np.ldexp(T.astype(np.float64), E.astype(np.int64))
+    E = np.where(bad, 0, ea[:, None] + eb[None, :])
+    val = np.ldexp(T, E.astype(np.int64))
     val = np.where(bad, np.nan, val)
     if beta == 0.0:
         out = alpha * val
