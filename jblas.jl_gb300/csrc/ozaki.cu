@@ -432,11 +432,13 @@ int oz_grid_for(int sms, int64_t M, int64_t N) {
 }  // namespace gb
 
 namespace gb {
-// Relative cost of a plan for one 128 x 256 output tile: tensor work (products x K panels)
-// and FP64 drains (one per group and K chunk; a drain of a 128 x 256 FP32 group costs about
-// as much as DRAIN_PANELS K panels of MMA) overlap, so the larger dominates.
+// Relative cost of a plan for one output tile: tensor work (products x K panels) and FP64
+// drains (one per group and K chunk) overlap, so the larger dominates.  DRAIN_PANELS is the
+// measured cost of draining one 128 x 256 group into the FP64 tile buffer, in units of one
+// 64-wide K panel of MMA work (GB300: ~29 us per drain, bound by the FP64 adds, vs ~0.35 us
+// per panel).
 double oz_plan_cost(const OzPlan& p) {
-  constexpr double DRAIN_PANELS = 40.0;
+  constexpr double DRAIN_PANELS = 80.0;
   const double mma = static_cast<double>(p.products) * p.kb_total;
   const double drain = static_cast<double>(p.groups) * p.nchunks * DRAIN_PANELS;
   return (mma > drain ? mma : drain) + 0.1 * (mma < drain ? mma : drain);
