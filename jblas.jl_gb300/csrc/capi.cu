@@ -171,6 +171,7 @@ static double ozaki_tolerance() {
 
 // Host copy of the split statistics of both operands.
 struct HostStats {
+  int64_t K = 0;
   std::vector<unsigned long long> amax_a, amax_b;
   std::vector<double> sabs_a, sabs_b, ssq_a, ssq_b;
 };
@@ -210,20 +211,30 @@ static BoundStats bound_stats(const HostStats& h) {
     if (e == INT32_MAX) r.nonfinite = true; else if (bits && e > ref_b) ref_b = e;
   }
   if (r.nonfinite) return r;
+  // The device sums are FP32 sums of truncated values |x| 2^-e (e: the row's exponent) over
+  // K terms: sum |x| <= s1 (1 + 2^-23) / (1 - K 2^-24) + K 2^-126 (flushed tiny terms), and
+  // sum x^2 >= s2 / (1 + K 2^-23) — one-sided bounds, as the error bound needs.
+  const double Kd = static_cast<double>(h.K);
+  const double gk = Kd * std::ldexp(1.0, -24);
+  const double up = gk < 0.5 ? (1.0 + std::ldexp(1.0, -23)) / (1.0 - gk) : 4.0;
+  const double down = 1.0 / (1.0 + 2.0 * gk);
+  const double tiny = Kd * std::ldexp(1.0, -126);
   double e2a = 0, e2b = 0, na2 = 0, nb2 = 0, sa2 = 0, sb2 = 0;
   for (size_t i = 0; i < h.amax_a.size(); ++i) {
     if (!h.amax_a[i]) continue;
-    e2a += std::ldexp(1.0, 2 * (exp_of(h.amax_a[i]) - ref_a));
-    const double sa = std::ldexp(h.sabs_a[i], -ref_a);
+    const int e = exp_of(h.amax_a[i]);
+    e2a += std::ldexp(1.0, 2 * (e - ref_a));
+    const double sa = std::ldexp(h.sabs_a[i] * up + tiny, e - ref_a);
     sa2 += sa * sa;
-    na2 += std::ldexp(h.ssq_a[i], -2 * ref_a);
+    na2 += std::ldexp(h.ssq_a[i] * down, 2 * (e - ref_a));
   }
   for (size_t j = 0; j < h.amax_b.size(); ++j) {
     if (!h.amax_b[j]) continue;
-    e2b += std::ldexp(1.0, 2 * (exp_of(h.amax_b[j]) - ref_b));
-    const double sb = std::ldexp(h.sabs_b[j], -ref_b);
+    const int e = exp_of(h.amax_b[j]);
+    e2b += std::ldexp(1.0, 2 * (e - ref_b));
+    const double sb = std::ldexp(h.sabs_b[j] * up + tiny, e - ref_b);
     sb2 += sb * sb;
-    nb2 += std::ldexp(h.ssq_b[j], -2 * ref_b);
+    nb2 += std::ldexp(h.ssq_b[j] * down, 2 * (e - ref_b));
   }
   r.na = std::sqrt(na2); r.nb = std::sqrt(nb2);
   r.EA = std::sqrt(e2a); r.EB = std::sqrt(e2b);
@@ -294,6 +305,7 @@ static int ozaki_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int
   int s_use = slices;
   if (slices == 0 || err_bound_out) {
     HostStats h;
+    h.K = K;
     h.amax_a.resize(M); h.amax_b.resize(N);
     h.sabs_a.resize(M); h.sabs_b.resize(N);
     h.ssq_a.resize(M); h.ssq_b.resize(N);

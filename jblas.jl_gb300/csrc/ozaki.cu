@@ -123,33 +123,56 @@ __device__ __forceinline__ unsigned long long abs_bits(double x) {
   return static_cast<unsigned long long>(__double_as_longlong(x)) & 0x7FFFFFFFFFFFFFFFull;
 }
 
+// |x| * 2^-e as FP32 from the IEEE fields of |x| (abits), truncated so it never exceeds
+// the true value (relative error below 2^-23); 0 when below FP32's normal range.
+__device__ __forceinline__ float scaled_f32_trunc(unsigned long long abits, int e) {
+  const int ex = static_cast<int>(abits >> 52);
+  const int fe = ex - 1023 - e + 127;   // <= 126 because |x| < 2^e
+  if (ex == 0 || fe < 1) return 0.0f;
+  return __uint_as_float((static_cast<uint32_t>(fe) << 23) | static_cast<uint32_t>((abits >> 29) & 0x7FFFFF));
+}
+
+__device__ __forceinline__ int row_exponent_of(unsigned long long amax_bits);
+
+// Row statistics in two passes without FP64 arithmetic (GB300's FP64 pipe is narrow):
+// the exact max |x| by integer compare, then sum |x| 2^-e and sum x^2 2^-2e in FP32 over
+// truncated scaled values (e: row exponent).  The host turns the scaled sums into rigorous
+// one-sided bounds (see bound_stats).
 // k contiguous (ks == 1): one warp per row.
 __global__ void stats_kc_kernel(const double* __restrict__ X, int64_t R, int64_t K, int64_t rs,
                                 OzRowStats st) {
   const int lane = threadIdx.x & 31;
   const int64_t r = static_cast<int64_t>(blockIdx.x) * (blockDim.x / 32) + (threadIdx.x >> 5);
   if (r >= R) return;
-  const double* row = X + r * rs;
+  const unsigned long long* row = reinterpret_cast<const unsigned long long*>(X + r * rs);
   unsigned long long mx = 0;
-  double sa = 0.0, sq = 0.0;
   for (int64_t k = lane; k < K; k += 32) {
-    const double x = row[k];
-    const unsigned long long b = abs_bits(x);
+    const unsigned long long b = row[k] & 0x7FFFFFFFFFFFFFFFull;
     mx = b > mx ? b : mx;
-    sa += fabs(x);
-    sq = fma(x, x, sq);
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     const unsigned long long m2 = __shfl_xor_sync(0xffffffffu, mx, o);
     mx = m2 > mx ? m2 : mx;
+  }
+  const int e = row_exponent_of(mx);
+  float sa = 0.0f, sq = 0.0f;
+  if (e != 0x7FFFFFFF) {
+    for (int64_t k = lane; k < K; k += 32) {
+      const float f = scaled_f32_trunc(row[k] & 0x7FFFFFFFFFFFFFFFull, e);
+      sa += f;
+      sq = fmaf(f, f, sq);
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
     sa += __shfl_xor_sync(0xffffffffu, sa, o);
     sq += __shfl_xor_sync(0xffffffffu, sq, o);
   }
   if (lane == 0) {
     st.amax_bits[r] = mx;
-    st.sum_abs[r] = sa;
-    st.sum_sq[r] = sq;
+    st.sum_abs[r] = static_cast<double>(sa);
+    st.sum_sq[r] = static_cast<double>(sq);
   }
 }
 
@@ -157,33 +180,40 @@ __global__ void stats_kc_kernel(const double* __restrict__ X, int64_t R, int64_t
 __global__ void stats_rc_kernel(const double* __restrict__ X, int64_t R, int64_t K, int64_t ks,
                                 OzRowStats st) {
   __shared__ unsigned long long smx[8][32];
-  __shared__ double ssa[8][32], ssq[8][32];
+  __shared__ float ssa[8][32], ssq[8][32];
   const int tr = threadIdx.x & 31, tk = threadIdx.x >> 5;
   const int64_t r = static_cast<int64_t>(blockIdx.x) * 32 + tr;
+  const unsigned long long* Xb = reinterpret_cast<const unsigned long long*>(X);
   unsigned long long mx = 0;
-  double sa = 0.0, sq = 0.0;
   if (r < R) {
     for (int64_t k = tk; k < K; k += 8) {
-      const double x = X[r + k * ks];
-      const unsigned long long b = abs_bits(x);
+      const unsigned long long b = Xb[r + k * ks] & 0x7FFFFFFFFFFFFFFFull;
       mx = b > mx ? b : mx;
-      sa += fabs(x);
-      sq = fma(x, x, sq);
     }
   }
   smx[tk][tr] = mx;
+  __syncthreads();
+  for (int w = 0; w < 8; ++w) mx = smx[w][tr] > mx ? smx[w][tr] : mx;
+  const int e = row_exponent_of(mx);
+  float sa = 0.0f, sq = 0.0f;
+  if (r < R && e != 0x7FFFFFFF) {
+    for (int64_t k = tk; k < K; k += 8) {
+      const float f = scaled_f32_trunc(Xb[r + k * ks] & 0x7FFFFFFFFFFFFFFFull, e);
+      sa += f;
+      sq = fmaf(f, f, sq);
+    }
+  }
   ssa[tk][tr] = sa;
   ssq[tk][tr] = sq;
   __syncthreads();
   if (tk == 0 && r < R) {
     for (int w = 1; w < 8; ++w) {
-      mx = smx[w][tr] > mx ? smx[w][tr] : mx;
       sa += ssa[w][tr];
       sq += ssq[w][tr];
     }
     st.amax_bits[r] = mx;
-    st.sum_abs[r] = sa;
-    st.sum_sq[r] = sq;
+    st.sum_abs[r] = static_cast<double>(sa);
+    st.sum_sq[r] = static_cast<double>(sq);
   }
 }
 
@@ -206,6 +236,12 @@ int oz_row_stats(const double* X, int64_t R, int64_t K, int64_t rs, int64_t ks, 
 // ============================================================== split kernels
 
 constexpr int OZ_EXP_NONFINITE = 0x7FFFFFFF;
+
+__device__ __forceinline__ int row_exponent_of(unsigned long long amax_bits) {
+  if (amax_bits >= 0x7FF0000000000000ull) return OZ_EXP_NONFINITE;  // Inf or NaN in the row
+  if (amax_bits == 0) return 0;
+  return ilogb(__longlong_as_double(static_cast<long long>(amax_bits))) + 1;  // amax < 2^e
+}
 
 __device__ __forceinline__ int row_exponent(unsigned long long amax_bits) {
   if (amax_bits >= 0x7FF0000000000000ull) return OZ_EXP_NONFINITE;  // Inf or NaN in the row
@@ -273,20 +309,25 @@ __device__ __forceinline__ void split_16(const double (&x)[16], int e, int slice
   const bool nonfinite = (e == 0x7FFFFFFF);
 #pragma unroll
   for (int j = 0; j < 16; ++j) y[j] = nonfinite ? static_cast<Word>(0) : fixed_point<Word>(x[j], e, SB);
-  // least significant digit first
+  // Balanced digits with one bias add: Z = Y + sum_{i < s-1} H 2^(i b) has plain base-2^b
+  // digits d_i + H in its low s-1 positions (no carries, since d_i + H lies in [0, 2^b)),
+  // and Z >> ((s-1) b) (arithmetic) is the top digit.
+  Word hsum = 0;
+  for (int i = 0; i + 1 < slices; ++i) hsum += static_cast<Word>(H) << (i * bits);
+#pragma unroll
+  for (int j = 0; j < 16; ++j) y[j] += hsum;
   for (int p = slices - 1; p >= 0; --p) {
     uint32_t packed[8];
+    const int shift = (slices - 1 - p) * bits;   // plane p holds the digit at bit position shift
 #pragma unroll
     for (int j = 0; j < 16; j += 2) {
       int d0, d1;
       if (p > 0) {
-        d0 = static_cast<int>(static_cast<int64_t>((y[j] + H) & MASK)) - H;
-        d1 = static_cast<int>(static_cast<int64_t>((y[j + 1] + H) & MASK)) - H;
-        y[j] = sar<Word>(y[j] - static_cast<Word>(static_cast<int64_t>(d0)), bits);
-        y[j + 1] = sar<Word>(y[j + 1] - static_cast<Word>(static_cast<int64_t>(d1)), bits);
+        d0 = static_cast<int>(static_cast<uint32_t>(y[j] >> shift) & static_cast<uint32_t>(MASK)) - H;
+        d1 = static_cast<int>(static_cast<uint32_t>(y[j + 1] >> shift) & static_cast<uint32_t>(MASK)) - H;
       } else {
-        d0 = static_cast<int>(static_cast<int64_t>(y[j]));
-        d1 = static_cast<int>(static_cast<int64_t>(y[j + 1]));
+        d0 = static_cast<int>(static_cast<int64_t>(sar<Word>(y[j], shift)));
+        d1 = static_cast<int>(static_cast<int64_t>(sar<Word>(y[j + 1], shift)));
       }
       packed[j / 2] = bf16_bits_of_int(d0) | (bf16_bits_of_int(d1) << 16);
     }

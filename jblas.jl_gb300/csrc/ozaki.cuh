@@ -34,8 +34,9 @@ int oz_make_plan_chunks(int64_t M, int64_t N, int64_t K, int slices, int min_chu
 // Relative per-tile cost of a plan (tensor work vs FP64 drains), for choosing among plans.
 double oz_plan_cost(const OzPlan& p);
 
-// Per-row statistics of op(X) (rows r < R, contraction index k < K):
-// amax bits of |x| (as uint64), sum |x|, sum x^2.
+// Per-row statistics of op(X) (rows r < R, contraction index k < K): amax bits of |x|
+// (as uint64, exact), and FP32 sums of |x| 2^-e and x^2 2^-2e over truncated values, e the
+// row exponent (max |x| < 2^e); the host turns them into one-sided bounds.
 struct OzRowStats {
   unsigned long long* amax_bits;
   double* sum_abs;
