@@ -379,12 +379,10 @@ def main():
             dist.barrier()
         torch.cuda.synchronize()
 
+    from gbblas import replicas
+
     def max_over_ranks(x):
-        if dist is None:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return replicas.job_time_and_throughput(x, 0.0, device=dev)[0] if dist is not None else x
 
     n = args.size
     M = N = K = n
