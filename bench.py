@@ -433,16 +433,45 @@ def main():
     value = world * flops / (ms_step * 1e-3) / 1e12
 
     # ---------------------------------------------------------------- timed: end to end
+    # Every step copies its inputs host -> device (pinned) and its result device -> host.
+    # Copies run on a second stream with double-buffered device inputs/outputs, so step
+    # i+1's uploads and step i's download overlap step i's compute (a serving pipeline).
     barrier()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    A_e = torch.empty_like(A_pin, device=dev)
-    B_e = torch.empty_like(B_pin, device=dev)
+    copy_stream = torch.cuda.Stream(dev)
+    A_e = [torch.empty_like(A_pin, device=dev) for _ in range(2)]
+    B_e = [torch.empty_like(B_pin, device=dev) for _ in range(2)]
+    C_e = [torch.empty((N, M), dtype=torch.float64, device=dev) for _ in range(2)]
+    up_done = [torch.cuda.Event() for _ in range(2)]
+    comp_done = [torch.cuda.Event() for _ in range(2)]
+    down_done = [torch.cuda.Event() for _ in range(2)]
     e0.record(stream)
-    for _ in range(args.steps):
-        A_e.copy_(A_pin, non_blocking=True)
-        B_e.copy_(B_pin, non_blocking=True)
-        gbblas.gemm_(C_d, A_e.t(), B_e.t(), mode="ozaki", slices=args.slices)
-        C_pin.copy_(C_d.t(), non_blocking=True)
+    copy_stream.wait_stream(stream)
+
+    def upload(i):
+        b = i % 2
+        with torch.cuda.stream(copy_stream):
+            if i >= 2:
+                copy_stream.wait_event(comp_done[b])     # buffer b's previous compute is done
+            A_e[b].copy_(A_pin, non_blocking=True)
+            B_e[b].copy_(B_pin, non_blocking=True)
+            up_done[b].record(copy_stream)
+
+    upload(0)
+    for i in range(args.steps):
+        b = i % 2
+        if i + 1 < args.steps:
+            upload(i + 1)
+        stream.wait_event(up_done[b])
+        if i >= 2:
+            stream.wait_event(down_done[b])              # C_e[b] of step i-2 has been read
+        gbblas.gemm_(C_e[b].t(), A_e[b].t(), B_e[b].t(), mode="ozaki", slices=args.slices)
+        comp_done[b].record(stream)
+        with torch.cuda.stream(copy_stream):
+            copy_stream.wait_event(comp_done[b])
+            C_pin.copy_(C_e[b], non_blocking=True)
+            down_done[b].record(copy_stream)
+    stream.wait_stream(copy_stream)
     e1.record(stream)
     torch.cuda.synchronize()
     barrier()
@@ -510,6 +539,7 @@ def main():
             "kernel_ms_per_step": {k: v / args.steps for k, v in prof.ms.items()},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "TFLOP/s", "ms_per_step": ms_e2e,
+                    "pipeline": "double-buffered: uploads of step i+1 and download of step i overlap step i",
                     "h2d_bytes_per_step": int(A_pin.numel() * 8 + B_pin.numel() * 8),
                     "d2h_bytes_per_step": int(C_pin.numel() * 8)},
             "gpu_launches": launches,
