@@ -1,0 +1,92 @@
+"""Small single-kernel cases for profiling each gbblas kernel family under ncu.
+
+    python -m gbblas.profile_cases <case>        (run from jblas.jl_gb300/, or with it on sys.path)
+
+Each case runs one warm-up call and one measured call of the library on seeded inputs
+sized for a quick capture (inputs larger than L2 where the kernel streams memory, a few GB
+on the device at most), then prints the CUDA-event time of the measured call.
+
+cases:
+  native_f64     gb_gemm_f64 NATIVE, 4096^3
+  native_f32     gb_gemm_f32, 4096^3
+  ozaki          gb_gemm_f64 OZAKI (stats, split, slice products), 4096 x 4096 x 8192
+  grouped_f64    gb_gemm_grouped_f64, 4096 problems with m, n, k log-uniform in [8, 512]
+  adjoint        gb_gemm_adjoint_f32, A 4096 x 2048, B 2048 x 4096
+"""
+import sys
+
+import numpy as np
+import torch
+
+from . import api, grouped, workloads
+
+
+def _dev_cm(x):
+    return torch.from_numpy(np.ascontiguousarray(np.asarray(x).T)).cuda().t()
+
+
+def _timed(fn):
+    fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def case_native(dtype, n):
+    A = (torch.rand((n, n), dtype=dtype, device="cuda") * 2 - 1).t()
+    B = (torch.rand((n, n), dtype=dtype, device="cuda") * 2 - 1).t()
+    C = torch.empty((n, n), dtype=dtype, device="cuda").t()
+    return _timed(lambda: api.gemm_(C, A, B))
+
+
+def case_ozaki():
+    M, N, K = 4096, 4096, 8192
+    A = _dev_cm(workloads.ozaki_matrix(M, K, per="row", stream=1))
+    B = _dev_cm(workloads.ozaki_matrix(K, N, per="col", stream=2))
+    C = torch.empty((N, M), dtype=torch.float64, device="cuda").t()
+    return _timed(lambda: api.gemm_(C, A, B, mode="ozaki", slices=10))
+
+
+def case_grouped():
+    sizes = [tuple(int(x) for x in r) for r in workloads.grouped_sizes(4096)]
+    As = [(torch.rand((k, m), dtype=torch.float64, device="cuda") * 2 - 1).t() for m, n, k in sizes]
+    Bs = [(torch.rand((n, k), dtype=torch.float64, device="cuda") * 2 - 1).t() for m, n, k in sizes]
+    Cs = [torch.empty((n, m), dtype=torch.float64, device="cuda").t() for m, n, k in sizes]
+    plan = grouped.GroupedGemm(As, Bs, Cs)
+    return _timed(plan.run)
+
+
+def case_adjoint():
+    M, K, N = 4096, 2048, 4096
+    A = _dev_cm(workloads.normal(M, K, stream=51))
+    B = _dev_cm(workloads.normal(K, N, stream=52))
+    W = _dev_cm(workloads.normal(M, N, stream=53))
+    dA = torch.empty((K, M), dtype=torch.float32, device="cuda").t()
+    dB = torch.empty((N, K), dtype=torch.float32, device="cuda").t()
+    return _timed(lambda: api.gemm_adjoint_(dA, dB, A, B, W))
+
+
+CASES = {
+    "native_f64": lambda: case_native(torch.float64, 4096),
+    "native_f32": lambda: case_native(torch.float32, 4096),
+    "ozaki": case_ozaki,
+    "grouped_f64": case_grouped,
+    "adjoint": case_adjoint,
+}
+
+
+def main(argv):
+    if len(argv) != 1 or argv[0] not in CASES:
+        print(__doc__)
+        return 2
+    ms = CASES[argv[0]]()
+    print("%s: %.3f ms" % (argv[0], ms))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main(sys.argv[1:]))
