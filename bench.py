@@ -1,10 +1,12 @@
 #!/usr/bin/env python
-"""FP64-accurate GEMM throughput on GB300: Ozaki BF16 split vs native FP64.
+"""FP64-accurate GEMM throughput on GB300: Ozaki emulation on BF16 tensor cores vs native FP64.
 
 Workload (default): C = A * B, M = N = K = 8192, float64, A and B from the emulated-FP64
 configuration (sign * U[1,2) * 2^(e_line + e_elem), e_line in [-30, 30] per row of A /
-column of B, e_elem in [-8, 8] per element; seeded, synthetic), slice count chosen per
-problem by the library (slices = 0) to meet its normwise tolerance.
+column of B, e_elem in [-8, 8] per element; seeded, synthetic), emulated by the CRT method
+(--method crt: exact integer product of t-bit scaled operands from BF16 residue products
+modulo n coprime moduli) or by digit slices (--method slices); moduli / slices and t chosen
+per problem by the library (slices = 0) to meet its normwise tolerance.
 
 One JSON line (rank 0):
   value      FP64-equivalent TFLOP/s (2*M*N*K / time) of gb_gemm_f64 in Ozaki mode, inputs
@@ -45,7 +47,11 @@ def parse_args():
     p.add_argument("--impl", choices=["gbblas", "reference"], default="gbblas")
     p.add_argument("--size", type=int, default=8192)
     p.add_argument("--mnk", type=str, default=None, help="M,N,K override of --size (profiling cases)")
-    p.add_argument("--slices", type=int, default=0, help="0 = automatic (library tolerance)")
+    p.add_argument("--slices", type=int, default=0,
+                   help="digit slices (slice method) or moduli (crt method); 0 = automatic (library tolerance)")
+    p.add_argument("--method", choices=["crt", "slices"], default="crt",
+                   help="FP64 emulation: residue products + Chinese remainder theorem, or digit slices")
+    p.add_argument("--no-alt", action="store_true", help="skip timing the other emulation method")
     p.add_argument("--no-native", action="store_true", help="skip the native FP64 comparison")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU sample")
@@ -403,10 +409,11 @@ def main():
     C_d = torch.empty((N, M), dtype=torch.float64, device=dev).t()
     stream = torch.cuda.current_stream(dev)
 
-    # warm-up (also fixes the slice plan the library picks for these inputs)
+    mode = "ozaki_crt" if args.method == "crt" else "ozaki"
+    # warm-up (also fixes the plan the library picks for these inputs)
     bound = None
     for _ in range(args.warmup):
-        _, bound = gbblas.gemm_(C_d, A_d, B_d, mode="ozaki", slices=args.slices, return_bound=True)
+        _, bound = gbblas.gemm_(C_d, A_d, B_d, mode=mode, slices=args.slices, return_bound=True)
     torch.cuda.synchronize()
     gbblas.check_device_status()
     C_oz = np.asfortranarray(C_d.cpu().numpy())
@@ -421,7 +428,7 @@ def main():
     with gbblas.profile() as prof:
         ev0.record(stream)
         for _ in range(args.steps):
-            gbblas.gemm_(C_d, A_d, B_d, mode="ozaki", slices=args.slices)
+            gbblas.gemm_(C_d, A_d, B_d, mode=mode, slices=args.slices)
         ev1.record(stream)
         torch.cuda.synchronize()
     barrier()
@@ -465,7 +472,7 @@ def main():
         stream.wait_event(up_done[b])
         if i >= 2:
             stream.wait_event(down_done[b])              # C_e[b] of step i-2 has been read
-        gbblas.gemm_(C_e[b].t(), A_e[b].t(), B_e[b].t(), mode="ozaki", slices=args.slices)
+        gbblas.gemm_(C_e[b].t(), A_e[b].t(), B_e[b].t(), mode=mode, slices=args.slices)
         comp_done[b].record(stream)
         with torch.cuda.stream(copy_stream):
             copy_stream.wait_event(comp_done[b])
@@ -478,16 +485,36 @@ def main():
     ms_e2e = max_over_ranks(e0.elapsed_time(e1) / args.steps)
     e2e_value = world * flops / (ms_e2e * 1e-3) / 1e12
 
-    plan = None
+    plan = gbblas.last_ozaki_plan()   # the plan the automatic choice used
+    alt = None
+    if not args.no_alt:
+        # the other emulation method on the same inputs (automatic plan), for comparison
+        alt_mode = "ozaki" if mode == "ozaki_crt" else "ozaki_crt"
+        C_alt = torch.empty_like(C_d.t()).t()
+        for _ in range(2):
+            _, alt_bound = gbblas.gemm_(C_alt, A_d, B_d, mode=alt_mode, return_bound=True)
+        alt_plan = gbblas.last_ozaki_plan()
+        torch.cuda.synchronize()
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record(stream)
+        for _ in range(args.steps):
+            gbblas.gemm_(C_alt, A_d, B_d, mode=alt_mode)
+        a1.record(stream)
+        torch.cuda.synchronize()
+        alt_ms = a0.elapsed_time(a1) / args.steps
+        alt = {"method": "slices" if alt_mode == "ozaki" else "crt", "value": flops / (alt_ms * 1e-3) / 1e12,
+               "ms_per_step": alt_ms, "bound": alt_bound, "slices_or_moduli": alt_plan["slices"],
+               "bits": alt_plan["bits"], "tensor_products": alt_plan["products"]}
+        C_alt_h = np.asfortranarray(C_alt.cpu().numpy())
+        del C_alt
     line = None
     if rank == 0:
-        plan = gbblas.last_ozaki_plan()   # the plan the automatic slice choice used
         mma_ms = prof.ms.get("ozaki_slice_mma", float("nan")) / max(1, prof.launches.get("ozaki_slice_mma", 1))
         peaks, peak_src = load_peaks()
         timed_s = ms_step * args.steps / 1e3
         peak_key = "bf16_tflops_sustained" if timed_s >= 1.0 else "bf16_tflops"
         achieved = plan["flops_tensor"] / (mma_ms * 1e-3) / 1e12
-        traffic = committed_traffic("%d" % n) if not args.mnk else None
+        traffic = committed_traffic("%s_%d" % (args.method, n)) if not args.mnk else None
 
         # ------------------------------------------------------------ accuracy and native
         import oracle
@@ -495,6 +522,8 @@ def main():
         rows, cols = g.integers(0, M, 4096), g.integers(0, N, 4096)
         hi, lo, _ = oracle.dot2_entries(A_h, B_h, rows, cols)
         err_oz = normwise_err(C_oz, A_h, B_h, rows, cols, hi, lo)
+        if alt is not None:
+            alt["normwise_err"] = normwise_err(C_alt_h, A_h, B_h, rows, cols, hi, lo)
         native = None
         if not args.no_native:
             Cn = torch.empty_like(C_d.t()).t()
@@ -524,8 +553,12 @@ def main():
                        "ozaki_fp64_gemm_%dx%dx%d" % (M, N, K), "M": M, "N": N, "K": K,
                        "distribution": "sign*U[1,2)*2^(e_line+e_elem), e_line in [-30,30] per row/col, "
                                        "e_elem in [-8,8]",
-                       "slices": plan["slices"], "bits": plan["bits"], "slice_products": plan["products"],
-                       "accumulation_groups": plan["groups"], "alpha": 1.0, "beta": 0.0,
+                       "method": args.method,
+                       **({"moduli": plan["slices"], "integer_bits": plan["bits"],
+                           "residue_products": plan["products"]} if args.method == "crt" else
+                          {"slices": plan["slices"], "bits": plan["bits"], "slice_products": plan["products"],
+                           "accumulation_groups": plan["groups"]}),
+                       "k_chunk": plan["k_chunk"], "alpha": 1.0, "beta": 0.0,
                        "parallelism": "replicas" if world > 1 else "single",
                        "l2": "inputs larger than L2 (512 MiB per operand)"},
             "accuracy": {"normwise_err": err_oz, "bound": bound,
@@ -535,7 +568,9 @@ def main():
                          "frac": achieved / peaks[peak_key], "traffic": traffic,
                          "kernel": "ozaki_slice_mma", "ms_per_launch": mma_ms,
                          "peak_source": "%s %s" % (peak_src, peak_key),
-                         "work": "BF16 tensor flops per launch = slice_products * 2*M*N*ceil(K/64)*64"},
+                         "work": "BF16 tensor flops per launch = %s * 2*M*N*ceil(K/64)*64"
+                                 % ("moduli" if args.method == "crt" else "slice_products")},
+            "other_method": alt,
             "kernel_ms_per_step": {k: v / args.steps for k, v in prof.ms.items()},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "TFLOP/s", "ms_per_step": ms_e2e,

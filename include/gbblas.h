@@ -48,7 +48,9 @@ typedef enum {
 typedef enum {
   GB_MODE_NATIVE = 0,     /* FP64 FMA chain on the CUDA cores, jBLAS's per-element order */
   GB_MODE_OZAKI_BF16 = 1, /* FP64-accurate emulation: BF16 slices on tcgen05, exact FP32 sums */
-  GB_MODE_OZAKI_INT8 = 2  /* INT8 slices: GB_ERR_UNSUPPORTED on sm_103a (no tcgen05 kind::i8) */
+  GB_MODE_OZAKI_INT8 = 2, /* INT8 slices: GB_ERR_UNSUPPORTED on sm_103a (no tcgen05 kind::i8) */
+  GB_MODE_OZAKI_CRT = 3   /* FP64-accurate emulation: exact integer product from BF16 residues
+                             modulo pairwise coprime moduli (Chinese remainder theorem) */
 } gb_mode_t;
 
 const char* gb_status_string(int status);
@@ -93,6 +95,7 @@ typedef enum {
   GB_KERNEL_GROUPED_GEMM = 5,
   GB_KERNEL_ADJOINT_SPLIT = 6,
   GB_KERNEL_ADJOINT_MMA = 7,
+  GB_KERNEL_OZAKI_COMBINE = 8,   /* CRT reconstruction of the residue products */
   GB_KERNEL_KINDS = 16
 } gb_kernel_kind_t;
 const char* gb_kernel_kind_name(int kind);
@@ -126,6 +129,13 @@ int gb_jmul_f32(float* D, const float* A, const float* X, int64_t M, int64_t N, 
  *   the library's default tolerance, 2^-50 normwise); slice products run on tcgen05
  *   with exact FP32 accumulation and are recombined in FP64.  Rows of A or columns of
  *   B holding Inf/NaN give NaN in the outputs they touch.
+ * mode GB_MODE_OZAKI_CRT: rows of op(A) and columns of op(B) are scaled by powers of two
+ *   and rounded (half away from zero) to integers of t bits; their product is formed
+ *   exactly from `slices` residue products (one BF16 tcgen05 GEMM per modulus, moduli
+ *   <= 256, exact FP32 sums) and the Chinese remainder theorem, then rounded once to
+ *   FP64 and rescaled.  slices = number of moduli (1..20; t follows from K, see
+ *   gb_plan_ozaki_crt); slices = 0 picks the fewest moduli whose bound meets the
+ *   library tolerance (t then also uses the operands' row sums).  Inf/NaN as for BF16.
  * err_bound_out (host pointer, may be NULL): for OZAKI, an a-priori bound on
  *   ||C - C_exact||_F / (|alpha| ||A||_F ||B||_F) from the slicing truncation;
  *   the call then synchronises `stream` to read the split statistics.  For NATIVE it
@@ -220,8 +230,13 @@ typedef struct {
   double  flops_tensor;  /* BF16 tensor flops the plan issues */
 } gb_ozaki_plan_t;
 int gb_plan_ozaki(int64_t M, int64_t N, int64_t K, int slices, gb_ozaki_plan_t* out);
-/* The plan of the most recent OZAKI gb_gemm_f64 call made by the calling thread (zeroes
- * before the first), e.g. the slice count an automatic call picked. */
+/* CRT plan for `moduli` moduli (1..20): slices = moduli, bits = t (the integer width of
+ * the scaled operands: largest t <= 62 with 4 K 2^(2t) <= product of the moduli and
+ * K 2^(2t) <= 2^125), k_chunk, products = groups = moduli, flops_tensor.
+ * GB_ERR_UNSUPPORTED when no t >= 1 fits. */
+int gb_plan_ozaki_crt(int64_t M, int64_t N, int64_t K, int moduli, gb_ozaki_plan_t* out);
+/* The plan of the most recent OZAKI (BF16 or CRT) gb_gemm_f64 call made by the calling
+ * thread (zeroes before the first), e.g. the slice count an automatic call picked. */
 int gb_last_ozaki_plan(gb_ozaki_plan_t* out);
 
 #ifdef __cplusplus

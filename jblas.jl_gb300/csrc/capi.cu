@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 #include <cudaTypedefs.h>
 
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -197,6 +198,7 @@ static int exp_of(unsigned long long bits) {
 struct BoundStats {
   bool nonfinite = false;
   double na = 0, nb = 0, EA = 0, EB = 0, SA = 0, SB = 0;  // scaled by 2^-ref_a, 2^-ref_b
+  double sa_max = 0, sb_max = 0;   // max over rows of sum_k |x| 2^-e (upper bounds, unscaled)
 };
 
 static BoundStats bound_stats(const HostStats& h) {
@@ -216,8 +218,9 @@ static BoundStats bound_stats(const HostStats& h) {
   // sum x^2 >= s2 / (1 + K 2^-23) — one-sided bounds, as the error bound needs.
   const double Kd = static_cast<double>(h.K);
   const double gk = Kd * std::ldexp(1.0, -24);
-  const double up = gk < 0.5 ? (1.0 + std::ldexp(1.0, -23)) / (1.0 - gk) : 4.0;
-  const double down = 1.0 / (1.0 + 2.0 * gk);
+  // (the host sum of the K-slice partials adds at most a few ulps of FP64: 2^-40 slack)
+  const double up = (gk < 0.5 ? (1.0 + std::ldexp(1.0, -23)) / (1.0 - gk) : 4.0) * (1.0 + std::ldexp(1.0, -40));
+  const double down = (1.0 - std::ldexp(1.0, -40)) / (1.0 + 2.0 * gk);
   const double tiny = Kd * std::ldexp(1.0, -126);
   double e2a = 0, e2b = 0, na2 = 0, nb2 = 0, sa2 = 0, sb2 = 0;
   for (size_t i = 0; i < h.amax_a.size(); ++i) {
@@ -226,6 +229,7 @@ static BoundStats bound_stats(const HostStats& h) {
     e2a += std::ldexp(1.0, 2 * (e - ref_a));
     const double sa = std::ldexp(h.sabs_a[i] * up + tiny, e - ref_a);
     sa2 += sa * sa;
+    r.sa_max = std::max(r.sa_max, h.sabs_a[i] * up + tiny);
     na2 += std::ldexp(h.ssq_a[i] * down, 2 * (e - ref_a));
   }
   for (size_t j = 0; j < h.amax_b.size(); ++j) {
@@ -234,12 +238,74 @@ static BoundStats bound_stats(const HostStats& h) {
     e2b += std::ldexp(1.0, 2 * (e - ref_b));
     const double sb = std::ldexp(h.sabs_b[j] * up + tiny, e - ref_b);
     sb2 += sb * sb;
+    r.sb_max = std::max(r.sb_max, h.sabs_b[j] * up + tiny);
     nb2 += std::ldexp(h.ssq_b[j] * down, 2 * (e - ref_b));
   }
   r.na = std::sqrt(na2); r.nb = std::sqrt(nb2);
   r.EA = std::sqrt(e2a); r.EB = std::sqrt(e2b);
   r.SA = std::sqrt(sa2); r.SB = std::sqrt(sb2);
   return r;
+}
+
+static inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Statistics of both operands: run on the device; when `host` is set, copied back and the
+// K-slice sums rescaled to each row's exponent (Sum_s sum_s 2^(e_s - e)) into HostStats.
+struct OperandStats {
+  char* ws = nullptr;
+  OzRowStats a{}, b{};
+};
+
+static int run_stats(DeviceInfo* dev, const double* A, int64_t M, int64_t a_rs, int64_t a_ks, const double* B,
+                     int64_t N, int64_t b_rs, int64_t b_ks, int64_t K, bool host, OperandStats* os, HostStats* h,
+                     cudaStream_t s) {
+  const int Sa = oz_stats_kslices(M, K, a_ks, dev->sms), Sb = oz_stats_kslices(N, K, b_ks, dev->sms);
+  const int64_t pa = Sa * M, pb = Sb * N;
+  const size_t amax_bytes = align256((M + N) * sizeof(unsigned long long));
+  const size_t part_bytes = align256((pa + pb) * sizeof(int32_t));
+  GB_CUDA_TRY(cudaMallocFromPoolAsync(reinterpret_cast<void**>(&os->ws), amax_bytes + 3 * part_bytes, dev->pool, s));
+  os->a.amax_bits = reinterpret_cast<unsigned long long*>(os->ws);
+  os->b.amax_bits = os->a.amax_bits + M;
+  os->a.part_e = reinterpret_cast<int32_t*>(os->ws + amax_bytes);
+  os->b.part_e = os->a.part_e + pa;
+  os->a.part_sa = reinterpret_cast<float*>(os->ws + amax_bytes + part_bytes);
+  os->b.part_sa = os->a.part_sa + pa;
+  os->a.part_sq = reinterpret_cast<float*>(os->ws + amax_bytes + 2 * part_bytes);
+  os->b.part_sq = os->a.part_sq + pa;
+  os->a.kslices = Sa;
+  os->b.kslices = Sb;
+  int rc = oz_row_stats(A, M, K, a_rs, a_ks, os->a, host, s);
+  if (!rc) rc = oz_row_stats(B, N, K, b_rs, b_ks, os->b, host, s);
+  if (rc || !host) return rc;
+  std::vector<unsigned long long> amax(M + N);
+  std::vector<int32_t> pe(pa + pb);
+  std::vector<float> psa(pa + pb), psq(pa + pb);
+  cudaMemcpyAsync(amax.data(), os->a.amax_bits, (M + N) * 8, cudaMemcpyDeviceToHost, s);
+  cudaMemcpyAsync(pe.data(), os->a.part_e, (pa + pb) * 4, cudaMemcpyDeviceToHost, s);
+  cudaMemcpyAsync(psa.data(), os->a.part_sa, (pa + pb) * 4, cudaMemcpyDeviceToHost, s);
+  cudaMemcpyAsync(psq.data(), os->a.part_sq, (pa + pb) * 4, cudaMemcpyDeviceToHost, s);
+  const cudaError_t e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return gb_set_cuda_error(e, "ozaki statistics");
+  h->K = K;
+  auto combine = [&](int64_t R, int S, int64_t off_amax, int64_t off_part, std::vector<unsigned long long>& am,
+                     std::vector<double>& sabs, std::vector<double>& ssq) {
+    am.assign(amax.begin() + off_amax, amax.begin() + off_amax + R);
+    sabs.assign(R, 0.0);
+    ssq.assign(R, 0.0);
+    for (int64_t i = 0; i < R; ++i) {
+      const int er = exp_of(am[i]);
+      if (er == INT32_MAX || am[i] == 0) continue;
+      for (int sl = 0; sl < S; ++sl) {
+        const int64_t o = off_part + static_cast<int64_t>(sl) * R + i;
+        if (pe[o] == INT32_MAX) continue;
+        sabs[i] += std::ldexp(static_cast<double>(psa[o]), pe[o] - er);
+        ssq[i] += std::ldexp(static_cast<double>(psq[o]), 2 * (pe[o] - er));
+      }
+    }
+  };
+  combine(M, Sa, 0, 0, h->amax_a, h->sabs_a, h->ssq_a);
+  combine(N, Sb, M, pa, h->amax_b, h->sabs_b, h->ssq_b);
+  return GB_OK;
 }
 
 static double ozaki_bound(const BoundStats& st, int64_t K, const OzPlan& plan) {
@@ -270,8 +336,6 @@ static double ozaki_bound(const BoundStats& st, int64_t K, const OzPlan& plan) {
   return 1.01 * (trunc + recomb + fin) / (na * nb);
 }
 
-static inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
-
 static int ozaki_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int64_t K, double alpha,
                       const double* A, int64_t lda, const double* B, int64_t ldb, double beta,
                       double* C, int64_t ldc, int slices, double* err_bound_out, cudaStream_t s) {
@@ -282,44 +346,21 @@ static int ozaki_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int
   const int64_t b_rs = tb ? 1 : ldb, b_ks = tb ? ldb : 1;
   const int64_t pitch = ((K + 63) / 64) * 64;
 
-  // statistics workspace
-  const size_t st_bytes = align256((M + N) * sizeof(unsigned long long)) + 2 * align256((M + N) * sizeof(double));
-  char* st_ws = nullptr;
-  GB_CUDA_TRY(cudaMallocFromPoolAsync(reinterpret_cast<void**>(&st_ws), st_bytes, dev->pool, s));
-  OzRowStats sa, sb;
-  sa.amax_bits = reinterpret_cast<unsigned long long*>(st_ws);
-  sb.amax_bits = sa.amax_bits + M;
-  sa.sum_abs = reinterpret_cast<double*>(st_ws + align256((M + N) * sizeof(unsigned long long)));
-  sb.sum_abs = sa.sum_abs + M;
-  sa.sum_sq = reinterpret_cast<double*>(st_ws + align256((M + N) * sizeof(unsigned long long)) +
-                                        align256((M + N) * sizeof(double)));
-  sb.sum_sq = sa.sum_sq + M;
-  int rc = oz_row_stats(A, M, K, a_rs, a_ks, sa, s);
-  if (!rc) rc = oz_row_stats(B, N, K, b_rs, b_ks, sb, s);
+  OperandStats os;
+  HostStats h;
+  const bool host_stats = (slices == 0 || err_bound_out);
+  int rc = run_stats(dev, A, M, a_rs, a_ks, B, N, b_rs, b_ks, K, host_stats, &os, &h, s);
   if (rc) {
-    cudaFreeAsync(st_ws, s);
+    if (os.ws) cudaFreeAsync(os.ws, s);
     return rc;
   }
+  char* st_ws = os.ws;
+  OzRowStats& sa = os.a;
+  OzRowStats& sb = os.b;
 
   OzPlan plan;
   int s_use = slices;
-  if (slices == 0 || err_bound_out) {
-    HostStats h;
-    h.K = K;
-    h.amax_a.resize(M); h.amax_b.resize(N);
-    h.sabs_a.resize(M); h.sabs_b.resize(N);
-    h.ssq_a.resize(M); h.ssq_b.resize(N);
-    cudaMemcpyAsync(h.amax_a.data(), sa.amax_bits, M * 8, cudaMemcpyDeviceToHost, s);
-    cudaMemcpyAsync(h.amax_b.data(), sb.amax_bits, N * 8, cudaMemcpyDeviceToHost, s);
-    cudaMemcpyAsync(h.sabs_a.data(), sa.sum_abs, M * 8, cudaMemcpyDeviceToHost, s);
-    cudaMemcpyAsync(h.sabs_b.data(), sb.sum_abs, N * 8, cudaMemcpyDeviceToHost, s);
-    cudaMemcpyAsync(h.ssq_a.data(), sa.sum_sq, M * 8, cudaMemcpyDeviceToHost, s);
-    cudaMemcpyAsync(h.ssq_b.data(), sb.sum_sq, N * 8, cudaMemcpyDeviceToHost, s);
-    cudaError_t e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) {
-      cudaFreeAsync(st_ws, s);
-      return gb_set_cuda_error(e, "ozaki statistics");
-    }
+  if (host_stats) {
     const BoundStats bst = bound_stats(h);
     if (slices == 0) {
       // Cheapest plan (slices, K chunking -> digit width) whose bound meets the tolerance.
@@ -415,6 +456,145 @@ static int ozaki_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int
   return rc;
 }
 
+// ------------------------------------------------------------------ CRT driver
+// Normwise bound for the CRT mode with t integer bits (alpha = 1, beta = 0): rounding A and
+// B to the 2^(e - t) grid moves each element by at most 2^(e - t - 1); the integer product is
+// exact; the conversion to FP64 and the alpha product round once each.
+static double crt_bound(const BoundStats& st, int64_t K, int t) {
+  if (st.nonfinite) return INFINITY;
+  const double na = st.na, nb = st.nb;
+  if (na == 0.0 || nb == 0.0) return 0.0;
+  const double h = std::ldexp(1.0, -t - 1);
+  const double Kd = static_cast<double>(K);
+  const double trunc = h * (st.EA * st.SB + st.EB * st.SA) + Kd * h * h * st.EA * st.EB;
+  const double fin = 2.0 * std::ldexp(1.0, -53) * (na * nb + trunc);
+  return 1.01 * (trunc + fin) / (na * nb);
+}
+
+// Largest t for n moduli given row-sum statistics: |C'| <= 2^(2t) (min(max sa, max sb) +
+// K 2^(-t-1)) must stay <= M / 4 and <= 2^125 (checked in log2 with a safety margin).
+static int crt_bits_from_stats(const BoundStats& st, int64_t K, int n) {
+  const double lm = crt_log2_product(n);
+  const double Kd = static_cast<double>(K < 1 ? 1 : K);
+  for (int t = 62; t >= 1; --t) {
+    double S = std::min(st.sa_max, st.sb_max) + Kd * std::ldexp(1.0, -t - 1);
+    S = std::min(S, Kd) * (1.0 + 1e-12);
+    const double need = 2.0 * t + std::log2(S);
+    if (need + 2.0 <= lm - 1e-9 && need <= 125.0 - 1e-9) return t;
+  }
+  return 0;
+}
+
+static int crt_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int64_t K, double alpha, const double* A,
+                    int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc, int moduli,
+                    double* err_bound_out, cudaStream_t s) {
+  if (moduli < 0 || moduli > TC_MAX_MODULI) return GB_ERR_INVALID_VALUE;
+  if ((M + 255) / 256 * ((N + 255) / 256) > 0x7FFFFFFF) return GB_ERR_UNSUPPORTED;
+  const int64_t a_rs = ta ? lda : 1, a_ks = ta ? 1 : lda;
+  const int64_t b_rs = tb ? 1 : ldb, b_ks = tb ? ldb : 1;
+  const int64_t pitch = ((K + 63) / 64) * 64;
+
+  OperandStats os;
+  HostStats h;
+  const bool host_stats = (moduli == 0 || err_bound_out);
+  int rc = run_stats(dev, A, M, a_rs, a_ks, B, N, b_rs, b_ks, K, host_stats, &os, &h, s);
+  if (rc) {
+    if (os.ws) cudaFreeAsync(os.ws, s);
+    return rc;
+  }
+  char* st_ws = os.ws;
+  OzRowStats& sa = os.a;
+  OzRowStats& sb = os.b;
+
+  CrtPlan plan;
+  if (host_stats) {
+    const BoundStats bst = bound_stats(h);
+    if (moduli == 0) {
+      // fewest moduli (each one BF16 GEMM) whose bound, at the widest t they allow, meets
+      // the tolerance
+      const double tol = ozaki_tolerance();
+      int n_use = 0, t_use = 0;
+      for (int n = 1; n <= TC_MAX_MODULI && !n_use; ++n) {
+        const int t = bst.nonfinite ? crt_bits_for(K, n) : crt_bits_from_stats(bst, K, n);
+        if (t >= 1 && (bst.nonfinite || crt_bound(bst, K, t) <= tol)) {
+          n_use = n;
+          t_use = t;
+        }
+      }
+      if (!n_use) {   // tolerance out of reach: the most moduli
+        n_use = TC_MAX_MODULI;
+        t_use = bst.nonfinite ? crt_bits_for(K, n_use) : crt_bits_from_stats(bst, K, n_use);
+        if (t_use < 1) t_use = crt_bits_for(K, n_use);
+      }
+      rc = crt_make_plan(M, N, K, n_use, t_use, &plan);
+    } else {
+      rc = crt_make_plan(M, N, K, moduli, 0, &plan);
+    }
+    if (!rc && err_bound_out) *err_bound_out = crt_bound(bst, K, plan.t);
+  } else {
+    rc = crt_make_plan(M, N, K, moduli, 0, &plan);
+  }
+  if (rc) {
+    cudaFreeAsync(st_ws, s);
+    return rc;
+  }
+
+  g_last_plan.slices = plan.n;
+  g_last_plan.bits = plan.t;
+  g_last_plan.k_chunk = static_cast<int32_t>(plan.k_chunk);
+  g_last_plan.products = plan.n;
+  g_last_plan.groups = plan.n;
+  g_last_plan.flops_tensor = plan.flops_tensor;
+
+  const int n = plan.n;
+  const int64_t mpad = (M + 255) / 256 * 256, npad = (N + 255) / 256 * 256;
+  const size_t pa_bytes = align256(static_cast<size_t>(n) * M * pitch * 2);
+  const size_t pb_bytes = align256(static_cast<size_t>(n) * N * pitch * 2);
+  const size_t res_bytes = align256(static_cast<size_t>(n) * mpad * npad);
+  const size_t ex_bytes = align256((M + N) * sizeof(int32_t));
+  char* ws = nullptr;
+  cudaError_t e = cudaMallocFromPoolAsync(reinterpret_cast<void**>(&ws), pa_bytes + pb_bytes + res_bytes + ex_bytes,
+                                          dev->pool, s);
+  if (e != cudaSuccess) {
+    cudaFreeAsync(st_ws, s);
+    return gb_set_cuda_error(e, "ozaki crt workspace");
+  }
+  __nv_bfloat16* pa = reinterpret_cast<__nv_bfloat16*>(ws);
+  __nv_bfloat16* pb = reinterpret_cast<__nv_bfloat16*>(ws + pa_bytes);
+  uint8_t* res = reinterpret_cast<uint8_t*>(ws + pa_bytes + pb_bytes);
+  int32_t* ea = reinterpret_cast<int32_t*>(ws + pa_bytes + pb_bytes + res_bytes);
+  int32_t* eb = ea + M;
+  rc = crt_split(A, M, K, a_rs, a_ks, sa.amax_bits, plan, pa, pitch, ea, s);
+  if (!rc) rc = crt_split(B, N, K, b_rs, b_ks, sb.amax_bits, plan, pb, pitch, eb, s);
+  if (!rc) {
+    CrtGemmArgs ga;
+    ga.planes_a = pa;
+    ga.planes_b = pb;
+    ga.pitch = pitch;
+    ga.M = M;
+    ga.N = N;
+    ga.K = K;
+    ga.ea = ea;
+    ga.eb = eb;
+    ga.alpha = alpha;
+    ga.beta = beta;
+    ga.C = C;
+    ga.ldc = ldc;
+    ga.res = res;
+    ga.res_ld = mpad;
+    ga.res_plane = mpad * npad;
+    ga.status = dev->status;
+    ga.wait_limit_ns = g_wait_limit_ns.load();
+    const int64_t ctas = 2 * static_cast<int64_t>(tc_pair_tiles(M, N));
+    const int64_t cap = dev->sms & ~1;
+    ga.grid = static_cast<int>(ctas < cap ? ctas : cap);
+    rc = crt_gemm_launch(ga, plan, s);
+  }
+  cudaFreeAsync(ws, s);
+  cudaFreeAsync(st_ws, s);
+  return rc;
+}
+
 }  // namespace gb
 
 using namespace gb;
@@ -492,7 +672,8 @@ int gb_check_status(void* stream) {
 int gb_gemm_f64(int transA, int transB, int64_t M, int64_t N, int64_t K, double alpha, const double* A,
                 int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc, int mode,
                 int slices, double* err_bound_out, void* stream) {
-  if (mode != GB_MODE_NATIVE && mode != GB_MODE_OZAKI_BF16 && mode != GB_MODE_OZAKI_INT8)
+  if (mode != GB_MODE_NATIVE && mode != GB_MODE_OZAKI_BF16 && mode != GB_MODE_OZAKI_INT8 &&
+      mode != GB_MODE_OZAKI_CRT)
     return GB_ERR_INVALID_VALUE;
   DeviceInfo* dev = nullptr;
   int rc = device_info(&dev);
@@ -516,6 +697,8 @@ int gb_gemm_f64(int transA, int transB, int64_t M, int64_t N, int64_t K, double 
     }
     return native_gemm_f64(transA, transB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, s);
   }
+  if (mode == GB_MODE_OZAKI_CRT)
+    return crt_gemm(dev, transA, transB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, slices, err_bound_out, s);
   return ozaki_gemm(dev, transA, transB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, slices,
                     err_bound_out, s);
 }
@@ -645,6 +828,20 @@ int gb_plan_ozaki(int64_t M, int64_t N, int64_t K, int slices, gb_ozaki_plan_t* 
   out->k_chunk = static_cast<int32_t>(p.k_chunk);
   out->products = p.products;
   out->groups = p.groups;
+  out->flops_tensor = p.flops_tensor;
+  return GB_OK;
+}
+
+int gb_plan_ozaki_crt(int64_t M, int64_t N, int64_t K, int moduli, gb_ozaki_plan_t* out) {
+  if (!out || M < 0 || N < 0 || K < 0 || moduli < 1 || moduli > TC_MAX_MODULI) return GB_ERR_INVALID_VALUE;
+  CrtPlan p;
+  const int rc = crt_make_plan(M, N, K, moduli, 0, &p);
+  if (rc) return rc;
+  out->slices = p.n;
+  out->bits = p.t;
+  out->k_chunk = static_cast<int32_t>(p.k_chunk);
+  out->products = p.n;
+  out->groups = p.n;
   out->flops_tensor = p.flops_tensor;
   return GB_OK;
 }

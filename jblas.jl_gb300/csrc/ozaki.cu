@@ -32,6 +32,7 @@
 #include <cstring>
 
 #include "gb_common.cuh"
+#include "oz_fixed.cuh"
 #include "ozaki.cuh"
 #include "profile.cuh"
 #include "tc_gemm.cuh"
@@ -132,34 +133,42 @@ __device__ __forceinline__ float scaled_f32_trunc(unsigned long long abits, int 
   return __uint_as_float((static_cast<uint32_t>(fe) << 23) | static_cast<uint32_t>((abits >> 29) & 0x7FFFFF));
 }
 
-__device__ __forceinline__ int row_exponent_of(unsigned long long amax_bits);
 
-// Row statistics in two passes without FP64 arithmetic (GB300's FP64 pipe is narrow):
-// the exact max |x| by integer compare, then sum |x| 2^-e and sum x^2 2^-2e in FP32 over
-// truncated scaled values (e: row exponent).  The host turns the scaled sums into rigorous
-// one-sided bounds (see bound_stats).
-// k contiguous (ks == 1): one warp per row.
-__global__ void stats_kc_kernel(const double* __restrict__ X, int64_t R, int64_t K, int64_t rs,
-                                OzRowStats st) {
+// Row statistics without FP64 arithmetic (GB300's FP64 pipe is narrow), in one read of X:
+// the exact max |x| by integer compare (atomicMax across K slices), then, when the host
+// asks for them, sums of |x| 2^-e_s and x^2 2^-2e_s in FP32 over truncated scaled values,
+// e_s the exponent of the slice's own max (the second sweep of a slice hits L1/L2).  The
+// host rescales the slice sums to the row exponent and turns them into rigorous one-sided
+// bounds (see bound_stats).
+__device__ __forceinline__ unsigned long long umax64(unsigned long long a, unsigned long long b) {
+  return a > b ? a : b;
+}
+
+// k contiguous (ks == 1): one warp per row, one K slice.
+template <bool SUMS>
+__global__ void __launch_bounds__(256) stats_kc_kernel(const double* __restrict__ X, int64_t R, int64_t K,
+                                                       int64_t rs, OzRowStats st) {
   const int lane = threadIdx.x & 31;
   const int64_t r = static_cast<int64_t>(blockIdx.x) * (blockDim.x / 32) + (threadIdx.x >> 5);
   if (r >= R) return;
   const unsigned long long* row = reinterpret_cast<const unsigned long long*>(X + r * rs);
   unsigned long long mx = 0;
-  for (int64_t k = lane; k < K; k += 32) {
-    const unsigned long long b = row[k] & 0x7FFFFFFFFFFFFFFFull;
-    mx = b > mx ? b : mx;
+  int64_t k = lane;
+  for (; k + 96 < K; k += 128) {
+    const unsigned long long b0 = row[k], b1 = row[k + 32], b2 = row[k + 64], b3 = row[k + 96];
+    mx = umax64(mx, umax64(umax64(b0 & 0x7FFFFFFFFFFFFFFFull, b1 & 0x7FFFFFFFFFFFFFFFull),
+                           umax64(b2 & 0x7FFFFFFFFFFFFFFFull, b3 & 0x7FFFFFFFFFFFFFFFull)));
   }
+  for (; k < K; k += 32) mx = umax64(mx, row[k] & 0x7FFFFFFFFFFFFFFFull);
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    const unsigned long long m2 = __shfl_xor_sync(0xffffffffu, mx, o);
-    mx = m2 > mx ? m2 : mx;
-  }
+  for (int o = 16; o > 0; o >>= 1) mx = umax64(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if (lane == 0) st.amax_bits[r] = mx;
+  if (!SUMS) return;
   const int e = row_exponent_of(mx);
   float sa = 0.0f, sq = 0.0f;
-  if (e != 0x7FFFFFFF) {
-    for (int64_t k = lane; k < K; k += 32) {
-      const float f = scaled_f32_trunc(row[k] & 0x7FFFFFFFFFFFFFFFull, e);
+  if (e != OZ_EXP_NONFINITE) {
+    for (int64_t k2 = lane; k2 < K; k2 += 32) {
+      const float f = scaled_f32_trunc(row[k2] & 0x7FFFFFFFFFFFFFFFull, e);
       sa += f;
       sq = fmaf(f, f, sq);
     }
@@ -170,34 +179,43 @@ __global__ void stats_kc_kernel(const double* __restrict__ X, int64_t R, int64_t
     sq += __shfl_xor_sync(0xffffffffu, sq, o);
   }
   if (lane == 0) {
-    st.amax_bits[r] = mx;
-    st.sum_abs[r] = static_cast<double>(sa);
-    st.sum_sq[r] = static_cast<double>(sq);
+    st.part_e[r] = e;
+    st.part_sa[r] = sa;
+    st.part_sq[r] = sq;
   }
 }
 
-// rows contiguous (rs == 1): 32 rows per block, 8 warps stride over k.
-__global__ void stats_rc_kernel(const double* __restrict__ X, int64_t R, int64_t K, int64_t ks,
-                                OzRowStats st) {
+// rows contiguous (rs == 1): 32 rows x one K slice per block, 8 warps stride over k.
+template <bool SUMS>
+__global__ void __launch_bounds__(256) stats_rc_kernel(const double* __restrict__ X, int64_t R, int64_t K,
+                                                       int64_t ks, int64_t kslice, OzRowStats st) {
   __shared__ unsigned long long smx[8][32];
   __shared__ float ssa[8][32], ssq[8][32];
   const int tr = threadIdx.x & 31, tk = threadIdx.x >> 5;
   const int64_t r = static_cast<int64_t>(blockIdx.x) * 32 + tr;
+  const int64_t k0 = static_cast<int64_t>(blockIdx.y) * kslice;
+  const int64_t k1 = (k0 + kslice < K) ? k0 + kslice : K;
   const unsigned long long* Xb = reinterpret_cast<const unsigned long long*>(X);
   unsigned long long mx = 0;
   if (r < R) {
-    for (int64_t k = tk; k < K; k += 8) {
-      const unsigned long long b = Xb[r + k * ks] & 0x7FFFFFFFFFFFFFFFull;
-      mx = b > mx ? b : mx;
+    int64_t k = k0 + tk;
+    for (; k + 24 < k1; k += 32) {
+      const unsigned long long b0 = Xb[r + k * ks], b1 = Xb[r + (k + 8) * ks];
+      const unsigned long long b2 = Xb[r + (k + 16) * ks], b3 = Xb[r + (k + 24) * ks];
+      mx = umax64(mx, umax64(umax64(b0 & 0x7FFFFFFFFFFFFFFFull, b1 & 0x7FFFFFFFFFFFFFFFull),
+                             umax64(b2 & 0x7FFFFFFFFFFFFFFFull, b3 & 0x7FFFFFFFFFFFFFFFull)));
     }
+    for (; k < k1; k += 8) mx = umax64(mx, Xb[r + k * ks] & 0x7FFFFFFFFFFFFFFFull);
   }
   smx[tk][tr] = mx;
   __syncthreads();
-  for (int w = 0; w < 8; ++w) mx = smx[w][tr] > mx ? smx[w][tr] : mx;
+  for (int w = 0; w < 8; ++w) mx = umax64(mx, smx[w][tr]);
+  if (tk == 0 && r < R && mx) atomicMax(st.amax_bits + r, mx);
+  if (!SUMS) return;
   const int e = row_exponent_of(mx);
   float sa = 0.0f, sq = 0.0f;
-  if (r < R && e != 0x7FFFFFFF) {
-    for (int64_t k = tk; k < K; k += 8) {
+  if (r < R && e != OZ_EXP_NONFINITE) {
+    for (int64_t k = k0 + tk; k < k1; k += 8) {
       const float f = scaled_f32_trunc(Xb[r + k * ks] & 0x7FFFFFFFFFFFFFFFull, e);
       sa += f;
       sq = fmaf(f, f, sq);
@@ -211,92 +229,51 @@ __global__ void stats_rc_kernel(const double* __restrict__ X, int64_t R, int64_t
       sa += ssa[w][tr];
       sq += ssq[w][tr];
     }
-    st.amax_bits[r] = mx;
-    st.sum_abs[r] = static_cast<double>(sa);
-    st.sum_sq[r] = static_cast<double>(sq);
+    const int64_t o = static_cast<int64_t>(blockIdx.y) * R + r;
+    st.part_e[o] = e;
+    st.part_sa[o] = sa;
+    st.part_sq[o] = sq;
   }
 }
 
-int oz_row_stats(const double* X, int64_t R, int64_t K, int64_t rs, int64_t ks, OzRowStats st,
+int oz_stats_kslices(int64_t R, int64_t K, int64_t ks, int sms) {
+  if (ks == 1 || R <= 0 || K <= 0) return 1;
+  const int64_t row_blocks = (R + 31) / 32;
+  int64_t S = (4 * static_cast<int64_t>(sms) + row_blocks - 1) / row_blocks;
+  const int64_t smax = (K + 255) / 256;
+  if (S > smax) S = smax;
+  if (S > 65535) S = 65535;
+  if (S < 1) S = 1;
+  const int64_t kslice = (K + S - 1) / S;
+  return static_cast<int>((K + kslice - 1) / kslice);
+}
+
+int oz_row_stats(const double* X, int64_t R, int64_t K, int64_t rs, int64_t ks, OzRowStats st, bool sums,
                  cudaStream_t s) {
   if (R <= 0) return GB_OK;
+  GB_CUDA_TRY(cudaMemsetAsync(st.amax_bits, 0, R * sizeof(unsigned long long), s));
+  if (K <= 0) return GB_OK;
   if (ks == 1) {
     const int64_t blocks = (R + 7) / 8;
-    GB_LAUNCH(GB_KERNEL_OZAKI_STATS, s,
-              stats_kc_kernel<<<static_cast<unsigned>(blocks), 256, 0, s>>>(X, R, K, rs, st));
+    if (sums)
+      GB_LAUNCH(GB_KERNEL_OZAKI_STATS, s,
+                stats_kc_kernel<true><<<static_cast<unsigned>(blocks), 256, 0, s>>>(X, R, K, rs, st));
+    else
+      GB_LAUNCH(GB_KERNEL_OZAKI_STATS, s,
+                stats_kc_kernel<false><<<static_cast<unsigned>(blocks), 256, 0, s>>>(X, R, K, rs, st));
   } else {
-    const int64_t blocks = (R + 31) / 32;
-    GB_LAUNCH(GB_KERNEL_OZAKI_STATS, s,
-              stats_rc_kernel<<<static_cast<unsigned>(blocks), 256, 0, s>>>(X, R, K, ks, st));
+    const int64_t kslice = (K + st.kslices - 1) / st.kslices;
+    dim3 grid(static_cast<unsigned>((R + 31) / 32), static_cast<unsigned>(st.kslices));
+    if (sums)
+      GB_LAUNCH(GB_KERNEL_OZAKI_STATS, s, stats_rc_kernel<true><<<grid, 256, 0, s>>>(X, R, K, ks, kslice, st));
+    else
+      GB_LAUNCH(GB_KERNEL_OZAKI_STATS, s, stats_rc_kernel<false><<<grid, 256, 0, s>>>(X, R, K, ks, kslice, st));
   }
   GB_CUDA_TRY(cudaGetLastError());
   return GB_OK;
 }
 
 // ============================================================== split kernels
-
-constexpr int OZ_EXP_NONFINITE = 0x7FFFFFFF;
-
-__device__ __forceinline__ int row_exponent_of(unsigned long long amax_bits) {
-  if (amax_bits >= 0x7FF0000000000000ull) return OZ_EXP_NONFINITE;  // Inf or NaN in the row
-  if (amax_bits == 0) return 0;
-  return ilogb(__longlong_as_double(static_cast<long long>(amax_bits))) + 1;  // amax < 2^e
-}
-
-__device__ __forceinline__ int row_exponent(unsigned long long amax_bits) {
-  if (amax_bits >= 0x7FF0000000000000ull) return OZ_EXP_NONFINITE;  // Inf or NaN in the row
-  if (amax_bits == 0) return 0;
-  return ilogb(__longlong_as_double(static_cast<long long>(amax_bits))) + 1;  // amax < 2^e
-}
-
-// Digit extraction in integer arithmetic (GB300's FP64 pipe is ~1/64 of FP32, so the
-// split never touches it).  For a row with exponent e (amax < 2^e) and SB = slices*bits:
-//   Y = round-half-away(x * 2^(SB-1-e))          an integer, |Y| <= 2^(SB-1)
-//   digits d_s..d_2 = balanced base-2^b digits of Y, in [-2^(b-1), 2^(b-1));  d_1 the rest
-//   so x * 2^-e = sum_p d_p 2^(1 - p*b) + delta,  |delta| <= 2^-SB,  |d_1| <= 2^(b-1).
-// Y is built from the IEEE fields of x (m * 2^(ex-52)) with shifts only.  Word = uint64_t
-// for SB <= 62, unsigned __int128 beyond.
-template <typename Word>
-__device__ __forceinline__ Word fixed_point(double x, int e, int SB) {
-  const unsigned long long bits = static_cast<unsigned long long>(__double_as_longlong(x));
-  const int biased = static_cast<int>((bits >> 52) & 0x7FF);
-  unsigned long long m = bits & 0x000FFFFFFFFFFFFFull;
-  int ex = -1022;
-  if (biased) {
-    m |= 0x0010000000000000ull;
-    ex = biased - 1023;
-  }
-  Word mag = 0;
-  if (m) {
-    const int sh = ex - 53 + SB - e;   // v = m * 2^sh
-    if (sh >= 0) {
-      mag = static_cast<Word>(m) << sh;
-    } else {
-      const int t = -sh;
-      if (t < 64) mag = static_cast<Word>((m + (1ull << (t - 1))) >> t);
-    }
-  }
-  return (bits >> 63) ? static_cast<Word>(0) - mag : mag;
-}
-
-// Signed arithmetic shift of a two's-complement word.
-template <typename Word>
-__device__ __forceinline__ Word sar(Word y, int b);
-template <>
-__device__ __forceinline__ uint64_t sar<uint64_t>(uint64_t y, int b) {
-  return static_cast<uint64_t>(static_cast<int64_t>(y) >> b);
-}
-template <>
-__device__ __forceinline__ unsigned __int128 sar<unsigned __int128>(unsigned __int128 y, int b) {
-  return static_cast<unsigned __int128>(static_cast<__int128>(y) >> b);
-}
-
-// Exact BF16 of a small integer |d| <= 2^22 without a conversion instruction:
-// float(d) = bits(1.5*2^23 + d) - 1.5*2^23, then the upper half of the float is the BF16.
-__device__ __forceinline__ uint32_t bf16_bits_of_int(int d) {
-  const float f = __int_as_float(0x4B400000 + d) - 12582912.0f;
-  return __float_as_uint(f) >> 16;
-}
 
 // 16 consecutive k of one row -> `slices` planes of 16 BF16 digits (two 16-byte stores each).
 template <typename Word>

@@ -34,16 +34,22 @@ int oz_make_plan_chunks(int64_t M, int64_t N, int64_t K, int slices, int min_chu
 // Relative per-tile cost of a plan (tensor work vs FP64 drains), for choosing among plans.
 double oz_plan_cost(const OzPlan& p);
 
-// Per-row statistics of op(X) (rows r < R, contraction index k < K): amax bits of |x|
-// (as uint64, exact), and FP32 sums of |x| 2^-e and x^2 2^-2e over truncated values, e the
-// row exponent (max |x| < 2^e); the host turns them into one-sided bounds.
+// Per-row statistics of op(X) (rows r < R, contraction index k < K), cut into `kslices`
+// K slices: amax bits of |x| per row (uint64, exact; zeroed and filled by oz_row_stats),
+// and per slice s the exponent e_s of the slice's max (max < 2^e_s) with FP32 sums of
+// |x| 2^-e_s and x^2 2^-2e_s over truncated values ([s][R] arrays; only with sums = true).
+// The host rescales the slice sums to the row exponent and bounds them one-sidedly.
 struct OzRowStats {
   unsigned long long* amax_bits;
-  double* sum_abs;
-  double* sum_sq;
+  int32_t* part_e;
+  float* part_sa;
+  float* part_sq;
+  int32_t kslices;
 };
 
-int oz_row_stats(const double* X, int64_t R, int64_t K, int64_t rs, int64_t ks, OzRowStats st,
+// K slices the statistics kernel uses for this layout (1 when k is contiguous).
+int oz_stats_kslices(int64_t R, int64_t K, int64_t ks, int sms);
+int oz_row_stats(const double* X, int64_t R, int64_t K, int64_t rs, int64_t ks, OzRowStats st, bool sums,
                  cudaStream_t s);
 // Writes `slices` digit planes (BF16, [slice][row][pitch]) and per-row exponents.
 int oz_split(const double* X, int64_t R, int64_t K, int64_t rs, int64_t ks,
@@ -69,6 +75,62 @@ struct OzGemmArgs {
 int oz_gemm_launch(const OzGemmArgs& a, const OzPlan& plan, cudaStream_t s);
 // Persistent grid size: one CTA per SM, at most one per output tile.
 int oz_grid_for(int sms, int64_t M, int64_t N);
+
+// ---------------------------------------------------------------- CRT mode (ozaki_crt.cu)
+// Constants of one CRT product, passed by value to the split and combine kernels.
+struct CrtConsts {
+  int32_t n;                       // moduli
+  int32_t t;                       // integer bits: |A'|, |B'| <= 2^t
+  uint32_t p[TC_MAX_MODULI];       // the moduli (pairwise coprime, <= 256)
+  uint32_t c21[TC_MAX_MODULI];     // 2^21 mod p
+  uint32_t c42[TC_MAX_MODULI];     // 2^42 mod p
+  uint32_t bias[TC_MAX_MODULI];    // -2^62 mod p
+  uint32_t mg[TC_MAX_MODULI];      // floor(2^32 / p)
+  float finv[TC_MAX_MODULI];       // fl32(inv_g / p_g), inv_g = (M / p_g)^-1 mod p_g
+  uint32_t w[TC_MAX_MODULI][4];    // (M / p_g) inv_g mod 2^128, little-endian 32-bit words
+  uint32_t m[4];                   // M mod 2^128
+};
+
+struct CrtPlan {
+  int n, t;
+  int64_t k_chunk;
+  int32_t kb_total;
+  int nchunks;
+  double flops_tensor;
+  double log2_m;
+  SliceSchedule sched;   // one group per modulus, pair (g, g)
+  CrtConsts cc;
+};
+
+const uint32_t* crt_moduli();       // TC_MAX_MODULI moduli, in the order they are used
+double crt_log2_product(int n);     // log2 of the product of the first n moduli
+// Largest t <= 62 with 4 K 2^(2t) <= prod(first n moduli) and K 2^(2t) <= 2^125 (0: none).
+int crt_bits_for(int64_t K, int n);
+// Plan for n moduli and t integer bits (t = 0: crt_bits_for(K, n)).
+int crt_make_plan(int64_t M, int64_t N, int64_t K, int n, int t, CrtPlan* plan);
+// Residue planes (BF16, [modulus][row][pitch]) and row exponents of op(X).
+int crt_split(const double* X, int64_t R, int64_t K, int64_t rs, int64_t ks, const unsigned long long* amax_bits,
+              const CrtPlan& plan, __nv_bfloat16* planes, int64_t pitch, int32_t* exps, cudaStream_t s);
+
+struct CrtGemmArgs {
+  const void* planes_a;   // [n][M][pitch] bf16
+  const void* planes_b;   // [n][N][pitch] bf16
+  int64_t pitch;
+  int64_t M, N, K;
+  const int32_t* ea;
+  const int32_t* eb;
+  double alpha, beta;
+  double* C;
+  int64_t ldc;
+  uint8_t* res;           // [n][ceil(N/256)*256][res_ld] residues
+  int64_t res_ld;         // ceil(M/256)*256
+  int64_t res_plane;
+  DeviceStatus* status;
+  uint64_t wait_limit_ns;
+  int grid;               // even (CTA pairs)
+};
+// Residue products on the CTA-pair engine, then the CRT reconstruction into C.
+int crt_gemm_launch(const CrtGemmArgs& a, const CrtPlan& plan, cudaStream_t s);
 
 
 }  // namespace gb

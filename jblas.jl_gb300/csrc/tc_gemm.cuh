@@ -6,6 +6,8 @@
 //   TC_EPI_OZAKI_F64  exact integer group sums, accumulated in FP64 per tile (smallest
 //                     level first), rescaled by 2^(ea_i + eb_j) with alpha/beta, FP64 out
 //   TC_EPI_F32        one group, C = alpha * sum + beta * C in FP32 (split-BF16 products)
+//   TC_EPI_CRT        one group per modulus p_g: the exact chunk sum is reduced mod p_g and
+//                     added (mod p_g) into a uint8 residue plane (CTA-pair engine only)
 // One launch may carry two independent problems (the adjoint's dA and dB); CTAs walk
 // the concatenated tile list.
 #pragma once
@@ -24,7 +26,8 @@ constexpr int TC_BN = 256;   // tile columns (TMEM columns per accumulator)
 constexpr int TC_BK = 64;    // BF16 elements per 128-byte swizzled row
 constexpr int TC_STAGES = 4;
 
-enum TcEpilogue { TC_EPI_OZAKI_F64 = 0, TC_EPI_F32 = 1 };
+enum TcEpilogue { TC_EPI_OZAKI_F64 = 0, TC_EPI_F32 = 1, TC_EPI_CRT = 2 };
+constexpr int TC_MAX_MODULI = 20;
 
 // Group g sums the products (pp[off+i], pq[off+i]), i < npairs[g], of level[g].
 struct SliceSchedule {
@@ -60,6 +63,13 @@ struct TcParams {
   double* tws;          // per-CTA FP64 tile buffers (Ozaki, more than one drain per tile)
   DeviceStatus* status;
   uint64_t wait_limit_ns;
+  // TC_EPI_CRT: residue planes res[g][col][row] (uint8, rows padded to res_ld, column
+  // count padded to whole tiles) and, per modulus g (= group), p_g and fl32(1 / p_g)
+  uint8_t* res;
+  int64_t res_ld;
+  int64_t res_plane;
+  float crt_p[TC_MAX_MODULI];
+  float crt_inv[TC_MAX_MODULI];
 };
 
 // Tensor maps for problem 0 and (optionally) problem 1; box 64 x 128 for A, 64 x 256 for B.

@@ -30,6 +30,11 @@ constexpr int P2_B_BYTES = 128 * TC_BK * 2;     // 16 KB: this CTA's half of B
 constexpr int P2_STAGE_BYTES = P2_A_BYTES + P2_B_BYTES;
 constexpr int P2_TMEM_COLS = 512;
 constexpr int P2_SMEM_BYTES = P2_STAGES * P2_STAGE_BYTES + 1024 + 256;
+// TC_EPI_CRT keeps each CTA's running residues (128 rows x 256 columns, one byte each) in
+// shared memory after the barriers: row r's 64 words are rotated by r so that the 32 rows
+// of a warp hit 32 different banks.
+constexpr int P2_RES_BYTES = 128 * 256;
+constexpr int P2_SMEM_BYTES_CRT = P2_SMEM_BYTES + P2_RES_BYTES;
 constexpr int P2_EXP_NONFINITE = 0x7FFFFFFF;
 constexpr uint64_t P2_CLEANUP_WAIT_NS = 2000000000ull;
 
@@ -241,9 +246,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(P2_THREADS, 1)
       const double alpha = P.alpha, beta = P.beta;
       int ea = 0;
       if (EPI == TC_EPI_OZAKI_F64) ea = row_ok ? P.ea[row] : 0;
-      double* __restrict__ tws = prm.tws + static_cast<int64_t>(blockIdx.x) * (TC_BM * TC_BN);
+      double* __restrict__ tws = prm.tws ? prm.tws + static_cast<int64_t>(blockIdx.x) * (TC_BM * TC_BN) : nullptr;
       int step = 0;
       const int nsteps = G * P.nchunks;
+      uint32_t* res_s = reinterpret_cast<uint32_t*>(smem + P2_STAGES * P2_STAGE_BYTES + 256) + row_l * 64;
       for (int g = 0; g < G && ok; ++g) {
         const int wexp = 2 - sched.level[g] * sched.bits;
         const unsigned long long wbias = static_cast<unsigned long long>(896 + wexp) << 23;
@@ -254,6 +260,45 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(P2_THREADS, 1)
           tc_fence_after();
           const bool first = (step == 0), last = (step == nsteps - 1);
           const uint32_t taddr = tmem_base + (static_cast<uint32_t>(q * 32) << 16) + static_cast<uint32_t>(buf * TC_BN);
+          if (EPI == TC_EPI_CRT) {
+            // The chunk sum (an exact integer, |S| <= 2^24) is reduced mod p_g in FP32 and
+            // added mod p_g into this thread's running residues (its row x 128 columns, 4
+            // per shared-memory word); the last chunk stores them as bytes into the residue
+            // plane (rows and columns padded to whole tiles, so always in bounds).
+            const float pf = prm.crt_p[g], inv = prm.crt_inv[g];
+            const int pi = static_cast<int>(pf);
+            const bool first_c = (c == 0), last_c = (c == P.nchunks - 1);
+            const int64_t ld = prm.res_ld;
+#pragma unroll
+            for (int bi = 0; bi < 8; ++bi) {   // 16 columns per TMEM load
+              uint32_t v[16];
+              tmem_ld_32x32b_x16(taddr + col0 + bi * 16, v);
+              tc_wait_ld();
+#pragma unroll
+              for (int j4 = 0; j4 < 4; ++j4) {
+                const int widx = ((col0 >> 2) + bi * 4 + j4 + row_l) & 63;
+                const uint32_t old = first_c ? 0u : res_s[widx];
+                uint32_t nw = 0;
+#pragma unroll
+                for (int jj = 0; jj < 4; ++jj) {
+                  const float vf = __uint_as_float(v[j4 * 4 + jj]);
+                  const float qf = fmaf(vf, inv, 12582912.0f) - 12582912.0f;   // S/p rounded (+-1)
+                  const float rf = fmaf(-pf, qf, vf);                           // exact, |rf| <= p/2 + 1
+                  int r = (__float_as_int(rf + 12582912.0f) - 0x4B400000) + static_cast<int>((old >> (8 * jj)) & 0xFFu);
+                  r += (r < 0) ? pi : 0;
+                  r -= (r >= pi) ? pi : 0;
+                  nw |= static_cast<uint32_t>(r) << (8 * jj);
+                }
+                if (last_c) {
+                  uint8_t* __restrict__ dst = prm.res + g * prm.res_plane + (n0 + col0 + bi * 16 + j4 * 4) * ld + row;
+#pragma unroll
+                  for (int jj = 0; jj < 4; ++jj) dst[jj * ld] = static_cast<uint8_t>(nw >> (8 * jj));
+                } else {
+                  res_s[widx] = nw;
+                }
+              }
+            }
+          } else
 #pragma unroll 1
           for (int cb = col0; cb < col0 + TC_BN / 2; cb += 32) {
             uint32_t v[32];
@@ -340,7 +385,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(P2_THREADS, 1)
 int tc_gemm_pair_launch(int epi, const CUtensorMap& ta0, const CUtensorMap& tb0, const CUtensorMap* ta1,
                         const CUtensorMap* tb1, const SliceSchedule& sched, const TcParams& prm, int grid,
                         int kernel_kind, cudaStream_t s) {
-  static bool attr_set[2] = {false, false};
+  static bool attr_set[3] = {false, false, false};
   const CUtensorMap& a1 = ta1 ? *ta1 : ta0;
   const CUtensorMap& b1 = tb1 ? *tb1 : tb0;
   if (grid < 2) grid = 2;
@@ -354,6 +399,15 @@ int tc_gemm_pair_launch(int epi, const CUtensorMap& ta0, const CUtensorMap& tb0,
     GB_LAUNCH(kernel_kind, s,
               (tc_gemm_pair_kernel<TC_EPI_OZAKI_F64><<<grid, P2_THREADS, P2_SMEM_BYTES, s>>>(ta0, tb0, a1, b1, sched,
                                                                                              prm)));
+  } else if (epi == TC_EPI_CRT) {
+    if (!attr_set[2]) {
+      GB_CUDA_TRY(cudaFuncSetAttribute(tc_gemm_pair_kernel<TC_EPI_CRT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       P2_SMEM_BYTES_CRT));
+      attr_set[2] = true;
+    }
+    GB_LAUNCH(kernel_kind, s,
+              (tc_gemm_pair_kernel<TC_EPI_CRT><<<grid, P2_THREADS, P2_SMEM_BYTES_CRT, s>>>(ta0, tb0, a1, b1, sched,
+                                                                                           prm)));
   } else {
     if (!attr_set[1]) {
       GB_CUDA_TRY(cudaFuncSetAttribute(tc_gemm_pair_kernel<TC_EPI_F32>, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -20,6 +20,7 @@ GB_ERR_NO_DEVICE = -6
 MODE_NATIVE = 0
 MODE_OZAKI_BF16 = 1
 MODE_OZAKI_INT8 = 2
+MODE_OZAKI_CRT = 3
 
 c_i64 = ctypes.c_int64
 c_int = ctypes.c_int
@@ -77,6 +78,7 @@ SIGNATURES = {
     "gb_gemm_f32": (c_int, [c_int, c_int, c_i64, c_i64, c_i64, c_float, c_vp, c_i64, c_vp, c_i64,
                             c_float, c_vp, c_i64, c_vp]),
     "gb_plan_ozaki": (c_int, [c_i64, c_i64, c_i64, c_int, ctypes.POINTER(OzakiPlan)]),
+    "gb_plan_ozaki_crt": (c_int, [c_i64, c_i64, c_i64, c_int, ctypes.POINTER(OzakiPlan)]),
     "gb_gemm_adjoint_f32": (c_int, [c_i64, c_i64, c_i64, c_vp, c_i64, c_vp, c_i64, c_vp, c_i64, c_vp, c_i64,
                                     c_vp, c_i64, c_vp]),
     "gb_last_ozaki_plan": (c_int, [ctypes.POINTER(OzakiPlan)]),

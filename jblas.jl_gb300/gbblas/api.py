@@ -78,15 +78,17 @@ def gemm_raw(transA, transB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, *, dt
 
 
 _MODES = {"native": _lib.MODE_NATIVE, "ozaki": _lib.MODE_OZAKI_BF16,
-          "ozaki_bf16": _lib.MODE_OZAKI_BF16, "ozaki_int8": _lib.MODE_OZAKI_INT8}
+          "ozaki_bf16": _lib.MODE_OZAKI_BF16, "ozaki_int8": _lib.MODE_OZAKI_INT8,
+          "ozaki_crt": _lib.MODE_OZAKI_CRT}
 
 
 def gemm_(C, A, B, alpha=1.0, beta=0.0, *, mode="native", slices=0, return_bound=False):
     """C = alpha * A @ B + beta * C in place; A (M x K), B (K x N), C (M x N).
 
     mode "native": the jmul! FMA chain (bit-identical to the oracle); "ozaki": FP64
-    emulation on BF16 tensor cores (float64 only; slices = 0 picks the count for the
-    library tolerance).  With return_bound the a-priori normwise error bound is
+    emulation on BF16 tensor cores by digit slices (float64 only; slices = 0 picks the
+    count for the library tolerance); "ozaki_crt": FP64 emulation by residue products
+    and the Chinese remainder theorem (slices = number of moduli, 0 = automatic).  With return_bound the a-priori normwise error bound is
     returned alongside C.
     """
     dt = _dtype_of(C, A, B)
@@ -128,6 +130,14 @@ def ozaki_plan(M, N, K, slices):
     p = _lib.OzakiPlan()
     check(_lib.lib().gb_plan_ozaki(M, N, K, slices, ctypes.byref(p)), "gb_plan_ozaki")
     return {"slices": p.slices, "bits": p.bits, "k_chunk": p.k_chunk, "products": p.products,
+            "groups": p.groups, "flops_tensor": p.flops_tensor}
+
+
+def ozaki_crt_plan(M, N, K, moduli):
+    """The CRT plan for `moduli` moduli: integer bits t ("bits"), K chunk, tensor flops."""
+    p = _lib.OzakiPlan()
+    check(_lib.lib().gb_plan_ozaki_crt(M, N, K, moduli, ctypes.byref(p)), "gb_plan_ozaki_crt")
+    return {"moduli": p.slices, "bits": p.bits, "k_chunk": p.k_chunk, "products": p.products,
             "groups": p.groups, "flops_tensor": p.flops_tensor}
 
 

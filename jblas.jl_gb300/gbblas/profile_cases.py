@@ -10,6 +10,8 @@ cases:
   native_f64     gb_gemm_f64 NATIVE, 4096^3
   native_f32     gb_gemm_f32, 4096^3
   ozaki          gb_gemm_f64 OZAKI (stats, split, slice products), 4096 x 4096 x 8192
+  ozaki_crt      gb_gemm_f64 OZAKI_CRT, 15 moduli (stats, residue split, residue products,
+                 CRT combine), 4096 x 4096 x 8192
   grouped_f64    gb_gemm_grouped_f64, 4096 problems with m, n, k log-uniform in [8, 512]
   adjoint        gb_gemm_adjoint_f32, A 4096 x 2048, B 2048 x 4096
 """
@@ -51,6 +53,14 @@ def case_ozaki():
     return _timed(lambda: api.gemm_(C, A, B, mode="ozaki", slices=10))
 
 
+def case_ozaki_crt():
+    M, N, K = 4096, 4096, 8192
+    A = _dev_cm(workloads.ozaki_matrix(M, K, per="row", stream=1))
+    B = _dev_cm(workloads.ozaki_matrix(K, N, per="col", stream=2))
+    C = torch.empty((N, M), dtype=torch.float64, device="cuda").t()
+    return _timed(lambda: api.gemm_(C, A, B, mode="ozaki_crt", slices=15))
+
+
 def case_grouped():
     sizes = [tuple(int(x) for x in r) for r in workloads.grouped_sizes(4096)]
     As = [(torch.rand((k, m), dtype=torch.float64, device="cuda") * 2 - 1).t() for m, n, k in sizes]
@@ -74,6 +84,7 @@ CASES = {
     "native_f64": lambda: case_native(torch.float64, 4096),
     "native_f32": lambda: case_native(torch.float32, 4096),
     "ozaki": case_ozaki,
+    "ozaki_crt": case_ozaki_crt,
     "grouped_f64": case_grouped,
     "adjoint": case_adjoint,
 }

@@ -340,3 +340,95 @@ def ozaki_gemm(A, B, C=None, alpha=1.0, beta=0.0, slices=8, min_chunks=1):
     else:
         out = fma(np.full_like(val, alpha), val, beta * np.asarray(C, dtype=np.float64))
     return np.asfortranarray(out)
+
+
+# ------------------------------------------------------------------ CRT (Ozaki scheme II)
+
+CRT_MAX_MODULI = 20
+
+
+def crt_moduli(n):
+    """The first n moduli: 256, then descending integers coprime to all taken so far."""
+    out, c = [], 256
+    while len(out) < n:
+        if all(math.gcd(c, m) == 1 for m in out):
+            out.append(c)
+        c -= 1
+    return out
+
+
+def crt_bits_for(K, n):
+    """Largest t <= 62 with 4 K 2^(2t) <= prod(moduli) and K 2^(2t) <= 2^125 (0: none)."""
+    Mp = math.prod(crt_moduli(n))
+    K = max(1, K)
+    for t in range(62, 0, -1):
+        if 4 * K * 4 ** t <= Mp and K * 4 ** t <= 2 ** 125:
+            return t
+    return 0
+
+
+def _fixed_rows(X, t):
+    """Row exponents e (max|x| < 2^e; Inf/NaN rows flagged) and Y = round-half-away(x 2^(t-e))
+    as int64 (|Y| <= 2^t), the integer operand of the CRT product."""
+    X = np.asarray(X, dtype=np.float64)
+    R, K = X.shape
+    nonfinite = ~np.isfinite(X).all(axis=1) if K else np.zeros(R, bool)
+    amax = np.abs(np.where(nonfinite[:, None], 0.0, X)).max(axis=1) if K else np.zeros(R)
+    _, ex = np.frexp(amax)
+    e = np.where(amax == 0, 0, ex).astype(np.int64)
+    v = np.ldexp(np.where(nonfinite[:, None], 0.0, X), (t - e)[:, None].astype(np.int32))
+    mag = np.abs(v)
+    fl = np.floor(mag)
+    Y = (np.sign(v) * (fl + (mag - fl >= 0.5))).astype(np.int64)
+    return Y, np.where(nonfinite, 2**31 - 1, e)
+
+
+def _exact_int_product(Ya, Yb):
+    """Exact integer Ya @ Yb.T (|entries| <= 2^62, K <= 2^19) as an object array of Python
+    ints.  The operands are cut into 17-bit limbs (the top one signed, |.| <= 2^11), so every
+    partial sum of a limb product is an integer below 2^53 and the float64 matrix products
+    are exact in any summation order."""
+    def limbs(Y):
+        out = []
+        for _ in range(3):
+            out.append((Y & ((1 << 17) - 1)).astype(np.float64))
+            Y = Y >> 17
+        out.append(Y.astype(np.float64))
+        return out
+    if Ya.shape[1] > (1 << 19):
+        raise ValueError("K too large for the exact limb product")
+    la, lb = limbs(Ya), limbs(Yb)
+    total = None
+    for d in range(7):
+        S = None
+        for l in range(4):
+            m = d - l
+            if 0 <= m < 4:
+                P = (la[l] @ lb[m].T).astype(np.int64)
+                S = P if S is None else S + P
+        term = S.astype(object) * (1 << (17 * d))
+        total = term if total is None else total + term
+    return total
+
+
+def ozaki_crt_gemm(A, B, C=None, alpha=1.0, beta=0.0, moduli=16, bits=0):
+    """The GPU CRT-mode result restated: C = alpha * fl(A'B' 2^(ea+eb-2t)) + beta * C with
+    A', B' the t-bit integer operands and A'B' computed exactly (no residues needed for the
+    restatement: the CRT reconstruction on the GPU must give this exact product)."""
+    A = np.asarray(A, dtype=np.float64)
+    B = np.asarray(B, dtype=np.float64)
+    M, K = A.shape
+    N = B.shape[1]
+    t = bits or crt_bits_for(K, moduli)
+    Ya, ea = _fixed_rows(A, t)
+    Yb, eb = _fixed_rows(B.T, t)
+    Cint = _exact_int_product(Ya, Yb) if K else np.zeros((M, N), dtype=object)
+    T = np.array([float(v) for v in Cint.ravel()], dtype=np.float64).reshape(M, N)
+    bad = (ea[:, None] == 2**31 - 1) | (eb[None, :] == 2**31 - 1)
+    E = np.where(bad, 0, ea[:, None] + eb[None, :] - 2 * t)
+    val = np.where(bad, np.nan, np.ldexp(T, E.astype(np.int64)))
+    if beta == 0.0:
+        out = alpha * val
+    else:
+        out = fma(np.full_like(val, alpha), val, beta * np.asarray(C, dtype=np.float64))
+    return np.asfortranarray(out)

@@ -68,3 +68,19 @@ def test_setters():
     assert L.gb_set_wait_limit_ns(0) == 0
     assert L.gb_set_ozaki_tolerance(-1.0) == _lib.GB_ERR_INVALID_VALUE
     assert L.gb_set_ozaki_tolerance(0.0) == 0
+
+
+@pytest.mark.parametrize("K", [1, 16, 64, 1000, 4100, 8192, 70000, 1 << 19])
+@pytest.mark.parametrize("moduli", [1, 2, 3, 8, 15, 16, 17, 20])
+def test_ozaki_crt_plan_matches_restatement(K, moduli):
+    t = oracle.crt_bits_for(K, moduli)
+    if t == 0:
+        with pytest.raises(gbblas.GBError):
+            gbblas.ozaki_crt_plan(256, 128, K, moduli)
+        return
+    got = gbblas.ozaki_crt_plan(256, 128, K, moduli)
+    assert got["bits"] == t and got["moduli"] == moduli and got["products"] == moduli
+    kb = max(1, (K + 63) // 64)
+    nch = (kb + 15) // 16
+    assert got["k_chunk"] == 64 * ((kb + nch - 1) // nch)
+    assert got["flops_tensor"] == 2.0 * 256 * 128 * kb * 64 * moduli

@@ -124,3 +124,31 @@ def test_ozaki_plan_grouping_respects_exactness():
             for level, pairs in p["groups"]:
                 assert all(a + b + 2 == level for a, b in pairs)
                 assert len(pairs) * p["k_chunk"] * 2.0 ** (2 * p["bits"] - 2) <= 2.0 ** 24
+
+
+def test_crt_restatement_against_exact_rationals():
+    """The CRT-mode restatement: exact integer product of the t-bit operands, rounded once
+    to FP64 (checked here with Python rationals), and its error small against the exact
+    product of the unrounded inputs."""
+    from fractions import Fraction
+    g = np.random.default_rng(8)
+    A = g.uniform(-1, 1, (9, 40)) * np.ldexp(1.0, g.integers(-6, 7, (9, 40)))
+    B = g.uniform(-1, 1, (40, 7)) * np.ldexp(1.0, g.integers(-6, 7, (40, 7)))
+    t = oracle.crt_bits_for(40, 16)
+    C = oracle.ozaki_crt_gemm(A, B, moduli=16)
+    Ya, ea = oracle._fixed_rows(A, t)
+    Yb, eb = oracle._fixed_rows(B.T, t)
+    for i in range(9):
+        for j in range(7):
+            exact_int = sum(int(Ya[i, k]) * int(Yb[j, k]) for k in range(40))
+            assert C[i, j] == float(Fraction(exact_int) * Fraction(2) ** int(ea[i] + eb[j] - 2 * t))
+            exact = sum(Fraction(A[i, k]) * Fraction(B[k, j]) for k in range(40))
+            scale = float(np.abs(A[i]).max() * np.abs(B[:, j]).max())
+            assert abs(float(Fraction(C[i, j]) - exact)) <= 40 * scale * 2.0 ** -t + 2.0 ** -52 * abs(C[i, j])
+
+
+def test_crt_moduli_pairwise_coprime():
+    import math
+    m = oracle.crt_moduli(20)
+    assert m[0] == 256 and len(set(m)) == 20 and max(m) <= 256
+    assert all(math.gcd(a, b) == 1 for i, a in enumerate(m) for b in m[i + 1:])
