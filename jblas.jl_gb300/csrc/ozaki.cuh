@@ -81,7 +81,7 @@ int oz_grid_for(int sms, int64_t M, int64_t N);
 struct CrtConsts {
   int32_t n;                       // moduli
   int32_t t;                       // integer bits: |A'|, |B'| <= 2^t
-  uint32_t p[TC_MAX_MODULI];       // the moduli (pairwise coprime, <= 256)
+  uint32_t p[TC_MAX_MODULI];       // the moduli (pairwise coprime, <= 253)
   uint32_t c21[TC_MAX_MODULI];     // 2^21 mod p
   uint32_t c42[TC_MAX_MODULI];     // 2^42 mod p
   uint32_t bias[TC_MAX_MODULI];    // -2^62 mod p
@@ -89,6 +89,9 @@ struct CrtConsts {
   float finv[TC_MAX_MODULI];       // fl32(inv_g / p_g), inv_g = (M / p_g)^-1 mod p_g
   uint32_t w[TC_MAX_MODULI][4];    // (M / p_g) inv_g mod 2^128, little-endian 32-bit words
   uint32_t m[4];                   // M mod 2^128
+  uint32_t bw[4];                  // 128 * sum_g W_g mod 2^128 (bias of the residue bytes)
+  float bias_k;                    // 128 * sum_g finv[g]
+  int32_t ab;                      // 0: C = v; 1: C = alpha v; 2: C = fma(alpha, v, beta C)
 };
 
 struct CrtPlan {
@@ -122,7 +125,7 @@ struct CrtGemmArgs {
   double alpha, beta;
   double* C;
   int64_t ldc;
-  uint8_t* res;           // [n][ceil(N/256)*256][res_ld] residues
+  uint8_t* res;           // [n][ceil(N/256)*256][res_ld] residues, biased bytes r + 128
   int64_t res_ld;         // ceil(M/256)*256
   int64_t res_plane;
   DeviceStatus* status;

@@ -5,10 +5,10 @@
 //
 //   A'[i,k] = round-half-away(op(A)[i,k] * 2^(t - ea_i))    |A'| <= 2^t  (ea_i: row exponent)
 //   B'[k,j] = round-half-away(op(B)[k,j] * 2^(t - eb_j))    |B'| <= 2^t
-//   C' = A' B' exactly, from its residues modulo n pairwise coprime p_g <= 256:
-//     R_g = (A' mod p_g)(B' mod p_g)    balanced residues, |r| <= 128 (exact in BF16); FP32
-//                                       sums over K chunks of <= 1024 stay exact
-//                                       (1024 * 128^2 = 2^24) and are reduced mod p_g
+//   C' = A' B' exactly, from its residues modulo n pairwise coprime p_g <= 253:
+//     R_g = (A' mod p_g)(B' mod p_g)    balanced residues, |r| <= 126 (exact in BF16); FP32
+//                                       sums over K chunks of <= 1024 stay exact (1024 *
+//                                       126^2 + 127 < 2^24) and are reduced mod p_g
 //     C' = CRT(R_1, ..., R_n)           exact because |C'| <= M/4, M = prod p_g
 //   C = alpha * fl(C' * 2^(ea_i + eb_j - 2t)) + beta * C
 // Only the rounding of A and B to t-bit integers and the final conversion round; the
@@ -46,12 +46,13 @@ uint32_t gcd_u32(uint32_t a, uint32_t b) {
   return a;
 }
 
-// 256 first, then descending integers coprime to every modulus taken so far.
+// 253 first, then descending integers coprime to every modulus taken so far.  p <= 253
+// keeps one FP32 reduction of (chunk sum + running residue) within |r| <= 127.
 struct ModuliTable {
   uint32_t p[TC_MAX_MODULI];
   ModuliTable() {
     int cnt = 0;
-    for (uint32_t c = 256; cnt < TC_MAX_MODULI; --c) {
+    for (uint32_t c = 253; cnt < TC_MAX_MODULI; --c) {
       bool ok = true;
       for (int i = 0; i < cnt && ok; ++i) ok = gcd_u32(c, p[i]) == 1;
       if (ok) p[cnt++] = c;
@@ -149,7 +150,7 @@ int crt_make_plan(int64_t M, int64_t N, int64_t K, int n, int t, CrtPlan* plan) 
   P.t = t;
   int64_t kb_total = (K + TC_BK - 1) / TC_BK;
   if (kb_total < 1) kb_total = 1;
-  // exact FP32 chunk sums: at most 16 panels (1024 products of |r| <= 128)
+  // exact FP32 chunk sums: at most 16 panels (1024 products of |r| <= 126)
   int64_t nchunks = (kb_total + 15) / 16;
   const int64_t kb_chunk = (kb_total + nchunks - 1) / nchunks;
   nchunks = (kb_total + kb_chunk - 1) / kb_chunk;
@@ -177,6 +178,8 @@ int crt_make_plan(int64_t M, int64_t N, int64_t K, int n, int t, CrtPlan* plan) 
   unsigned __int128 m128 = 1;
   for (int g = 0; g < n; ++g) m128 *= moduli_table().p[g];
   for (int w = 0; w < 4; ++w) cc.m[w] = static_cast<uint32_t>(m128 >> (32 * w));
+  unsigned __int128 bias128 = 0;
+  double bias_k = 0.0;
   for (int g = 0; g < n; ++g) {
     const uint32_t p = moduli_table().p[g];
     const uint64_t c21 = (uint64_t(1) << 21) % p;
@@ -199,7 +202,11 @@ int crt_make_plan(int64_t M, int64_t N, int64_t K, int n, int t, CrtPlan* plan) 
     cc.finv[g] = static_cast<float>(static_cast<double>(inv) / static_cast<double>(p));
     const unsigned __int128 w128 = rest128 * inv;
     for (int w = 0; w < 4; ++w) cc.w[g][w] = static_cast<uint32_t>(w128 >> (32 * w));
+    bias128 += w128 * 128u;
+    bias_k += 128.0 * static_cast<double>(cc.finv[g]);
   }
+  for (int w = 0; w < 4; ++w) cc.bw[w] = static_cast<uint32_t>(bias128 >> (32 * w));
+  cc.bias_k = static_cast<float>(bias_k);
   return GB_OK;
 }
 
@@ -341,10 +348,12 @@ __device__ __forceinline__ double i128_times_pow2(uint64_t hi, uint64_t lo, int 
   return neg ? -d : d;
 }
 
-// One thread = 4 consecutive rows of one column (a 32-bit load per residue plane).
-//   X = sum_g u_g W_g (mod 2^128),  W_g = (M/p_g) ((M/p_g)^-1 mod p_g)
-//   k = round(sum_g u_g inv_g / p_g) = round(X / M), exact in FP32 because |C'| <= M/4
-//   C' = X - k M (mod 2^128), a two's-complement 128-bit integer
+// One thread = 4 consecutive rows of one column (a 32-bit load per residue plane).  The
+// planes hold biased bytes u_g = r_g + 128 with r_g = C' mod p_g (|r_g| <= 127), so
+//   X = sum_g r_g W_g = sum_g u_g W_g - 128 sum_g W_g   (mod 2^128),
+//       W_g = (M/p_g) ((M/p_g)^-1 mod p_g)
+//   k = round(sum_g r_g inv_g / p_g) = round(X / M), exact in FP32 because |C'| <= M/4
+//   C' = X - k M  (mod 2^128), a two's-complement 128-bit integer
 __global__ void __launch_bounds__(256) crt_combine_kernel(const uint8_t* __restrict__ res, int64_t res_ld,
                                                           int64_t res_plane, int64_t M, int64_t N,
                                                           const int32_t* __restrict__ ea,
@@ -358,19 +367,19 @@ __global__ void __launch_bounds__(256) crt_combine_kernel(const uint8_t* __restr
   for (int q = 0; q < 4; ++q) eai[q] = (i0 + q < M) ? ea[i0 + q] : 0;
   const int two_t = 2 * cc.t;
   for (int64_t j = blockIdx.y; j < N; j += gridDim.y) {
-    uint64_t acc[4][4];
-    float ks[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      ks[q] = 0.0f;
-#pragma unroll
-      for (int w = 0; w < 4; ++w) acc[q][w] = 0ull;
-    }
     const uint8_t* base = res + j * res_ld + i0;
     uint32_t words[TC_MAX_MODULI];   // all loads in flight before any use
 #pragma unroll
     for (int g = 0; g < TC_MAX_MODULI; ++g)
       words[g] = (g < cc.n) ? __ldg(reinterpret_cast<const uint32_t*>(base + g * res_plane)) : 0u;
+    uint64_t acc[4][4];
+    float ks[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      ks[q] = -cc.bias_k;
+#pragma unroll
+      for (int w = 0; w < 4; ++w) acc[q][w] = 0ull;
+    }
 #pragma unroll
     for (int g = 0; g < TC_MAX_MODULI; ++g) {
       if (g >= cc.n) break;
@@ -392,12 +401,13 @@ __global__ void __launch_bounds__(256) crt_combine_kernel(const uint8_t* __restr
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       if (i0 + q >= M) continue;
-      const int64_t k = __float_as_int(ks[q] + 12582912.0f) - 0x4B400000;   // round(X / M) >= 0
+      const int64_t k = __float_as_int(ks[q] + 12582912.0f) - 0x4B400000;   // round(X / M)
       int64_t c = 0;
       uint32_t word[4];
 #pragma unroll
       for (int w = 0; w < 4; ++w) {
-        const int64_t v = static_cast<int64_t>(acc[q][w]) - k * static_cast<int64_t>(cc.m[w]) + c;
+        const int64_t v = static_cast<int64_t>(acc[q][w]) - static_cast<int64_t>(cc.bw[w]) -
+                          k * static_cast<int64_t>(cc.m[w]) + c;
         word[w] = static_cast<uint32_t>(v);
         c = v >> 32;
       }
@@ -409,12 +419,11 @@ __global__ void __launch_bounds__(256) crt_combine_kernel(const uint8_t* __restr
         const uint64_t hi = (static_cast<uint64_t>(word[3]) << 32) | word[2];
         val = i128_times_pow2(hi, lo, eai[q] + ebj - two_t);
       }
-      double out;
-      if (beta == 0.0)
-        out = (alpha == 1.0) ? val : alpha * val;
-      else
-        out = fma(alpha, val, beta * ccol[i0 + q]);
-      ccol[i0 + q] = out;
+      if (cc.ab == 1)
+        val = alpha * val;
+      else if (cc.ab == 2)
+        val = fma(alpha, val, beta * ccol[i0 + q]);
+      ccol[i0 + q] = val;
     }
   }
 }
@@ -455,9 +464,11 @@ int crt_gemm_launch(const CrtGemmArgs& a, const CrtPlan& plan, cudaStream_t s) {
   const int64_t by = a.N < 65535 ? a.N : 65535;
   if (bx > 0x7FFFFFFF) return GB_ERR_UNSUPPORTED;
   dim3 grid(static_cast<unsigned>(bx), static_cast<unsigned>(by));
+  CrtConsts cc = plan.cc;   // output rule decided once on the host (no FP64 compares per element)
+  cc.ab = (a.beta != 0.0) ? 2 : (a.alpha != 1.0 ? 1 : 0);
   GB_LAUNCH(GB_KERNEL_OZAKI_COMBINE, s,
             (crt_combine_kernel<<<grid, 256, 0, s>>>(a.res, a.res_ld, a.res_plane, a.M, a.N, a.ea, a.eb, a.alpha, a.beta,
-                                                     a.C, a.ldc, plan.cc)));
+                                                     a.C, a.ldc, cc)));
   GB_CUDA_TRY(cudaGetLastError());
   return GB_OK;
 }

@@ -6,8 +6,9 @@
 //   TC_EPI_OZAKI_F64  exact integer group sums, accumulated in FP64 per tile (smallest
 //                     level first), rescaled by 2^(ea_i + eb_j) with alpha/beta, FP64 out
 //   TC_EPI_F32        one group, C = alpha * sum + beta * C in FP32 (split-BF16 products)
-//   TC_EPI_CRT        one group per modulus p_g: the exact chunk sum is reduced mod p_g and
-//                     added (mod p_g) into a uint8 residue plane (CTA-pair engine only)
+//   TC_EPI_CRT        one group per modulus p_g <= 253: exact chunk sums accumulated mod p_g,
+//                     written as biased bytes r + 128 (|r| <= 127, r = C' mod p_g) to a
+//                     residue plane (CTA-pair engine only)
 // One launch may carry two independent problems (the adjoint's dA and dB); CTAs walk
 // the concatenated tile list.
 #pragma once

@@ -10,8 +10,9 @@
 //               are counted on the LEADER's (rank 0) full barrier
 //   warp 1      TMEM allocation (both CTAs, pair-wide); in the leader one lane issues the
 //               M = 256, N = 256 MMAs and commits to the barriers of both CTAs
-//   warps 2-9   epilogue in both CTAs: each drains its 128 rows x 256 columns, exactly as the
-//               single-CTA kernel (tc_gemm.cu), and arrives on the leader's tmem_empty
+//   warps 2-9   epilogue in both CTAs (warps 2-17 for the CRT epilogue): each CTA drains its
+//               128 rows x 256 columns, as the single-CTA kernel (tc_gemm.cu) does, and every
+//               epilogue warp arrives on the leader's tmem_empty
 // Waits are bounded as in tc_gemm.cu; both CTAs meet at a cluster barrier before TMEM is
 // released.
 #include <cuda_bf16.h>
@@ -22,19 +23,22 @@
 
 namespace gb {
 
-constexpr int P2_THREADS = 320;
-constexpr int P2_EPI_THREADS = 256;
+// Threads per CTA: 2 role warps + 8 epilogue warps, or 16 for the CRT epilogue, whose drains
+// come every 16 K panels and need more warps to hide their latency (4 per TMEM lane quadrant,
+// 64 columns each; 96 registers per thread fit 18 warps).
+template <int EPI>
+struct P2Shape {
+  static constexpr int THREADS = (EPI == TC_EPI_CRT) ? 576 : 320;
+  static constexpr int EPI_WARPS = THREADS / 32 - 2;
+  static constexpr int COLS = TC_BN / (EPI_WARPS / 4);   // columns per epilogue warp
+};
 constexpr int P2_STAGES = 6;
 constexpr int P2_A_BYTES = 128 * TC_BK * 2;     // 16 KB: this CTA's 128 rows of A
 constexpr int P2_B_BYTES = 128 * TC_BK * 2;     // 16 KB: this CTA's half of B
 constexpr int P2_STAGE_BYTES = P2_A_BYTES + P2_B_BYTES;
 constexpr int P2_TMEM_COLS = 512;
 constexpr int P2_SMEM_BYTES = P2_STAGES * P2_STAGE_BYTES + 1024 + 256;
-// TC_EPI_CRT keeps each CTA's running residues (128 rows x 256 columns, one byte each) in
-// shared memory after the barriers: row r's 64 words are rotated by r so that the 32 rows
-// of a warp hit 32 different banks.
-constexpr int P2_RES_BYTES = 128 * 256;
-constexpr int P2_SMEM_BYTES_CRT = P2_SMEM_BYTES + P2_RES_BYTES;
+
 constexpr int P2_EXP_NONFINITE = 0x7FFFFFFF;
 constexpr uint64_t P2_CLEANUP_WAIT_NS = 2000000000ull;
 
@@ -61,7 +65,7 @@ __device__ __forceinline__ int p2_problem_of(const TcParams& prm, int t) {
 }
 
 template <int EPI>
-__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(P2_THREADS, 1)
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(P2Shape<EPI>::THREADS, 1)
     tc_gemm_pair_kernel(const __grid_constant__ CUtensorMap tmap_a0, const __grid_constant__ CUtensorMap tmap_b0,
                         const __grid_constant__ CUtensorMap tmap_a1, const __grid_constant__ CUtensorMap tmap_b1,
                         const __grid_constant__ SliceSchedule sched, const __grid_constant__ TcParams prm) {
@@ -89,7 +93,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(P2_THREADS, 1)
     }
     for (int i = 0; i < 2; ++i) {
       mbar_init(&tfull[i], 1);
-      mbar_init(&tempty[i], 2 * P2_EPI_THREADS / 32);   // one arrival per epilogue warp of both CTAs
+      mbar_init(&tempty[i], 2 * P2Shape<EPI>::EPI_WARPS);   // one arrival per epilogue warp of both CTAs
     }
     mbar_init(drain, 1);
     *abort_flag = 0;
@@ -230,7 +234,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(P2_THREADS, 1)
     // ------------------------------------------------------------ epilogue (both CTAs)
     const int q = warp & 3;
     const int row_l = q * 32 + lane;
-    const int col0 = ((warp - 2) >> 2) * (TC_BN / 2);
+    constexpr int COLS = P2Shape<EPI>::COLS;
+    const int col0 = ((warp - 2) >> 2) * COLS;
     const uint64_t keep = l2_policy_evict_last();
     int buf = 0;
     uint32_t acc_phase = 0;
@@ -249,7 +254,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(P2_THREADS, 1)
       double* __restrict__ tws = prm.tws ? prm.tws + static_cast<int64_t>(blockIdx.x) * (TC_BM * TC_BN) : nullptr;
       int step = 0;
       const int nsteps = G * P.nchunks;
-      uint32_t* res_s = reinterpret_cast<uint32_t*>(smem + P2_STAGES * P2_STAGE_BYTES + 256) + row_l * 64;
+      uint32_t racc[EPI == TC_EPI_CRT ? COLS / 4 : 1];   // CRT: running residues, 4 bytes per register
       for (int g = 0; g < G && ok; ++g) {
         const int wexp = 2 - sched.level[g] * sched.bits;
         const unsigned long long wbias = static_cast<unsigned long long>(896 + wexp) << 23;
@@ -261,46 +266,53 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(P2_THREADS, 1)
           const bool first = (step == 0), last = (step == nsteps - 1);
           const uint32_t taddr = tmem_base + (static_cast<uint32_t>(q * 32) << 16) + static_cast<uint32_t>(buf * TC_BN);
           if (EPI == TC_EPI_CRT) {
-            // The chunk sum (an exact integer, |S| <= 2^24) is reduced mod p_g in FP32 and
-            // added mod p_g into this thread's running residues (its row x 128 columns, 4
-            // per shared-memory word); the last chunk stores them as bytes into the residue
-            // plane (rows and columns padded to whole tiles, so always in bounds).
+            // The chunk sum S (an exact integer, |S| <= 1024 * 126^2) plus this thread's
+            // running residue r (|r| <= 127, kept as the biased byte r + 128, four to a
+            // register) is exact in FP32; one reduction t - p * rint(t / p) returns |r| <= 127 because
+            // p <= 253.  All in FP32 and byte permutes: no integer range fixes.  The last
+            // chunk writes the biased bytes to the residue plane (rows and columns padded to
+            // whole tiles, so always in bounds).
+            constexpr float MAGIC = 12582912.0f;   // 1.5 * 2^23: x + MAGIC - MAGIC = rint(x), |x| < 2^22
+            constexpr float BIAS_F = 8388736.0f;   // 2^23 + 128: the low byte of (r + BIAS_F) is r + 128
             const float pf = prm.crt_p[g], inv = prm.crt_inv[g];
-            const int pi = static_cast<int>(pf);
             const bool first_c = (c == 0), last_c = (c == P.nchunks - 1);
             const int64_t ld = prm.res_ld;
 #pragma unroll
-            for (int bi = 0; bi < 8; ++bi) {   // 16 columns per TMEM load
+            for (int bi = 0; bi < COLS / 16; ++bi) {   // 16 columns per TMEM load
               uint32_t v[16];
               tmem_ld_32x32b_x16(taddr + col0 + bi * 16, v);
               tc_wait_ld();
 #pragma unroll
               for (int j4 = 0; j4 < 4; ++j4) {
-                const int widx = ((col0 >> 2) + bi * 4 + j4 + row_l) & 63;
-                const uint32_t old = first_c ? 0u : res_s[widx];
-                uint32_t nw = 0;
+                const uint32_t old = first_c ? 0x80808080u : racc[bi * 4 + j4];
+                uint32_t rb[4];
 #pragma unroll
                 for (int jj = 0; jj < 4; ++jj) {
-                  const float vf = __uint_as_float(v[j4 * 4 + jj]);
-                  const float qf = fmaf(vf, inv, 12582912.0f) - 12582912.0f;   // S/p rounded (+-1)
-                  const float rf = fmaf(-pf, qf, vf);                           // exact, |rf| <= p/2 + 1
-                  int r = (__float_as_int(rf + 12582912.0f) - 0x4B400000) + static_cast<int>((old >> (8 * jj)) & 0xFFu);
-                  r += (r < 0) ? pi : 0;
-                  r -= (r >= pi) ? pi : 0;
-                  nw |= static_cast<uint32_t>(r) << (8 * jj);
+                  // 0x4B0000bb as a float is 2^23 + bb: the old residue is that minus BIAS_F
+                  const float prev = __uint_as_float(__byte_perm(old, 0x4B000000u, 0x7540u + jj)) - BIAS_F;
+                  const float t = __uint_as_float(v[j4 * 4 + jj]) + prev;
+                  const float q = fmaf(t, inv, MAGIC) - MAGIC;
+                  const float r = fmaf(-pf, q, t);
+                  rb[jj] = __float_as_uint(r + BIAS_F);
                 }
-                if (last_c) {
-                  uint8_t* __restrict__ dst = prm.res + g * prm.res_plane + (n0 + col0 + bi * 16 + j4 * 4) * ld + row;
+                racc[bi * 4 + j4] =
+                    __byte_perm(__byte_perm(rb[0], rb[1], 0x0040u), __byte_perm(rb[2], rb[3], 0x0040u), 0x5410u);
+              }
+            }
+            if (last_c) {
+              uint8_t* __restrict__ dst = prm.res + g * prm.res_plane + (n0 + col0) * ld + row;
 #pragma unroll
-                  for (int jj = 0; jj < 4; ++jj) dst[jj * ld] = static_cast<uint8_t>(nw >> (8 * jj));
-                } else {
-                  res_s[widx] = nw;
+              for (int w = 0; w < COLS / 4; ++w) {
+#pragma unroll
+                for (int jj = 0; jj < 4; ++jj) {
+                  *dst = static_cast<uint8_t>(racc[w] >> (8 * jj));
+                  dst += ld;
                 }
               }
             }
           } else
 #pragma unroll 1
-          for (int cb = col0; cb < col0 + TC_BN / 2; cb += 32) {
+          for (int cb = col0; cb < col0 + COLS; cb += 32) {
             uint32_t v[32];
             tmem_ld_32x32b_x32(taddr + cb, v);
             tc_wait_ld();
@@ -397,16 +409,16 @@ int tc_gemm_pair_launch(int epi, const CUtensorMap& ta0, const CUtensorMap& tb0,
       attr_set[0] = true;
     }
     GB_LAUNCH(kernel_kind, s,
-              (tc_gemm_pair_kernel<TC_EPI_OZAKI_F64><<<grid, P2_THREADS, P2_SMEM_BYTES, s>>>(ta0, tb0, a1, b1, sched,
+              (tc_gemm_pair_kernel<TC_EPI_OZAKI_F64><<<grid, P2Shape<TC_EPI_OZAKI_F64>::THREADS, P2_SMEM_BYTES, s>>>(ta0, tb0, a1, b1, sched,
                                                                                              prm)));
   } else if (epi == TC_EPI_CRT) {
     if (!attr_set[2]) {
       GB_CUDA_TRY(cudaFuncSetAttribute(tc_gemm_pair_kernel<TC_EPI_CRT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       P2_SMEM_BYTES_CRT));
+                                       P2_SMEM_BYTES));
       attr_set[2] = true;
     }
     GB_LAUNCH(kernel_kind, s,
-              (tc_gemm_pair_kernel<TC_EPI_CRT><<<grid, P2_THREADS, P2_SMEM_BYTES_CRT, s>>>(ta0, tb0, a1, b1, sched,
+              (tc_gemm_pair_kernel<TC_EPI_CRT><<<grid, P2Shape<TC_EPI_CRT>::THREADS, P2_SMEM_BYTES, s>>>(ta0, tb0, a1, b1, sched,
                                                                                            prm)));
   } else {
     if (!attr_set[1]) {
@@ -415,7 +427,7 @@ int tc_gemm_pair_launch(int epi, const CUtensorMap& ta0, const CUtensorMap& tb0,
       attr_set[1] = true;
     }
     GB_LAUNCH(kernel_kind, s,
-              (tc_gemm_pair_kernel<TC_EPI_F32><<<grid, P2_THREADS, P2_SMEM_BYTES, s>>>(ta0, tb0, a1, b1, sched, prm)));
+              (tc_gemm_pair_kernel<TC_EPI_F32><<<grid, P2Shape<TC_EPI_F32>::THREADS, P2_SMEM_BYTES, s>>>(ta0, tb0, a1, b1, sched, prm)));
   }
   GB_CUDA_TRY(cudaGetLastError());
   return GB_OK;

@@ -348,8 +348,8 @@ CRT_MAX_MODULI = 20
 
 
 def crt_moduli(n):
-    """The first n moduli: 256, then descending integers coprime to all taken so far."""
-    out, c = [], 256
+    """The first n moduli: 253, then descending integers coprime to all taken so far."""
+    out, c = [], 253
     while len(out) < n:
         if all(math.gcd(c, m) == 1 for m in out):
             out.append(c)

@@ -150,5 +150,5 @@ def test_crt_restatement_against_exact_rationals():
 def test_crt_moduli_pairwise_coprime():
     import math
     m = oracle.crt_moduli(20)
-    assert m[0] == 256 and len(set(m)) == 20 and max(m) <= 256
+    assert m[0] == 253 and len(set(m)) == 20 and max(m) <= 253
     assert all(math.gcd(a, b) == 1 for i, a in enumerate(m) for b in m[i + 1:])
