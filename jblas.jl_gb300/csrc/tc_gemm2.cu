@@ -195,7 +195,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(P2Shape<EPI>::THREAD
             }
             tc_fence_after();
             const uint32_t d_tmem = tmem_base + static_cast<uint32_t>(buf * TC_BN);
-            uint32_t accumulate = 0;
+            // CRT: chunk c accumulates onto the residue of chunk c - 2, which the epilogue
+            // stored back into this buffer
+            uint32_t accumulate = (EPI == TC_EPI_CRT && c >= 2) ? 1u : 0u;
             for (int i = 0; i < sched.npairs[g] && ok; ++i) {
               for (int kb = kb0; kb < kb1; ++kb) {
                 if (!mbar_wait_bounded(&full[stage], phase, prm.wait_limit_ns, abort_flag, prm.status, 3)) {
@@ -266,16 +268,19 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(P2Shape<EPI>::THREAD
           const bool first = (step == 0), last = (step == nsteps - 1);
           const uint32_t taddr = tmem_base + (static_cast<uint32_t>(q * 32) << 16) + static_cast<uint32_t>(buf * TC_BN);
           if (EPI == TC_EPI_CRT) {
-            // The chunk sum S (an exact integer, |S| <= 1024 * 126^2) plus this thread's
-            // running residue r (|r| <= 127, kept as the biased byte r + 128, four to a
-            // register) is exact in FP32; one reduction t - p * rint(t / p) returns |r| <= 127 because
-            // p <= 253.  All in FP32 and byte permutes: no integer range fixes.  The last
-            // chunk writes the biased bytes to the residue plane (rows and columns padded to
-            // whole tiles, so always in bounds).
+            // Chunk c of modulus p holds D = S_c + r_{c-2} (the MMA accumulated onto the residue
+            // the drain of chunk c - 2 stored back into this buffer; S_c is the exact integer
+            // chunk sum, |D| <= 1024 * 126^2 + 127 < 2^24, exact in FP32).  One reduction
+            // r_c = D - p * rint(D / p) gives |r_c| <= 127 since p <= 253, and r_c goes back to
+            // TMEM for chunk c + 2.  The two chains (even and odd chunks) meet at the end: the
+            // drain of chunk nc - 2 keeps its residue in registers (biased bytes r + 128), the
+            // last drain adds it and writes the biased bytes to the residue plane (rows and
+            // columns padded to whole tiles, so always in bounds).
             constexpr float MAGIC = 12582912.0f;   // 1.5 * 2^23: x + MAGIC - MAGIC = rint(x), |x| < 2^22
             constexpr float BIAS_F = 8388736.0f;   // 2^23 + 128: the low byte of (r + BIAS_F) is r + 128
             const float pf = prm.crt_p[g], inv = prm.crt_inv[g];
-            const bool first_c = (c == 0), last_c = (c == P.nchunks - 1);
+            const int nc = P.nchunks;
+            const bool to_tmem = (c + 2 < nc), final_c = (c == nc - 1);
             const int64_t ld = prm.res_ld;
 #pragma unroll
             for (int bi = 0; bi < COLS / 16; ++bi) {   // 16 columns per TMEM load
@@ -283,23 +288,35 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(P2Shape<EPI>::THREAD
               tmem_ld_32x32b_x16(taddr + col0 + bi * 16, v);
               tc_wait_ld();
 #pragma unroll
-              for (int j4 = 0; j4 < 4; ++j4) {
-                const uint32_t old = first_c ? 0x80808080u : racc[bi * 4 + j4];
-                uint32_t rb[4];
+              for (int j = 0; j < 16; ++j) {
+                const float d = __uint_as_float(v[j]);
+                const float q = fmaf(d, inv, MAGIC) - MAGIC;
+                v[j] = __float_as_uint(fmaf(-pf, q, d));
+              }
+              if (to_tmem) {
+                tmem_st_32x32b_x16(taddr + col0 + bi * 16, v);
+              } else {
 #pragma unroll
-                for (int jj = 0; jj < 4; ++jj) {
-                  // 0x4B0000bb as a float is 2^23 + bb: the old residue is that minus BIAS_F
-                  const float prev = __uint_as_float(__byte_perm(old, 0x4B000000u, 0x7540u + jj)) - BIAS_F;
-                  const float t = __uint_as_float(v[j4 * 4 + jj]) + prev;
-                  const float q = fmaf(t, inv, MAGIC) - MAGIC;
-                  const float r = fmaf(-pf, q, t);
-                  rb[jj] = __float_as_uint(r + BIAS_F);
+                for (int j4 = 0; j4 < 4; ++j4) {
+                  uint32_t rb[4];
+#pragma unroll
+                  for (int jj = 0; jj < 4; ++jj) {
+                    float r = __uint_as_float(v[j4 * 4 + jj]);
+                    if (final_c && nc >= 2) {
+                      // add the other chain's residue (0x4B0000bb as a float is 2^23 + bb)
+                      const float t = r + (__uint_as_float(__byte_perm(racc[bi * 4 + j4], 0x4B000000u, 0x7540u + jj)) - BIAS_F);
+                      const float q = fmaf(t, inv, MAGIC) - MAGIC;
+                      r = fmaf(-pf, q, t);
+                    }
+                    rb[jj] = __float_as_uint(r + BIAS_F);
+                  }
+                  racc[bi * 4 + j4] =
+                      __byte_perm(__byte_perm(rb[0], rb[1], 0x0040u), __byte_perm(rb[2], rb[3], 0x0040u), 0x5410u);
                 }
-                racc[bi * 4 + j4] =
-                    __byte_perm(__byte_perm(rb[0], rb[1], 0x0040u), __byte_perm(rb[2], rb[3], 0x0040u), 0x5410u);
               }
             }
-            if (last_c) {
+            if (to_tmem) tc_wait_st();
+            if (final_c) {
               uint8_t* __restrict__ dst = prm.res + g * prm.res_plane + (n0 + col0) * ld + row;
 #pragma unroll
               for (int w = 0; w < COLS / 4; ++w) {
