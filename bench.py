@@ -441,29 +441,35 @@ def main():
 
     # ---------------------------------------------------------------- timed: end to end
     # Every step copies its inputs host -> device (pinned) and its result device -> host.
-    # Copies run on a second stream with double-buffered device inputs/outputs, so step
-    # i+1's uploads and step i's download overlap step i's compute (a serving pipeline).
+    # Uploads and downloads run on their own streams (the two copy directions overlap) with
+    # double-buffered device inputs/outputs, so step i+1's uploads and step i-1's download
+    # overlap step i's compute (a serving pipeline).
     barrier()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    copy_stream = torch.cuda.Stream(dev)
+    up_stream, down_stream = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
     A_e = [torch.empty_like(A_pin, device=dev) for _ in range(2)]
     B_e = [torch.empty_like(B_pin, device=dev) for _ in range(2)]
     C_e = [torch.empty((N, M), dtype=torch.float64, device=dev) for _ in range(2)]
     up_done = [torch.cuda.Event() for _ in range(2)]
     comp_done = [torch.cuda.Event() for _ in range(2)]
     down_done = [torch.cuda.Event() for _ in range(2)]
+    comp_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(args.steps)]
     e0.record(stream)
-    copy_stream.wait_stream(stream)
+    up_stream.wait_stream(stream)
+    down_stream.wait_stream(stream)
 
     def upload(i):
         b = i % 2
-        with torch.cuda.stream(copy_stream):
+        with torch.cuda.stream(up_stream):
             if i >= 2:
-                copy_stream.wait_event(comp_done[b])     # buffer b's previous compute is done
+                up_stream.wait_event(comp_done[b])       # buffer b's previous compute is done
             A_e[b].copy_(A_pin, non_blocking=True)
             B_e[b].copy_(B_pin, non_blocking=True)
-            up_done[b].record(copy_stream)
+            up_done[b].record(up_stream)
 
+    pipe_prof = gbblas.profile()
+    pipe_prof.__enter__()
     upload(0)
     for i in range(args.steps):
         b = i % 2
@@ -472,18 +478,37 @@ def main():
         stream.wait_event(up_done[b])
         if i >= 2:
             stream.wait_event(down_done[b])              # C_e[b] of step i-2 has been read
+        comp_ev[i][0].record(stream)
         gbblas.gemm_(C_e[b].t(), A_e[b].t(), B_e[b].t(), mode=mode, slices=args.slices)
+        comp_ev[i][1].record(stream)
         comp_done[b].record(stream)
-        with torch.cuda.stream(copy_stream):
-            copy_stream.wait_event(comp_done[b])
+        with torch.cuda.stream(down_stream):
+            down_stream.wait_event(comp_done[b])
             C_pin.copy_(C_e[b], non_blocking=True)
-            down_done[b].record(copy_stream)
-    stream.wait_stream(copy_stream)
+            down_done[b].record(down_stream)
+    stream.wait_stream(up_stream)
+    stream.wait_stream(down_stream)
     e1.record(stream)
     torch.cuda.synchronize()
+    pipe_prof.__exit__(None, None, None)
     barrier()
     ms_e2e = max_over_ranks(e0.elapsed_time(e1) / args.steps)
     e2e_value = world * flops / (ms_e2e * 1e-3) / 1e12
+    comp_in_pipeline = statistics.median(a.elapsed_time(z) for a, z in comp_ev)
+    copy_stream = up_stream
+
+    # the host link alone: one step's uploads and download on the copy stream, no compute
+    c0, c1, c2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    with torch.cuda.stream(copy_stream):
+        c0.record(copy_stream)
+        A_e[0].copy_(A_pin, non_blocking=True)
+        B_e[0].copy_(B_pin, non_blocking=True)
+        c1.record(copy_stream)
+        C_pin.copy_(C_e[0], non_blocking=True)
+        c2.record(copy_stream)
+    torch.cuda.synchronize()
+    h2d_gbs = (A_pin.numel() + B_pin.numel()) * 8 / (c0.elapsed_time(c1) * 1e-3) / 1e9
+    d2h_gbs = C_pin.numel() * 8 / (c1.elapsed_time(c2) * 1e-3) / 1e9
 
     plan = gbblas.last_ozaki_plan()   # the plan the automatic choice used
     alt = None
@@ -575,6 +600,9 @@ def main():
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "TFLOP/s", "ms_per_step": ms_e2e,
                     "pipeline": "double-buffered: uploads of step i+1 and download of step i overlap step i",
+                    "h2d_GBps": h2d_gbs, "d2h_GBps": d2h_gbs,
+                    "compute_ms_in_pipeline": comp_in_pipeline,
+                    "kernel_ms_in_pipeline": {k: v / args.steps for k, v in pipe_prof.ms.items()},
                     "h2d_bytes_per_step": int(A_pin.numel() * 8 + B_pin.numel() * 8),
                     "d2h_bytes_per_step": int(C_pin.numel() * 8)},
             "gpu_launches": launches,

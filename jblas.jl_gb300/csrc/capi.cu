@@ -161,6 +161,15 @@ int make_plane_tmap(CUtensorMap* map, const void* base, int64_t K, int64_t rows,
   return GB_OK;
 }
 
+// The last CRT call's plan lives on the device until someone asks for it.
+struct PendingCrtPlan {
+  bool pending = false;
+  CrtDevicePlan* slot = nullptr;
+  cudaEvent_t done = nullptr;
+  int64_t M = 0, N = 0, kb_total = 0, k_chunk = 0;
+};
+static thread_local PendingCrtPlan g_pending_crt;
+
 // ------------------------------------------------------------------ Ozaki driver
 static double ozaki_tolerance() {
   uint64_t b = g_ozaki_tol_bits.load();
@@ -257,8 +266,8 @@ struct OperandStats {
 };
 
 static int run_stats(DeviceInfo* dev, const double* A, int64_t M, int64_t a_rs, int64_t a_ks, const double* B,
-                     int64_t N, int64_t b_rs, int64_t b_ks, int64_t K, bool host, OperandStats* os, HostStats* h,
-                     cudaStream_t s) {
+                     int64_t N, int64_t b_rs, int64_t b_ks, int64_t K, bool sums, bool host, OperandStats* os,
+                     HostStats* h, cudaStream_t s) {
   const int Sa = oz_stats_kslices(M, K, a_ks, dev->sms), Sb = oz_stats_kslices(N, K, b_ks, dev->sms);
   const int64_t pa = Sa * M, pb = Sb * N;
   const size_t amax_bytes = align256((M + N) * sizeof(unsigned long long));
@@ -274,8 +283,8 @@ static int run_stats(DeviceInfo* dev, const double* A, int64_t M, int64_t a_rs, 
   os->b.part_sq = os->a.part_sq + pa;
   os->a.kslices = Sa;
   os->b.kslices = Sb;
-  int rc = oz_row_stats(A, M, K, a_rs, a_ks, os->a, host, s);
-  if (!rc) rc = oz_row_stats(B, N, K, b_rs, b_ks, os->b, host, s);
+  int rc = oz_row_stats(A, M, K, a_rs, a_ks, os->a, sums || host, s);
+  if (!rc) rc = oz_row_stats(B, N, K, b_rs, b_ks, os->b, sums || host, s);
   if (rc || !host) return rc;
   std::vector<unsigned long long> amax(M + N);
   std::vector<int32_t> pe(pa + pb);
@@ -349,7 +358,7 @@ static int ozaki_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int
   OperandStats os;
   HostStats h;
   const bool host_stats = (slices == 0 || err_bound_out);
-  int rc = run_stats(dev, A, M, a_rs, a_ks, B, N, b_rs, b_ks, K, host_stats, &os, &h, s);
+  int rc = run_stats(dev, A, M, a_rs, a_ks, B, N, b_rs, b_ks, K, host_stats, host_stats, &os, &h, s);
   if (rc) {
     if (os.ws) cudaFreeAsync(os.ws, s);
     return rc;
@@ -402,6 +411,7 @@ static int ozaki_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int
     }
   }
 
+  g_pending_crt.pending = false;
   g_last_plan.slices = plan.slices;
   g_last_plan.bits = plan.bits;
   g_last_plan.k_chunk = static_cast<int32_t>(plan.k_chunk);
@@ -457,33 +467,10 @@ static int ozaki_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int
 }
 
 // ------------------------------------------------------------------ CRT driver
-// Normwise bound for the CRT mode with t integer bits (alpha = 1, beta = 0): rounding A and
-// B to the 2^(e - t) grid moves each element by at most 2^(e - t - 1); the integer product is
-// exact; the conversion to FP64 and the alpha product round once each.
-static double crt_bound(const BoundStats& st, int64_t K, int t) {
-  if (st.nonfinite) return INFINITY;
-  const double na = st.na, nb = st.nb;
-  if (na == 0.0 || nb == 0.0) return 0.0;
-  const double h = std::ldexp(1.0, -t - 1);
-  const double Kd = static_cast<double>(K);
-  const double trunc = h * (st.EA * st.SB + st.EB * st.SA) + Kd * h * h * st.EA * st.EB;
-  const double fin = 2.0 * std::ldexp(1.0, -53) * (na * nb + trunc);
-  return 1.01 * (trunc + fin) / (na * nb);
-}
-
-// Largest t for n moduli given row-sum statistics: |C'| <= 2^(2t) (min(max sa, max sb) +
-// K 2^(-t-1)) must stay <= M / 4 and <= 2^125 (checked in log2 with a safety margin).
-static int crt_bits_from_stats(const BoundStats& st, int64_t K, int n) {
-  const double lm = crt_log2_product(n);
-  const double Kd = static_cast<double>(K < 1 ? 1 : K);
-  for (int t = 62; t >= 1; --t) {
-    double S = std::min(st.sa_max, st.sb_max) + Kd * std::ldexp(1.0, -t - 1);
-    S = std::min(S, Kd) * (1.0 + 1e-12);
-    const double need = 2.0 * t + std::log2(S);
-    if (need + 2.0 <= lm - 1e-9 && need <= 125.0 - 1e-9) return t;
-  }
-  return 0;
-}
+// The plan (moduli n and integer bits t) is chosen on the device from the statistics
+// (crt_plan_device), so an automatic call has no host round trip; the workspace is sized for
+// the largest n the call may take.  The host only learns the plan when asked for it
+// (err_bound_out, gb_last_ozaki_plan).
 
 static int crt_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int64_t K, double alpha, const double* A,
                     int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc, int moduli,
@@ -493,70 +480,66 @@ static int crt_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int64
   const int64_t a_rs = ta ? lda : 1, a_ks = ta ? 1 : lda;
   const int64_t b_rs = tb ? 1 : ldb, b_ks = tb ? ldb : 1;
   const int64_t pitch = ((K + 63) / 64) * 64;
+  int t_fixed = 0;
+  if (moduli > 0) {
+    t_fixed = crt_bits_for(K, moduli);
+    if (t_fixed < 1) return GB_ERR_UNSUPPORTED;   // too few moduli for this K
+  }
+  const int n_ws = moduli ? moduli : TC_MAX_MODULI;
+  CrtPlan plan;   // K chunking and a schedule for up to n_ws moduli
+  int rc = crt_make_plan(M, N, K, n_ws, t_fixed, &plan);
+  if (rc) return rc;
+  CrtDevicePlan* slot = nullptr;
+  rc = crt_plan_slot(&slot);
+  if (rc) return rc;
 
+  const bool sums = (moduli == 0 || err_bound_out);
   OperandStats os;
   HostStats h;
-  const bool host_stats = (moduli == 0 || err_bound_out);
-  int rc = run_stats(dev, A, M, a_rs, a_ks, B, N, b_rs, b_ks, K, host_stats, &os, &h, s);
+  rc = run_stats(dev, A, M, a_rs, a_ks, B, N, b_rs, b_ks, K, sums, false, &os, &h, s);
   if (rc) {
     if (os.ws) cudaFreeAsync(os.ws, s);
     return rc;
   }
-  char* st_ws = os.ws;
-  OzRowStats& sa = os.a;
-  OzRowStats& sb = os.b;
-
-  CrtPlan plan;
-  if (host_stats) {
-    const BoundStats bst = bound_stats(h);
-    if (moduli == 0) {
-      // fewest moduli (each one BF16 GEMM) whose bound, at the widest t they allow, meets
-      // the tolerance
-      const double tol = ozaki_tolerance();
-      int n_use = 0, t_use = 0;
-      for (int n = 1; n <= TC_MAX_MODULI && !n_use; ++n) {
-        const int t = bst.nonfinite ? crt_bits_for(K, n) : crt_bits_from_stats(bst, K, n);
-        if (t >= 1 && (bst.nonfinite || crt_bound(bst, K, t) <= tol)) {
-          n_use = n;
-          t_use = t;
-        }
-      }
-      if (!n_use) {   // tolerance out of reach: the most moduli
-        n_use = TC_MAX_MODULI;
-        t_use = bst.nonfinite ? crt_bits_for(K, n_use) : crt_bits_from_stats(bst, K, n_use);
-        if (t_use < 1) t_use = crt_bits_for(K, n_use);
-      }
-      rc = crt_make_plan(M, N, K, n_use, t_use, &plan);
-    } else {
-      rc = crt_make_plan(M, N, K, moduli, 0, &plan);
-    }
-    if (!rc && err_bound_out) *err_bound_out = crt_bound(bst, K, plan.t);
-  } else {
-    rc = crt_make_plan(M, N, K, moduli, 0, &plan);
+  CrtPlanParams pp;
+  std::memset(&pp, 0, sizeof(pp));
+  pp.M = M;
+  pp.N = N;
+  pp.K = K;
+  pp.n_fixed = moduli;
+  pp.t_fixed = t_fixed;
+  pp.with_sums = sums ? 1 : 0;
+  pp.tol = ozaki_tolerance();
+  for (int n = 1; n <= TC_MAX_MODULI; ++n) {
+    pp.log2m[n] = crt_log2_product(n);
+    pp.tk[n] = crt_bits_for(K, n);
+  }
+  void* scratch = nullptr;
+  GB_CUDA_TRY(cudaMallocFromPoolAsync(&scratch, crt_plan_scratch_bytes(), dev->pool, s));
+  rc = crt_plan_device(os.a, os.b, pp, slot, scratch, s);
+  cudaFreeAsync(scratch, s);
+  if (!rc && err_bound_out) {
+    CrtDevicePlan hp;
+    cudaError_t e = cudaMemcpyAsync(&hp, slot, sizeof(hp), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) rc = gb_set_cuda_error(e, "ozaki crt plan");
+    else *err_bound_out = hp.bound;
   }
   if (rc) {
-    cudaFreeAsync(st_ws, s);
+    cudaFreeAsync(os.ws, s);
     return rc;
   }
 
-  g_last_plan.slices = plan.n;
-  g_last_plan.bits = plan.t;
-  g_last_plan.k_chunk = static_cast<int32_t>(plan.k_chunk);
-  g_last_plan.products = plan.n;
-  g_last_plan.groups = plan.n;
-  g_last_plan.flops_tensor = plan.flops_tensor;
-
-  const int n = plan.n;
   const int64_t mpad = (M + 255) / 256 * 256, npad = (N + 255) / 256 * 256;
-  const size_t pa_bytes = align256(static_cast<size_t>(n) * M * pitch * 2);
-  const size_t pb_bytes = align256(static_cast<size_t>(n) * N * pitch * 2);
-  const size_t res_bytes = align256(static_cast<size_t>(n) * mpad * npad);
+  const size_t pa_bytes = align256(static_cast<size_t>(n_ws) * M * pitch * 2);
+  const size_t pb_bytes = align256(static_cast<size_t>(n_ws) * N * pitch * 2);
+  const size_t res_bytes = align256(static_cast<size_t>(n_ws) * mpad * npad);
   const size_t ex_bytes = align256((M + N) * sizeof(int32_t));
   char* ws = nullptr;
   cudaError_t e = cudaMallocFromPoolAsync(reinterpret_cast<void**>(&ws), pa_bytes + pb_bytes + res_bytes + ex_bytes,
                                           dev->pool, s);
   if (e != cudaSuccess) {
-    cudaFreeAsync(st_ws, s);
+    cudaFreeAsync(os.ws, s);
     return gb_set_cuda_error(e, "ozaki crt workspace");
   }
   __nv_bfloat16* pa = reinterpret_cast<__nv_bfloat16*>(ws);
@@ -564,8 +547,8 @@ static int crt_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int64
   uint8_t* res = reinterpret_cast<uint8_t*>(ws + pa_bytes + pb_bytes);
   int32_t* ea = reinterpret_cast<int32_t*>(ws + pa_bytes + pb_bytes + res_bytes);
   int32_t* eb = ea + M;
-  rc = crt_split(A, M, K, a_rs, a_ks, sa.amax_bits, plan, pa, pitch, ea, s);
-  if (!rc) rc = crt_split(B, N, K, b_rs, b_ks, sb.amax_bits, plan, pb, pitch, eb, s);
+  rc = crt_split(A, M, K, a_rs, a_ks, os.a.amax_bits, slot, pa, pitch, ea, s);
+  if (!rc) rc = crt_split(B, N, K, b_rs, b_ks, os.b.amax_bits, slot, pb, pitch, eb, s);
   if (!rc) {
     CrtGemmArgs ga;
     ga.planes_a = pa;
@@ -588,11 +571,40 @@ static int crt_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int64
     const int64_t ctas = 2 * static_cast<int64_t>(tc_pair_tiles(M, N));
     const int64_t cap = dev->sms & ~1;
     ga.grid = static_cast<int>(ctas < cap ? ctas : cap);
+    ga.plan = slot;
     rc = crt_gemm_launch(ga, plan, s);
   }
+  if (!rc) {
+    PendingCrtPlan& pd = g_pending_crt;
+    if (!pd.done && cudaEventCreateWithFlags(&pd.done, cudaEventDisableTiming) != cudaSuccess) pd.done = nullptr;
+    pd.pending = pd.done && cudaEventRecord(pd.done, s) == cudaSuccess;
+    pd.slot = slot;
+    pd.M = M;
+    pd.N = N;
+    pd.kb_total = plan.kb_total;
+    pd.k_chunk = plan.k_chunk;
+  }
   cudaFreeAsync(ws, s);
-  cudaFreeAsync(st_ws, s);
+  cudaFreeAsync(os.ws, s);
   return rc;
+}
+
+// Fills g_last_plan from the device plan of the last CRT call of this thread, if any.
+static int resolve_pending_crt_plan() {
+  PendingCrtPlan& pd = g_pending_crt;
+  if (!pd.pending) return GB_OK;
+  pd.pending = false;
+  GB_CUDA_TRY(cudaEventSynchronize(pd.done));
+  CrtDevicePlan hp;
+  GB_CUDA_TRY(cudaMemcpy(&hp, pd.slot, sizeof(hp), cudaMemcpyDeviceToHost));
+  g_last_plan.slices = hp.n;
+  g_last_plan.bits = hp.t;
+  g_last_plan.k_chunk = static_cast<int32_t>(pd.k_chunk);
+  g_last_plan.products = hp.n;
+  g_last_plan.groups = hp.n;
+  g_last_plan.flops_tensor = 2.0 * static_cast<double>(pd.M) * static_cast<double>(pd.N) *
+                             static_cast<double>(pd.kb_total * TC_BK) * hp.n;
+  return GB_OK;
 }
 
 }  // namespace gb
@@ -814,6 +826,8 @@ int gb_jmul_f32(float* D, const float* A, const float* X, int64_t M, int64_t N, 
 
 int gb_last_ozaki_plan(gb_ozaki_plan_t* out) {
   if (!out) return GB_ERR_INVALID_VALUE;
+  const int rc = resolve_pending_crt_plan();
+  if (rc) return rc;
   *out = g_last_plan;
   return GB_OK;
 }

@@ -77,21 +77,44 @@ int oz_gemm_launch(const OzGemmArgs& a, const OzPlan& plan, cudaStream_t s);
 int oz_grid_for(int sms, int64_t M, int64_t N);
 
 // ---------------------------------------------------------------- CRT mode (ozaki_crt.cu)
-// Constants of one CRT product, passed by value to the split and combine kernels.
-struct CrtConsts {
-  int32_t n;                       // moduli
-  int32_t t;                       // integer bits: |A'|, |B'| <= 2^t
-  uint32_t p[TC_MAX_MODULI];       // the moduli (pairwise coprime, <= 253)
-  uint32_t c21[TC_MAX_MODULI];     // 2^21 mod p
-  uint32_t c42[TC_MAX_MODULI];     // 2^42 mod p
-  uint32_t bias[TC_MAX_MODULI];    // -2^62 mod p
-  uint32_t mg[TC_MAX_MODULI];      // floor(2^32 / p)
-  float finv[TC_MAX_MODULI];       // fl32(inv_g / p_g), inv_g = (M / p_g)^-1 mod p_g
-  uint32_t w[TC_MAX_MODULI][4];    // (M / p_g) inv_g mod 2^128, little-endian 32-bit words
-  uint32_t m[4];                   // M mod 2^128
-  uint32_t bw[4];                  // 128 * sum_g W_g mod 2^128 (bias of the residue bytes)
-  float bias_k;                    // 128 * sum_g finv[g]
-  int32_t ab;                      // 0: C = v; 1: C = alpha v; 2: C = fma(alpha, v, beta C)
+// Constants of the CRT mode, fixed by the moduli table; passed by value to the kernels.
+struct CrtModuli {                  // per modulus g (independent of how many a call uses)
+  uint32_t p[TC_MAX_MODULI];        // the moduli (pairwise coprime, <= 253)
+  float climb[TC_MAX_MODULI][6];    // split: 2^(12 l) mod p for l = 1..5, and -2^62 mod p in [0]
+  float pf[TC_MAX_MODULI];          // p as a float
+  float pinv[TC_MAX_MODULI];        // fl32(1 / p)
+};
+struct CrtRecon {                   // reconstruction with the first n moduli, M = their product
+  float finv[TC_MAX_MODULI];        // fl32(inv_g / p_g), inv_g = (M / p_g)^-1 mod p_g
+  uint32_t w[TC_MAX_MODULI][4];     // (M / p_g) inv_g mod 2^128, little-endian 32-bit words
+  uint32_t m[4];                    // M mod 2^128
+  uint32_t bw[4];                   // 128 * sum_g W_g mod 2^128 (bias of the residue bytes)
+  float bias_k;                     // 128 * sum_g finv[g]
+  int32_t pad;
+};
+struct CrtTable {
+  CrtModuli mod;
+  CrtRecon rec[TC_MAX_MODULI];      // rec[n - 1]: the first n moduli
+};
+
+// The plan of one CRT call, written on the device by the planner kernel (no host round trip)
+// and read by the split, residue-product and combine kernels.
+struct CrtDevicePlan {
+  int32_t n;        // moduli
+  int32_t t;        // integer bits of the scaled operands
+  double bound;     // a-priori normwise error bound of the plan
+};
+
+// Inputs of the planner besides the statistics.
+struct CrtPlanParams {
+  int64_t M, N, K;
+  int32_t n_fixed;                      // > 0: this many moduli with t = t_fixed
+  int32_t t_fixed;
+  int32_t with_sums;                    // the statistics carry K-slice sums (else no bound)
+  int32_t pad;
+  double tol;                           // normwise tolerance for the automatic choice
+  double log2m[TC_MAX_MODULI + 1];      // log2 of the product of the first n moduli
+  int32_t tk[TC_MAX_MODULI + 1];        // crt_bits_for(K, n), used when statistics are not finite
 };
 
 struct CrtPlan {
@@ -102,7 +125,6 @@ struct CrtPlan {
   double flops_tensor;
   double log2_m;
   SliceSchedule sched;   // one group per modulus, pair (g, g)
-  CrtConsts cc;
 };
 
 const uint32_t* crt_moduli();       // TC_MAX_MODULI moduli, in the order they are used
@@ -111,9 +133,19 @@ double crt_log2_product(int n);     // log2 of the product of the first n moduli
 int crt_bits_for(int64_t K, int n);
 // Plan for n moduli and t integer bits (t = 0: crt_bits_for(K, n)).
 int crt_make_plan(int64_t M, int64_t N, int64_t K, int n, int t, CrtPlan* plan);
-// Residue planes (BF16, [modulus][row][pitch]) and row exponents of op(X).
+// The constant table (built once on the host).
+const CrtTable& crt_table();
+// A plan slot from the current device's ring of plan records (reused after 256 calls).
+int crt_plan_slot(CrtDevicePlan** slot);
+// Planner: from the statistics (with sums), the fewest moduli whose bound meets pp.tol (or
+// pp.n_fixed) and the widest t they allow; writes *plan on the device.  `scratch` holds
+// crt_plan_scratch_bytes() bytes of stream-ordered workspace.
+size_t crt_plan_scratch_bytes();
+int crt_plan_device(const OzRowStats& sa, const OzRowStats& sb, const CrtPlanParams& pp, CrtDevicePlan* plan,
+                    void* scratch, cudaStream_t s);
+// Residue planes (BF16, [modulus][row][pitch], plan->n of them) and row exponents of op(X).
 int crt_split(const double* X, int64_t R, int64_t K, int64_t rs, int64_t ks, const unsigned long long* amax_bits,
-              const CrtPlan& plan, __nv_bfloat16* planes, int64_t pitch, int32_t* exps, cudaStream_t s);
+              const CrtDevicePlan* plan, __nv_bfloat16* planes, int64_t pitch, int32_t* exps, cudaStream_t s);
 
 struct CrtGemmArgs {
   const void* planes_a;   // [n][M][pitch] bf16
@@ -131,8 +163,11 @@ struct CrtGemmArgs {
   DeviceStatus* status;
   uint64_t wait_limit_ns;
   int grid;               // even (CTA pairs)
+  const CrtDevicePlan* plan;
 };
-// Residue products on the CTA-pair engine, then the CRT reconstruction into C.
+// Residue products on the CTA-pair engine, then the CRT reconstruction into C.  `plan`
+// (host) gives the K chunking and a schedule for up to plan.n moduli; the kernels run
+// the device plan's n <= plan.n.
 int crt_gemm_launch(const CrtGemmArgs& a, const CrtPlan& plan, cudaStream_t s);
 
 

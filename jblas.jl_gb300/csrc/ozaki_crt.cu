@@ -6,9 +6,9 @@
 //   A'[i,k] = round-half-away(op(A)[i,k] * 2^(t - ea_i))    |A'| <= 2^t  (ea_i: row exponent)
 //   B'[k,j] = round-half-away(op(B)[k,j] * 2^(t - eb_j))    |B'| <= 2^t
 //   C' = A' B' exactly, from its residues modulo n pairwise coprime p_g <= 253:
-//     R_g = (A' mod p_g)(B' mod p_g)    balanced residues, |r| <= 126 (exact in BF16); FP32
-//                                       sums over K chunks of <= 1024 stay exact (1024 *
-//                                       126^2 + 127 < 2^24) and are reduced mod p_g
+//     R_g = (A' mod p_g)(B' mod p_g)    residues |r| <= 127 (exact in BF16); FP32 sums over
+//                                       K chunks of <= 1024 stay exact (1024 * 127^2 + 127
+//                                       < 2^24) and are reduced mod p_g
 //     C' = CRT(R_1, ..., R_n)           exact because |C'| <= M/4, M = prod p_g
 //   C = alpha * fl(C' * 2^(ea_i + eb_j - 2t)) + beta * C
 // Only the rounding of A and B to t-bit integers and the final conversion round; the
@@ -22,7 +22,10 @@
 #include <cuda_bf16.h>
 
 #include <cmath>
+#include <atomic>
 #include <cstring>
+#include <memory>
+#include <mutex>
 #include <vector>
 
 #include "gb_common.cuh"
@@ -140,6 +143,60 @@ int crt_bits_for(int64_t K, int n) {
   return 0;
 }
 
+namespace {
+CrtTable build_table() {
+  CrtTable tab;
+  std::memset(&tab, 0, sizeof(tab));
+  CrtModuli& md = tab.mod;
+  for (int g = 0; g < TC_MAX_MODULI; ++g) {
+    const uint32_t p = moduli_table().p[g];
+    md.p[g] = p;
+    md.pf[g] = static_cast<float>(p);
+    md.pinv[g] = 1.0f / static_cast<float>(p);
+    uint64_t pw = 1;   // 2^(12 l) mod p
+    for (int l = 1; l <= 5; ++l) {
+      pw = (pw << 12) % p;
+      md.climb[g][l] = static_cast<float>(pw);
+    }
+    const uint64_t c62 = (((uint64_t(1) << 31) % p) * ((uint64_t(1) << 31) % p)) % p;
+    md.climb[g][0] = static_cast<float>((p - c62) % p);
+  }
+  for (int n = 1; n <= TC_MAX_MODULI; ++n) {
+    CrtRecon& rc = tab.rec[n - 1];
+    unsigned __int128 m128 = 1;
+    for (int g = 0; g < n; ++g) m128 *= moduli_table().p[g];
+    for (int w = 0; w < 4; ++w) rc.m[w] = static_cast<uint32_t>(m128 >> (32 * w));
+    unsigned __int128 bias128 = 0;
+    double bias_k = 0.0;
+    for (int g = 0; g < n; ++g) {
+      // M / p_g modulo p_g and modulo 2^128
+      const uint32_t p = moduli_table().p[g];
+      uint64_t rest_mod_p = 1;
+      unsigned __int128 rest128 = 1;
+      for (int h = 0; h < n; ++h) {
+        if (h == g) continue;
+        rest_mod_p = (rest_mod_p * (moduli_table().p[h] % p)) % p;
+        rest128 *= moduli_table().p[h];
+      }
+      const uint32_t inv = inverse_mod(static_cast<uint32_t>(rest_mod_p), p);
+      rc.finv[g] = static_cast<float>(static_cast<double>(inv) / static_cast<double>(p));
+      const unsigned __int128 w128 = rest128 * inv;
+      for (int w = 0; w < 4; ++w) rc.w[g][w] = static_cast<uint32_t>(w128 >> (32 * w));
+      bias128 += w128 * 128u;
+      bias_k += 128.0 * static_cast<double>(rc.finv[g]);
+    }
+    for (int w = 0; w < 4; ++w) rc.bw[w] = static_cast<uint32_t>(bias128 >> (32 * w));
+    rc.bias_k = static_cast<float>(bias_k);
+  }
+  return tab;
+}
+}  // namespace
+
+const CrtTable& crt_table() {
+  static const CrtTable tab = build_table();
+  return tab;
+}
+
 int crt_make_plan(int64_t M, int64_t N, int64_t K, int n, int t, CrtPlan* plan) {
   if (n < 1 || n > TC_MAX_MODULI || t < 0 || t > 62) return GB_ERR_INVALID_VALUE;
   if (t == 0) t = crt_bits_for(K, n);
@@ -150,7 +207,7 @@ int crt_make_plan(int64_t M, int64_t N, int64_t K, int n, int t, CrtPlan* plan) 
   P.t = t;
   int64_t kb_total = (K + TC_BK - 1) / TC_BK;
   if (kb_total < 1) kb_total = 1;
-  // exact FP32 chunk sums: at most 16 panels (1024 products of |r| <= 126)
+  // exact FP32 chunk sums: at most 16 panels (1024 products of |r| <= 127)
   int64_t nchunks = (kb_total + 15) / 16;
   const int64_t kb_chunk = (kb_total + nchunks - 1) / nchunks;
   nchunks = (kb_total + kb_chunk - 1) / kb_chunk;
@@ -172,107 +229,358 @@ int crt_make_plan(int64_t M, int64_t N, int64_t K, int n, int t, CrtPlan* plan) 
     S.pq[g] = static_cast<uint8_t>(g);
   }
 
-  CrtConsts& cc = P.cc;
-  cc.n = n;
-  cc.t = t;
-  unsigned __int128 m128 = 1;
-  for (int g = 0; g < n; ++g) m128 *= moduli_table().p[g];
-  for (int w = 0; w < 4; ++w) cc.m[w] = static_cast<uint32_t>(m128 >> (32 * w));
-  unsigned __int128 bias128 = 0;
-  double bias_k = 0.0;
-  for (int g = 0; g < n; ++g) {
-    const uint32_t p = moduli_table().p[g];
-    const uint64_t c21 = (uint64_t(1) << 21) % p;
-    const uint64_t c42 = (c21 * c21) % p;
-    const uint64_t c62 = (c42 * ((uint64_t(1) << 20) % p)) % p;
-    cc.p[g] = p;
-    cc.c21[g] = static_cast<uint32_t>(c21);
-    cc.c42[g] = static_cast<uint32_t>(c42);
-    cc.bias[g] = static_cast<uint32_t>((p - c62) % p);
-    cc.mg[g] = static_cast<uint32_t>((uint64_t(1) << 32) / p);
-    // M / p_g modulo p_g and modulo 2^128
-    uint64_t rest_mod_p = 1;
-    unsigned __int128 rest128 = 1;
-    for (int h = 0; h < n; ++h) {
-      if (h == g) continue;
-      rest_mod_p = (rest_mod_p * (moduli_table().p[h] % p)) % p;
-      rest128 *= moduli_table().p[h];
+  return GB_OK;
+}
+
+// ============================================================== device table and plans
+
+namespace {
+struct CrtDeviceState {
+  CrtDevicePlan* ring = nullptr;
+  std::atomic<uint32_t> next{0};
+};
+constexpr int CRT_PLAN_RING = 256;
+std::mutex g_crt_mu;
+std::vector<std::unique_ptr<CrtDeviceState>> g_crt_dev;
+}  // namespace
+
+int crt_plan_slot(CrtDevicePlan** slot) {
+  int dev = 0;
+  GB_CUDA_TRY(cudaGetDevice(&dev));
+  CrtDeviceState* st = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_crt_mu);
+    if (static_cast<int>(g_crt_dev.size()) <= dev) g_crt_dev.resize(dev + 1);
+    if (!g_crt_dev[dev]) {
+      auto fresh = std::make_unique<CrtDeviceState>();
+      GB_CUDA_TRY(cudaMalloc(&fresh->ring, sizeof(CrtDevicePlan) * CRT_PLAN_RING));
+      GB_CUDA_TRY(cudaMemset(fresh->ring, 0, sizeof(CrtDevicePlan) * CRT_PLAN_RING));
+      g_crt_dev[dev] = std::move(fresh);
     }
-    const uint32_t inv = inverse_mod(static_cast<uint32_t>(rest_mod_p), p);
-    cc.finv[g] = static_cast<float>(static_cast<double>(inv) / static_cast<double>(p));
-    const unsigned __int128 w128 = rest128 * inv;
-    for (int w = 0; w < 4; ++w) cc.w[g][w] = static_cast<uint32_t>(w128 >> (32 * w));
-    bias128 += w128 * 128u;
-    bias_k += 128.0 * static_cast<double>(cc.finv[g]);
+    st = g_crt_dev[dev].get();
   }
-  for (int w = 0; w < 4; ++w) cc.bw[w] = static_cast<uint32_t>(bias128 >> (32 * w));
-  cc.bias_k = static_cast<float>(bias_k);
+  *slot = st->ring + (st->next.fetch_add(1) % CRT_PLAN_RING);
+  return GB_OK;
+}
+
+// ---------------------------------------------------------------- planner
+// Restates, on the device, the one-sided bounds of the statistics (the FP32 K-slice sums are
+// rescaled to each row's exponent; |x| sums rounded up, x^2 sums rounded down), then picks
+//   t(n)  largest t <= 62 with |C'| <= 2^(2t) (min(max sa, max sb) + K 2^(-t-1)) <= M_n / 4
+//         and <= 2^125 (checked in log2 with a safety margin)
+//   bound(t) = 1.01 (h (EA SB + EB SA) + K h^2 EA EB + 2u (na nb + trunc)) / (na nb),
+//         h = 2^(-t-1): rounding A and B to the 2^(e - t) grid moves each element by at most
+//         h 2^e; the integer product is exact; the FP64 conversion and alpha round once each
+//   n     the fewest moduli with bound(t(n)) <= tol (or pp.n_fixed with t = pp.t_fixed).
+// Many blocks reduce row ranges (sums relative to the block's largest row exponent); the
+// last block to finish combines them in block order and chooses the plan.  Terms smaller
+// than 2^-1022 of the largest are dropped: far inside the 1.01 slack of the bound.
+constexpr int CRT_PLAN_THREADS = 256;
+constexpr int CRT_PLAN_BLOCKS = 128;   // per operand at most
+
+struct CrtPlanPartial {
+  double e2, s2, n2, smax;   // sums of 4^(e - ref), (sa 2^(e - ref))^2, x^2 sums, max sa
+  int32_t ref, nonfinite, any, pad;
+};
+
+size_t crt_plan_scratch_bytes() { return sizeof(CrtPlanPartial) * 2 * CRT_PLAN_BLOCKS + 256; }
+
+__device__ __forceinline__ int exp_of_bits_dev(unsigned long long bits) {
+  if (bits >= 0x7FF0000000000000ull) return 0x7FFFFFFF;
+  if (bits == 0) return 0;
+  return ilogb(__longlong_as_double(static_cast<long long>(bits))) + 1;
+}
+
+// 2^k for k <= 1023; 0 below the normal range.
+__device__ __forceinline__ double pow2_or_zero(int k) {
+  return k < -1022 ? 0.0 : __longlong_as_double(static_cast<long long>(k + 1023) << 52);
+}
+
+__device__ __forceinline__ double warp_sum(double x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  return x;
+}
+
+__device__ double crt_bound_dev(bool nonfinite, double na, double nb, double EA, double EB, double SA, double SB,
+                                int64_t K, int t) {
+  if (nonfinite) return INFINITY;
+  if (na == 0.0 || nb == 0.0) return 0.0;
+  const double h = ldexp(1.0, -t - 1);
+  const double Kd = static_cast<double>(K);
+  const double trunc = h * (EA * SB + EB * SA) + Kd * h * h * EA * EB;
+  const double fin = 2.0 * 0x1p-53 * (na * nb + trunc);
+  return 1.01 * (trunc + fin) / (na * nb);
+}
+
+__device__ int crt_bits_dev(double sa_max, double sb_max, int64_t K, double lm) {
+  const double Kd = static_cast<double>(K < 1 ? 1 : K);
+  // S(t) >= min(sa_max, sb_max, K): start from the t that bound allows and step down
+  const double ls = log2(fmin(fmin(sa_max, sb_max), Kd));
+  int t0 = 62;
+  const double cap = fmin(lm - 2.0, 125.0) - ls;
+  if (cap < 124.0) t0 = min(62, static_cast<int>(floor(cap * 0.5)) + 1);
+  for (int t = t0; t >= 1; --t) {
+    double S = fmin(sa_max, sb_max) + Kd * ldexp(1.0, -t - 1);
+    S = fmin(S, Kd) * (1.0 + 1e-12);
+    const double need = 2.0 * t + log2(S);
+    if (need + 2.0 <= lm - 1e-9 && need <= 125.0 - 1e-9) return t;
+  }
+  return 0;
+}
+
+__global__ void __launch_bounds__(CRT_PLAN_THREADS) crt_plan_kernel(const OzRowStats sa, const OzRowStats sb,
+                                                                    const __grid_constant__ CrtPlanParams pp,
+                                                                    int blocks_a, CrtPlanPartial* __restrict__ part,
+                                                                    unsigned int* __restrict__ counter,
+                                                                    CrtDevicePlan* __restrict__ out) {
+  __shared__ int s_ref[CRT_PLAN_THREADS / 32], s_nf[CRT_PLAN_THREADS / 32];
+  __shared__ double s_acc[4][CRT_PLAN_THREADS / 32];
+  __shared__ int s_last;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (!pp.with_sums) {   // fixed plan, no bound asked for
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      out->n = pp.n_fixed;
+      out->t = pp.t_fixed;
+      out->bound = __longlong_as_double(0x7FF8000000000000ll);
+    }
+    return;
+  }
+  const bool is_b = static_cast<int>(blockIdx.x) >= blocks_a;
+  const OzRowStats& st = is_b ? sb : sa;
+  const int64_t R = is_b ? pp.N : pp.M;
+  const int nb = is_b ? gridDim.x - blocks_a : blocks_a;
+  const int bi = is_b ? blockIdx.x - blocks_a : blockIdx.x;
+  const int64_t per = (R + nb - 1) / nb;
+  const int64_t r0 = bi * per, r1 = (r0 + per < R) ? r0 + per : R;
+  // block's reference exponent and non-finite flag
+  int ref = -1100, nf = 0;
+  for (int64_t i = r0 + threadIdx.x; i < r1; i += CRT_PLAN_THREADS) {
+    const unsigned long long b = st.amax_bits[i];
+    const int e = exp_of_bits_dev(b);
+    if (e == 0x7FFFFFFF) nf = 1;
+    else if (b && e > ref) ref = e;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    ref = max(ref, __shfl_xor_sync(0xffffffffu, ref, o));
+    nf |= __shfl_xor_sync(0xffffffffu, nf, o);
+  }
+  if (lane == 0) {
+    s_ref[wid] = ref;
+    s_nf[wid] = nf;
+  }
+  __syncthreads();
+  ref = -1100;
+  nf = 0;
+  for (int w = 0; w < CRT_PLAN_THREADS / 32; ++w) {
+    ref = max(ref, s_ref[w]);
+    nf |= s_nf[w];
+  }
+  // one-sided row sums, as the host bound restates them
+  const double Kd = static_cast<double>(pp.K);
+  const double gk = Kd * 0x1p-24;
+  const double up = (gk < 0.5 ? (1.0 + 0x1p-23) / (1.0 - gk) : 4.0) * (1.0 + 0x1p-40);
+  const double down = (1.0 - 0x1p-40) / (1.0 + 2.0 * gk);
+  const double tiny = Kd * 0x1p-126;
+  double e2 = 0.0, s2 = 0.0, n2 = 0.0, smax = 0.0;
+  if (!nf) {
+    for (int64_t i = r0 + threadIdx.x; i < r1; i += CRT_PLAN_THREADS) {
+      const unsigned long long b = st.amax_bits[i];
+      if (!b) continue;
+      const int e = exp_of_bits_dev(b);
+      double sabs = 0.0, ssq = 0.0;
+      for (int sl = 0; sl < st.kslices; ++sl) {
+        const int64_t o = static_cast<int64_t>(sl) * R + i;
+        const int pe = st.part_e[o];
+        if (pe == 0x7FFFFFFF) continue;
+        sabs += static_cast<double>(st.part_sa[o]) * pow2_or_zero(pe - e);
+        ssq += static_cast<double>(st.part_sq[o]) * pow2_or_zero(2 * (pe - e));
+      }
+      const double su = sabs * up + tiny;
+      const double sc = pow2_or_zero(e - ref);
+      e2 += sc * sc;
+      s2 += (su * sc) * (su * sc);
+      n2 += ssq * down * (sc * sc);
+      smax = fmax(smax, su);
+    }
+  }
+  e2 = warp_sum(e2);
+  s2 = warp_sum(s2);
+  n2 = warp_sum(n2);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) smax = fmax(smax, __shfl_xor_sync(0xffffffffu, smax, o));
+  __syncthreads();
+  if (lane == 0) {
+    s_acc[0][wid] = e2;
+    s_acc[1][wid] = s2;
+    s_acc[2][wid] = n2;
+    s_acc[3][wid] = smax;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    CrtPlanPartial pt;
+    pt.e2 = pt.s2 = pt.n2 = pt.smax = 0.0;
+    for (int w = 0; w < CRT_PLAN_THREADS / 32; ++w) {
+      pt.e2 += s_acc[0][w];
+      pt.s2 += s_acc[1][w];
+      pt.n2 += s_acc[2][w];
+      pt.smax = fmax(pt.smax, s_acc[3][w]);
+    }
+    pt.ref = ref;
+    pt.nonfinite = nf;
+    pt.any = (ref > -1100) ? 1 : 0;
+    pt.pad = 0;
+    part[blockIdx.x] = pt;
+    __threadfence();
+    s_last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!s_last || threadIdx.x >= 32) return;
+  __threadfence();
+  // last block, warp 0: combine the partials of each operand in block order (every lane the
+  // same), then lane c - 1 evaluates c moduli and a ballot picks the fewest that pass
+  double nrm[2], E[2], S[2], smx[2];
+  int nonfinite = 0;
+#pragma unroll
+  for (int op = 0; op < 2; ++op) {
+    const int b0 = op ? blocks_a : 0, b1 = op ? static_cast<int>(gridDim.x) : blocks_a;
+    int gref = -1100;
+    for (int b = b0; b < b1; ++b) {
+      const CrtPlanPartial& q = part[b];
+      nonfinite |= q.nonfinite;
+      if (q.any && q.ref > gref) gref = q.ref;
+    }
+    double ae2 = 0.0, as2 = 0.0, an2 = 0.0, amx = 0.0;
+    for (int b = b0; b < b1; ++b) {
+      const CrtPlanPartial& q = part[b];
+      if (!q.any) continue;
+      const double f = pow2_or_zero(2 * (q.ref - gref));
+      ae2 += q.e2 * f;
+      as2 += q.s2 * f;
+      an2 += q.n2 * f;
+      amx = fmax(amx, q.smax);
+    }
+    nrm[op] = sqrt(an2);
+    E[op] = sqrt(ae2);
+    S[op] = sqrt(as2);
+    smx[op] = amx;
+  }
+  int n = pp.n_fixed, t = pp.t_fixed;
+  if (n == 0) {
+    const int c = lane + 1;
+    int tc = 0;
+    bool ok = false;
+    if (c <= TC_MAX_MODULI) {
+      tc = nonfinite ? pp.tk[c] : crt_bits_dev(smx[0], smx[1], pp.K, pp.log2m[c]);
+      ok = tc >= 1 && (nonfinite || crt_bound_dev(false, nrm[0], nrm[1], E[0], E[1], S[0], S[1], pp.K, tc) <= pp.tol);
+    }
+    const unsigned pass = __ballot_sync(0xffffffffu, ok);
+    const int tmax = __shfl_sync(0xffffffffu, tc, TC_MAX_MODULI - 1);
+    if (pass) {
+      const int first = __ffs(pass) - 1;
+      n = first + 1;
+      t = __shfl_sync(0xffffffffu, tc, first);
+    } else {   // tolerance out of reach: the most moduli
+      n = TC_MAX_MODULI;
+      t = tmax >= 1 ? tmax : pp.tk[n];
+    }
+  }
+  if (lane == 0) {
+    out->n = n;
+    out->t = t;
+    out->bound = crt_bound_dev(nonfinite, nrm[0], nrm[1], E[0], E[1], S[0], S[1], pp.K, t);
+    *counter = 0u;
+  }
+}
+
+int crt_plan_device(const OzRowStats& sa, const OzRowStats& sb, const CrtPlanParams& pp, CrtDevicePlan* plan,
+                    void* scratch, cudaStream_t s) {
+  auto blocks_for = [](int64_t R) {
+    int64_t b = (R + CRT_PLAN_THREADS - 1) / CRT_PLAN_THREADS;
+    if (b > CRT_PLAN_BLOCKS) b = CRT_PLAN_BLOCKS;
+    return static_cast<int>(b < 1 ? 1 : b);
+  };
+  const int ba = blocks_for(pp.M), bb = blocks_for(pp.N);
+  CrtPlanPartial* part = static_cast<CrtPlanPartial*>(scratch);
+  unsigned int* counter = reinterpret_cast<unsigned int*>(static_cast<char*>(scratch) +
+                                                          sizeof(CrtPlanPartial) * 2 * CRT_PLAN_BLOCKS);
+  GB_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(unsigned int), s));
+  GB_LAUNCH(GB_KERNEL_OZAKI_STATS, s,
+            (crt_plan_kernel<<<ba + bb, CRT_PLAN_THREADS, 0, s>>>(sa, sb, pp, ba, part, counter, plan)));
+  GB_CUDA_TRY(cudaGetLastError());
   return GB_OK;
 }
 
 // ============================================================== residue split
 
-// Residue of the two's-complement integer Y (|Y| <= 2^62) modulo p from 21-bit limbs of
-// Y + 2^62 (bias folds the 2^62 back out), reduced with a multiply-high by floor(2^32 / p):
-// the quotient estimate is low by at most one, so one conditional subtraction finishes.
-__device__ __forceinline__ uint32_t residue_of(uint32_t y0, uint32_t y1, uint32_t y2, uint32_t p, uint32_t c21,
-                                               uint32_t c42, uint32_t bias, uint32_t mg) {
-  const uint32_t s = y0 + y1 * c21 + y2 * c42 + bias;   // < 2^30
-  uint32_t r = s - __umulhi(s, mg) * p;                 // in [0, 2p)
-  return r >= p ? r - p : r;
-}
-
-// One thread = one row r and 16 consecutive k, as in split_kernel; n planes of 16 BF16
-// balanced residues (r > p/2 becomes r - p), two 16-byte stores per plane.
+// One thread = one row r and 8 consecutive k (rows contiguous: two neighbouring threads share
+// a row and cover 16 k, so each warp store fills whole 32-byte sectors; k contiguous:
+// neighbouring threads cover neighbouring k).  Y = round-half-away(x 2^(t - e)) (|Y| <= 2^t,
+// t <= 62) is shifted to Y + 2^62 >= 0 and cut into six 12-bit limbs held as exact FP32 values;
+// per modulus p (<= 253)
+//   s = (-2^62 mod p) + sum_l limb_l (2^(12 l) mod p)     an integer below 2^23, exact in FP32
+//   r = s - p rint(s / p)                                  |r| <= p/2 + 1/2, so |r| <= 127
+// all on the FMA pipe; r has at most 7 significant bits, so its BF16 is the upper half of its
+// FP32 bits.  One 16-byte store per plane.
 template <bool RC>
 __global__ void __launch_bounds__(256) crt_split_kernel(const double* __restrict__ X, int64_t R, int64_t K,
                                                         int64_t rs, int64_t ks,
                                                         const unsigned long long* __restrict__ amax_bits,
                                                         __nv_bfloat16* __restrict__ planes, int64_t pitch,
-                                                        int32_t* __restrict__ exps, const __grid_constant__ CrtConsts cc) {
+                                                        int32_t* __restrict__ exps, const __grid_constant__ CrtModuli mod,
+                                                        const CrtDevicePlan* __restrict__ plan) {
+  constexpr float MAGIC = 12582912.0f;   // 1.5 * 2^23: x + MAGIC - MAGIC = rint(x), |x| < 2^22
   int64_t r, kc;
   if (RC) {
-    r = static_cast<int64_t>(blockIdx.x) * 256 + threadIdx.x;
-    kc = blockIdx.y;
+    r = static_cast<int64_t>(blockIdx.x) * 128 + (threadIdx.x >> 1);
+    kc = static_cast<int64_t>(blockIdx.y) * 2 + (threadIdx.x & 1);
   } else {
     kc = static_cast<int64_t>(blockIdx.x) * 256 + threadIdx.x;
     r = blockIdx.y;
   }
-  const int64_t k0 = kc * 16;
+  const int64_t k0 = kc * 8;
   if (r >= R || k0 >= K) return;
+  const int nmod = plan->n, tbits = plan->t;
   const int e = row_exponent(amax_bits[r]);
   if (k0 == 0) exps[r] = e;
   const bool nonfinite = (e == OZ_EXP_NONFINITE);
-  const int nvalid = static_cast<int>(K - k0 < 16 ? K - k0 : 16);
+  const int nvalid = static_cast<int>(K - k0 < 8 ? K - k0 : 8);
   const double* src = X + r * rs + k0 * ks;
-  uint32_t y0[16], y1[16], y2[16];
+  float yl[6][8];
 #pragma unroll
-  for (int j = 0; j < 16; ++j) {
+  for (int j = 0; j < 8; ++j) {
     const double x = (j < nvalid) ? src[j * ks] : 0.0;
-    const uint64_t y = (nonfinite ? 0ull : fixed_point<uint64_t>(x, e, cc.t + 1)) + (1ull << 62);
-    y0[j] = static_cast<uint32_t>(y) & 0x1FFFFFu;
-    y1[j] = static_cast<uint32_t>(y >> 21) & 0x1FFFFFu;
-    y2[j] = static_cast<uint32_t>(y >> 42);
+    const uint64_t y = (nonfinite ? 0ull : fixed_point<uint64_t>(x, e, tbits + 1)) + (1ull << 62);
+#pragma unroll
+    for (int l = 0; l < 6; ++l)
+      yl[l][j] = __uint_as_float(0x4B000000u | (static_cast<uint32_t>(y >> (12 * l)) & 0xFFFu)) - 8388608.0f;
   }
   __nv_bfloat16* out0 = planes + r * pitch + k0;
   const int64_t plane_stride = R * pitch;
-  for (int g = 0; g < cc.n; ++g) {
-    const uint32_t p = cc.p[g], c21 = cc.c21[g], c42 = cc.c42[g], bias = cc.bias[g], mg = cc.mg[g];
-    const uint32_t half = p >> 1;
-    uint32_t packed[8];
+  for (int g = 0; g < nmod; ++g) {
+    const float c0 = mod.climb[g][0], c1 = mod.climb[g][1], c2 = mod.climb[g][2], c3 = mod.climb[g][3];
+    const float c4 = mod.climb[g][4], c5 = mod.climb[g][5], pf = mod.pf[g], inv = mod.pinv[g];
+    uint32_t packed[4];
 #pragma unroll
-    for (int j = 0; j < 16; j += 2) {
-      const uint32_t r0 = residue_of(y0[j], y1[j], y2[j], p, c21, c42, bias, mg);
-      const uint32_t r1 = residue_of(y0[j + 1], y1[j + 1], y2[j + 1], p, c21, c42, bias, mg);
-      const int d0 = static_cast<int>(r0) - (r0 > half ? static_cast<int>(p) : 0);
-      const int d1 = static_cast<int>(r1) - (r1 > half ? static_cast<int>(p) : 0);
-      packed[j / 2] = bf16_bits_of_int(d0) | (bf16_bits_of_int(d1) << 16);
+    for (int j = 0; j < 8; j += 2) {
+      float rr[2];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        float sj = yl[0][j + h] + c0;
+        sj = fmaf(yl[1][j + h], c1, sj);
+        sj = fmaf(yl[2][j + h], c2, sj);
+        sj = fmaf(yl[3][j + h], c3, sj);
+        sj = fmaf(yl[4][j + h], c4, sj);
+        sj = fmaf(yl[5][j + h], c5, sj);
+        const float q = fmaf(sj, inv, MAGIC) - MAGIC;
+        rr[h] = fmaf(-pf, q, sj);
+      }
+      packed[j / 2] = __byte_perm(__float_as_uint(rr[0]), __float_as_uint(rr[1]), 0x7632u);
     }
     __nv_bfloat16* dst = out0 + g * plane_stride;
-    if (nvalid == 16) {
-      uint4* d4 = reinterpret_cast<uint4*>(dst);
-      d4[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
-      d4[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+    if (nvalid == 8) {
+      *reinterpret_cast<uint4*>(dst) = make_uint4(packed[0], packed[1], packed[2], packed[3]);
     } else {
       unsigned short* d2 = reinterpret_cast<unsigned short*>(dst);
       for (int j = 0; j < nvalid; ++j) d2[j] = static_cast<unsigned short>(packed[j / 2] >> (16 * (j & 1)));
@@ -281,21 +589,22 @@ __global__ void __launch_bounds__(256) crt_split_kernel(const double* __restrict
 }
 
 int crt_split(const double* X, int64_t R, int64_t K, int64_t rs, int64_t ks, const unsigned long long* amax_bits,
-              const CrtPlan& plan, __nv_bfloat16* planes, int64_t pitch, int32_t* exps, cudaStream_t s) {
+              const CrtDevicePlan* plan, __nv_bfloat16* planes, int64_t pitch, int32_t* exps, cudaStream_t s) {
+  const CrtModuli& mod = crt_table().mod;
   if (R <= 0 || K <= 0) return GB_OK;
-  const int64_t kchunks = (K + 15) / 16;
+  const int64_t kchunks = (K + 7) / 8;
   if (rs == 1 && R > 1) {
-    if (kchunks > 65535) return GB_ERR_UNSUPPORTED;
-    dim3 grid(static_cast<unsigned>((R + 255) / 256), static_cast<unsigned>(kchunks));
+    if ((kchunks + 1) / 2 > 65535) return GB_ERR_UNSUPPORTED;
+    dim3 grid(static_cast<unsigned>((R + 127) / 128), static_cast<unsigned>((kchunks + 1) / 2));
     GB_LAUNCH(GB_KERNEL_OZAKI_SPLIT, s,
-              (crt_split_kernel<true><<<grid, 256, 0, s>>>(X, R, K, rs, ks, amax_bits, planes, pitch, exps, plan.cc)));
+              (crt_split_kernel<true><<<grid, 256, 0, s>>>(X, R, K, rs, ks, amax_bits, planes, pitch, exps, mod, plan)));
   } else {
     for (int64_t r0 = 0; r0 < R; r0 += 65535) {   // rows beyond the grid's y range: bands
       const int64_t rb = (R - r0 < 65535) ? R - r0 : 65535;
       dim3 grid(static_cast<unsigned>((kchunks + 255) / 256), static_cast<unsigned>(rb));
       GB_LAUNCH(GB_KERNEL_OZAKI_SPLIT, s,
                 (crt_split_kernel<false><<<grid, 256, 0, s>>>(X + r0 * rs, rb, K, rs, ks, amax_bits + r0,
-                                                               planes + r0 * pitch, pitch, exps + r0, plan.cc)));
+                                                               planes + r0 * pitch, pitch, exps + r0, mod, plan)));
     }
   }
   GB_CUDA_TRY(cudaGetLastError());
@@ -358,20 +667,23 @@ __global__ void __launch_bounds__(256) crt_combine_kernel(const uint8_t* __restr
                                                           int64_t res_plane, int64_t M, int64_t N,
                                                           const int32_t* __restrict__ ea,
                                                           const int32_t* __restrict__ eb, double alpha, double beta,
-                                                          double* __restrict__ C, int64_t ldc,
-                                                          const __grid_constant__ CrtConsts cc) {
+                                                          double* __restrict__ C, int64_t ldc, int ab,
+                                                          const __grid_constant__ CrtTable tab,
+                                                          const CrtDevicePlan* __restrict__ plan) {
   const int64_t i0 = (static_cast<int64_t>(blockIdx.x) * 256 + threadIdx.x) * 4;
   if (i0 >= M) return;
+  const int nmod = plan->n;
+  const CrtRecon& cc = tab.rec[nmod - 1];
   int eai[4];
 #pragma unroll
   for (int q = 0; q < 4; ++q) eai[q] = (i0 + q < M) ? ea[i0 + q] : 0;
-  const int two_t = 2 * cc.t;
+  const int two_t = 2 * plan->t;
   for (int64_t j = blockIdx.y; j < N; j += gridDim.y) {
     const uint8_t* base = res + j * res_ld + i0;
     uint32_t words[TC_MAX_MODULI];   // all loads in flight before any use
 #pragma unroll
     for (int g = 0; g < TC_MAX_MODULI; ++g)
-      words[g] = (g < cc.n) ? __ldg(reinterpret_cast<const uint32_t*>(base + g * res_plane)) : 0u;
+      words[g] = (g < nmod) ? __ldg(reinterpret_cast<const uint32_t*>(base + g * res_plane)) : 0u;
     uint64_t acc[4][4];
     float ks[4];
 #pragma unroll
@@ -382,7 +694,7 @@ __global__ void __launch_bounds__(256) crt_combine_kernel(const uint8_t* __restr
     }
 #pragma unroll
     for (int g = 0; g < TC_MAX_MODULI; ++g) {
-      if (g >= cc.n) break;
+      if (g >= nmod) break;
       const uint32_t word = words[g];
       const float fi = cc.finv[g];
       const uint32_t w0 = cc.w[g][0], w1 = cc.w[g][1], w2 = cc.w[g][2], w3 = cc.w[g][3];
@@ -419,9 +731,9 @@ __global__ void __launch_bounds__(256) crt_combine_kernel(const uint8_t* __restr
         const uint64_t hi = (static_cast<uint64_t>(word[3]) << 32) | word[2];
         val = i128_times_pow2(hi, lo, eai[q] + ebj - two_t);
       }
-      if (cc.ab == 1)
+      if (ab == 1)
         val = alpha * val;
-      else if (cc.ab == 2)
+      else if (ab == 2)
         val = fma(alpha, val, beta * ccol[i0 + q]);
       ccol[i0 + q] = val;
     }
@@ -432,6 +744,7 @@ __global__ void __launch_bounds__(256) crt_combine_kernel(const uint8_t* __restr
 
 int crt_gemm_launch(const CrtGemmArgs& a, const CrtPlan& plan, cudaStream_t s) {
   CUtensorMap ta, tb;
+  // maps and schedule cover plan.n planes; the kernels run the device plan's n of them
   int rc = make_plane_tmap(&ta, a.planes_a, a.K, a.M, plan.n, a.pitch, 128);
   if (rc) return rc;
   rc = make_plane_tmap(&tb, a.planes_b, a.K, a.N, plan.n, a.pitch, 128);
@@ -454,9 +767,10 @@ int crt_gemm_launch(const CrtGemmArgs& a, const CrtPlan& plan, cudaStream_t s) {
   prm.res = a.res;
   prm.res_ld = a.res_ld;
   prm.res_plane = a.res_plane;
+  prm.dev_ngroups = &a.plan->n;
   for (int g = 0; g < plan.n; ++g) {
-    prm.crt_p[g] = static_cast<float>(plan.cc.p[g]);
-    prm.crt_inv[g] = 1.0f / static_cast<float>(plan.cc.p[g]);
+    prm.crt_p[g] = crt_table().mod.pf[g];
+    prm.crt_inv[g] = crt_table().mod.pinv[g];
   }
   rc = tc_gemm_pair_launch(TC_EPI_CRT, ta, tb, nullptr, nullptr, plan.sched, prm, a.grid, GB_KERNEL_OZAKI_SLICE_MMA, s);
   if (rc) return rc;
@@ -464,11 +778,10 @@ int crt_gemm_launch(const CrtGemmArgs& a, const CrtPlan& plan, cudaStream_t s) {
   const int64_t by = a.N < 65535 ? a.N : 65535;
   if (bx > 0x7FFFFFFF) return GB_ERR_UNSUPPORTED;
   dim3 grid(static_cast<unsigned>(bx), static_cast<unsigned>(by));
-  CrtConsts cc = plan.cc;   // output rule decided once on the host (no FP64 compares per element)
-  cc.ab = (a.beta != 0.0) ? 2 : (a.alpha != 1.0 ? 1 : 0);
+  const int ab = (a.beta != 0.0) ? 2 : (a.alpha != 1.0 ? 1 : 0);   // output rule, decided on the host
   GB_LAUNCH(GB_KERNEL_OZAKI_COMBINE, s,
             (crt_combine_kernel<<<grid, 256, 0, s>>>(a.res, a.res_ld, a.res_plane, a.M, a.N, a.ea, a.eb, a.alpha, a.beta,
-                                                     a.C, a.ldc, cc)));
+                                                     a.C, a.ldc, ab, crt_table(), a.plan)));
   GB_CUDA_TRY(cudaGetLastError());
   return GB_OK;
 }

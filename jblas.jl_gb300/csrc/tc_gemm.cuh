@@ -71,6 +71,7 @@ struct TcParams {
   int64_t res_plane;
   float crt_p[TC_MAX_MODULI];
   float crt_inv[TC_MAX_MODULI];
+  const int32_t* dev_ngroups;   // when set, the number of schedule groups to run (read on the device)
 };
 
 // Tensor maps for problem 0 and (optionally) problem 1; box 64 x 128 for A, 64 x 256 for B.

@@ -84,7 +84,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(P2Shape<EPI>::THREAD
   const bool leader = (rank == 0);
   const int cluster = blockIdx.x >> 1, nclusters = gridDim.x >> 1;
   const int ntiles = prm.total_tiles;   // pair tiles
-  const int G = sched.ngroups;
+  const int G = prm.dev_ngroups ? *prm.dev_ngroups : sched.ngroups;   // CRT: the device plan's moduli
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < P2_STAGES; ++i) {
@@ -270,7 +270,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(P2Shape<EPI>::THREAD
           if (EPI == TC_EPI_CRT) {
             // Chunk c of modulus p holds D = S_c + r_{c-2} (the MMA accumulated onto the residue
             // the drain of chunk c - 2 stored back into this buffer; S_c is the exact integer
-            // chunk sum, |D| <= 1024 * 126^2 + 127 < 2^24, exact in FP32).  One reduction
+            // chunk sum, |D| <= 1024 * 127^2 + 127 < 2^24, exact in FP32).  One reduction
             // r_c = D - p * rint(D / p) gives |r_c| <= 127 since p <= 253, and r_c goes back to
             // TMEM for chunk c + 2.  The two chains (even and odd chunks) meet at the end: the
             // drain of chunk nc - 2 keeps its residue in registers (biased bytes r + 128), the
