@@ -6,7 +6,7 @@ layer over the C ABI in `include/gbblas.h`:
 
     jmul!(D, A, X)                 D = A * X, jBLAS's per-element FMA order (src/gemm.jl:244)
     gemm!(C, A, B)                 the same call spelled as in the task (`jmul!` semantics)
-    gemm!(C, A, B, α, β; mode, slices)   BLAS-3 form; mode = :native | :ozaki
+    gemm!(C, A, B, α, β; mode, slices)   BLAS-3 form; mode = :native | :ozaki | :ozaki_crt
     gemm_adjoint!(dA, dB, A, B, dC)      dA = dC*B', dB = A'*dC in one launch (Float32)
     ChainRulesCore.rrule(::typeof(gemm), A, B)   pullback through gemm_adjoint!
 
@@ -19,7 +19,8 @@ module GBBLAS
 const libgbblas = get(ENV, "GBBLAS_LIB", joinpath(@__DIR__, "..", "lib", "libgbblas.so"))
 
 const GB_OK = Cint(0)
-const MODE = Dict(:native => Cint(0), :ozaki => Cint(1), :ozaki_bf16 => Cint(1), :ozaki_int8 => Cint(2))
+const MODE = Dict(:native => Cint(0), :ozaki => Cint(1), :ozaki_bf16 => Cint(1), :ozaki_int8 => Cint(2),
+                  :ozaki_crt => Cint(3))
 
 struct GBError <: Exception
     status::Cint
@@ -68,7 +69,9 @@ end
     gemm!(C, A, B, α, β; mode=:native, slices=0) -> C
 
 `C = α A B + β C`.  `mode = :ozaki` (Float64) emulates FP64 on the BF16 tensor cores with
-`slices` digit planes (0 = the library picks the count for its normwise tolerance).
+`slices` digit planes; `mode = :ozaki_crt` forms the exact product of the t-bit scaled
+operands from `slices` residue products (Chinese remainder theorem; the faster mode).
+`slices = 0`: the library picks the count for its normwise tolerance.
 """
 gemm!(C, A, B) = jmul!(C, A, B)
 function gemm!(C::AbstractMatrix{Float64}, A::AbstractMatrix{Float64}, B::AbstractMatrix{Float64}, α::Real, β::Real;
@@ -133,8 +136,8 @@ if Base.find_package("ChainRulesCore") !== nothing
         C = gemm(A, B)
         function gemm_pullback(ΔC)
             dC = convert(typeof(C), ChainRulesCore.unthunk(ΔC))
-            dA = gemm!(similar(A), dC, permutedims(B), 1.0, 0.0; mode = :ozaki)
-            dB = gemm!(similar(B), permutedims(A), dC, 1.0, 0.0; mode = :ozaki)
+            dA = gemm!(similar(A), dC, permutedims(B), 1.0, 0.0; mode = :ozaki_crt)
+            dB = gemm!(similar(B), permutedims(A), dC, 1.0, 0.0; mode = :ozaki_crt)
             return ChainRulesCore.NoTangent(), dA, dB
         end
         return C, gemm_pullback
