@@ -58,6 +58,23 @@ __device__ __forceinline__ double p2_exact_int_f32_times_pow2(uint32_t u, unsign
   return __longlong_as_double(static_cast<long long>(sign | body));
 }
 
+// Work units: a whole tile (all groups) or, for TC_EPI_CRT, one (tile, modulus) pair,
+// modulus-major, so the last round of a persistent grid is nearly full (1024 tiles x 15
+// moduli over 76 clusters: 99.6% instead of 96%) and concurrently active units share the
+// same modulus' planes.
+template <int EPI>
+__device__ __forceinline__ void p2_unit(int u, int ntiles, int G, int& t, int& g0, int& g1) {
+  if (EPI == TC_EPI_CRT) {
+    g0 = u / ntiles;
+    g1 = g0 + 1;
+    t = u - g0 * ntiles;
+  } else {
+    t = u;
+    g0 = 0;
+    g1 = G;
+  }
+}
+
 // TcProblem fields are reused with pair tiles: tiles_m = ceil(M / 256), tiles_n = ceil(N / 256),
 // tile_begin in pair-tile units.
 __device__ __forceinline__ int p2_problem_of(const TcParams& prm, int t) {
@@ -85,6 +102,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(P2Shape<EPI>::THREAD
   const int cluster = blockIdx.x >> 1, nclusters = gridDim.x >> 1;
   const int ntiles = prm.total_tiles;   // pair tiles
   const int G = prm.dev_ngroups ? *prm.dev_ngroups : sched.ngroups;   // CRT: the device plan's moduli
+  const int nunits = (EPI == TC_EPI_CRT) ? ntiles * G : ntiles;
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < P2_STAGES; ++i) {
@@ -125,7 +143,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(P2Shape<EPI>::THREAD
       int issued_parity[P2_STAGES];
       for (int i = 0; i < P2_STAGES; ++i) issued_parity[i] = -1;
       bool ok = true;
-      for (int t = cluster; t < ntiles && ok; t += nclusters) {
+      for (int u = cluster; u < nunits && ok; u += nclusters) {
+        int t, g0, g1;
+        p2_unit<EPI>(u, ntiles, G, t, g0, g1);
         const int pr = p2_problem_of(prm, t);
         const TcProblem& P = prm.prob[pr];
         const CUtensorMap* ta = pr ? &tmap_a1 : &tmap_a0;
@@ -134,7 +154,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(P2Shape<EPI>::THREAD
         p2_tile_coords(t - P.tile_begin, P.tiles_m, P.tiles_n, tm, tn);
         const int m0 = tm * 256 + 128 * static_cast<int>(rank);
         const int n0 = tn * 256 + 128 * static_cast<int>(rank);
-        for (int g = 0; g < G && ok; ++g) {
+        for (int g = g0; g < g1 && ok; ++g) {
           for (int c = 0; c < P.nchunks && ok; ++c) {
             const int kb0 = c * sched.kb_chunk;
             const int kb1 = min(kb0 + sched.kb_chunk, P.kb_total);
@@ -183,9 +203,11 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(P2Shape<EPI>::THREAD
       uint32_t acc_phase = 0;
       bool ok = true;
       bool issued_any = false;
-      for (int t = cluster; t < ntiles && ok; t += nclusters) {
+      for (int u = cluster; u < nunits && ok; u += nclusters) {
+        int t, g0, g1;
+        p2_unit<EPI>(u, ntiles, G, t, g0, g1);
         const TcProblem& P = prm.prob[p2_problem_of(prm, t)];
-        for (int g = 0; g < G && ok; ++g) {
+        for (int g = g0; g < g1 && ok; ++g) {
           for (int c = 0; c < P.nchunks && ok; ++c) {
             const int kb0 = c * sched.kb_chunk;
             const int kb1 = min(kb0 + sched.kb_chunk, P.kb_total);
@@ -242,7 +264,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(P2Shape<EPI>::THREAD
     int buf = 0;
     uint32_t acc_phase = 0;
     bool ok = true;
-    for (int t = cluster; t < ntiles && ok; t += nclusters) {
+    for (int u = cluster; u < nunits && ok; u += nclusters) {
+      int t, g0, g1;
+      p2_unit<EPI>(u, ntiles, G, t, g0, g1);
       const int pr = p2_problem_of(prm, t);
       const TcProblem& P = prm.prob[pr];
       int tm, tn;
@@ -257,7 +281,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(P2Shape<EPI>::THREAD
       int step = 0;
       const int nsteps = G * P.nchunks;
       uint32_t racc[EPI == TC_EPI_CRT ? COLS / 4 : 1];   // CRT: running residues, 4 bytes per register
-      for (int g = 0; g < G && ok; ++g) {
+      for (int g = g0; g < g1 && ok; ++g) {
         const int wexp = 2 - sched.level[g] * sched.bits;
         const unsigned long long wbias = static_cast<unsigned long long>(896 + wexp) << 23;
         for (int c = 0; c < P.nchunks; ++c, ++step) {
