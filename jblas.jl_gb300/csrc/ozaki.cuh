@@ -84,13 +84,24 @@ struct CrtModuli {                  // per modulus g (independent of how many a 
   float pf[TC_MAX_MODULI];          // p as a float
   float pinv[TC_MAX_MODULI];        // fl32(1 / p)
 };
-struct CrtRecon {                   // reconstruction with the first n moduli, M = their product
-  float finv[TC_MAX_MODULI];        // fl32(inv_g / p_g), inv_g = (M / p_g)^-1 mod p_g
-  uint32_t w[TC_MAX_MODULI][4];     // (M / p_g) inv_g mod 2^128, little-endian 32-bit words
-  uint32_t m[4];                    // M mod 2^128
-  uint32_t bw[4];                   // 128 * sum_g W_g mod 2^128 (bias of the residue bytes)
-  float bias_k;                     // 128 * sum_g finv[g]
+// Reconstruction with the first n moduli, M = their product.  The moduli are taken in
+// groups of up to three consecutive ones (P_G = their product < 2^24); the residue planes
+// hold x_g = psi_G C' mod p_g (psi_G = (M / P_G)^-1 mod P_G, applied in the last drain of
+// the residue products), so that v_G = CRT_G(x) = psi_G C' mod P_G and
+// C' = sum_G v_G (M / P_G) - k M.
+constexpr int CRT_MAX_GROUPS = (TC_MAX_MODULI + 2) / 3;
+struct CrtRecon {
+  int32_t ngroups;
   int32_t pad;
+  float psi[TC_MAX_MODULI];         // psi_G mod p_g for the group G holding modulus g
+  float a1[CRT_MAX_GROUPS];         // (p_a)^-1 mod p_b          (group moduli a, b, c)
+  float pa[CRT_MAX_GROUPS];         // p_a
+  float a2[CRT_MAX_GROUPS];         // (p_a p_b)^-1 mod p_c
+  float pab[CRT_MAX_GROUPS];        // p_a p_b
+  float P[CRT_MAX_GROUPS];          // P_G
+  float Pinv[CRT_MAX_GROUPS];       // fl32(1 / P_G)
+  uint32_t w[CRT_MAX_GROUPS][4];    // M / P_G mod 2^128, little-endian 32-bit words
+  uint32_t m[4];                    // M mod 2^128
 };
 struct CrtTable {
   CrtModuli mod;

@@ -121,6 +121,21 @@ uint32_t inverse_mod(uint32_t a, uint32_t p) {   // a * x == 1 (mod p), gcd(a, p
   return static_cast<uint32_t>(t);
 }
 
+uint64_t inverse_mod64(uint64_t a, uint64_t m) {   // a * x == 1 (mod m), gcd(a, m) = 1, m < 2^31
+  int64_t t = 0, nt = 1, r = static_cast<int64_t>(m), nr = static_cast<int64_t>(a % m);
+  while (nr) {
+    const int64_t q = r / nr;
+    int64_t tmp = t - q * nt;
+    t = nt;
+    nt = tmp;
+    tmp = r - q * nr;
+    r = nr;
+    nr = tmp;
+  }
+  if (t < 0) t += static_cast<int64_t>(m);
+  return static_cast<uint64_t>(t);
+}
+
 }  // namespace
 
 const uint32_t* crt_moduli() { return moduli_table().p; }
@@ -163,30 +178,35 @@ CrtTable build_table() {
   }
   for (int n = 1; n <= TC_MAX_MODULI; ++n) {
     CrtRecon& rc = tab.rec[n - 1];
+    const uint32_t* p = moduli_table().p;
     unsigned __int128 m128 = 1;
-    for (int g = 0; g < n; ++g) m128 *= moduli_table().p[g];
+    for (int g = 0; g < n; ++g) m128 *= p[g];
     for (int w = 0; w < 4; ++w) rc.m[w] = static_cast<uint32_t>(m128 >> (32 * w));
-    unsigned __int128 bias128 = 0;
-    double bias_k = 0.0;
-    for (int g = 0; g < n; ++g) {
-      // M / p_g modulo p_g and modulo 2^128
-      const uint32_t p = moduli_table().p[g];
-      uint64_t rest_mod_p = 1;
+    rc.ngroups = (n + 2) / 3;
+    for (int G = 0; G < rc.ngroups; ++G) {
+      const int a = 3 * G, b = a + 1, c = a + 2;
+      uint64_t P = p[a];
+      if (b < n) P *= p[b];
+      if (c < n) P *= p[c];
+      // M / P_G modulo P_G and modulo 2^128
+      uint64_t rest_mod = 1;
       unsigned __int128 rest128 = 1;
       for (int h = 0; h < n; ++h) {
-        if (h == g) continue;
-        rest_mod_p = (rest_mod_p * (moduli_table().p[h] % p)) % p;
-        rest128 *= moduli_table().p[h];
+        if (h >= a && h <= c) continue;
+        rest_mod = (rest_mod * (p[h] % P)) % P;
+        rest128 *= p[h];
       }
-      const uint32_t inv = inverse_mod(static_cast<uint32_t>(rest_mod_p), p);
-      rc.finv[g] = static_cast<float>(static_cast<double>(inv) / static_cast<double>(p));
-      const unsigned __int128 w128 = rest128 * inv;
-      for (int w = 0; w < 4; ++w) rc.w[g][w] = static_cast<uint32_t>(w128 >> (32 * w));
-      bias128 += w128 * 128u;
-      bias_k += 128.0 * static_cast<double>(rc.finv[g]);
+      const uint64_t psi = inverse_mod64(rest_mod, P);
+      for (int g = a; g <= c && g < n; ++g) rc.psi[g] = static_cast<float>(psi % p[g]);
+      rc.pa[G] = static_cast<float>(p[a]);
+      rc.a1[G] = (b < n) ? static_cast<float>(inverse_mod(p[a] % p[b], p[b])) : 0.0f;
+      rc.pab[G] = (b < n) ? static_cast<float>(p[a] * p[b]) : 0.0f;
+      rc.a2[G] = (c < n) ? static_cast<float>(inverse_mod(static_cast<uint32_t>((uint64_t(p[a]) * p[b]) % p[c]), p[c]))
+                         : 0.0f;
+      rc.P[G] = static_cast<float>(P);
+      rc.Pinv[G] = 1.0f / static_cast<float>(P);
+      for (int w = 0; w < 4; ++w) rc.w[G][w] = static_cast<uint32_t>(rest128 >> (32 * w));
     }
-    for (int w = 0; w < 4; ++w) rc.bw[w] = static_cast<uint32_t>(bias128 >> (32 * w));
-    rc.bias_k = static_cast<float>(bias_k);
   }
   return tab;
 }
@@ -658,11 +678,85 @@ __device__ __forceinline__ double i128_times_pow2(uint64_t hi, uint64_t lo, int 
 }
 
 // One thread = 4 consecutive rows of one column (a 32-bit load per residue plane).  The
-// planes hold biased bytes u_g = r_g + 128 with r_g = C' mod p_g (|r_g| <= 127), so
-//   X = sum_g r_g W_g = sum_g u_g W_g - 128 sum_g W_g   (mod 2^128),
-//       W_g = (M/p_g) ((M/p_g)^-1 mod p_g)
-//   k = round(sum_g r_g inv_g / p_g) = round(X / M), exact in FP32 because |C'| <= M/4
-//   C' = X - k M  (mod 2^128), a two's-complement 128-bit integer
+// planes hold biased bytes x_g + 128, x_g = psi_G C' mod p_g (|x_g| <= 127).  Per group of
+// up to three moduli (a, b, c), in exact FP32 (every value stays below 2^23):
+//   r  = x_a + p_a ((x_b - x_a) a1 mod p_b)           = psi_G C' mod p_a p_b
+//   v  = r + p_a p_b ((x_c - r) a2 mod p_c)            = psi_G C' mod P_G, |v| < P_G
+//   v += P_G if v < 0                                  (0 <= v < P_G)
+// then  X = sum_G v_G (M / P_G)  (mod 2^128),  k = round(sum_G v_G / P_G) = round(X / M) (each
+// term in [0, 1): exact in FP32 because |C'| <= M/4),  C' = X - k M as a two's-complement
+// 128-bit integer, rounded to FP64 by integer arithmetic.
+__device__ __forceinline__ float mods_f32(float x, float p, float pinv) {   // x - p rint(x / p)
+  const float q = fmaf(x, pinv, 12582912.0f) - 12582912.0f;
+  return fmaf(-p, q, x);
+}
+
+// The element loop for NMOD moduli: every table index is a compile-time constant, so the
+// constants are direct operands (no per-use constant loads) and the group loop is straight.
+template <int NMOD>
+__device__ __forceinline__ void crt_combine_column(const uint8_t* __restrict__ base, int64_t res_plane, int64_t i0,
+                                                   int64_t M, const int (&eai)[4], int ebj, int two_t, double alpha,
+                                                   double beta, double* __restrict__ ccol, int ab,
+                                                   const CrtTable& tab) {
+  constexpr float BIAS_F = 8388736.0f;   // 2^23 + 128
+  constexpr int NG = (NMOD + 2) / 3;
+  const CrtRecon& rc = tab.rec[NMOD - 1];
+  const CrtModuli& md = tab.mod;
+  uint32_t words[NMOD];   // all loads in flight before any use
+#pragma unroll
+  for (int g = 0; g < NMOD; ++g) words[g] = __ldg(reinterpret_cast<const uint32_t*>(base + g * res_plane));
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {   // one element at a time: only its accumulators are live
+    if (i0 + q >= M) continue;
+    const uint32_t sel = 0x7540u + q;   // byte q of a word over 0x4B0000..: 2^23 + byte
+    uint64_t acc0 = 0, acc1 = 0, acc2 = 0, acc3 = 0;
+    float ks = 0.0f;
+#pragma unroll
+    for (int G = 0; G < NG; ++G) {
+      const int a = 3 * G;
+      float v = __uint_as_float(__byte_perm(words[a], 0x4B000000u, sel)) - BIAS_F;
+      if (a + 1 < NMOD) {
+        const float xb = __uint_as_float(__byte_perm(words[(a + 1) % NMOD], 0x4B000000u, sel)) - BIAS_F;
+        v = fmaf(rc.pa[G], mods_f32((xb - v) * rc.a1[G], md.pf[a + 1], md.pinv[a + 1]), v);
+        if (a + 2 < NMOD) {
+          const float xc = __uint_as_float(__byte_perm(words[(a + 2) % NMOD], 0x4B000000u, sel)) - BIAS_F;
+          v = fmaf(rc.pab[G], mods_f32((xc - v) * rc.a2[G], md.pf[a + 2], md.pinv[a + 2]), v);
+        }
+      }
+      v = (v < 0.0f) ? v + rc.P[G] : v;
+      ks = fmaf(v, rc.Pinv[G], ks);
+      const uint32_t vi = static_cast<uint32_t>(v);
+      acc0 += static_cast<uint64_t>(vi) * rc.w[G][0];
+      acc1 += static_cast<uint64_t>(vi) * rc.w[G][1];
+      acc2 += static_cast<uint64_t>(vi) * rc.w[G][2];
+      acc3 += static_cast<uint64_t>(vi) * rc.w[G][3];
+    }
+    const int64_t k = __float_as_int(ks + 12582912.0f) - 0x4B400000;   // round(X / M)
+    const uint64_t accw[4] = {acc0, acc1, acc2, acc3};
+    int64_t c = 0;
+    uint32_t word[4];
+#pragma unroll
+    for (int w = 0; w < 4; ++w) {
+      const int64_t v = static_cast<int64_t>(accw[w]) - k * static_cast<int64_t>(rc.m[w]) + c;
+      word[w] = static_cast<uint32_t>(v);
+      c = v >> 32;
+    }
+    double val;
+    if (eai[q] == OZ_EXP_NONFINITE || ebj == OZ_EXP_NONFINITE) {
+      val = __longlong_as_double(0x7FF8000000000000ll);
+    } else {
+      const uint64_t lo = (static_cast<uint64_t>(word[1]) << 32) | word[0];
+      const uint64_t hi = (static_cast<uint64_t>(word[3]) << 32) | word[2];
+      val = i128_times_pow2(hi, lo, eai[q] + ebj - two_t);
+    }
+    if (ab == 1)
+      val = alpha * val;
+    else if (ab == 2)
+      val = fma(alpha, val, beta * ccol[i0 + q]);
+    ccol[i0 + q] = val;
+  }
+}
+
 __global__ void __launch_bounds__(256) crt_combine_kernel(const uint8_t* __restrict__ res, int64_t res_ld,
                                                           int64_t res_plane, int64_t M, int64_t N,
                                                           const int32_t* __restrict__ ea,
@@ -673,70 +767,24 @@ __global__ void __launch_bounds__(256) crt_combine_kernel(const uint8_t* __restr
   const int64_t i0 = (static_cast<int64_t>(blockIdx.x) * 256 + threadIdx.x) * 4;
   if (i0 >= M) return;
   const int nmod = plan->n;
-  const CrtRecon& cc = tab.rec[nmod - 1];
   int eai[4];
 #pragma unroll
   for (int q = 0; q < 4; ++q) eai[q] = (i0 + q < M) ? ea[i0 + q] : 0;
   const int two_t = 2 * plan->t;
   for (int64_t j = blockIdx.y; j < N; j += gridDim.y) {
     const uint8_t* base = res + j * res_ld + i0;
-    uint32_t words[TC_MAX_MODULI];   // all loads in flight before any use
-#pragma unroll
-    for (int g = 0; g < TC_MAX_MODULI; ++g)
-      words[g] = (g < nmod) ? __ldg(reinterpret_cast<const uint32_t*>(base + g * res_plane)) : 0u;
-    uint64_t acc[4][4];
-    float ks[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      ks[q] = -cc.bias_k;
-#pragma unroll
-      for (int w = 0; w < 4; ++w) acc[q][w] = 0ull;
-    }
-#pragma unroll
-    for (int g = 0; g < TC_MAX_MODULI; ++g) {
-      if (g >= nmod) break;
-      const uint32_t word = words[g];
-      const float fi = cc.finv[g];
-      const uint32_t w0 = cc.w[g][0], w1 = cc.w[g][1], w2 = cc.w[g][2], w3 = cc.w[g][3];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const uint32_t u = (word >> (8 * q)) & 0xFFu;
-        ks[q] = fmaf(__uint_as_float(0x4B000000u | u) - 8388608.0f, fi, ks[q]);
-        acc[q][0] += static_cast<uint64_t>(u) * w0;
-        acc[q][1] += static_cast<uint64_t>(u) * w1;
-        acc[q][2] += static_cast<uint64_t>(u) * w2;
-        acc[q][3] += static_cast<uint64_t>(u) * w3;
-      }
-    }
     const int ebj = eb[j];
     double* ccol = C + j * ldc;
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      if (i0 + q >= M) continue;
-      const int64_t k = __float_as_int(ks[q] + 12582912.0f) - 0x4B400000;   // round(X / M)
-      int64_t c = 0;
-      uint32_t word[4];
-#pragma unroll
-      for (int w = 0; w < 4; ++w) {
-        const int64_t v = static_cast<int64_t>(acc[q][w]) - static_cast<int64_t>(cc.bw[w]) -
-                          k * static_cast<int64_t>(cc.m[w]) + c;
-        word[w] = static_cast<uint32_t>(v);
-        c = v >> 32;
-      }
-      double val;
-      if (eai[q] == OZ_EXP_NONFINITE || ebj == OZ_EXP_NONFINITE) {
-        val = __longlong_as_double(0x7FF8000000000000ll);
-      } else {
-        const uint64_t lo = (static_cast<uint64_t>(word[1]) << 32) | word[0];
-        const uint64_t hi = (static_cast<uint64_t>(word[3]) << 32) | word[2];
-        val = i128_times_pow2(hi, lo, eai[q] + ebj - two_t);
-      }
-      if (ab == 1)
-        val = alpha * val;
-      else if (ab == 2)
-        val = fma(alpha, val, beta * ccol[i0 + q]);
-      ccol[i0 + q] = val;
+#define GB_CRT_CASE(n) \
+  case n: crt_combine_column<n>(base, res_plane, i0, M, eai, ebj, two_t, alpha, beta, ccol, ab, tab); break;
+    switch (nmod) {
+      GB_CRT_CASE(1) GB_CRT_CASE(2) GB_CRT_CASE(3) GB_CRT_CASE(4) GB_CRT_CASE(5) GB_CRT_CASE(6) GB_CRT_CASE(7)
+      GB_CRT_CASE(8) GB_CRT_CASE(9) GB_CRT_CASE(10) GB_CRT_CASE(11) GB_CRT_CASE(12) GB_CRT_CASE(13)
+      GB_CRT_CASE(14) GB_CRT_CASE(15) GB_CRT_CASE(16) GB_CRT_CASE(17) GB_CRT_CASE(18) GB_CRT_CASE(19)
+      GB_CRT_CASE(20)
+      default: break;
     }
+#undef GB_CRT_CASE
   }
 }
 
@@ -772,6 +820,8 @@ int crt_gemm_launch(const CrtGemmArgs& a, const CrtPlan& plan, cudaStream_t s) {
     prm.crt_p[g] = crt_table().mod.pf[g];
     prm.crt_inv[g] = crt_table().mod.pinv[g];
   }
+  for (int n = 1; n <= plan.n; ++n)
+    for (int g = 0; g < n; ++g) prm.crt_psi[n - 1][g] = crt_table().rec[n - 1].psi[g];
   rc = tc_gemm_pair_launch(TC_EPI_CRT, ta, tb, nullptr, nullptr, plan.sched, prm, a.grid, GB_KERNEL_OZAKI_SLICE_MMA, s);
   if (rc) return rc;
   const int64_t bx = (a.M + 1023) / 1024;

@@ -72,6 +72,7 @@ struct TcParams {
   float crt_p[TC_MAX_MODULI];
   float crt_inv[TC_MAX_MODULI];
   const int32_t* dev_ngroups;   // when set, the number of schedule groups to run (read on the device)
+  float crt_psi[TC_MAX_MODULI][TC_MAX_MODULI];   // [n - 1][g]: multiplier of the final residue
 };
 
 // Tensor maps for problem 0 and (optionally) problem 1; box 64 x 128 for A, 64 x 256 for B.

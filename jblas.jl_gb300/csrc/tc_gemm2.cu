@@ -298,11 +298,12 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(P2Shape<EPI>::THREAD
             // r_c = D - p * rint(D / p) gives |r_c| <= 127 since p <= 253, and r_c goes back to
             // TMEM for chunk c + 2.  The two chains (even and odd chunks) meet at the end: the
             // drain of chunk nc - 2 keeps its residue in registers (biased bytes r + 128), the
-            // last drain adds it and writes the biased bytes to the residue plane (rows and
-            // columns padded to whole tiles, so always in bounds).
+            // last drain adds it, multiplies by the reconstruction's psi (mod p) and writes the
+            // biased bytes to the residue plane (rows and columns padded to whole tiles, so
+            // always in bounds).
             constexpr float MAGIC = 12582912.0f;   // 1.5 * 2^23: x + MAGIC - MAGIC = rint(x), |x| < 2^22
             constexpr float BIAS_F = 8388736.0f;   // 2^23 + 128: the low byte of (r + BIAS_F) is r + 128
-            const float pf = prm.crt_p[g], inv = prm.crt_inv[g];
+            const float pf = prm.crt_p[g], inv = prm.crt_inv[g], psi = prm.crt_psi[G - 1][g];
             const int nc = P.nchunks;
             const bool to_tmem = (c + 2 < nc), final_c = (c == nc - 1);
             const int64_t ld = prm.res_ld;
@@ -326,11 +327,17 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(P2Shape<EPI>::THREAD
 #pragma unroll
                   for (int jj = 0; jj < 4; ++jj) {
                     float r = __uint_as_float(v[j4 * 4 + jj]);
-                    if (final_c && nc >= 2) {
-                      // add the other chain's residue (0x4B0000bb as a float is 2^23 + bb)
-                      const float t = r + (__uint_as_float(__byte_perm(racc[bi * 4 + j4], 0x4B000000u, 0x7540u + jj)) - BIAS_F);
-                      const float q = fmaf(t, inv, MAGIC) - MAGIC;
-                      r = fmaf(-pf, q, t);
+                    if (final_c) {
+                      if (nc >= 2) {
+                        // add the other chain's residue (0x4B0000bb as a float is 2^23 + bb)
+                        const float t = r + (__uint_as_float(__byte_perm(racc[bi * 4 + j4], 0x4B000000u, 0x7540u + jj)) - BIAS_F);
+                        const float q = fmaf(t, inv, MAGIC) - MAGIC;
+                        r = fmaf(-pf, q, t);
+                      }
+                      // times the reconstruction multiplier psi (|r psi| <= 127 * 252, exact)
+                      const float t2 = r * psi;
+                      const float q2 = fmaf(t2, inv, MAGIC) - MAGIC;
+                      r = fmaf(-pf, q2, t2);
                     }
                     rb[jj] = __float_as_uint(r + BIAS_F);
                   }
