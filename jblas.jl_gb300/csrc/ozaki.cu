@@ -124,22 +124,89 @@ __device__ __forceinline__ unsigned long long abs_bits(double x) {
   return static_cast<unsigned long long>(__double_as_longlong(x)) & 0x7FFFFFFFFFFFFFFFull;
 }
 
-// |x| * 2^-e as FP32 from the IEEE fields of |x| (abits), truncated so it never exceeds
-// the true value (relative error below 2^-23); 0 when below FP32's normal range.
-__device__ __forceinline__ float scaled_f32_trunc(unsigned long long abits, int e) {
-  const int ex = static_cast<int>(abits >> 52);
-  const int fe = ex - 1023 - e + 127;   // <= 126 because |x| < 2^e
-  if (ex == 0 || fe < 1) return 0.0f;
-  return __uint_as_float((static_cast<uint32_t>(fe) << 23) | static_cast<uint32_t>((abits >> 29) & 0x7FFFFF));
+// Exponent e of |x| with |x| < 2^e (e = ilogb|x| + 1, as row_exponent_of), from the IEEE
+// fields of |x| (abits); 0 for x = 0, OZ_EXP_NONFINITE for Inf / NaN.
+__device__ __forceinline__ int exp_of_abits(unsigned long long a) {
+  const int ex = static_cast<int>(a >> 52);
+  if (ex == 0x7FF) return OZ_EXP_NONFINITE;
+  if (ex) return ex - 1022;
+  if (a == 0) return 0;
+  return -1010 - __clzll(static_cast<long long>(a));   // subnormal: m 2^-1074, m = a
 }
 
+// v * 2^d for d <= 0 rounded toward zero (never above the true value), 0 below FP32's range.
+__device__ __forceinline__ float scale_down_rz(float v, int d) {
+  if (d == 0 || v == 0.0f) return v;
+  if (d < -300) return 0.0f;
+  while (d < -126) {
+    v = __fmul_rz(v, 0x1p-126f);
+    d += 126;
+  }
+  return __fmul_rz(v, __uint_as_float(static_cast<uint32_t>(d + 127) << 23));
+}
+
+// |x| * 2^-e as FP32 from the IEEE fields of |x| (abits), never above the true value (the
+// mantissa is truncated; relative error below 2^-23 in FP32's normal range); subnormal x are
+// scaled exactly (rounded toward zero), values below FP32's range give 0.
+__device__ __forceinline__ float scaled_f32_trunc(unsigned long long abits, int e) {
+  const int ex = static_cast<int>(abits >> 52);
+  if (ex) {
+    const int fe = ex - 1023 - e + 127;   // <= 126 because |x| < 2^e
+    if (fe < 1) return 0.0f;
+    return __uint_as_float((static_cast<uint32_t>(fe) << 23) | static_cast<uint32_t>((abits >> 29) & 0x7FFFFF));
+  }
+  if (abits == 0) return 0.0f;
+  // subnormal: m 2^-1074 with m = abits < 2^52; m truncated to FP32, then times 2^(-1074 - e)
+  const int sh = -1074 - e;
+  if (sh < -300) return 0.0f;
+  const float fm = __ull2float_rz(abits);
+  if (sh >= 0) return fm;   // cannot happen while |x| < 2^e and the max is subnormal; kept exact-safe
+  return scale_down_rz(fm, sh);
+}
+
+// Running statistics of one thread's elements: exponent e of its max, sums of |x| 2^-e and
+// x^2 2^-2e in FP32.  When a larger exponent arrives the sums are rescaled by an exact power
+// of two (rounded toward zero below FP32's normal range), so one read of X suffices.
+struct RunStats {
+  unsigned long long mx = 0;
+  int e = -2000;   // no element yet
+  bool nonfinite = false;
+  float sa = 0.0f, sq = 0.0f;
+
+  __device__ __forceinline__ void add(unsigned long long bits, bool sums) {
+    const unsigned long long a = bits & 0x7FFFFFFFFFFFFFFFull;
+    mx = a > mx ? a : mx;
+    if (!sums || a == 0) return;
+    const int ea = exp_of_abits(a);
+    if (ea == OZ_EXP_NONFINITE) {
+      nonfinite = true;
+      return;
+    }
+    if (ea > e) {
+      sa = scale_down_rz(sa, e - ea);
+      sq = scale_down_rz(sq, 2 * (e - ea));
+      e = ea;
+    }
+    const float f = scaled_f32_trunc(a, e);
+    sa += f;
+    sq = fmaf(f, f, sq);
+  }
+  // rescales this thread's sums to exponent e2 >= e
+  __device__ __forceinline__ void to(int e2) {
+    if (e2 != e && e > -2000) {
+      sa = scale_down_rz(sa, e - e2);
+      sq = scale_down_rz(sq, 2 * (e - e2));
+    }
+    e = e2;
+  }
+};
 
 // Row statistics without FP64 arithmetic (GB300's FP64 pipe is narrow), in one read of X:
-// the exact max |x| by integer compare (atomicMax across K slices), then, when the host
-// asks for them, sums of |x| 2^-e_s and x^2 2^-2e_s in FP32 over truncated scaled values,
-// e_s the exponent of the slice's own max (the second sweep of a slice hits L1/L2).  The
-// host rescales the slice sums to the row exponent and turns them into rigorous one-sided
-// bounds (see bound_stats).
+// the exact max |x| by integer compare (atomicMax across K slices) and, when asked, the FP32
+// sums of |x| 2^-e_s and x^2 2^-2e_s over truncated scaled values, e_s the exponent of the
+// slice's own max (running per thread, combined by exact rescaling).  The host or the
+// device planner rescales the slice sums to the row exponent and turns them into rigorous
+// one-sided bounds (every FP32 rounding is one of the K - 1 additions of a K-term sum).
 __device__ __forceinline__ unsigned long long umax64(unsigned long long a, unsigned long long b) {
   return a > b ? a : b;
 }
@@ -152,14 +219,17 @@ __global__ void __launch_bounds__(256) stats_kc_kernel(const double* __restrict_
   const int64_t r = static_cast<int64_t>(blockIdx.x) * (blockDim.x / 32) + (threadIdx.x >> 5);
   if (r >= R) return;
   const unsigned long long* row = reinterpret_cast<const unsigned long long*>(X + r * rs);
-  unsigned long long mx = 0;
+  RunStats rs_;
   int64_t k = lane;
   for (; k + 96 < K; k += 128) {
     const unsigned long long b0 = row[k], b1 = row[k + 32], b2 = row[k + 64], b3 = row[k + 96];
-    mx = umax64(mx, umax64(umax64(b0 & 0x7FFFFFFFFFFFFFFFull, b1 & 0x7FFFFFFFFFFFFFFFull),
-                           umax64(b2 & 0x7FFFFFFFFFFFFFFFull, b3 & 0x7FFFFFFFFFFFFFFFull)));
+    rs_.add(b0, SUMS);
+    rs_.add(b1, SUMS);
+    rs_.add(b2, SUMS);
+    rs_.add(b3, SUMS);
   }
-  for (; k < K; k += 32) mx = umax64(mx, row[k] & 0x7FFFFFFFFFFFFFFFull);
+  for (; k < K; k += 32) rs_.add(row[k], SUMS);
+  unsigned long long mx = rs_.mx;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) mx = umax64(mx, __shfl_xor_sync(0xffffffffu, mx, o));
   if (lane == 0) st.amax_bits[r] = mx;
@@ -167,11 +237,9 @@ __global__ void __launch_bounds__(256) stats_kc_kernel(const double* __restrict_
   const int e = row_exponent_of(mx);
   float sa = 0.0f, sq = 0.0f;
   if (e != OZ_EXP_NONFINITE) {
-    for (int64_t k2 = lane; k2 < K; k2 += 32) {
-      const float f = scaled_f32_trunc(row[k2] & 0x7FFFFFFFFFFFFFFFull, e);
-      sa += f;
-      sq = fmaf(f, f, sq);
-    }
+    rs_.to(e);
+    sa = rs_.sa;
+    sq = rs_.sq;
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -196,36 +264,33 @@ __global__ void __launch_bounds__(256) stats_rc_kernel(const double* __restrict_
   const int64_t k0 = static_cast<int64_t>(blockIdx.y) * kslice;
   const int64_t k1 = (k0 + kslice < K) ? k0 + kslice : K;
   const unsigned long long* Xb = reinterpret_cast<const unsigned long long*>(X);
-  unsigned long long mx = 0;
+  RunStats rs_;
   if (r < R) {
     int64_t k = k0 + tk;
     for (; k + 24 < k1; k += 32) {
       const unsigned long long b0 = Xb[r + k * ks], b1 = Xb[r + (k + 8) * ks];
       const unsigned long long b2 = Xb[r + (k + 16) * ks], b3 = Xb[r + (k + 24) * ks];
-      mx = umax64(mx, umax64(umax64(b0 & 0x7FFFFFFFFFFFFFFFull, b1 & 0x7FFFFFFFFFFFFFFFull),
-                             umax64(b2 & 0x7FFFFFFFFFFFFFFFull, b3 & 0x7FFFFFFFFFFFFFFFull)));
+      rs_.add(b0, SUMS);
+      rs_.add(b1, SUMS);
+      rs_.add(b2, SUMS);
+      rs_.add(b3, SUMS);
     }
-    for (; k < k1; k += 8) mx = umax64(mx, Xb[r + k * ks] & 0x7FFFFFFFFFFFFFFFull);
+    for (; k < k1; k += 8) rs_.add(Xb[r + k * ks], SUMS);
   }
-  smx[tk][tr] = mx;
+  smx[tk][tr] = rs_.mx;
   __syncthreads();
+  unsigned long long mx = 0;
   for (int w = 0; w < 8; ++w) mx = umax64(mx, smx[w][tr]);
   if (tk == 0 && r < R && mx) atomicMax(st.amax_bits + r, mx);
   if (!SUMS) return;
   const int e = row_exponent_of(mx);
-  float sa = 0.0f, sq = 0.0f;
-  if (r < R && e != OZ_EXP_NONFINITE) {
-    for (int64_t k = k0 + tk; k < k1; k += 8) {
-      const float f = scaled_f32_trunc(Xb[r + k * ks] & 0x7FFFFFFFFFFFFFFFull, e);
-      sa += f;
-      sq = fmaf(f, f, sq);
-    }
-  }
-  ssa[tk][tr] = sa;
-  ssq[tk][tr] = sq;
+  if (e != OZ_EXP_NONFINITE) rs_.to(e);
+  ssa[tk][tr] = (e != OZ_EXP_NONFINITE) ? rs_.sa : 0.0f;
+  ssq[tk][tr] = (e != OZ_EXP_NONFINITE) ? rs_.sq : 0.0f;
   __syncthreads();
   if (tk == 0 && r < R) {
-    for (int w = 1; w < 8; ++w) {
+    float sa = 0.0f, sq = 0.0f;
+    for (int w = 0; w < 8; ++w) {
       sa += ssa[w][tr];
       sq += ssq[w][tr];
     }

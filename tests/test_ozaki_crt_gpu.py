@@ -101,6 +101,25 @@ def test_auto_plan_bit_exact(cuda, shape):
     assert_bit_equal(got, ref)
 
 
+def test_auto_plan_with_subnormal_rows(cuda):
+    """Rows whose every entry is subnormal (and columns scaled near the top of the range):
+    the statistics scale subnormals exactly, so the automatic t keeps |C'| inside the CRT
+    range and the result equals the restatement of the reported plan."""
+    M, K, N = 96, 700, 80
+    g = np.random.default_rng(91)
+    A = g.uniform(-1, 1, (M, K)) * np.ldexp(1.0, g.integers(-3, 4, (M, K)))
+    B = g.uniform(-1, 1, (K, N)) * np.ldexp(1.0, g.integers(-3, 4, (K, N)))
+    A[:24] *= 2.0 ** -1060      # every entry subnormal
+    A[24:30] *= 2.0 ** -1030    # mixed subnormal / normal magnitudes
+    B[:, :10] *= 2.0 ** 900
+    A, B = np.asfortranarray(A), np.asfortranarray(B)
+    got, bound = _run(A, B, moduli=0, want_bound=True)
+    plan = gbblas.last_ozaki_plan()
+    ref = oracle.ozaki_crt_gemm(A, B, moduli=plan["slices"], bits=plan["bits"])
+    assert_bit_equal(got, ref)
+    assert bound <= 2.0 ** -50
+
+
 def test_long_k_many_chunks(cuda):
     """K = 70000: 69 exact accumulation chunks per modulus, summed mod p in the residue planes."""
     M, K, N = 64, 70000, 40
