@@ -168,9 +168,9 @@ CrtTable build_table() {
     md.p[g] = p;
     md.pf[g] = static_cast<float>(p);
     md.pinv[g] = 1.0f / static_cast<float>(p);
-    uint64_t pw = 1;   // 2^(12 l) mod p
-    for (int l = 1; l <= 5; ++l) {
-      pw = (pw << 12) % p;
+    uint64_t pw = 1;   // 2^(13 l) mod p
+    for (int l = 1; l <= 4; ++l) {
+      pw = (pw << 13) % p;
       md.climb[g][l] = static_cast<float>(pw);
     }
     const uint64_t c62 = (((uint64_t(1) << 31) % p) * ((uint64_t(1) << 31) % p)) % p;
@@ -537,9 +537,10 @@ int crt_plan_device(const OzRowStats& sa, const OzRowStats& sb, const CrtPlanPar
 // One thread = one row r and 8 consecutive k (rows contiguous: two neighbouring threads share
 // a row and cover 16 k, so each warp store fills whole 32-byte sectors; k contiguous:
 // neighbouring threads cover neighbouring k).  Y = round-half-away(x 2^(t - e)) (|Y| <= 2^t,
-// t <= 62) is shifted to Y + 2^62 >= 0 and cut into six 12-bit limbs held as exact FP32 values;
+// t <= 62) is shifted to Y + 2^62 >= 0 and cut into five 13-bit limbs held as exact FP32 values;
 // per modulus p (<= 253)
-//   s = (-2^62 mod p) + sum_l limb_l (2^(12 l) mod p)     an integer below 2^23, exact in FP32
+//   s = (-2^62 mod p) + sum_l limb_l (2^(13 l) mod p)     below 8191 (1 + 4 * 252) + 252 < 2^23,
+//                                                          exact in FP32
 //   r = s - p rint(s / p)                                  |r| <= p/2 + 1/2, so |r| <= 127
 // all on the FMA pipe; r has at most 7 significant bits, so its BF16 is the upper half of its
 // FP32 bits.  One 16-byte store per plane.
@@ -567,20 +568,20 @@ __global__ void __launch_bounds__(256) crt_split_kernel(const double* __restrict
   const bool nonfinite = (e == OZ_EXP_NONFINITE);
   const int nvalid = static_cast<int>(K - k0 < 8 ? K - k0 : 8);
   const double* src = X + r * rs + k0 * ks;
-  float yl[6][8];
+  float yl[5][8];
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
     const double x = (j < nvalid) ? src[j * ks] : 0.0;
     const uint64_t y = (nonfinite ? 0ull : fixed_point<uint64_t>(x, e, tbits + 1)) + (1ull << 62);
 #pragma unroll
-    for (int l = 0; l < 6; ++l)
-      yl[l][j] = __uint_as_float(0x4B000000u | (static_cast<uint32_t>(y >> (12 * l)) & 0xFFFu)) - 8388608.0f;
+    for (int l = 0; l < 5; ++l)
+      yl[l][j] = __uint_as_float(0x4B000000u | (static_cast<uint32_t>(y >> (13 * l)) & 0x1FFFu)) - 8388608.0f;
   }
   __nv_bfloat16* out0 = planes + r * pitch + k0;
   const int64_t plane_stride = R * pitch;
   for (int g = 0; g < nmod; ++g) {
     const float c0 = mod.climb[g][0], c1 = mod.climb[g][1], c2 = mod.climb[g][2], c3 = mod.climb[g][3];
-    const float c4 = mod.climb[g][4], c5 = mod.climb[g][5], pf = mod.pf[g], inv = mod.pinv[g];
+    const float c4 = mod.climb[g][4], pf = mod.pf[g], inv = mod.pinv[g];
     uint32_t packed[4];
 #pragma unroll
     for (int j = 0; j < 8; j += 2) {
@@ -592,7 +593,6 @@ __global__ void __launch_bounds__(256) crt_split_kernel(const double* __restrict
         sj = fmaf(yl[2][j + h], c2, sj);
         sj = fmaf(yl[3][j + h], c3, sj);
         sj = fmaf(yl[4][j + h], c4, sj);
-        sj = fmaf(yl[5][j + h], c5, sj);
         const float q = fmaf(sj, inv, MAGIC) - MAGIC;
         rr[h] = fmaf(-pf, q, sj);
       }
