@@ -199,6 +199,20 @@ int gb_gemm_grouped_f32(const gb_problem_t* problems, int count, const gb_groupe
 #define GB_GROUPED_NOALLOC_MAX 65536
 int gb_gemm_grouped_f64_noalloc(const gb_problem_t* problems, int count, const gb_grouped_tuning_t* tuning,
                                 void* stream);
+/* Strided batched GEMM: C_i = alpha A_i B_i + beta C_i for i < count, where A_i = A + i*strideA,
+ * B_i = B + i*strideB, C_i = C + i*strideC (strides in elements, >= 0; a stride of 0 shares
+ * that operand), each product M x N x K, column-major, no transposes, device pointers; the
+ * C_i must not overlap.  The batch form of jBLAS's fastmul!/kernel! on many small static
+ * matrices (src/kernels.jl:1-208, 239): per element the jmul! FMA chain (bit-identical, with
+ * the alpha/beta extension of gb_gemm_*), run as one grouped persistent launch over a
+ * problem table built on the device (table and workspace from the library pool).
+ * count <= 2^31 - 1. */
+int gb_gemm_strided_batched_f64(int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t lda,
+                                int64_t strideA, const double* B, int64_t ldb, int64_t strideB, double beta,
+                                double* C, int64_t ldc, int64_t strideC, int64_t count, void* stream);
+int gb_gemm_strided_batched_f32(int64_t M, int64_t N, int64_t K, float alpha, const float* A, int64_t lda,
+                                int64_t strideA, const float* B, int64_t ldb, int64_t strideB, float beta,
+                                float* C, int64_t ldc, int64_t strideC, int64_t count, void* stream);
 /* Autotuner: times every configuration per size class on the given problems (HOST copy
  * of the table; their C buffers are left untouched, results go to scratch) with `reps`
  * timed repetitions and writes the fastest configuration per class; class_ms (may be

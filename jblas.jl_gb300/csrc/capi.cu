@@ -803,6 +803,47 @@ int gb_gemm_grouped_f64_noalloc(const gb_problem_t* problems, int count, const g
   return grouped_f64_noalloc(problems, count, tuning, static_cast<cudaStream_t>(stream));
 }
 
+static int strided_batched(int dtype_bytes, int64_t M, int64_t N, int64_t K, double alpha, const void* A,
+                           int64_t lda, int64_t sa, const void* B, int64_t ldb, int64_t sb, double beta, void* C,
+                           int64_t ldc, int64_t sc, int64_t count, void* stream) {
+  DeviceInfo* dev = nullptr;
+  int rc = device_info(&dev);
+  if (rc) return rc;
+  if (M < 0 || N < 0 || K < 0 || count < 0 || count > 0x7FFFFFFF || sa < 0 || sb < 0 || sc < 0)
+    return GB_ERR_INVALID_VALUE;
+  if (lda < (M > 1 ? M : 1) || ldb < (K > 1 ? K : 1) || ldc < (M > 1 ? M : 1)) return GB_ERR_INVALID_VALUE;
+  if (count == 0 || M == 0 || N == 0) return GB_OK;
+  if (count > 1 && sc < ldc * (N - 1) + M) return GB_ERR_INVALID_VALUE;   // C_i would overlap
+  if (!is_device_ptr(C)) return GB_ERR_INVALID_VALUE;
+  if (alpha != 0.0 && K > 0 && (!is_device_ptr(A) || !is_device_ptr(B))) return GB_ERR_INVALID_VALUE;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int n = static_cast<int>(count);
+  const size_t tab_bytes = (sizeof(gb_problem_t) * static_cast<size_t>(n) + 255) & ~size_t(255);
+  const size_t ws_bytes = grouped_workspace_bytes(n);
+  char* ws = nullptr;
+  GB_CUDA_TRY(cudaMallocFromPoolAsync(reinterpret_cast<void**>(&ws), tab_bytes + ws_bytes, dev->pool, s));
+  gb_problem_t* tab = reinterpret_cast<gb_problem_t*>(ws);
+  rc = grouped_fill_strided(tab, n, M, N, K, lda, ldb, ldc, A, B, C, sa * dtype_bytes, sb * dtype_bytes,
+                            sc * dtype_bytes, alpha, beta, s);
+  if (!rc)
+    rc = grouped_launch(dtype_bytes, tab, n, grouped_default_tuning(dtype_bytes),
+                        reinterpret_cast<long long*>(ws + tab_bytes), dev->sms, s);
+  cudaFreeAsync(ws, s);
+  return rc;
+}
+
+int gb_gemm_strided_batched_f64(int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t lda,
+                                int64_t strideA, const double* B, int64_t ldb, int64_t strideB, double beta,
+                                double* C, int64_t ldc, int64_t strideC, int64_t count, void* stream) {
+  return strided_batched(8, M, N, K, alpha, A, lda, strideA, B, ldb, strideB, beta, C, ldc, strideC, count, stream);
+}
+
+int gb_gemm_strided_batched_f32(int64_t M, int64_t N, int64_t K, float alpha, const float* A, int64_t lda,
+                                int64_t strideA, const float* B, int64_t ldb, int64_t strideB, float beta,
+                                float* C, int64_t ldc, int64_t strideC, int64_t count, void* stream) {
+  return strided_batched(4, M, N, K, alpha, A, lda, strideA, B, ldb, strideB, beta, C, ldc, strideC, count, stream);
+}
+
 int gb_autotune_grouped(int dtype_bytes, const gb_problem_t* host_problems, int count, int reps,
                         gb_grouped_tuning_t* out, float* class_ms, void* stream) {
   if (!out || count < 0 || (count > 0 && !host_problems) || (dtype_bytes != 4 && dtype_bytes != 8))

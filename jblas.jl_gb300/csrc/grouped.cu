@@ -389,4 +389,39 @@ int grouped_f64_noalloc(const gb_problem_t* d_probs, int count, const gb_grouped
   return GB_OK;
 }
 
+
+// ------------------------------------------------------------------ strided batches
+__global__ void grouped_fill_strided_kernel(gb_problem_t* __restrict__ probs, int count, int64_t M, int64_t N,
+                                            int64_t K, int64_t lda, int64_t ldb, int64_t ldc, const char* A,
+                                            const char* B, char* C, int64_t sa, int64_t sb, int64_t sc, double alpha,
+                                            double beta) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  gb_problem_t p;
+  p.m = M;
+  p.n = N;
+  p.k = K;
+  p.lda = lda;
+  p.ldb = ldb;
+  p.ldc = ldc;
+  p.A = A + static_cast<int64_t>(i) * sa;
+  p.B = B + static_cast<int64_t>(i) * sb;
+  p.C = C + static_cast<int64_t>(i) * sc;
+  p.alpha = alpha;
+  p.beta = beta;
+  probs[i] = p;
+}
+
+int grouped_fill_strided(gb_problem_t* d_probs, int count, int64_t M, int64_t N, int64_t K, int64_t lda, int64_t ldb,
+                         int64_t ldc, const void* A, const void* B, void* C, int64_t strideA_bytes,
+                         int64_t strideB_bytes, int64_t strideC_bytes, double alpha, double beta, cudaStream_t s) {
+  if (count <= 0) return GB_OK;
+  const int blocks = (count + 255) / 256;
+  grouped_fill_strided_kernel<<<blocks, 256, 0, s>>>(d_probs, count, M, N, K, lda, ldb, ldc,
+                                                      static_cast<const char*>(A), static_cast<const char*>(B),
+                                                      static_cast<char*>(C), strideA_bytes, strideB_bytes,
+                                                      strideC_bytes, alpha, beta);
+  GB_CUDA_TRY(cudaGetLastError());
+  return GB_OK;
+}
 }  // namespace gb

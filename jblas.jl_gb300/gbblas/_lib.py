@@ -85,6 +85,10 @@ SIGNATURES = {
     "gb_kernel_kind_name": (ctypes.c_char_p, [c_int]),
     "gb_grouped_default_tuning": (c_int, [c_int, ctypes.POINTER(Tuning)]),
     "gb_grouped_workspace_size": (ctypes.c_size_t, [c_int]),
+    "gb_gemm_strided_batched_f64": (c_int, [c_i64, c_i64, c_i64, ctypes.c_double, c_vp, c_i64, c_i64, c_vp, c_i64,
+                                            c_i64, ctypes.c_double, c_vp, c_i64, c_i64, c_i64, c_vp]),
+    "gb_gemm_strided_batched_f32": (c_int, [c_i64, c_i64, c_i64, ctypes.c_float, c_vp, c_i64, c_i64, c_vp, c_i64,
+                                            c_i64, ctypes.c_float, c_vp, c_i64, c_i64, c_i64, c_vp]),
     "gb_gemm_grouped_f64": (c_int, [c_vp, c_int, ctypes.POINTER(Tuning), c_vp, ctypes.c_size_t, c_vp]),
     "gb_gemm_grouped_f32": (c_int, [c_vp, c_int, ctypes.POINTER(Tuning), c_vp, ctypes.c_size_t, c_vp]),
     "gb_gemm_grouped_f64_noalloc": (c_int, [c_vp, c_int, ctypes.POINTER(Tuning), c_vp]),

@@ -118,6 +118,36 @@ def jmul_(D, A, X):
     return gemm_(D, A, X, 1.0, 0.0, mode="native")
 
 
+def gemm_strided_batched_(C, A, B, alpha=1.0, beta=0.0):
+    """C[i] = alpha * A[i] @ B[i] + beta * C[i] for every i, in place (jmul!'s FMA chain).
+
+    A (count, M, K), B (count, K, N), C (count, M, N): CUDA tensors of one dtype whose
+    matrices are column-major (stride 1 along rows, e.g. ``X.transpose(1, 2)`` of a
+    contiguous tensor); A or B may be broadcast along the batch (stride 0).  Returns C."""
+    dt = _dtype_of(C, A, B)
+    cnt, M, K = A.shape
+    cnt2, K2, N = B.shape
+    if K2 != K or cnt2 != cnt or tuple(C.shape) != (cnt, M, N):
+        raise DimensionMismatch("A %s, B %s, C %s" % (tuple(A.shape), tuple(B.shape), tuple(C.shape)))
+
+    def batch_cm(X, rows, cols, name):
+        sb, sr, sc = X.stride()
+        if rows > 1 and sr != 1:
+            raise ValueError("%s: matrices must be column-major (stride 1 along rows)" % name)
+        return sb, (sc if cols > 1 else max(1, rows))
+
+    sa, lda = batch_cm(A, M, K, "A")
+    sb, ldb = batch_cm(B, K, N, "B")
+    sc, ldc = batch_cm(C, M, N, "C")
+    name = "gb_gemm_strided_batched_f64" if dt == torch.float64 else "gb_gemm_strided_batched_f32"
+    st = torch.cuda.current_stream(C.device).cuda_stream
+    rc = getattr(_lib.lib(), name)(M, N, K, float(alpha), ctypes.c_void_p(A.data_ptr()), max(1, lda), sa,
+                                  ctypes.c_void_p(B.data_ptr()), max(1, ldb), sb, float(beta),
+                                  ctypes.c_void_p(C.data_ptr()), max(1, ldc), sc, cnt, ctypes.c_void_p(st))
+    check(rc, name)
+    return C
+
+
 def gemm(A, B, *, mode="native", slices=0):
     """Allocating form: returns A @ B as a new column-major tensor."""
     dt = _dtype_of(A, B)
