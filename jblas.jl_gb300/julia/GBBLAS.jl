@@ -8,6 +8,10 @@ layer over the C ABI in `include/gbblas.h`:
     gemm!(C, A, B)                 the same call spelled as in the task (`jmul!` semantics)
     gemm!(C, A, B, α, β; mode, slices)   BLAS-3 form; mode = :native | :ozaki | :ozaki_crt
     gemm_adjoint!(dA, dB, A, B, dC)      dA = dC*B', dB = A'*dC in one launch (Float32)
+    mul!(C, A, B, α, β; mode, slices)    LinearAlgebra.mul! semantics, A and B may be
+                                         transpose/adjoint views (real element types)
+    enable_mul!(T)                       routes LinearAlgebra.mul! for device matrix type T here
+    gemm_strided_batched!(C, A, B, α, β) C[:,:,i] = α A[:,:,i] B[:,:,i] + β C[:,:,i]
     ChainRulesCore.rrule(::typeof(gemm), A, B)   pullback through gemm_adjoint!
 
 Matrices are device arrays (anything with `pointer` to CUDA device memory and a column-
@@ -93,6 +97,84 @@ function gemm!(C::AbstractMatrix{Float32}, A::AbstractMatrix{Float32}, B::Abstra
                  Ptr{Cfloat}, Int64, Ptr{Cvoid}),
                 0, 0, M, N, K, α, pointer(A), ld(A), pointer(B), ld(B), β, pointer(C), ld(C), current_stream()))
     C
+end
+
+# ------------------------------------------------------------------ mul! with transposes
+import LinearAlgebra
+using LinearAlgebra: Transpose, Adjoint
+
+const Wrapped{T} = Union{Transpose{T}, Adjoint{T}}
+op_flag(::AbstractMatrix) = Cint(0)
+op_flag(::Wrapped{<:Real}) = Cint(1)        # a real adjoint is a transpose
+storage(X::AbstractMatrix) = X
+storage(X::Wrapped{<:Real}) = parent(X)
+
+"""
+    mul!(C, A, B, α=true, β=false; mode=:native, slices=0) -> C
+
+`C = α op(A) op(B) + β C` with LinearAlgebra's argument meaning, on device matrices; `A`
+and `B` may be `transpose`/`adjoint` views (passed to the library as transpose flags, the
+data is not copied).  Float64 accepts `mode` (`:native`, `:ozaki`, `:ozaki_crt`), Float32
+runs natively.
+"""
+function mul!(C::AbstractMatrix{Float64}, A::AbstractMatrix{Float64}, B::AbstractMatrix{Float64},
+              α::Number = true, β::Number = false; mode::Symbol = :native, slices::Integer = 0)
+    M, K = size(A); N = size(B, 2)
+    size(B, 1) == K && size(C) == (M, N) || throw(DimensionMismatch("mul!: $(size(C)) = $(size(A)) * $(size(B))"))
+    As, Bs = storage(A), storage(B)
+    check(ccall((:gb_gemm_f64, libgbblas), Cint,
+                (Cint, Cint, Int64, Int64, Int64, Cdouble, Ptr{Cdouble}, Int64, Ptr{Cdouble}, Int64, Cdouble,
+                 Ptr{Cdouble}, Int64, Cint, Cint, Ptr{Cdouble}, Ptr{Cvoid}),
+                op_flag(A), op_flag(B), M, N, K, Float64(α), pointer(As), ld(As), pointer(Bs), ld(Bs), Float64(β),
+                pointer(C), ld(C), MODE[mode], slices, C_NULL, current_stream()))
+    C
+end
+function mul!(C::AbstractMatrix{Float32}, A::AbstractMatrix{Float32}, B::AbstractMatrix{Float32},
+              α::Number = true, β::Number = false)
+    M, K = size(A); N = size(B, 2)
+    size(B, 1) == K && size(C) == (M, N) || throw(DimensionMismatch("mul!: $(size(C)) = $(size(A)) * $(size(B))"))
+    As, Bs = storage(A), storage(B)
+    check(ccall((:gb_gemm_f32, libgbblas), Cint,
+                (Cint, Cint, Int64, Int64, Int64, Cfloat, Ptr{Cfloat}, Int64, Ptr{Cfloat}, Int64, Cfloat,
+                 Ptr{Cfloat}, Int64, Ptr{Cvoid}),
+                op_flag(A), op_flag(B), M, N, K, Float32(α), pointer(As), ld(As), pointer(Bs), ld(Bs), Float32(β),
+                pointer(C), ld(C), current_stream()))
+    C
+end
+
+"""
+    enable_mul!(T)
+
+Make `LinearAlgebra.mul!(C, A, B, α, β)` call this library when `C` is a `T` (a device
+matrix type such as CUDA.jl's `CuMatrix{Float64}`) and `A`, `B` are `T`s or their
+transpose/adjoint views.  Opt-in, so host arrays keep LinearAlgebra's own methods.
+"""
+function enable_mul!(::Type{T}) where {T <: AbstractMatrix}
+    @eval function LinearAlgebra.mul!(C::$T, A::Union{$T, Wrapped{<:Real, <:$T}}, B::Union{$T, Wrapped{<:Real, <:$T}},
+                                      α::Number, β::Number)
+        GBBLAS.mul!(C, A, B, α, β)
+    end
+    nothing
+end
+
+"""
+    gemm_strided_batched!(C, A, B, α=1, β=0) -> C
+
+`C[:,:,i] = α A[:,:,i] B[:,:,i] + β C[:,:,i]` for every `i`, one launch (the batch form of
+jBLAS's `fastmul!`), per element jBLAS's FMA chain.  Arrays are column-major device arrays.
+"""
+for (T, f) in ((Float64, :gb_gemm_strided_batched_f64), (Float32, :gb_gemm_strided_batched_f32))
+    @eval function gemm_strided_batched!(C::AbstractArray{$T,3}, A::AbstractArray{$T,3}, B::AbstractArray{$T,3},
+                                         α::Number = one($T), β::Number = zero($T))
+        M, K, n = size(A); N = size(B, 2)
+        size(B) == (K, N, n) && size(C) == (M, N, n) || throw(DimensionMismatch("gemm_strided_batched!"))
+        check(ccall(($(QuoteNode(f)), libgbblas), Cint,
+                    (Int64, Int64, Int64, $T, Ptr{$T}, Int64, Int64, Ptr{$T}, Int64, Int64, $T, Ptr{$T}, Int64, Int64,
+                     Int64, Ptr{Cvoid}),
+                    M, N, K, $T(α), pointer(A), max(1, stride(A, 2)), stride(A, 3), pointer(B), max(1, stride(B, 2)),
+                    stride(B, 3), $T(β), pointer(C), max(1, stride(C, 2)), stride(C, 3), n, current_stream()))
+        C
+    end
 end
 
 """
