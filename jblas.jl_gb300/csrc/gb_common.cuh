@@ -75,20 +75,49 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 
 // Bounded wait: returns false (and records the error) when the deadline passes or when
 // another role of this CTA has already aborted (*abort != 0).
+// try_wait with an explicit suspend-time hint (ns): the thread sleeps at most about that long
+// when the phase is not complete, and wakes as soon as it completes.
+__device__ __forceinline__ bool mbar_try_wait_hint(uint64_t* bar, uint32_t parity, uint32_t hint_ns) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity), "r"(hint_ns)
+      : "memory");
+  return ok != 0;
+}
+
+// Non-blocking test of the phase.
+__device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// The first test does not block; afterwards the deadline is read after every try_wait, whose
+// suspension is capped at a quarter of the limit (0.2 us .. 1 ms), so a wait gives up within
+// about 1.25 x limit_ns.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint64_t limit_ns,
                                                   volatile int* abort, DeviceStatus* st, int where) {
-  if (mbar_try_wait(bar, parity)) return true;
+  if (mbar_test_wait(bar, parity)) return true;
   const uint64_t t0 = globaltimer_ns();
-  uint32_t spins = 0;
+  uint64_t h = limit_ns / 4;
+  const uint32_t hint = static_cast<uint32_t>(h < 200 ? 200 : (h > 1000000 ? 1000000 : h));
   while (true) {
-    if (mbar_try_wait(bar, parity)) return true;
-    if ((++spins & 15u) == 0) {
-      if (*abort) return false;
-      if (globaltimer_ns() - t0 > limit_ns) {
-        report_error(st, GB_ERR_PIPELINE_TIMEOUT, where);
-        *abort = 1;
-        return false;
-      }
+    if (mbar_try_wait_hint(bar, parity, hint)) return true;
+    if (*abort) return false;
+    if (globaltimer_ns() - t0 > limit_ns) {
+      report_error(st, GB_ERR_PIPELINE_TIMEOUT, where);
+      *abort = 1;
+      return false;
     }
   }
 }

@@ -42,3 +42,28 @@ def test_short_wait_limit_reports_timeout_and_context_survives(cuda):
     torch.cuda.synchronize()
     gbblas.check_device_status()
     assert_bit_equal(to_host(C), oracle.ozaki_gemm(A, B, slices=4))
+
+
+def test_short_wait_limit_crt_mode(cuda):
+    """The same bounded waits guard the residue products of the CRT mode (planner, split and
+    combine still run, on whatever the aborted kernel left; the status word says so)."""
+    g = np.random.default_rng(22)
+    M, K, N = 256, 8192, 512
+    A = np.asfortranarray(g.uniform(-1, 1, (M, K)))
+    B = np.asfortranarray(g.uniform(-1, 1, (K, N)))
+    Ad, Bd = to_dev(A), to_dev(B)
+    C = torch.zeros((N, M), dtype=torch.float64, device="cuda").t()
+    gbblas.check_device_status()
+    gbblas.set_wait_limit_ns(2000)
+    try:
+        gbblas.gemm_(C, Ad, Bd, mode="ozaki_crt", slices=16)
+        torch.cuda.synchronize()
+    finally:
+        gbblas.set_wait_limit_ns(0)
+    with pytest.raises(gbblas.GBError) as e:
+        gbblas.check_device_status()
+    assert e.value.status == _lib.GB_ERR_PIPELINE_TIMEOUT
+    gbblas.gemm_(C, Ad, Bd, mode="ozaki_crt", slices=16)
+    torch.cuda.synchronize()
+    gbblas.check_device_status()
+    assert_bit_equal(to_host(C), oracle.ozaki_crt_gemm(A, B, moduli=16))
