@@ -202,7 +202,7 @@ def reference_arm(args, rank, world):
         "impl": "reference", "metric": METRIC, "value": v, "unit": "TFLOP/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "gemm_fp64_%d^3" % n, "M": n, "N": n, "K": n,
+        "config": {"workload": "ozaki_fp64_gemm_%d^3" % n, "M": n, "N": n, "K": n,
                    "distribution": "sign*U[1,2)*2^(e_line+e_elem), e_line in [-30,30], e_elem in [-8,8]",
                    "algorithm": "jmul! FMA chain, register-tiled (oracle port; Julia reference cannot run)"},
         "cpu_baseline": {"value": v, "unit": "TFLOP/s", "cores": threads, "kind": "port", "sample": sample},
