@@ -59,15 +59,22 @@ template <>
 __device__ __forceinline__ float fmad<float>(float a, float b, float c) { return fmaf(a, b, c); }
 
 constexpr int GROUPED_THREADS = 256;
-constexpr int GROUPED_SMEM = 2 * 16 * 64 * 8;  // largest As + Bs of any configuration (bytes)
+// largest As + Bs of any configuration (bytes): 16 x 64 + 16 x (64 + 1) FP64 words
+constexpr int GROUPED_SMEM = (16 * 64 + 16 * 65) * 8;
 
 // One BM x BN tile of problem `p` (column-major, no transposes).  Per element the FMA chain
 // runs k = 0..K-1 in order from -0.0 (equal to jmul!'s a1*x1 first step, bit for bit).
+// The next K slab is loaded into registers while the current one is multiplied from shared
+// memory; B's slab is stored [k][n] with rows padded by one word, so the k-fastest global
+// reads land in distinct banks.
 template <typename T, int BM, int BN, int BK, int TM, int TN>
 __device__ __forceinline__ void grouped_tile(const gb_problem_t& p, int tm, int tn, unsigned char* smem) {
   static_assert((BM / TM) * (BN / TN) == GROUPED_THREADS, "configuration must use 256 threads");
+  constexpr int LA = (BM * BK + GROUPED_THREADS - 1) / GROUPED_THREADS;   // A elements per thread
+  constexpr int LB = (BK * BN + GROUPED_THREADS - 1) / GROUPED_THREADS;   // B elements per thread
+  constexpr int BNP = BN + 1;
   T* As = reinterpret_cast<T*>(smem);   // [BK][BM]
-  T* Bs = As + BK * BM;                 // [BK][BN]
+  T* Bs = As + BK * BM;                 // [BK][BN + 1]
   const int tid = threadIdx.x;
   const int tx = tid % (BN / TN), ty = tid / (BN / TN);
   const int64_t M = p.m, N = p.n, K = p.k;
@@ -81,27 +88,44 @@ __device__ __forceinline__ void grouped_tile(const gb_problem_t& p, int tm, int 
     for (int j = 0; j < TN; ++j) acc[i][j] = T(-0.0);
 
   const int64_t Kc = (p.alpha == 0.0) ? 0 : K;   // alpha == 0: A and B are not read
+  T ra[LA], rb[LB];
+  auto load = [&](int64_t k0) {
+#pragma unroll
+    for (int l = 0; l < LA; ++l) {
+      const int e = tid + l * GROUPED_THREADS;
+      const int ml = e % BM, kl = e / BM;
+      const int64_t m = m0 + ml, k = k0 + kl;
+      ra[l] = (e < BM * BK && m < M && k < K) ? A[m + k * p.lda] : T(0);
+    }
+#pragma unroll
+    for (int l = 0; l < LB; ++l) {
+      const int e = tid + l * GROUPED_THREADS;
+      const int kl = e % BK, nl = e / BK;
+      const int64_t n = n0 + nl, k = k0 + kl;
+      rb[l] = (e < BK * BN && n < N && k < K) ? B[k + n * p.ldb] : T(0);
+    }
+  };
+  if (Kc > 0) load(0);
   for (int64_t k0 = 0; k0 < Kc; k0 += BK) {
     const int kc = static_cast<int>(K - k0 < BK ? K - k0 : BK);
 #pragma unroll
-    for (int e = tid; e < BM * BK; e += GROUPED_THREADS) {
-      const int ml = e % BM, kl = e / BM;
-      const int64_t m = m0 + ml, k = k0 + kl;
-      As[kl * BM + ml] = (m < M && k < K) ? A[m + k * p.lda] : T(0);
+    for (int l = 0; l < LA; ++l) {
+      const int e = tid + l * GROUPED_THREADS;
+      if (e < BM * BK) As[(e / BM) * BM + e % BM] = ra[l];
     }
 #pragma unroll
-    for (int e = tid; e < BK * BN; e += GROUPED_THREADS) {
-      const int kl = e % BK, nl = e / BK;
-      const int64_t n = n0 + nl, k = k0 + kl;
-      Bs[kl * BN + nl] = (n < N && k < K) ? B[k + n * p.ldb] : T(0);
+    for (int l = 0; l < LB; ++l) {
+      const int e = tid + l * GROUPED_THREADS;
+      if (e < BK * BN) Bs[(e % BK) * BNP + e / BK] = rb[l];
     }
     __syncthreads();
+    if (k0 + BK < Kc) load(k0 + BK);   // in flight while this slab is multiplied
     for (int kk = 0; kk < kc; ++kk) {
       T a[TM], b[TN];
 #pragma unroll
       for (int i = 0; i < TM; ++i) a[i] = As[kk * BM + ty + i * (BM / TM)];
 #pragma unroll
-      for (int j = 0; j < TN; ++j) b[j] = Bs[kk * BN + tx + j * (BN / TN)];
+      for (int j = 0; j < TN; ++j) b[j] = Bs[kk * BNP + tx + j * (BN / TN)];
 #pragma unroll
       for (int i = 0; i < TM; ++i)
 #pragma unroll
@@ -161,7 +185,7 @@ __global__ void __launch_bounds__(1024) grouped_prefix_kernel(const gb_problem_t
 }
 
 template <typename T>
-__global__ void __launch_bounds__(GROUPED_THREADS) grouped_gemm_kernel(const gb_problem_t* __restrict__ probs,
+__global__ void __launch_bounds__(GROUPED_THREADS, 2) grouped_gemm_kernel(const gb_problem_t* __restrict__ probs,
                                                                        int count, gb_grouped_tuning_t tuning,
                                                                        const long long* __restrict__ offsets) {
   __shared__ __align__(16) unsigned char smem[GROUPED_SMEM];

@@ -13,6 +13,7 @@ cases:
   ozaki_crt      gb_gemm_f64 OZAKI_CRT, 15 moduli (stats, residue split, residue products,
                  CRT combine), 4096 x 4096 x 8192
   grouped_f64    gb_gemm_grouped_f64, 4096 problems with m, n, k log-uniform in [8, 512]
+  grouped_f32    the same problems in FP32 (tuned configuration of the bench)
   adjoint        gb_gemm_adjoint_f32, A 4096 x 2048, B 2048 x 4096
 """
 import sys
@@ -61,12 +62,15 @@ def case_ozaki_crt():
     return _timed(lambda: api.gemm_(C, A, B, mode="ozaki_crt", slices=15))
 
 
-def case_grouped():
+def case_grouped(dtype=torch.float64, tuning=None):
     sizes = [tuple(int(x) for x in r) for r in workloads.grouped_sizes(4096)]
-    As = [(torch.rand((k, m), dtype=torch.float64, device="cuda") * 2 - 1).t() for m, n, k in sizes]
-    Bs = [(torch.rand((n, k), dtype=torch.float64, device="cuda") * 2 - 1).t() for m, n, k in sizes]
-    Cs = [torch.empty((n, m), dtype=torch.float64, device="cuda").t() for m, n, k in sizes]
+    As = [(torch.rand((k, m), dtype=dtype, device="cuda") * 2 - 1).t() for m, n, k in sizes]
+    Bs = [(torch.rand((n, k), dtype=dtype, device="cuda") * 2 - 1).t() for m, n, k in sizes]
+    Cs = [torch.empty((n, m), dtype=dtype, device="cuda").t() for m, n, k in sizes]
     plan = grouped.GroupedGemm(As, Bs, Cs)
+    if tuning is not None:
+        for i, c in enumerate(tuning):
+            plan.tuning.config[i] = c
     return _timed(plan.run)
 
 
@@ -86,6 +90,7 @@ CASES = {
     "ozaki": case_ozaki,
     "ozaki_crt": case_ozaki_crt,
     "grouped_f64": case_grouped,
+    "grouped_f32": lambda: case_grouped(torch.float32, [0, 0, 1, 1, 3, 5]),
     "adjoint": case_adjoint,
 }
 
