@@ -87,7 +87,29 @@ __device__ __forceinline__ void grouped_tile(const gb_problem_t& p, int tm, int 
 #pragma unroll
     for (int j = 0; j < TN; ++j) acc[i][j] = T(-0.0);
 
-  const int64_t Kc = (p.alpha == 0.0) ? 0 : K;   // alpha == 0: A and B are not read
+  // alpha and beta decoded once per warp (FP64 compares and conversions run on the narrow
+  // FP64 pipe) and broadcast
+  T alpha, beta;
+  bool alpha_zero;
+  {
+    const int lane = threadIdx.x & 31;
+    float2 ab = make_float2(0.0f, 0.0f);
+    double ad = 0.0, bd = 0.0;
+    if (sizeof(T) == 8) {
+      ad = p.alpha;
+      bd = p.beta;
+    } else if (lane == 0) {
+      ab = make_float2(static_cast<float>(p.alpha), static_cast<float>(p.beta));
+    }
+    if (sizeof(T) == 4) {
+      ab.x = __shfl_sync(0xffffffffu, ab.x, 0);
+      ab.y = __shfl_sync(0xffffffffu, ab.y, 0);
+    }
+    alpha = (sizeof(T) == 8) ? static_cast<T>(ad) : static_cast<T>(ab.x);
+    beta = (sizeof(T) == 8) ? static_cast<T>(bd) : static_cast<T>(ab.y);
+    alpha_zero = ((__double_as_longlong(p.alpha) & 0x7FFFFFFFFFFFFFFFll) == 0);
+  }
+  const int64_t Kc = alpha_zero ? 0 : K;   // alpha == 0: A and B are not read
   T ra[LA], rb[LB];
   auto load = [&](int64_t k0) {
 #pragma unroll
@@ -133,7 +155,6 @@ __device__ __forceinline__ void grouped_tile(const gb_problem_t& p, int tm, int 
     }
     __syncthreads();
   }
-  const T alpha = static_cast<T>(p.alpha), beta = static_cast<T>(p.beta);
   T* __restrict__ C = static_cast<T*>(p.C);
 #pragma unroll
   for (int i = 0; i < TM; ++i) {

@@ -8,10 +8,14 @@ namespace gb {
 
 constexpr int OZ_EXP_NONFINITE = 0x7FFFFFFF;
 
+// Row exponent e with amax < 2^e (e = ilogb(amax) + 1), from the IEEE fields in integer
+// arithmetic (GB300's FP64 pipe is narrow): biased exponent - 1022 for normal amax,
+// -1010 - clz(bits) for subnormal amax.
 __device__ __forceinline__ int row_exponent_of(unsigned long long amax_bits) {
   if (amax_bits >= 0x7FF0000000000000ull) return OZ_EXP_NONFINITE;  // Inf or NaN in the row
   if (amax_bits == 0) return 0;
-  return ilogb(__longlong_as_double(static_cast<long long>(amax_bits))) + 1;  // amax < 2^e
+  const int ex = static_cast<int>(amax_bits >> 52);
+  return ex ? ex - 1022 : -1010 - __clzll(static_cast<long long>(amax_bits));
 }
 
 __device__ __forceinline__ int row_exponent(unsigned long long amax_bits) { return row_exponent_of(amax_bits); }
