@@ -61,13 +61,14 @@ int gb_version(void);
  * GB_ERR_PIPELINE_TIMEOUT on a later gb_check_status(). */
 int gb_set_wait_limit_ns(uint64_t ns);
 
-/* Normwise tolerance the automatic Ozaki slice count must meet (slices = 0); 0 restores
+/* Normwise tolerance the automatic Ozaki slice or moduli count must meet (slices = 0); 0 restores
  * the default 2^-50. */
 int gb_set_ozaki_tolerance(double tol);
 
-/* Tensor-core engine for the Ozaki and adjoint products: 0 = automatic (CTA pairs),
- * 1 = one CTA per 128 x 256 tile, 2 = CTA pairs on 256 x 256 tiles (tcgen05 cta_group::2,
- * half of B per SM).  Ozaki results are identical under both engines. */
+/* Tensor-core engine for the Ozaki slice-mode and adjoint products: 0 = automatic (CTA
+ * pairs), 1 = one CTA per 128 x 256 tile, 2 = CTA pairs on 256 x 256 tiles (tcgen05
+ * cta_group::2, half of B per SM).  Ozaki results are identical under both engines.  The
+ * CRT mode always runs on CTA pairs. */
 int gb_set_tc_engine(int engine);
 
 /* K chunking used by OZAKI calls with an explicit slice count: K is cut into at least
@@ -132,13 +133,15 @@ int gb_jmul_f32(float* D, const float* A, const float* X, int64_t M, int64_t N, 
  * mode GB_MODE_OZAKI_CRT: rows of op(A) and columns of op(B) are scaled by powers of two
  *   and rounded (half away from zero) to integers of t bits; their product is formed
  *   exactly from `slices` residue products (one BF16 tcgen05 GEMM per modulus, moduli
- *   <= 256, exact FP32 sums) and the Chinese remainder theorem, then rounded once to
+ *   <= 253, exact FP32 sums) and the Chinese remainder theorem, then rounded once to
  *   FP64 and rescaled.  slices = number of moduli (1..20; t follows from K, see
  *   gb_plan_ozaki_crt); slices = 0 picks the fewest moduli whose bound meets the
  *   library tolerance (t then also uses the operands' row sums).  Inf/NaN as for BF16.
- * err_bound_out (host pointer, may be NULL): for OZAKI, an a-priori bound on
- *   ||C - C_exact||_F / (|alpha| ||A||_F ||B||_F) from the slicing truncation;
- *   the call then synchronises `stream` to read the split statistics.  For NATIVE it
+ * err_bound_out (host pointer, may be NULL): for OZAKI_BF16 / OZAKI_CRT, an a-priori bound
+ *   on ||C - C_exact||_F / (|alpha| ||A||_F ||B||_F) from the truncation of the operands;
+ *   the call then synchronises `stream` to read it.  Without it an OZAKI_CRT call never
+ *   synchronises (its plan is chosen on the device) and can be captured in a CUDA graph;
+ *   OZAKI_BF16 with slices = 0 synchronises once to read the split statistics.  For NATIVE it
  *   receives the standard bound K*u/(1-K*u) (u = 2^-53) of the same quantity. */
 int gb_gemm_f64(int transA, int transB, int64_t M, int64_t N, int64_t K, double alpha,
                 const double* A, int64_t lda, const double* B, int64_t ldb, double beta,
