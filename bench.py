@@ -42,7 +42,7 @@ METRIC = "FP64-accurate GEMM TFLOP/s, Ozaki split vs native FP64 on GB300 at sta
 def parse_args():
     p = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["gbblas", "reference"], default="gbblas")
     p.add_argument("--size", type=int, default=8192)
@@ -466,13 +466,20 @@ def main():
     up_stream.wait_stream(stream)
     down_stream.wait_stream(stream)
 
+    up_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+             for _ in range(args.steps)]
+    down_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(args.steps)]
+
     def upload(i):
         b = i % 2
         with torch.cuda.stream(up_stream):
             if i >= 2:
                 up_stream.wait_event(comp_done[b])       # buffer b's previous compute is done
+            up_ev[i][0].record(up_stream)
             A_e[b].copy_(A_pin, non_blocking=True)
             B_e[b].copy_(B_pin, non_blocking=True)
+            up_ev[i][1].record(up_stream)
             up_done[b].record(up_stream)
 
     pipe_prof = gbblas.profile()
@@ -491,7 +498,9 @@ def main():
         comp_done[b].record(stream)
         with torch.cuda.stream(down_stream):
             down_stream.wait_event(comp_done[b])
+            down_ev[i][0].record(down_stream)
             C_pin.copy_(C_e[b], non_blocking=True)
+            down_ev[i][1].record(down_stream)
             down_done[b].record(down_stream)
     stream.wait_stream(up_stream)
     stream.wait_stream(down_stream)
@@ -502,6 +511,8 @@ def main():
     ms_e2e = max_over_ranks(e0.elapsed_time(e1) / args.steps)
     e2e_value = world * flops / (ms_e2e * 1e-3) / 1e12
     comp_in_pipeline = statistics.median(a.elapsed_time(z) for a, z in comp_ev)
+    up_in_pipeline = statistics.median(a.elapsed_time(z) for a, z in up_ev)
+    down_in_pipeline = statistics.median(a.elapsed_time(z) for a, z in down_ev)
     copy_stream = up_stream
 
     # the host link alone: one step's uploads and download on the copy stream, no compute
@@ -614,6 +625,7 @@ def main():
                     "pipeline": "double-buffered: uploads of step i+1 and download of step i overlap step i",
                     "h2d_GBps": h2d_gbs, "d2h_GBps": d2h_gbs,
                     "compute_ms_in_pipeline": comp_in_pipeline,
+                    "upload_ms_in_pipeline": up_in_pipeline, "download_ms_in_pipeline": down_in_pipeline,
                     "kernel_ms_in_pipeline": {k: v / args.steps for k, v in pipe_prof.ms.items()},
                     "h2d_bytes_per_step": int(A_pin.numel() * 8 + B_pin.numel() * 8),
                     "d2h_bytes_per_step": int(C_pin.numel() * 8)},
