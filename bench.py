@@ -231,6 +231,39 @@ def _side_line(args, metric, value, unit, ms, config, extra):
     print(json.dumps(line), flush=True)
 
 
+def _native_sample_error(A, B, alpha, beta, dt, samples=1024):
+    """Errors of one fresh call C = alpha A B + beta C0 against Dot2 on sampled entries:
+    normwise ||dC|| sqrt(MN/s) / (|alpha| ||A||_F ||B||_F + |beta| ||C0||_F) and componentwise
+    max |dC|_ij / (|alpha| (|A||B|)_ij + |beta| |C0|_ij) (FP64 references for both dtypes)."""
+    import torch
+    import gbblas
+    import oracle
+    M, K = A.shape
+    N = B.shape[1]
+    g = np.random.default_rng(M + 3 * N + 7 * K)
+    rows, cols = g.integers(0, M, samples), g.integers(0, N, samples)
+    C0 = (torch.rand((N, M), dtype=dt, device=A.device) * 2 - 1).t()
+    C1 = C0.clone()
+    gbblas.gemm_(C1, A, B, alpha, beta)
+    torch.cuda.synchronize()
+    ri, ci = torch.from_numpy(rows).to(A.device), torch.from_numpy(cols).to(A.device)
+    As = np.asfortranarray(A[ri, :].double().cpu().numpy())
+    Bs = np.asfortranarray(B[:, ci].double().cpu().numpy())
+    idx = np.arange(samples)
+    hi, lo, ab = oracle.dot2_entries(As, Bs, idx, idx)
+    c0 = C0[ri, ci].double().cpu().numpy()
+    got = C1[ri, ci].double().cpu().numpy()
+    d = np.abs((got - alpha * hi) - (alpha * lo + beta * c0))
+    na = float(torch.linalg.norm(A.double()))
+    nb = float(torch.linalg.norm(B.double()))
+    nc = float(torch.linalg.norm(C0.double()))
+    normwise = float(np.linalg.norm(d) * np.sqrt(M * N / samples) / (abs(alpha) * na * nb + abs(beta) * nc))
+    den = abs(alpha) * ab + abs(beta) * np.abs(c0)
+    ok = den > 0
+    comp = float(np.max(d[ok] / den[ok])) if ok.any() else 0.0
+    return {"normwise_err": normwise, "componentwise_err": comp}
+
+
 def workload_native(args):
     """Config-2 sweep: native FP64 / FP32 GEMM, alpha = 1.5, beta = 0.5, uniform[-1, 1)."""
     import torch
@@ -252,8 +285,9 @@ def workload_native(args):
             gbblas.gemm_(C, A, B, 1.5, 0.5)
             torch.cuda.synchronize()
             ms = _event_ms(lambda: gbblas.gemm_(C, A, B, 1.5, 0.5), steps, stream)
+            err = _native_sample_error(A, B, 1.5, 0.5, dt)
             rows.append({"dtype": str(dt).replace("torch.", ""), "M": M, "N": N, "K": K, "ms": ms,
-                         "tflops": 2.0 * M * N * K / (ms * 1e-3) / 1e12})
+                         "tflops": 2.0 * M * N * K / (ms * 1e-3) / 1e12, **err})
             del A, B, C
     f64 = [r for r in rows if r["dtype"] == "float64" and r["M"] == r["N"] == r["K"] == 8192][0]
     _side_line(args, "native FP64 GEMM TFLOP/s (CUDA cores, jmul! FMA order)", f64["tflops"], "TFLOP/s",
