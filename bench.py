@@ -55,9 +55,9 @@ def parse_args():
     p.add_argument("--no-native", action="store_true", help="skip the native FP64 comparison")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU sample")
-    p.add_argument("--workload", choices=["ozaki", "native", "grouped", "adjoint"], default="ozaki",
+    p.add_argument("--workload", choices=["ozaki", "native", "grouped", "adjoint", "semiring"], default="ozaki",
                    help="ozaki: the headline (default); native: FP64/FP32 sweep; grouped: 4096 uneven "
-                        "problems; adjoint: fused dA/dB")
+                        "problems; adjoint: fused dA/dB; semiring: (min, +) and relatives")
     return p.parse_args()
 
 
@@ -300,6 +300,82 @@ def workload_native(args):
     return 0
 
 
+# Instructions per output element and k of each semiring's mainloop step, and the share of
+# them on the 64-lane min/max (ALU) pipe; the rest (add, mul) issue on the 128-lane FMA pipe.
+# Paired steps fold two k into one three-input min/max (float: all; int32: max-min, min-max).
+_SR_INSTR = {("float32", "min_plus"): (1.5, 0.5), ("float32", "max_plus"): (1.5, 0.5),
+             ("float32", "max_times"): (1.5, 0.5), ("float32", "max_min"): (1.5, 1.5),
+             ("float32", "min_max"): (1.5, 1.5), ("int32", "max_min"): (1.5, 1.5),
+             ("int32", "min_max"): (1.5, 1.5)}
+
+
+def _sr_bound(dtype, sr, sms, mhz):
+    """Issue bound in 1e12 semiring multiply-adds (M N K) per second: each SM issues 4 x 32
+    lanes per clock, and min/max run on a 64-lane pipe."""
+    if dtype == "float64":
+        return None
+    instr, alu = _SR_INSTR.get((dtype, sr), (2.0, 1.0))
+    per_clk = min(128.0 / instr, 64.0 / alu)
+    return sms * per_clk * mhz * 1e6 / 1e12
+
+
+def workload_semiring(args):
+    """Semiring GEMM sweep (no counterpart in the reference's code; jBLAS names min-plus algebra
+    as the use of its Vec fallback, src/jBLAS.jl:10): every semiring in float32 and int32 at
+    8192^3 and float64 at 4096^3, A, B uniform, each checked bit for bit against the oracle on
+    32 x 32 sampled outputs."""
+    import torch
+    import gbblas
+    import oracle
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev)
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    clocks = ClockSampler(0)
+    rows = []
+    clocks.start()
+    for dt, n in ((torch.float32, 8192), (torch.int32, 8192), (torch.float64, 4096)):
+        if dt == torch.int32:
+            A = torch.randint(-10**6, 10**6, (n, n), dtype=dt, device=dev).t()
+            B = torch.randint(-10**6, 10**6, (n, n), dtype=dt, device=dev).t()
+        else:
+            A = (torch.rand((n, n), dtype=dt, device=dev) * 200 - 100).t()
+            B = (torch.rand((n, n), dtype=dt, device=dev) * 200 - 100).t()
+        C = torch.empty((n, n), dtype=dt, device=dev).t()
+        g = np.random.default_rng(n)
+        ri = np.sort(g.choice(n, 32, replace=False))
+        ci = np.sort(g.choice(n, 32, replace=False))
+        As = np.asfortranarray(A[torch.as_tensor(ri, device=dev), :].cpu().numpy())
+        Bs = np.asfortranarray(B[:, torch.as_tensor(ci, device=dev)].cpu().numpy())
+        steps = max(1, min(args.steps, 3)) if dt == torch.float64 else args.steps
+        for sr in ("min_plus", "max_plus", "max_min", "min_max", "max_times"):
+            gbblas.gemm_semiring_(C, A, B, sr)
+            torch.cuda.synchronize()
+            ms = _event_ms(lambda: gbblas.gemm_semiring_(C, A, B, sr), steps, stream)
+            got = C[torch.as_tensor(ri, device=dev)][:, torch.as_tensor(ci, device=dev)].cpu().numpy()
+            ref = oracle.semiring_gemm(As, Bs, sr, dtype=As.dtype)
+            same = bool(np.array_equal(got, ref))
+            rows.append({"dtype": str(dt).replace("torch.", ""), "semiring": sr, "n": n, "ms": ms,
+                         "tera_mnk_per_s": n ** 3 / (ms * 1e-3) / 1e12, "sampled_bit_exact": same})
+        del A, B, C
+    clk = clocks.stop() or {}
+    mhz = clk.get("sm_mhz") or 2070.0
+    for r in rows:
+        bound = _sr_bound(r["dtype"], r["semiring"], sms, mhz)
+        r["issue_bound"] = bound
+        r["frac"] = r["tera_mnk_per_s"] / bound if bound else None
+    head = [r for r in rows if r["dtype"] == "float32" and r["semiring"] == "min_plus"][0]
+    _side_line(args, "semiring GEMM 1e12 (min,+) multiply-adds/s, float32 8192^3", head["tera_mnk_per_s"],
+               "T(min,+)/s", head["ms"],
+               {"workload": "semiring_gemm_sweep", "inputs": "uniform [-100, 100) / int32 [-1e6, 1e6)",
+                "headline_shape": "f32 min_plus 8192^3"},
+               {"dtype": "f32", "sweep": rows, "clocks": clk,
+                "roofline": {"bound": "issue", "achieved": head["tera_mnk_per_s"], "peak": head["issue_bound"],
+                             "unit": "T(min,+)/s", "frac": head["frac"],
+                             "peak_source": "%d SMs x 128 lanes/clk / 1.5 instructions per element x %.0f MHz "
+                                            "(median SM clock sampled during the sweep)" % (sms, mhz)}})
+    return 0
+
+
 def workload_grouped(args):
     """Config 4: 4096 problems, m, n, k log-uniform in [8, 512], one persistent grouped launch in a
     CUDA graph with autotuned tiles, against a loop of plain per-problem launches."""
@@ -407,7 +483,8 @@ def main():
         import __graft_entry__  # noqa: F401  (path setup only)
         if rank != 0:
             return 0
-        return {"native": workload_native, "grouped": workload_grouped, "adjoint": workload_adjoint}[args.workload](args)
+        return {"native": workload_native, "grouped": workload_grouped, "adjoint": workload_adjoint,
+                "semiring": workload_semiring}[args.workload](args)
 
     import torch
     import gbblas

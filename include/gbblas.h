@@ -97,6 +97,7 @@ typedef enum {
   GB_KERNEL_ADJOINT_SPLIT = 6,
   GB_KERNEL_ADJOINT_MMA = 7,
   GB_KERNEL_OZAKI_COMBINE = 8,   /* CRT reconstruction of the residue products */
+  GB_KERNEL_SEMIRING_GEMM = 9,
   GB_KERNEL_KINDS = 16
 } gb_kernel_kind_t;
 const char* gb_kernel_kind_name(int kind);
@@ -216,6 +217,37 @@ int gb_gemm_strided_batched_f64(int64_t M, int64_t N, int64_t K, double alpha, c
 int gb_gemm_strided_batched_f32(int64_t M, int64_t N, int64_t K, float alpha, const float* A, int64_t lda,
                                 int64_t strideA, const float* B, int64_t ldb, int64_t strideB, float beta,
                                 float* C, int64_t ldc, int64_t strideC, int64_t count, void* stream);
+
+/* ------------------------------------------------------------------ semiring GEMM */
+/* C = [C (+)] (+)_k op(A)[i,k] (x) op(B)[k,j] over a semiring ((+), (x)) instead of
+ * (+, *).  No counterpart in the reference's code: jBLAS keeps its tuple-SIMD Vec type
+ * (src/simd.jl) out of the module with the note "Maybe use that as a fallback for custom
+ * number types? Eg, so it works with min-plus algebra?" (src/jBLAS.jl:10).  Same layout,
+ * transposes and register-blocked CUDA-core mainloop as gb_gemm_* NATIVE.
+ *   (+) = min or max; for floating point a NaN operand is ignored (IEEE minNum/maxNum:
+ *         the result is NaN only when every candidate is NaN), and a zero result is
+ *         returned as +0.0, so the result does not depend on the K order;
+ *   (x) = +, *, min or max, rounded once (round to nearest); int32 + and * wrap modulo 2^32.
+ * accumulate = 0: C = (+)_k ...; the empty K gives the identity of (+) (+Inf / -Inf,
+ * INT32_MAX / INT32_MIN).  accumulate = 1: C is read and folded in with (+).
+ * Errors as gb_gemm_*: GB_ERR_INVALID_VALUE for an unknown semiring or accumulate flag. */
+typedef enum {
+  GB_SEMIRING_MIN_PLUS = 0,    /* (min, +): shortest paths (tropical) */
+  GB_SEMIRING_MAX_PLUS = 1,    /* (max, +): longest / critical paths, log-space Viterbi */
+  GB_SEMIRING_MAX_MIN = 2,     /* (max, min): widest (bottleneck) paths */
+  GB_SEMIRING_MIN_MAX = 3,     /* (min, max): minimax paths */
+  GB_SEMIRING_MAX_TIMES = 4,   /* (max, *): Viterbi on probabilities */
+  GB_SEMIRINGS = 5
+} gb_semiring_t;
+int gb_gemm_semiring_f64(int semiring, int transA, int transB, int64_t M, int64_t N, int64_t K,
+                         const double* A, int64_t lda, const double* B, int64_t ldb, int accumulate,
+                         double* C, int64_t ldc, void* stream);
+int gb_gemm_semiring_f32(int semiring, int transA, int transB, int64_t M, int64_t N, int64_t K,
+                         const float* A, int64_t lda, const float* B, int64_t ldb, int accumulate,
+                         float* C, int64_t ldc, void* stream);
+int gb_gemm_semiring_i32(int semiring, int transA, int transB, int64_t M, int64_t N, int64_t K,
+                         const int32_t* A, int64_t lda, const int32_t* B, int64_t ldb, int accumulate,
+                         int32_t* C, int64_t ldc, void* stream);
 /* Autotuner: times every configuration per size class on the given problems (HOST copy
  * of the table; their C buffers are left untouched, results go to scratch) with `reps`
  * timed repetitions and writes the fastest configuration per class; class_ms (may be

@@ -20,6 +20,7 @@
 #include "grouped.cuh"
 #include "native_gemm.cuh"
 #include "ozaki.cuh"
+#include "semiring.cuh"
 #include "tc_gemm.cuh"
 
 namespace gb {
@@ -612,6 +613,19 @@ static int resolve_pending_crt_plan() {
 using namespace gb;
 
 // ====================================================================== C ABI
+// Semiring GEMM entry points: argument checks as gb_gemm_*, then the typed launcher.
+template <typename T, typename Fn>
+static int semiring_entry(Fn fn, int sr, int ta, int tb, int64_t M, int64_t N, int64_t K, const T* A, int64_t lda,
+                          const T* B, int64_t ldb, int accumulate, T* C, int64_t ldc, void* stream) {
+  DeviceInfo* dev = nullptr;
+  int rc = device_info(&dev);
+  if (rc) return rc;
+  if (sr < 0 || sr >= GB_SEMIRINGS || (accumulate != 0 && accumulate != 1)) return GB_ERR_INVALID_VALUE;
+  rc = check_gemm_args(ta, tb, M, N, K, lda, ldb, ldc, A, B, C, true);
+  if (rc || M == 0 || N == 0) return rc;
+  return fn(sr, ta, tb, M, N, K, A, lda, B, ldb, accumulate, C, ldc, static_cast<cudaStream_t>(stream));
+}
+
 extern "C" {
 
 const char* gb_status_string(int status) {
@@ -842,6 +856,27 @@ int gb_gemm_strided_batched_f32(int64_t M, int64_t N, int64_t K, float alpha, co
                                 int64_t strideA, const float* B, int64_t ldb, int64_t strideB, float beta,
                                 float* C, int64_t ldc, int64_t strideC, int64_t count, void* stream) {
   return strided_batched(4, M, N, K, alpha, A, lda, strideA, B, ldb, strideB, beta, C, ldc, strideC, count, stream);
+}
+
+int gb_gemm_semiring_f64(int semiring, int transA, int transB, int64_t M, int64_t N, int64_t K, const double* A,
+                         int64_t lda, const double* B, int64_t ldb, int accumulate, double* C, int64_t ldc,
+                         void* stream) {
+  return semiring_entry(semiring_gemm_f64, semiring, transA, transB, M, N, K, A, lda, B, ldb, accumulate, C, ldc,
+                        stream);
+}
+
+int gb_gemm_semiring_f32(int semiring, int transA, int transB, int64_t M, int64_t N, int64_t K, const float* A,
+                         int64_t lda, const float* B, int64_t ldb, int accumulate, float* C, int64_t ldc,
+                         void* stream) {
+  return semiring_entry(semiring_gemm_f32, semiring, transA, transB, M, N, K, A, lda, B, ldb, accumulate, C, ldc,
+                        stream);
+}
+
+int gb_gemm_semiring_i32(int semiring, int transA, int transB, int64_t M, int64_t N, int64_t K, const int32_t* A,
+                         int64_t lda, const int32_t* B, int64_t ldb, int accumulate, int32_t* C, int64_t ldc,
+                         void* stream) {
+  return semiring_entry(semiring_gemm_i32, semiring, transA, transB, M, N, K, A, lda, B, ldb, accumulate, C, ldc,
+                        stream);
 }
 
 int gb_autotune_grouped(int dtype_bytes, const gb_problem_t* host_problems, int count, int reps,

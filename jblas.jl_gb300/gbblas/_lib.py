@@ -22,6 +22,8 @@ MODE_OZAKI_BF16 = 1
 MODE_OZAKI_INT8 = 2
 MODE_OZAKI_CRT = 3
 
+SEMIRINGS = {"min_plus": 0, "max_plus": 1, "max_min": 2, "min_max": 3, "max_times": 4}
+
 c_i64 = ctypes.c_int64
 c_int = ctypes.c_int
 c_vp = ctypes.c_void_p
@@ -89,6 +91,12 @@ SIGNATURES = {
                                             c_i64, ctypes.c_double, c_vp, c_i64, c_i64, c_i64, c_vp]),
     "gb_gemm_strided_batched_f32": (c_int, [c_i64, c_i64, c_i64, ctypes.c_float, c_vp, c_i64, c_i64, c_vp, c_i64,
                                             c_i64, ctypes.c_float, c_vp, c_i64, c_i64, c_i64, c_vp]),
+    "gb_gemm_semiring_f64": (c_int, [c_int, c_int, c_int, c_i64, c_i64, c_i64, c_vp, c_i64, c_vp, c_i64, c_int,
+                                     c_vp, c_i64, c_vp]),
+    "gb_gemm_semiring_f32": (c_int, [c_int, c_int, c_int, c_i64, c_i64, c_i64, c_vp, c_i64, c_vp, c_i64, c_int,
+                                     c_vp, c_i64, c_vp]),
+    "gb_gemm_semiring_i32": (c_int, [c_int, c_int, c_int, c_i64, c_i64, c_i64, c_vp, c_i64, c_vp, c_i64, c_int,
+                                     c_vp, c_i64, c_vp]),
     "gb_gemm_grouped_f64": (c_int, [c_vp, c_int, ctypes.POINTER(Tuning), c_vp, ctypes.c_size_t, c_vp]),
     "gb_gemm_grouped_f32": (c_int, [c_vp, c_int, ctypes.POINTER(Tuning), c_vp, ctypes.c_size_t, c_vp]),
     "gb_gemm_grouped_f64_noalloc": (c_int, [c_vp, c_int, ctypes.POINTER(Tuning), c_vp]),

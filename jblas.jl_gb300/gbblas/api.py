@@ -148,6 +148,54 @@ def gemm_strided_batched_(C, A, B, alpha=1.0, beta=0.0):
     return C
 
 
+_SEMIRING_FN = {torch.float64: "gb_gemm_semiring_f64", torch.float32: "gb_gemm_semiring_f32",
+                torch.int32: "gb_gemm_semiring_i32"}
+
+
+def gemm_semiring_(C, A, B, semiring="min_plus", accumulate=False):
+    """C = [C (+)] (+)_k A[:, k] (x) B[k, :] over a semiring, in place; returns C.
+
+    semiring: "min_plus" (shortest paths), "max_plus", "max_min" (widest paths), "min_max"
+    or "max_times"; (+) is the first operation, (x) the second.  float64, float32 or int32
+    CUDA tensors of one dtype.  For floating point (+) ignores NaN operands and a zero result
+    is +0.0; int32 + and * wrap modulo 2^32.  accumulate=False overwrites C (an empty
+    contraction gives the identity of (+)); accumulate=True folds C in with (+).  jBLAS names
+    min-plus algebra as the use of its Vec fallback (src/jBLAS.jl:10).
+    """
+    dt = C.dtype
+    if A.dtype != dt or B.dtype != dt:
+        raise TypeError("all operands must share one dtype, got %s, %s, %s" % (A.dtype, B.dtype, dt))
+    if dt not in _SEMIRING_FN:
+        raise TypeError("semiring GEMM computes in float64, float32 or int32, got %s" % dt)
+    if semiring not in _lib.SEMIRINGS:
+        raise ValueError("unknown semiring %r (one of %s)" % (semiring, ", ".join(_lib.SEMIRINGS)))
+    M, K = A.shape
+    K2, N = B.shape
+    if K2 != K or tuple(C.shape) != (M, N):
+        raise DimensionMismatch("A is %dx%d, B is %dx%d, C is %dx%d" % (M, K, K2, N, *C.shape))
+    Cs, ldc, tc = _storage(C, "C", allow_copy=False)
+    As, lda, ta = _storage(A, "A", allow_copy=True)
+    Bs, ldb, tb = _storage(B, "B", allow_copy=True)
+    fn = getattr(_lib.lib(), _SEMIRING_FN[dt])
+    sr = _lib.SEMIRINGS[semiring]
+    st = _stream_ptr(C)
+    if tc == 0:
+        rc = fn(sr, ta, tb, M, N, K, ctypes.c_void_p(As.data_ptr()), lda, ctypes.c_void_p(Bs.data_ptr()), ldb,
+                int(bool(accumulate)), ctypes.c_void_p(Cs.data_ptr()), ldc, st)
+    else:
+        # C stored row-major: C^T = B^T (x) A^T ((x) is commutative in every semiring offered)
+        rc = fn(sr, 1 - tb, 1 - ta, N, M, K, ctypes.c_void_p(Bs.data_ptr()), ldb, ctypes.c_void_p(As.data_ptr()),
+                lda, int(bool(accumulate)), ctypes.c_void_p(Cs.data_ptr()), ldc, st)
+    check(rc, _SEMIRING_FN[dt])
+    return C
+
+
+def gemm_semiring(A, B, semiring="min_plus"):
+    """Allocating form of gemm_semiring_: a new column-major M x N result."""
+    C = torch.empty((B.shape[1], A.shape[0]), dtype=A.dtype, device=A.device).t()
+    return gemm_semiring_(C, A, B, semiring)
+
+
 def gemm(A, B, *, mode="native", slices=0):
     """Allocating form: returns A @ B as a new column-major tensor."""
     dt = _dtype_of(A, B)

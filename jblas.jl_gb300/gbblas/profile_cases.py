@@ -15,6 +15,7 @@ cases:
   grouped_f64    gb_gemm_grouped_f64, 4096 problems with m, n, k log-uniform in [8, 512]
   grouped_f32    the same problems in FP32 (tuned configuration of the bench)
   adjoint        gb_gemm_adjoint_f32, A 4096 x 2048, B 2048 x 4096
+  semiring_f32   gb_gemm_semiring_f32 (min, +), 4096^3
 """
 import sys
 
@@ -84,6 +85,14 @@ def case_adjoint():
     return _timed(lambda: api.gemm_adjoint_(dA, dB, A, B, W))
 
 
+def case_semiring():
+    n = 4096
+    A = (torch.rand((n, n), device="cuda") * 200 - 100).t()
+    B = (torch.rand((n, n), device="cuda") * 200 - 100).t()
+    C = torch.empty((n, n), device="cuda").t()
+    return _timed(lambda: api.gemm_semiring_(C, A, B, "min_plus"))
+
+
 CASES = {
     "native_f64": lambda: case_native(torch.float64, 4096),
     "native_f32": lambda: case_native(torch.float32, 4096),
@@ -92,6 +101,7 @@ CASES = {
     "grouped_f64": case_grouped,
     "grouped_f32": lambda: case_grouped(torch.float32, [0, 0, 1, 1, 3, 5]),
     "adjoint": case_adjoint,
+    "semiring_f32": case_semiring,
 }
 
 

@@ -12,6 +12,8 @@ layer over the C ABI in `include/gbblas.h`:
                                          transpose/adjoint views (real element types)
     enable_mul!(T)                       routes LinearAlgebra.mul! for device matrix type T here
     gemm_strided_batched!(C, A, B, α, β) C[:,:,i] = α A[:,:,i] B[:,:,i] + β C[:,:,i]
+    semiring_mul!(C, A, B, semiring; accumulate)   C = [C ⊕] A ⊗ B over (min,+), (max,+),
+                                         (max,min), (min,max) or (max,*) (Float64/Float32/Int32)
     ChainRulesCore.rrule(::typeof(gemm), A, B)   pullback through gemm_adjoint!
 
 Matrices are device arrays (anything with `pointer` to CUDA device memory and a column-
@@ -173,6 +175,34 @@ for (T, f) in ((Float64, :gb_gemm_strided_batched_f64), (Float32, :gb_gemm_strid
                      Int64, Ptr{Cvoid}),
                     M, N, K, $T(α), pointer(A), max(1, stride(A, 2)), stride(A, 3), pointer(B), max(1, stride(B, 2)),
                     stride(B, 3), $T(β), pointer(C), max(1, stride(C, 2)), stride(C, 3), n, current_stream()))
+        C
+    end
+end
+
+const SEMIRING = Dict(:min_plus => Cint(0), :max_plus => Cint(1), :max_min => Cint(2), :min_max => Cint(3),
+                     :max_times => Cint(4))
+
+"""
+    semiring_mul!(C, A, B, semiring=:min_plus; accumulate=false) -> C
+
+`C[i,j] = ⊕_k A[i,k] ⊗ B[k,j]` (or `C[i,j] ⊕ ...` with `accumulate`) over the semiring
+`semiring` ∈ `:min_plus`, `:max_plus`, `:max_min`, `:min_max`, `:max_times` (⊕ first), the
+custom-number-type use jBLAS gives for its `Vec` fallback ("so it works with min-plus
+algebra", src/jBLAS.jl:10).  `A` and `B` may be transpose/adjoint views.  Floating point: ⊕
+ignores NaN operands and a zero result is +0.0; Int32 + and * wrap.
+"""
+for (T, f) in ((Float64, :gb_gemm_semiring_f64), (Float32, :gb_gemm_semiring_f32), (Int32, :gb_gemm_semiring_i32))
+    @eval function semiring_mul!(C::AbstractMatrix{$T}, A::AbstractMatrix{$T}, B::AbstractMatrix{$T},
+                                 semiring::Symbol = :min_plus; accumulate::Bool = false)
+        M, K = size(A); N = size(B, 2)
+        size(B, 1) == K && size(C) == (M, N) ||
+            throw(DimensionMismatch("semiring_mul!: $(size(C)) = $(size(A)) ⊗ $(size(B))"))
+        As, Bs = storage(A), storage(B)
+        check(ccall(($(QuoteNode(f)), libgbblas), Cint,
+                    (Cint, Cint, Cint, Int64, Int64, Int64, Ptr{$T}, Int64, Ptr{$T}, Int64, Cint, Ptr{$T}, Int64,
+                     Ptr{Cvoid}),
+                    SEMIRING[semiring], op_flag(A), op_flag(B), M, N, K, pointer(As), ld(As), pointer(Bs), ld(Bs),
+                    Cint(accumulate), pointer(C), ld(C), current_stream()))
         C
     end
 end

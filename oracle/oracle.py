@@ -16,7 +16,13 @@ restatements here are pinned against each other instead:
   * ``dot2_entries``         compensated dot products (Ogita-Rump-Oishi Dot2) for
                              near-exact values at sampled entries of large products;
   * ``ozaki_*``              numpy restatement of the Ozaki splitting and recombination
-                             the GPU kernel performs, operation for operation.
+                             the GPU kernel performs, operation for operation;
+  * ``semiring_gemm``        numpy restatement of the semiring product ((min, +) and its
+                             relatives, the use jBLAS names for its Vec fallback,
+                             src/jBLAS.jl:10), checked against ``semiring_gemm_reduce``
+                             (a K-axis reduction of the full product tensor, another
+                             order) and, for (min, +), against Floyd-Warshall distances
+                             computed with Python integers (``floyd_warshall``).
 """
 import ctypes
 import math
@@ -432,3 +438,84 @@ def ozaki_crt_gemm(A, B, C=None, alpha=1.0, beta=0.0, moduli=16, bits=0):
     else:
         out = fma(np.full_like(val, alpha), val, beta * np.asarray(C, dtype=np.float64))
     return np.asfortranarray(out)
+
+
+# ---------------------------------------------------------------------------- semirings
+SEMIRINGS = ("min_plus", "max_plus", "max_min", "min_max", "max_times")
+
+
+def _semiring_ops(semiring, dtype):
+    """(oplus, otimes, identity of oplus) for one semiring and element type.
+
+    Floating point: oplus is min/max ignoring NaN operands (np.fmin / np.fmax); otimes
+    is +, *, or the same NaN-ignoring min/max, rounded to nearest in `dtype`.  int32:
+    + and * wrap modulo 2^32 (numpy array arithmetic), min/max are exact."""
+    if semiring not in SEMIRINGS:
+        raise ValueError("unknown semiring %r" % (semiring,))
+    is_int = np.issubdtype(dtype, np.integer)
+    mn = np.minimum if is_int else np.fmin
+    mx = np.maximum if is_int else np.fmax
+    if semiring in ("min_plus", "min_max"):
+        oplus, ident = mn, (np.iinfo(dtype).max if is_int else np.inf)
+    else:
+        oplus, ident = mx, (np.iinfo(dtype).min if is_int else -np.inf)
+    otimes = {"min_plus": np.add, "max_plus": np.add, "max_min": mn, "min_max": mx,
+              "max_times": np.multiply}[semiring]
+    return oplus, otimes, dtype.type(ident)
+
+
+def _semiring_finish(acc, dtype):
+    if not np.issubdtype(dtype, np.integer):
+        acc[acc == 0] = 0   # a zero result is +0.0 (removes the K-order dependence of its sign)
+    return acc
+
+
+def semiring_gemm(A, B, semiring, C=None, accumulate=False, dtype=np.float64):
+    """C = [C (+)] (+)_k A[:, k] (x) B[k, :], folding k = 1..K in order (the sequential
+    K loop of jmul!'s register tile, src/gemm.jl:149-170, with the semiring's operations
+    in place of fma).  Returns a new array of `dtype`; K = 0 gives the identity of (+)."""
+    dtype = np.dtype(dtype)
+    A = np.asarray(A, dtype=dtype)
+    B = np.asarray(B, dtype=dtype)
+    M, K = A.shape
+    N = B.shape[1]
+    oplus, otimes, ident = _semiring_ops(semiring, dtype)
+    acc = np.full((M, N), ident, dtype=dtype)
+    with np.errstate(all="ignore"):
+        for k in range(K):
+            acc = oplus(acc, otimes(A[:, k:k + 1], B[k:k + 1, :]))
+        if accumulate:
+            acc = oplus(np.asarray(C, dtype=dtype), acc)
+    return _semiring_finish(np.asfortranarray(acc), dtype)
+
+
+def semiring_gemm_reduce(A, B, semiring, dtype=np.float64):
+    """The same product as one reduction over the K axis of the M x K x N tensor of (x)
+    products (numpy's pairwise reduction order): a second order for pinning ``semiring_gemm``
+    (small sizes only)."""
+    dtype = np.dtype(dtype)
+    A = np.asarray(A, dtype=dtype)
+    B = np.asarray(B, dtype=dtype)
+    oplus, otimes, ident = _semiring_ops(semiring, dtype)
+    with np.errstate(all="ignore"):
+        T = otimes(A[:, :, None], B[None, :, :])
+        acc = oplus.reduce(T, axis=1, initial=ident)
+    return _semiring_finish(np.asfortranarray(acc), dtype)
+
+
+def floyd_warshall(W):
+    """All-pairs shortest path lengths of a weighted digraph given as a list of lists of
+    Python ints (None = no edge), by Floyd-Warshall in exact integers; None = unreachable."""
+    n = len(W)
+    D = [[(0 if i == j else W[i][j]) for j in range(n)] for i in range(n)]
+    for k in range(n):
+        Dk = D[k]
+        for i in range(n):
+            dik = D[i][k]
+            if dik is None:
+                continue
+            Di = D[i]
+            for j in range(n):
+                if Dk[j] is not None and (Di[j] is None or dik + Dk[j] < Di[j]):
+                    Di[j] = dik + Dk[j]
+    return D

@@ -32,6 +32,13 @@ def assert_bit_equal(got, ref):
     got = np.asarray(got)
     ref = np.asarray(ref)
     assert got.shape == ref.shape and got.dtype == ref.dtype
+    if got.dtype.kind in "iu":
+        bad = got != ref
+        if bad.any():
+            idx = np.argwhere(bad)[:5]
+            raise AssertionError("%d mismatches, e.g. %s: got %r ref %r" % (
+                bad.sum(), idx.tolist(), [got[tuple(i)] for i in idx], [ref[tuple(i)] for i in idx]))
+        return
     nan_g, nan_r = np.isnan(got), np.isnan(ref)
     assert np.array_equal(nan_g, nan_r), "NaN positions differ"
     ok = nan_g | (bits(got) == bits(ref))

@@ -152,3 +152,81 @@ def test_crt_moduli_pairwise_coprime():
     m = oracle.crt_moduli(20)
     assert m[0] == 253 and len(set(m)) == 20 and max(m) <= 253
     assert all(math.gcd(a, b) == 1 for i, a in enumerate(m) for b in m[i + 1:])
+
+
+# ---------------------------------------------------------------------------- semirings
+SEMIRING_FIXTURE = os.path.join(os.path.dirname(__file__), "golden", "semiring", "apsp_48.npz")
+
+
+def _special_operands(g, dt, M, K, N):
+    if np.dtype(dt).kind == "i":
+        A = g.integers(-2**31, 2**31, (M, K)).astype(dt)
+        B = g.integers(-2**31, 2**31, (K, N)).astype(dt)
+        return A, B
+    A = g.uniform(-2, 2, (M, K)).astype(dt)
+    B = g.uniform(-2, 2, (K, N)).astype(dt)
+    A[0, 0] = np.nan
+    A[1, :] = -0.0
+    B[:, 2] = 0.0
+    A[2, 3] = np.inf
+    B[3, 1] = -np.inf
+    A[4, :] = np.nan
+    A[5, 5] = np.finfo(dt).tiny / 4     # subnormal
+    return A, B
+
+
+def _same(x, y):
+    x, y = np.ascontiguousarray(x), np.ascontiguousarray(y)
+    if x.dtype.kind == "i":
+        return np.array_equal(x, y)
+    nx, ny = np.isnan(x), np.isnan(y)
+    u = np.uint64 if x.dtype == np.float64 else np.uint32
+    return np.array_equal(nx, ny) and np.array_equal(np.where(nx, 0, x).view(u), np.where(ny, 0, y).view(u))
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.float32, np.int32])
+@pytest.mark.parametrize("sr", oracle.SEMIRINGS)
+def test_semiring_sequential_equals_reduction(dt, sr):
+    """The K-ordered fold and numpy's pairwise reduction give the same bits (NaN, +-0, Inf)."""
+    g = np.random.default_rng(7)
+    A, B = _special_operands(g, dt, 9, 11, 6)
+    assert _same(oracle.semiring_gemm(A, B, sr, dtype=dt), oracle.semiring_gemm_reduce(A, B, sr, dtype=dt))
+    # a reversed K order gives the same bits too
+    assert _same(oracle.semiring_gemm(A, B, sr, dtype=dt), oracle.semiring_gemm(A[:, ::-1], B[::-1, :], sr, dtype=dt))
+
+
+def test_semiring_identities_and_wrap():
+    e = np.zeros((3, 0))
+    f = np.zeros((0, 2))
+    assert np.all(oracle.semiring_gemm(e, f, "min_plus") == np.inf)
+    assert np.all(oracle.semiring_gemm(e, f, "max_times") == -np.inf)
+    ei, fi = e.astype(np.int32), f.astype(np.int32)
+    assert np.all(oracle.semiring_gemm(ei, fi, "min_max", dtype=np.int32) == 2**31 - 1)
+    assert np.all(oracle.semiring_gemm(ei, fi, "max_plus", dtype=np.int32) == -2**31)
+    big = np.array([[2**31 - 1]], dtype=np.int32)
+    one = np.array([[1]], dtype=np.int32)
+    assert oracle.semiring_gemm(big, one, "max_plus", dtype=np.int32)[0, 0] == -2**31   # wraps
+    z = oracle.semiring_gemm(np.array([[-0.0]]), np.array([[-0.0]]), "min_plus")
+    assert z[0, 0] == 0 and not np.signbit(z[0, 0])                                      # +0.0
+
+
+def test_semiring_fixture_is_floyd_warshall():
+    """The committed APSP fixture equals Floyd-Warshall recomputed here in Python integers."""
+    z = np.load(SEMIRING_FIXTURE)
+    W = [[None if not np.isfinite(v) or i == j else int(v) for j, v in enumerate(row)]
+         for i, row in enumerate(z["W"])]
+    D = oracle.floyd_warshall(W)
+    assert np.array_equal(np.array([[np.inf if v is None else v for v in r] for r in D]), z["D"])
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.float32, np.int32])
+def test_semiring_min_plus_closure_is_apsp(dt):
+    """Repeated (min, +) squaring of the weight matrix reproduces the fixture's distances."""
+    z = np.load(SEMIRING_FIXTURE)
+    W, Dref = z["W"], z["D"]
+    inf_i = 2**29      # int32 "no edge": sums of two stay below 2^31
+    X = np.where(np.isinf(W), inf_i, W).astype(dt) if dt == np.int32 else W.astype(dt)
+    for _ in range(6):   # 2^6 >= 47 edges
+        X = oracle.semiring_gemm(X, X, "min_plus", dtype=dt)
+    got = np.where(X >= inf_i, np.inf, X).astype(np.float64) if dt == np.int32 else X.astype(np.float64)
+    assert np.array_equal(got, Dref)
