@@ -15,8 +15,8 @@
 // product is exact.  n moduli cost n BF16 GEMMs, against s(s+1)/2 for s digit slices
 // (ozaki.cu), which is why this is the faster FP64-accurate mode.
 //
-// Kernels: crt_split_kernel (residue planes, [modulus][row][pitch] BF16, K-major, read by TMA
-// like the digit planes), the CTA-pair slice-product kernel with the TC_EPI_CRT epilogue
+// Kernels: crt_split_kc_kernel / crt_split_rc_kernel (residue planes, [modulus][row][pitch]
+// BF16, K-major, read by TMA like the digit planes; k-contiguous and row-contiguous operands), the CTA-pair slice-product kernel with the TC_EPI_CRT epilogue
 // (tc_gemm2.cu: one group per modulus, uint8 residue planes out), crt_combine_kernel
 // (reconstruction in 128-bit integer arithmetic, FP64 rounding by integer ops, alpha/beta).
 #include <cuda_bf16.h>
@@ -168,13 +168,11 @@ CrtTable build_table() {
     md.p[g] = p;
     md.pf[g] = static_cast<float>(p);
     md.pinv[g] = 1.0f / static_cast<float>(p);
-    uint64_t pw = 1;   // 2^(13 l) mod p
-    for (int l = 1; l <= 4; ++l) {
+    uint64_t pw = 1;   // 2^(13 (l + 1)) mod p
+    for (int l = 0; l < 4; ++l) {
       pw = (pw << 13) % p;
       md.climb[g][l] = static_cast<float>(pw);
     }
-    const uint64_t c62 = (((uint64_t(1) << 31) % p) * ((uint64_t(1) << 31) % p)) % p;
-    md.climb[g][0] = static_cast<float>((p - c62) % p);
   }
   for (int n = 1; n <= TC_MAX_MODULI; ++n) {
     CrtRecon& rc = tab.rec[n - 1];
@@ -534,32 +532,89 @@ int crt_plan_device(const OzRowStats& sa, const OzRowStats& sb, const CrtPlanPar
 
 // ============================================================== residue split
 
-// One thread = one row r and 8 consecutive k (rows contiguous: two neighbouring threads share
-// a row and cover 16 k, so each warp store fills whole 32-byte sectors; k contiguous:
-// neighbouring threads cover neighbouring k).  Y = round-half-away(x 2^(t - e)) (|Y| <= 2^t,
-// t <= 62) is shifted to Y + 2^62 >= 0 and cut into five 13-bit limbs held as exact FP32 values;
-// per modulus p (<= 253)
-//   s = (-2^62 mod p) + sum_l limb_l (2^(13 l) mod p)     below 8191 (1 + 4 * 252) + 252 < 2^23,
-//                                                          exact in FP32
-//   r = s - p rint(s / p)                                  |r| <= p/2 + 1/2, so |r| <= 127
+// round-half-away(x 2^(SB - 53 + ex - e)) as a two's-complement word, for the CRT split
+// (SB = t + 1 <= 63, every |x| < 2^e).  A subnormal significand is first normalised (its
+// leading bit moved to bit 52, the exponent lowered to match), so 2^ex <= |x| < 2^e and the
+// shift sh = ex - 53 + SB - e is at most 9: the significand is placed at bit 9 once and only
+// ever shifted right (by 9 - sh, with rounding).  Equal to fixed_point<uint64_t> for these
+// arguments, without its branches.
+__device__ __forceinline__ uint64_t crt_fixed_point(double x, int e, int SB) {
+  const unsigned long long bits = static_cast<unsigned long long>(__double_as_longlong(x));
+  const int biased = static_cast<int>((bits >> 52) & 0x7FF);
+  const unsigned long long frac = bits & 0x000FFFFFFFFFFFFFull;
+  const int lz = biased ? 0 : __clzll(static_cast<long long>(frac)) - 11;   // <= 53 (frac == 0: 53)
+  const unsigned long long m = biased ? (frac | 0x0010000000000000ull) : (frac << lz);
+  const int ex = biased ? biased - 1023 : -1022 - lz;
+  const int s = 9 - (ex - 53 + SB - e);   // >= 0 whenever m != 0
+  const unsigned long long m9 = m << 9;   // < 2^62
+  unsigned long long mag = 0;
+  if (s < 64) mag = s <= 0 ? m9 : (m9 + (1ull << (s - 1))) >> s;
+  return (bits >> 63) ? 0ull - mag : mag;
+}
+
+// Balanced digits of Y = round-half-away(x 2^(t - e)) (|Y| <= 2^t, t <= 62):
+// Y = sum_{l<4} d_l 2^(13 l) + d_4 2^52 with d_0..d_3 in [-4096, 4095] and |d_4| <= 1024, as
+// exact FP32 values.  Y + BAL (BAL = 4096 (1 + 2^13 + 2^26 + 2^39)) has the low digits + 4096
+// in its four 13-bit fields and d_4 in its signed top 12 bits.
+__device__ __forceinline__ void crt_digits(double x, int e, int tbits, bool nonfinite, float (&d)[5]) {
+  constexpr float DBIAS = 8388608.0f + 4096.0f;
+  constexpr unsigned long long BAL = 4096ull * (1ull + (1ull << 13) + (1ull << 26) + (1ull << 39));
+  const uint64_t u = (nonfinite ? 0ull : crt_fixed_point(x, e, tbits + 1)) + BAL;
+#pragma unroll
+  for (int l = 0; l < 4; ++l)
+    d[l] = __uint_as_float(0x4B000000u | (static_cast<uint32_t>(u >> (13 * l)) & 0x1FFFu)) - DBIAS;
+  const uint32_t top = static_cast<uint32_t>(static_cast<int64_t>(u) >> 52) + 4096u;
+  d[4] = __uint_as_float(0x4B000000u | (top & 0x1FFFu)) - DBIAS;
+}
+
+// Residues of 8 elements (digits d[.][j]) modulo p, packed as BF16 pairs.  Per element
+//   s = d_0 + sum_{l>=1} d_l (2^(13 l) mod p)     |s| <= 4096 (1 + 3 * 252) + 1024 * 252 < 2^22,
+//                                                 exact in FP32 (four FMAs)
+//   r = s - p rint(s / p)                         |r| <= p/2 + 1/2, so |r| <= 127
 // all on the FMA pipe; r has at most 7 significant bits, so its BF16 is the upper half of its
-// FP32 bits.  One 16-byte store per plane.
-template <bool RC>
-__global__ void __launch_bounds__(256) crt_split_kernel(const double* __restrict__ X, int64_t R, int64_t K,
-                                                        int64_t rs, int64_t ks,
-                                                        const unsigned long long* __restrict__ amax_bits,
-                                                        __nv_bfloat16* __restrict__ planes, int64_t pitch,
-                                                        int32_t* __restrict__ exps, const __grid_constant__ CrtModuli mod,
-                                                        const CrtDevicePlan* __restrict__ plan) {
+// FP32 bits.
+__device__ __forceinline__ uint4 crt_residues8(const float (&d)[5][8], const CrtModuli& mod, int g) {
   constexpr float MAGIC = 12582912.0f;   // 1.5 * 2^23: x + MAGIC - MAGIC = rint(x), |x| < 2^22
-  int64_t r, kc;
-  if (RC) {
-    r = static_cast<int64_t>(blockIdx.x) * 128 + (threadIdx.x >> 1);
-    kc = static_cast<int64_t>(blockIdx.y) * 2 + (threadIdx.x & 1);
-  } else {
-    kc = static_cast<int64_t>(blockIdx.x) * 256 + threadIdx.x;
-    r = blockIdx.y;
+  const float c1 = mod.climb[g][0], c2 = mod.climb[g][1], c3 = mod.climb[g][2], c4 = mod.climb[g][3];
+  const float pf = mod.pf[g], inv = mod.pinv[g];
+  uint32_t packed[4];
+#pragma unroll
+  for (int j = 0; j < 8; j += 2) {
+    float rr[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      float sj = fmaf(d[1][j + h], c1, d[0][j + h]);
+      sj = fmaf(d[2][j + h], c2, sj);
+      sj = fmaf(d[3][j + h], c3, sj);
+      sj = fmaf(d[4][j + h], c4, sj);
+      const float q = fmaf(sj, inv, MAGIC) - MAGIC;
+      rr[h] = fmaf(-pf, q, sj);
+    }
+    packed[j / 2] = __byte_perm(__float_as_uint(rr[0]), __float_as_uint(rr[1]), 0x7632u);
   }
+  return make_uint4(packed[0], packed[1], packed[2], packed[3]);
+}
+
+__device__ __forceinline__ void store_residues(__nv_bfloat16* dst, uint4 v, int nvalid) {
+  if (nvalid == 8) {
+    *reinterpret_cast<uint4*>(dst) = v;
+  } else {
+    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+    unsigned short* d2 = reinterpret_cast<unsigned short*>(dst);
+    for (int j = 0; j < nvalid; ++j) d2[j] = static_cast<unsigned short>(w[j / 2] >> (16 * (j & 1)));
+  }
+}
+
+// k contiguous: one thread = one row and 8 consecutive k, neighbouring threads neighbouring k
+// (a warp reads 2 KB and writes 512 B of one row per plane).  One 16-byte store per plane.
+__global__ void __launch_bounds__(256) crt_split_kc_kernel(const double* __restrict__ X, int64_t R, int64_t K,
+                                                           int64_t rs, int64_t ks,
+                                                           const unsigned long long* __restrict__ amax_bits,
+                                                           __nv_bfloat16* __restrict__ planes, int64_t pitch,
+                                                           int32_t* __restrict__ exps,
+                                                           const __grid_constant__ CrtModuli mod,
+                                                           const CrtDevicePlan* __restrict__ plan) {
+  const int64_t kc = static_cast<int64_t>(blockIdx.x) * 256 + threadIdx.x, r = blockIdx.y;
   const int64_t k0 = kc * 8;
   if (r >= R || k0 >= K) return;
   const int nmod = plan->n, tbits = plan->t;
@@ -568,43 +623,65 @@ __global__ void __launch_bounds__(256) crt_split_kernel(const double* __restrict
   const bool nonfinite = (e == OZ_EXP_NONFINITE);
   const int nvalid = static_cast<int>(K - k0 < 8 ? K - k0 : 8);
   const double* src = X + r * rs + k0 * ks;
-  float yl[5][8];
+  float d[5][8];
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
-    const double x = (j < nvalid) ? src[j * ks] : 0.0;
-    const uint64_t y = (nonfinite ? 0ull : fixed_point<uint64_t>(x, e, tbits + 1)) + (1ull << 62);
+    float dj[5];
+    crt_digits((j < nvalid) ? src[j * ks] : 0.0, e, tbits, nonfinite, dj);
 #pragma unroll
-    for (int l = 0; l < 5; ++l)
-      yl[l][j] = __uint_as_float(0x4B000000u | (static_cast<uint32_t>(y >> (13 * l)) & 0x1FFFu)) - 8388608.0f;
+    for (int l = 0; l < 5; ++l) d[l][j] = dj[l];
   }
   __nv_bfloat16* out0 = planes + r * pitch + k0;
   const int64_t plane_stride = R * pitch;
+  for (int g = 0; g < nmod; ++g) store_residues(out0 + g * plane_stride, crt_residues8(d, mod, g), nvalid);
+}
+
+// Rows contiguous: a CTA converts a 32-row x 64-k tile.  Warp w loads columns 8w..8w+7 of the
+// tile (lane = row: 256 contiguous bytes per load) into shared memory and computes the
+// residues of row `lane`, k 8w..8w+7; per modulus the residues pass through a padded shared
+// tile (double buffered) so that each warp stores 4 rows x 128 B, whole lines of the plane.
+// Bank spread: 16-byte accesses at word 36 row + 4 chunk touch each bank 4 times per warp
+// (the minimum for 512 B).
+__global__ void __launch_bounds__(256) crt_split_rc_kernel(const double* __restrict__ X, int64_t R, int64_t K,
+                                                           int64_t ks, const unsigned long long* __restrict__ amax_bits,
+                                                           __nv_bfloat16* __restrict__ planes, int64_t pitch,
+                                                           int32_t* __restrict__ exps,
+                                                           const __grid_constant__ CrtModuli mod,
+                                                           const CrtDevicePlan* __restrict__ plan) {
+  __shared__ double tile[64][33];
+  __shared__ __align__(16) uint32_t otile[2][32][36];   // 32 rows x (64 BF16 = 32 words, + 4 words pad)
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t r0 = static_cast<int64_t>(blockIdx.x) * 32, kb = static_cast<int64_t>(blockIdx.y) * 64;
+  const int64_t r = r0 + lane;
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    const int64_t k = kb + w * 8 + c;
+    tile[w * 8 + c][lane] = (r < R && k < K) ? X[r + k * ks] : 0.0;
+  }
+  __syncthreads();
+  const int nmod = plan->n, tbits = plan->t;
+  const int e = r < R ? row_exponent(amax_bits[r]) : 0;
+  if (r < R && kb == 0 && w == 0) exps[r] = e;
+  const bool nonfinite = (e == OZ_EXP_NONFINITE);
+  float d[5][8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    float dj[5];
+    crt_digits(tile[w * 8 + j][lane], e, tbits, nonfinite, dj);
+#pragma unroll
+    for (int l = 0; l < 5; ++l) d[l][j] = dj[l];
+  }
+  // store mapping: warp w owns tile rows 4w..4w+3; lane -> row 4w + lane / 8, 16-byte chunk lane % 8
+  const int orow = 4 * w + (lane >> 3), ochunk = lane & 7;
+  const int64_t gr = r0 + orow, gk = kb + ochunk * 8;
+  const int nvalid = gr < R && gk < K ? static_cast<int>(K - gk < 8 ? K - gk : 8) : 0;
+  __nv_bfloat16* gout = planes + gr * pitch + gk;
+  const int64_t plane_stride = R * pitch;
   for (int g = 0; g < nmod; ++g) {
-    const float c0 = mod.climb[g][0], c1 = mod.climb[g][1], c2 = mod.climb[g][2], c3 = mod.climb[g][3];
-    const float c4 = mod.climb[g][4], pf = mod.pf[g], inv = mod.pinv[g];
-    uint32_t packed[4];
-#pragma unroll
-    for (int j = 0; j < 8; j += 2) {
-      float rr[2];
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        float sj = yl[0][j + h] + c0;
-        sj = fmaf(yl[1][j + h], c1, sj);
-        sj = fmaf(yl[2][j + h], c2, sj);
-        sj = fmaf(yl[3][j + h], c3, sj);
-        sj = fmaf(yl[4][j + h], c4, sj);
-        const float q = fmaf(sj, inv, MAGIC) - MAGIC;
-        rr[h] = fmaf(-pf, q, sj);
-      }
-      packed[j / 2] = __byte_perm(__float_as_uint(rr[0]), __float_as_uint(rr[1]), 0x7632u);
-    }
-    __nv_bfloat16* dst = out0 + g * plane_stride;
-    if (nvalid == 8) {
-      *reinterpret_cast<uint4*>(dst) = make_uint4(packed[0], packed[1], packed[2], packed[3]);
-    } else {
-      unsigned short* d2 = reinterpret_cast<unsigned short*>(dst);
-      for (int j = 0; j < nvalid; ++j) d2[j] = static_cast<unsigned short>(packed[j / 2] >> (16 * (j & 1)));
-    }
+    *reinterpret_cast<uint4*>(&otile[g & 1][lane][w * 4]) = crt_residues8(d, mod, g);
+    __syncthreads();   // buffer g & 1 is rewritten two moduli later, after the next barrier
+    const uint4 v = *reinterpret_cast<const uint4*>(&otile[g & 1][orow][ochunk * 4]);
+    if (nvalid > 0) store_residues(gout + g * plane_stride, v, nvalid);
   }
 }
 
@@ -612,19 +689,20 @@ int crt_split(const double* X, int64_t R, int64_t K, int64_t rs, int64_t ks, con
               const CrtDevicePlan* plan, __nv_bfloat16* planes, int64_t pitch, int32_t* exps, cudaStream_t s) {
   const CrtModuli& mod = crt_table().mod;
   if (R <= 0 || K <= 0) return GB_OK;
-  const int64_t kchunks = (K + 7) / 8;
   if (rs == 1 && R > 1) {
-    if ((kchunks + 1) / 2 > 65535) return GB_ERR_UNSUPPORTED;
-    dim3 grid(static_cast<unsigned>((R + 127) / 128), static_cast<unsigned>((kchunks + 1) / 2));
+    const int64_t gy = (K + 63) / 64;
+    if (gy > 65535 || (R + 31) / 32 > 0x7FFFFFFF) return GB_ERR_UNSUPPORTED;
+    dim3 grid(static_cast<unsigned>((R + 31) / 32), static_cast<unsigned>(gy));
     GB_LAUNCH(GB_KERNEL_OZAKI_SPLIT, s,
-              (crt_split_kernel<true><<<grid, 256, 0, s>>>(X, R, K, rs, ks, amax_bits, planes, pitch, exps, mod, plan)));
+              (crt_split_rc_kernel<<<grid, 256, 0, s>>>(X, R, K, ks, amax_bits, planes, pitch, exps, mod, plan)));
   } else {
+    const int64_t kchunks = (K + 7) / 8;
     for (int64_t r0 = 0; r0 < R; r0 += 65535) {   // rows beyond the grid's y range: bands
       const int64_t rb = (R - r0 < 65535) ? R - r0 : 65535;
       dim3 grid(static_cast<unsigned>((kchunks + 255) / 256), static_cast<unsigned>(rb));
       GB_LAUNCH(GB_KERNEL_OZAKI_SPLIT, s,
-                (crt_split_kernel<false><<<grid, 256, 0, s>>>(X + r0 * rs, rb, K, rs, ks, amax_bits + r0,
-                                                               planes + r0 * pitch, pitch, exps + r0, mod, plan)));
+                (crt_split_kc_kernel<<<grid, 256, 0, s>>>(X + r0 * rs, rb, K, rs, ks, amax_bits + r0,
+                                                          planes + r0 * pitch, pitch, exps + r0, mod, plan)));
     }
   }
   GB_CUDA_TRY(cudaGetLastError());
