@@ -100,6 +100,8 @@ struct CrtRecon {
   float pab[CRT_MAX_GROUPS];        // p_a p_b
   float P[CRT_MAX_GROUPS];          // P_G
   float Pinv[CRT_MAX_GROUPS];       // fl32(1 / P_G)
+  int32_t voff[CRT_MAX_GROUPS];     // P_G - (2^23 + 128): biased group value -> v + P_G
+  float ks0;                        // fl32(sum_G (P_G - 2^23 - 128) / P_G)
   uint32_t w[CRT_MAX_GROUPS][4];    // M / P_G mod 2^128, little-endian 32-bit words
   uint32_t m[4];                    // M mod 2^128
 };

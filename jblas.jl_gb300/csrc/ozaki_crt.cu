@@ -181,6 +181,7 @@ CrtTable build_table() {
     for (int g = 0; g < n; ++g) m128 *= p[g];
     for (int w = 0; w < 4; ++w) rc.m[w] = static_cast<uint32_t>(m128 >> (32 * w));
     rc.ngroups = (n + 2) / 3;
+    double ks0 = 0.0;
     for (int G = 0; G < rc.ngroups; ++G) {
       const int a = 3 * G, b = a + 1, c = a + 2;
       uint64_t P = p[a];
@@ -203,8 +204,11 @@ CrtTable build_table() {
                          : 0.0f;
       rc.P[G] = static_cast<float>(P);
       rc.Pinv[G] = 1.0f / static_cast<float>(P);
+      rc.voff[G] = static_cast<int32_t>(static_cast<int64_t>(P) - 8388736);
+      ks0 += (static_cast<double>(P) - 8388736.0) / static_cast<double>(P);
       for (int w = 0; w < 4; ++w) rc.w[G][w] = static_cast<uint32_t>(rest128 >> (32 * w));
     }
+    rc.ks0 = static_cast<float>(ks0);
   }
   return tab;
 }
@@ -756,14 +760,18 @@ __device__ __forceinline__ double i128_times_pow2(uint64_t hi, uint64_t lo, int 
 }
 
 // One thread = 4 consecutive rows of one column (a 32-bit load per residue plane).  The
-// planes hold biased bytes x_g + 128, x_g = psi_G C' mod p_g (|x_g| <= 127).  Per group of
-// up to three moduli (a, b, c), in exact FP32 (every value stays below 2^23):
-//   r  = x_a + p_a ((x_b - x_a) a1 mod p_b)           = psi_G C' mod p_a p_b
-//   v  = r + p_a p_b ((x_c - r) a2 mod p_c)            = psi_G C' mod P_G, |v| < P_G
-//   v += P_G if v < 0                                  (0 <= v < P_G)
-// then  X = sum_G v_G (M / P_G)  (mod 2^128),  k = round(sum_G v_G / P_G) = round(X / M) (each
-// term in [0, 1): exact in FP32 because |C'| <= M/4),  C' = X - k M as a two's-complement
-// 128-bit integer, rounded to FP64 by integer arithmetic.
+// planes hold biased bytes x_g + 128, x_g = psi_G C' mod p_g (|x_g| <= 127), read as the exact
+// floats F + x_g (F = 2^23 + 128).  Per group of up to three moduli (a, b, c), in exact FP32
+// on biased values (the bias cancels in every difference; every value stays in (0, 2^24)):
+//   vb = F + x_a
+//   vb += p_a ((x_b - x_a) a1 mod p_b)                 vb = F + (psi_G C' mod p_a p_b)
+//   vb += p_a p_b ((x_c - (vb - F)) a2 mod p_c)        vb = F + v, v = psi_G C' mod P_G,
+//                                                      |v| < P_G / 2 + 2^15
+// then v' = int(vb) + (P_G - F) = v + P_G in (0, 2 P_G) (same class mod P_G),
+// X = sum_G v'_G (M / P_G) (mod 2^128), k = round(sum_G v'_G / P_G) = round(X / M) (the FP32
+// sum starts from the constant sum_G (P_G - F) / P_G and adds vb_G / P_G: error below 0.05,
+// within the 1/4 margin of |C'| <= M/4), C' = X - k M as a two's-complement 128-bit integer,
+// rounded to FP64 by integer arithmetic.
 __device__ __forceinline__ float mods_f32(float x, float p, float pinv) {   // x - p rint(x / p)
   const float q = fmaf(x, pinv, 12582912.0f) - 12582912.0f;
   return fmaf(-p, q, x);
@@ -776,7 +784,6 @@ __device__ __forceinline__ void crt_combine_column(const uint8_t* __restrict__ b
                                                    int64_t M, const int (&eai)[4], int ebj, int two_t, double alpha,
                                                    double beta, double* __restrict__ ccol, int ab,
                                                    const CrtTable& tab) {
-  constexpr float BIAS_F = 8388736.0f;   // 2^23 + 128
   constexpr int NG = (NMOD + 2) / 3;
   const CrtRecon& rc = tab.rec[NMOD - 1];
   const CrtModuli& md = tab.mod;
@@ -788,22 +795,21 @@ __device__ __forceinline__ void crt_combine_column(const uint8_t* __restrict__ b
     if (i0 + q >= M) continue;
     const uint32_t sel = 0x7540u + q;   // byte q of a word over 0x4B0000..: 2^23 + byte
     uint64_t acc0 = 0, acc1 = 0, acc2 = 0, acc3 = 0;
-    float ks = 0.0f;
+    float ks = rc.ks0;
 #pragma unroll
     for (int G = 0; G < NG; ++G) {
       const int a = 3 * G;
-      float v = __uint_as_float(__byte_perm(words[a], 0x4B000000u, sel)) - BIAS_F;
+      float vb = __uint_as_float(__byte_perm(words[a], 0x4B000000u, sel));
       if (a + 1 < NMOD) {
-        const float xb = __uint_as_float(__byte_perm(words[(a + 1) % NMOD], 0x4B000000u, sel)) - BIAS_F;
-        v = fmaf(rc.pa[G], mods_f32((xb - v) * rc.a1[G], md.pf[a + 1], md.pinv[a + 1]), v);
+        const float xb = __uint_as_float(__byte_perm(words[(a + 1) % NMOD], 0x4B000000u, sel));
+        vb = fmaf(rc.pa[G], mods_f32((xb - vb) * rc.a1[G], md.pf[a + 1], md.pinv[a + 1]), vb);
         if (a + 2 < NMOD) {
-          const float xc = __uint_as_float(__byte_perm(words[(a + 2) % NMOD], 0x4B000000u, sel)) - BIAS_F;
-          v = fmaf(rc.pab[G], mods_f32((xc - v) * rc.a2[G], md.pf[a + 2], md.pinv[a + 2]), v);
+          const float xc = __uint_as_float(__byte_perm(words[(a + 2) % NMOD], 0x4B000000u, sel));
+          vb = fmaf(rc.pab[G], mods_f32((xc - vb) * rc.a2[G], md.pf[a + 2], md.pinv[a + 2]), vb);
         }
       }
-      v = (v < 0.0f) ? v + rc.P[G] : v;
-      ks = fmaf(v, rc.Pinv[G], ks);
-      const uint32_t vi = static_cast<uint32_t>(v);
+      ks = fmaf(vb, rc.Pinv[G], ks);
+      const uint32_t vi = static_cast<uint32_t>(static_cast<int32_t>(vb) + rc.voff[G]);
       acc0 += static_cast<uint64_t>(vi) * rc.w[G][0];
       acc1 += static_cast<uint64_t>(vi) * rc.w[G][1];
       acc2 += static_cast<uint64_t>(vi) * rc.w[G][2];
