@@ -10,8 +10,8 @@
  * package cannot run here (no Julia; src/cpu_info.jl is missing and
  * src/gemm.jl:260 reads an undefined global).  The arithmetic below is pinned
  * instead by (i) an independent pure-Python exact-rational restatement of the
- * same fma chain (tests/golden/make_golden.py), bit-exact, and (ii) a
- * compensated (Dot2) dot product used as a near-exact reference.
+ * same fma chain (tests/golden/make_golden.py), bit-exact, and (ii) two near-exact
+ * dot products: a compensated one (Dot2) and one accumulated in IEEE binary128.
  *
  * Reference arithmetic restated here (paths relative to the jBLAS.jl tree):
  *   src/gemm.jl:71-91    initialize_block: D_rc = A[:,1] * X[1,c]   (a rounded product)
@@ -231,6 +231,34 @@ void or_dot2_entries(int ta, int tb, i64 K, const double* A, i64 lda, const doub
     hi[s] = p + q;
     lo[s] = q - (hi[s] - p);
     absdot[s] = ab;
+  }
+  (void)nthreads;
+}
+
+/*
+ * The same sampled entries accumulated in IEEE binary128 (113-bit significand): every
+ * product of two doubles is exact in it, and each addition rounds at 2^-113 relative, so
+ * |error| <= K 2^-113 sum_k |a_ik b_kj| — an independent near-exact reference next to Dot2.
+ * binary128 is __float128 on x86-64 and long double on AArch64 (both software-emulated by
+ * libgcc).  Outputs hi[s] + lo[s] (the quad sum rounded to a double-double).
+ */
+#if defined(__aarch64__)
+typedef long double or_quad;
+#else
+typedef __float128 or_quad;
+#endif
+void or_quad_entries(int ta, int tb, i64 K, const double* A, i64 lda, const double* B, i64 ldb, i64 nsamp,
+                     const i64* rows, const i64* cols, double* hi, double* lo, int nthreads) {
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(nthreads > 0 ? nthreads : 1)
+#endif
+  for (i64 s = 0; s < nsamp; ++s) {
+    const i64 i = rows[s], j = cols[s];
+    or_quad acc = 0;
+    for (i64 k = 0; k < K; ++k) acc += (or_quad)A[AIDX(ta, i, k, lda)] * (or_quad)B[BIDX(tb, k, j, ldb)];
+    const double h = (double)acc;
+    hi[s] = h;
+    lo[s] = (double)(acc - (or_quad)h);
   }
   (void)nthreads;
 }

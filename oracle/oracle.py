@@ -15,6 +15,8 @@ restatements here are pinned against each other instead:
                              is correctly rounded), following src/gemm.jl:76-89,154-168;
   * ``dot2_entries``         compensated dot products (Ogita-Rump-Oishi Dot2) for
                              near-exact values at sampled entries of large products;
+  * ``quad_entries``         the same entries accumulated in IEEE binary128, the second
+                             near-exact reference (pinned against exact rationals and Dot2);
   * ``ozaki_*``              numpy restatement of the Ozaki splitting and recombination
                              the GPU kernel performs, operation for operation;
   * ``semiring_gemm``        numpy restatement of the semiring product ((min, +) and its
@@ -57,6 +59,8 @@ def lib():
                                        ctypes.c_int]
         L.or_dot2_entries.argtypes = [ctypes.c_int, ctypes.c_int, c_i64, _vp, c_i64, _vp, c_i64, c_i64,
                                       _vp, _vp, _vp, _vp, _vp, ctypes.c_int]
+        L.or_quad_entries.argtypes = [ctypes.c_int, ctypes.c_int, c_i64, _vp, c_i64, _vp, c_i64, c_i64, _vp,
+                                      _vp, _vp, _vp, ctypes.c_int]
         L.or_fma_array.argtypes = [c_i64, _vp, _vp, _vp, _vp]
         L.or_chain_entries_f64.argtypes = [ctypes.c_int, ctypes.c_int, c_i64, ctypes.c_double, _vp, c_i64,
                                            _vp, c_i64, ctypes.c_double, _vp, c_i64, c_i64, _vp, _vp, _vp,
@@ -156,6 +160,23 @@ def dot2_entries(A, B, rows, cols, trans_a=False, trans_b=False, nthreads=None):
     lib().or_dot2_entries(int(trans_a), int(trans_b), K, _ptr(A), lda, _ptr(B), ldb, n, _ptr(rows),
                           _ptr(cols), _ptr(hi), _ptr(lo), _ptr(ab), nthreads or num_threads())
     return hi, lo, ab
+
+
+def quad_entries(A, B, rows, cols, trans_a=False, trans_b=False, nthreads=None):
+    """(hi, lo) of (op(A) op(B))[rows[s], cols[s]] accumulated in IEEE binary128 (__float128 /
+    AArch64 long double): |hi + lo - exact| <= K 2^-113 sum |a||b| (+ the final rounding to a
+    double-double).  The second near-exact reference beside ``dot2_entries``."""
+    A, lda = _colmajor(A, np.float64)
+    B, ldb = _colmajor(B, np.float64)
+    K = A.shape[0] if trans_a else A.shape[1]
+    rows = np.ascontiguousarray(rows, dtype=np.int64)
+    cols = np.ascontiguousarray(cols, dtype=np.int64)
+    n = rows.size
+    hi = np.empty(n)
+    lo = np.empty(n)
+    lib().or_quad_entries(int(trans_a), int(trans_b), K, _ptr(A), lda, _ptr(B), ldb, n, _ptr(rows), _ptr(cols),
+                          _ptr(hi), _ptr(lo), nthreads or num_threads())
+    return hi, lo
 
 
 def fma(a, b, c):

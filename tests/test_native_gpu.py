@@ -189,3 +189,28 @@ def test_config2_sampled_entries(cuda, dtype, shape):
     torch.cuda.synchronize()
     got = Cd[torch.from_numpy(rows).cuda(), torch.from_numpy(cols).cuda()].cpu().numpy()
     assert_bit_equal(got, ref)
+
+
+def test_native_fp64_error_within_standard_bound_against_binary128(cuda):
+    """8192^3 FP64 (alpha = 1, beta = 0): 2048 sampled entries against the binary128 oracle
+    lie within the standard bound gamma_K sum |a||b| (gamma_K = K u / (1 - K u), u = 2^-53),
+    and the binary128 and Dot2 references agree within Dot2's own error bound."""
+    from gbblas import workloads
+    M = N = K = 8192
+    A = workloads.uniform(M, K, stream=31)
+    B = workloads.uniform(K, N, stream=32)
+    Cd = torch.empty((N, M), dtype=torch.float64, device=cuda).t()
+    gbblas.gemm_(Cd, to_dev(A), to_dev(B))
+    g = np.random.default_rng(4)
+    rows = g.integers(0, M, 2048)
+    cols = g.integers(0, N, 2048)
+    qhi, qlo = oracle.quad_entries(A, B, rows, cols)
+    dhi, dlo, ab = oracle.dot2_entries(A, B, rows, cols)
+    torch.cuda.synchronize()
+    got = Cd[torch.from_numpy(rows).cuda(), torch.from_numpy(cols).cuda()].cpu().numpy()
+    u = 2.0 ** -53
+    gamma = K * u / (1 - K * u)
+    err = np.abs((got - qhi) - qlo)
+    assert np.all(err <= gamma * ab)
+    # Dot2 (Ogita-Rump-Oishi): |error| <= u^2 |x| + gamma_K^2 sum|a||b| for the double-double
+    assert np.all(np.abs((dhi - qhi) + (dlo - qlo)) <= 2 * (K * u) ** 2 * ab + 2.0 ** -104 * np.abs(qhi))

@@ -230,3 +230,26 @@ def test_semiring_min_plus_closure_is_apsp(dt):
         X = oracle.semiring_gemm(X, X, "min_plus", dtype=dt)
     got = np.where(X >= inf_i, np.inf, X).astype(np.float64) if dt == np.int32 else X.astype(np.float64)
     assert np.array_equal(got, Dref)
+
+
+def test_quad_is_near_exact_and_agrees_with_dot2():
+    """The binary128 dot product: within K 2^-113 sum|a||b| (+ double-double rounding) of the
+    exact rational value, and equal to Dot2 within Dot2's error bound."""
+    g = np.random.default_rng(17)
+    K = 400
+    A = np.asfortranarray(g.standard_normal((5, K)) * np.ldexp(1.0, g.integers(-30, 30, (5, K))))
+    B = np.asfortranarray(g.standard_normal((K, 4)) * np.ldexp(1.0, g.integers(-30, 30, (K, 4))))
+    rows = np.array([0, 1, 2, 3, 4, 0])
+    cols = np.array([0, 1, 2, 3, 0, 3])
+    qhi, qlo = oracle.quad_entries(A, B, rows, cols)
+    dhi, dlo, ab = oracle.dot2_entries(A, B, rows, cols)
+    for s in range(rows.size):
+        exact = sum(Fraction(A[rows[s], k]) * Fraction(B[k, cols[s]]) for k in range(K))
+        err = abs(Fraction(qhi[s]) + Fraction(qlo[s]) - exact)
+        assert float(err) <= K * 2.0 ** -113 * ab[s] + 2.0 ** -105 * abs(float(exact)) + 2.0 ** -1000
+        u = 2.0 ** -53   # Dot2's bound: u^2 |x| + gamma_K^2 sum|a||b|
+        assert abs((dhi[s] - qhi[s]) + (dlo[s] - qlo[s])) <= 2 * (K * u) ** 2 * ab[s] + 2.0 ** -104 * abs(qhi[s])
+    # transposed operands address the same values
+    qt, _ = oracle.quad_entries(np.asfortranarray(A.T), np.asfortranarray(B.T), rows, cols, trans_a=True,
+                                trans_b=True)
+    assert np.array_equal(qt, qhi)
