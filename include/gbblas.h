@@ -28,6 +28,14 @@
 #include <stddef.h>
 #include <stdint.h>
 
+/* Exported entry points: the library is built with hidden default visibility, so these
+ * declarations are its whole dynamic symbol table. */
+#if defined(__GNUC__)
+#define GB_API __attribute__((visibility("default")))
+#else
+#define GB_API
+#endif
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -53,37 +61,37 @@ typedef enum {
                              modulo pairwise coprime moduli (Chinese remainder theorem) */
 } gb_mode_t;
 
-const char* gb_status_string(int status);
-int gb_version(void);
+GB_API const char* gb_status_string(int status);
+GB_API int gb_version(void);
 
 /* Bounded-wait limit (nanoseconds) for every on-device pipeline wait; 0 restores the
  * default (4 s).  A wait that expires makes the kernel exit and the call report
  * GB_ERR_PIPELINE_TIMEOUT on a later gb_check_status(). */
-int gb_set_wait_limit_ns(uint64_t ns);
+GB_API int gb_set_wait_limit_ns(uint64_t ns);
 
 /* Normwise tolerance the automatic Ozaki slice or moduli count must meet (slices = 0); 0 restores
  * the default 2^-50. */
-int gb_set_ozaki_tolerance(double tol);
+GB_API int gb_set_ozaki_tolerance(double tol);
 
 /* Tensor-core engine for the Ozaki slice-mode and adjoint products: 0 = automatic (CTA
  * pairs), 1 = one CTA per 128 x 256 tile, 2 = CTA pairs on 256 x 256 tiles (tcgen05
  * cta_group::2, half of B per SM).  Ozaki results are identical under both engines.  The
  * CRT mode always runs on CTA pairs. */
-int gb_set_tc_engine(int engine);
+GB_API int gb_set_tc_engine(int engine);
 
 /* K chunking used by OZAKI calls with an explicit slice count: K is cut into at least
  * `min_chunks` exact accumulation chunks (shorter chunks allow wider digits, at the cost
  * of more accumulator drains); 0 or 1 restores the default (one chunk up to K = 65536).
  * slices = 0 ignores it and chooses slices and chunking together. */
-int gb_set_ozaki_min_chunks(int min_chunks);
+GB_API int gb_set_ozaki_min_chunks(int min_chunks);
 
 /* Returns the current device's cached workspace memory to the driver (synchronises the
  * device).  Workspace is otherwise kept between calls. */
-int gb_release_workspace(void);
+GB_API int gb_release_workspace(void);
 
 /* Reads and clears the device-side status word written by timed-out waits
  * (synchronises `stream`). */
-int gb_check_status(void* stream);
+GB_API int gb_check_status(void* stream);
 
 /* ------------------------------------------------------------------ tracing */
 /* Kernel kinds counted and timed by the tracing layer. */
@@ -100,23 +108,23 @@ typedef enum {
   GB_KERNEL_SEMIRING_GEMM = 9,
   GB_KERNEL_KINDS = 16
 } gb_kernel_kind_t;
-const char* gb_kernel_kind_name(int kind);
+GB_API const char* gb_kernel_kind_name(int kind);
 /* Launches of each kernel kind since the library was loaded (counts[0..n)). */
-int gb_launch_counts(long long* counts, int n);
+GB_API int gb_launch_counts(long long* counts, int n);
 /* Between start and stop, every launch is bracketed by CUDA events on its stream; stop
  * synchronises those events and returns the summed milliseconds and launch count of
  * each kind (ms[0..n), launches[0..n); either may be NULL). */
-int gb_profile_start(void);
-int gb_profile_stop(double* ms, long long* launches, int n);
+GB_API int gb_profile_start(void);
+GB_API int gb_profile_stop(double* ms, long long* launches, int n);
 
 /* ------------------------------------------------------------------ jmul! proper */
 /* D (M x P) = A (M x N) * X (N x P), contraction over N, leading dimensions M, N, M
  * exactly as an MMatrix (src/gemm.jl:244).  Per element d = a1*x1; d = fma(ak, xk, d)
  * for k = 2..N in order: results are bit-identical to jmul!'s arithmetic, and every
  * element is written (jmul! leaves remainder tiles unwritten, src/gemm.jl:340-345). */
-int gb_jmul_f64(double* D, const double* A, const double* X, int64_t M, int64_t N, int64_t P,
+GB_API int gb_jmul_f64(double* D, const double* A, const double* X, int64_t M, int64_t N, int64_t P,
                 void* stream);
-int gb_jmul_f32(float* D, const float* A, const float* X, int64_t M, int64_t N, int64_t P,
+GB_API int gb_jmul_f32(float* D, const float* A, const float* X, int64_t M, int64_t N, int64_t P,
                 void* stream);
 
 /* ------------------------------------------------------------------ BLAS-3 GEMM */
@@ -144,11 +152,11 @@ int gb_jmul_f32(float* D, const float* A, const float* X, int64_t M, int64_t N, 
  *   synchronises (its plan is chosen on the device) and can be captured in a CUDA graph;
  *   OZAKI_BF16 with slices = 0 synchronises once to read the split statistics.  For NATIVE it
  *   receives the standard bound K*u/(1-K*u) (u = 2^-53) of the same quantity. */
-int gb_gemm_f64(int transA, int transB, int64_t M, int64_t N, int64_t K, double alpha,
+GB_API int gb_gemm_f64(int transA, int transB, int64_t M, int64_t N, int64_t K, double alpha,
                 const double* A, int64_t lda, const double* B, int64_t ldb, double beta,
                 double* C, int64_t ldc, int mode, int slices, double* err_bound_out,
                 void* stream);
-int gb_gemm_f32(int transA, int transB, int64_t M, int64_t N, int64_t K, float alpha,
+GB_API int gb_gemm_f32(int transA, int transB, int64_t M, int64_t N, int64_t K, float alpha,
                 const float* A, int64_t lda, const float* B, int64_t ldb, float beta,
                 float* C, int64_t ldc, void* stream);
 
@@ -174,9 +182,9 @@ typedef struct {
   int32_t config[GB_GROUPED_CLASSES];
 } gb_grouped_tuning_t;
 
-int gb_grouped_default_tuning(int dtype_bytes, gb_grouped_tuning_t* out);
+GB_API int gb_grouped_default_tuning(int dtype_bytes, gb_grouped_tuning_t* out);
 /* Device workspace a grouped call over `count` problems needs (prefix sums of tiles). */
-size_t gb_grouped_workspace_size(int count);
+GB_API size_t gb_grouped_workspace_size(int count);
 /* All `count` products (table `problems` in DEVICE memory) in one persistent launch after
  * a prologue that counts tiles per problem.  tuning NULL = defaults.  workspace NULL =
  * taken from the library's pool; a caller-provided workspace (>= gb_grouped_workspace_size)
@@ -184,9 +192,9 @@ size_t gb_grouped_workspace_size(int count);
  * equals jmul!'s FMA chain (with the alpha/beta extension of gb_gemm_*).  The table's
  * sizes and pointers are trusted (device memory is not inspected on the host).
  * Reference: many fastmul!/kernel! products, src/kernels.jl:202-208, 239. */
-int gb_gemm_grouped_f64(const gb_problem_t* problems, int count, const gb_grouped_tuning_t* tuning,
+GB_API int gb_gemm_grouped_f64(const gb_problem_t* problems, int count, const gb_grouped_tuning_t* tuning,
                         void* workspace, size_t workspace_bytes, void* stream);
-int gb_gemm_grouped_f32(const gb_problem_t* problems, int count, const gb_grouped_tuning_t* tuning,
+GB_API int gb_gemm_grouped_f32(const gb_problem_t* problems, int count, const gb_grouped_tuning_t* tuning,
                         void* workspace, size_t workspace_bytes, void* stream);
 /* Allocation-free grouped FP64 GEMM.  No counterpart in the reference (jBLAS never
  * allocates because it only multiplies static-size arrays on the CPU).  For callers that
@@ -201,7 +209,7 @@ int gb_gemm_grouped_f32(const gb_problem_t* problems, int count, const gb_groupe
  * Every call shares the one array: calls that overlap on the GPU (other streams, other
  * threads) race and must be serialised by the caller.  Results equal gb_gemm_grouped_f64's. */
 #define GB_GROUPED_NOALLOC_MAX 65536
-int gb_gemm_grouped_f64_noalloc(const gb_problem_t* problems, int count, const gb_grouped_tuning_t* tuning,
+GB_API int gb_gemm_grouped_f64_noalloc(const gb_problem_t* problems, int count, const gb_grouped_tuning_t* tuning,
                                 void* stream);
 /* Strided batched GEMM: C_i = alpha A_i B_i + beta C_i for i < count, where A_i = A + i*strideA,
  * B_i = B + i*strideB, C_i = C + i*strideC (strides in elements, >= 0; a stride of 0 shares
@@ -211,10 +219,10 @@ int gb_gemm_grouped_f64_noalloc(const gb_problem_t* problems, int count, const g
  * the alpha/beta extension of gb_gemm_*), run as one grouped persistent launch over a
  * problem table built on the device (table and workspace from the library pool).
  * count <= 2^31 - 1. */
-int gb_gemm_strided_batched_f64(int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t lda,
+GB_API int gb_gemm_strided_batched_f64(int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t lda,
                                 int64_t strideA, const double* B, int64_t ldb, int64_t strideB, double beta,
                                 double* C, int64_t ldc, int64_t strideC, int64_t count, void* stream);
-int gb_gemm_strided_batched_f32(int64_t M, int64_t N, int64_t K, float alpha, const float* A, int64_t lda,
+GB_API int gb_gemm_strided_batched_f32(int64_t M, int64_t N, int64_t K, float alpha, const float* A, int64_t lda,
                                 int64_t strideA, const float* B, int64_t ldb, int64_t strideB, float beta,
                                 float* C, int64_t ldc, int64_t strideC, int64_t count, void* stream);
 
@@ -239,13 +247,13 @@ typedef enum {
   GB_SEMIRING_MAX_TIMES = 4,   /* (max, *): Viterbi on probabilities */
   GB_SEMIRINGS = 5
 } gb_semiring_t;
-int gb_gemm_semiring_f64(int semiring, int transA, int transB, int64_t M, int64_t N, int64_t K,
+GB_API int gb_gemm_semiring_f64(int semiring, int transA, int transB, int64_t M, int64_t N, int64_t K,
                          const double* A, int64_t lda, const double* B, int64_t ldb, int accumulate,
                          double* C, int64_t ldc, void* stream);
-int gb_gemm_semiring_f32(int semiring, int transA, int transB, int64_t M, int64_t N, int64_t K,
+GB_API int gb_gemm_semiring_f32(int semiring, int transA, int transB, int64_t M, int64_t N, int64_t K,
                          const float* A, int64_t lda, const float* B, int64_t ldb, int accumulate,
                          float* C, int64_t ldc, void* stream);
-int gb_gemm_semiring_i32(int semiring, int transA, int transB, int64_t M, int64_t N, int64_t K,
+GB_API int gb_gemm_semiring_i32(int semiring, int transA, int transB, int64_t M, int64_t N, int64_t K,
                          const int32_t* A, int64_t lda, const int32_t* B, int64_t ldb, int accumulate,
                          int32_t* C, int64_t ldc, void* stream);
 /* Autotuner: times every configuration per size class on the given problems (HOST copy
@@ -254,7 +262,7 @@ int gb_gemm_semiring_i32(int semiring, int transA, int transB, int64_t M, int64_
  * NULL) receives the best time per class in ms.  Synchronises `stream`.
  * Reference: pick_kernel_size / blocking_structure, src/kernel_structure.jl:76-99,
  * src/memory_management.jl:78-177. */
-int gb_autotune_grouped(int dtype_bytes, const gb_problem_t* host_problems, int count, int reps,
+GB_API int gb_autotune_grouped(int dtype_bytes, const gb_problem_t* host_problems, int count, int reps,
                         gb_grouped_tuning_t* out, float* class_ms, void* stream);
 
 /* ------------------------------------------------------------------ adjoint */
@@ -264,7 +272,7 @@ int gb_autotune_grouped(int dtype_bytes, const gb_problem_t* host_problems, int 
  * jmul!/gemm! (src/gemm.jl:244).  Products use the 3xBF16 split (x = hi + lo, the
  * lo*lo term dropped) with FP32 accumulation: per element |error| <= about
  * 2^-15 (|dC||B|^T)_ik plus FP32 summation error.  dC is read from memory once. */
-int gb_gemm_adjoint_f32(int64_t M, int64_t N, int64_t K, const float* A, int64_t lda, const float* B,
+GB_API int gb_gemm_adjoint_f32(int64_t M, int64_t N, int64_t K, const float* A, int64_t lda, const float* B,
                         int64_t ldb, const float* dC, int64_t lddc, float* dA, int64_t ldda, float* dB,
                         int64_t lddb, void* stream);
 
@@ -278,15 +286,15 @@ typedef struct {
   int32_t groups;        /* TMEM accumulation groups drained per output tile */
   double  flops_tensor;  /* BF16 tensor flops the plan issues */
 } gb_ozaki_plan_t;
-int gb_plan_ozaki(int64_t M, int64_t N, int64_t K, int slices, gb_ozaki_plan_t* out);
+GB_API int gb_plan_ozaki(int64_t M, int64_t N, int64_t K, int slices, gb_ozaki_plan_t* out);
 /* CRT plan for `moduli` moduli (1..20): slices = moduli, bits = t (the integer width of
  * the scaled operands: largest t <= 62 with 4 K 2^(2t) <= product of the moduli and
  * K 2^(2t) <= 2^125), k_chunk, products = groups = moduli, flops_tensor.
  * GB_ERR_UNSUPPORTED when no t >= 1 fits. */
-int gb_plan_ozaki_crt(int64_t M, int64_t N, int64_t K, int moduli, gb_ozaki_plan_t* out);
+GB_API int gb_plan_ozaki_crt(int64_t M, int64_t N, int64_t K, int moduli, gb_ozaki_plan_t* out);
 /* The plan of the most recent OZAKI (BF16 or CRT) gb_gemm_f64 call made by the calling
  * thread (zeroes before the first), e.g. the slice count an automatic call picked. */
-int gb_last_ozaki_plan(gb_ozaki_plan_t* out);
+GB_API int gb_last_ozaki_plan(gb_ozaki_plan_t* out);
 
 #ifdef __cplusplus
 }

@@ -3,7 +3,8 @@
 Compiles every ``csrc/*.cu`` translation unit in parallel with nvcc
 (``-gencode arch=compute_103a,code=sm_103a``) and links them into
 ``lib/libgbblas.so`` next to this file.  The CUDA runtime is linked statically, so
-the library only needs the driver at run time.  Objects go to ``_build/``.
+the library only needs the driver at run time.  Symbols are hidden by default; the
+header's ``GB_API`` entry points are the only exports.  Objects go to ``_build/``.
 """
 import concurrent.futures as cf
 import glob
@@ -19,8 +20,8 @@ LIB = os.path.join(LIBDIR, "libgbblas.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INCLUDE,
-              "-Xptxas", "-warn-spills"]
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
+              "-I" + INCLUDE, "-Xptxas", "-warn-spills"]
 
 
 def _nvcc():
@@ -74,7 +75,10 @@ def build(force=False, verbose=False, jobs=None):
             list(ex.map(compile_one, todo))
     if force or todo or _stale(LIB, objs):
         tmp = LIB + ".tmp%d" % os.getpid()
-        cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs
+        vscript = os.path.join(BUILD, "exports.map")   # the C ABI only (std templates stay local)
+        with open(vscript, "w") as f:
+            f.write("{ global: gb_*; local: *; };\n")
+        cmd = [nvcc] + ARCH + ["-shared", "-Xlinker", "--version-script=" + vscript, "-o", tmp] + objs
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -84,3 +84,13 @@ def test_ozaki_crt_plan_matches_restatement(K, moduli):
     nch = (kb + 15) // 16
     assert got["k_chunk"] == 64 * ((kb + nch - 1) // nch)
     assert got["flops_tensor"] == 2.0 * 256 * 128 * kb * 64 * moduli
+
+
+def test_only_the_c_abi_is_exported():
+    """The dynamic symbol table is exactly the header's gb_* functions (internal C++ hidden)."""
+    import subprocess
+    out = subprocess.run(["nm", "-D", "--defined-only", gbblas.LIB_PATH], capture_output=True, text=True)
+    if out.returncode != 0:
+        pytest.skip("nm unavailable")
+    syms = {line.split()[-1] for line in out.stdout.splitlines() if line.strip()}
+    assert syms == set(declared_functions()), sorted(syms ^ set(declared_functions()))[:10]
