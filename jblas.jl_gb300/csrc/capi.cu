@@ -721,7 +721,7 @@ int gb_gemm_f64(int transA, int transB, int64_t M, int64_t N, int64_t K, double 
       const double ku = static_cast<double>(K) * std::ldexp(1.0, -53);
       *err_bound_out = (alpha == 0.0 || K == 0) ? 0.0 : ku / (1.0 - ku);
     }
-    return native_gemm_f64(transA, transB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, s);
+    return native_gemm_f64(transA, transB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, dev->sms, s);
   }
   if (mode == GB_MODE_OZAKI_CRT)
     return crt_gemm(dev, transA, transB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, slices, err_bound_out, s);
@@ -736,7 +736,7 @@ int gb_gemm_f32(int transA, int transB, int64_t M, int64_t N, int64_t K, float a
   if (rc) return rc;
   rc = check_gemm_args(transA, transB, M, N, K, lda, ldb, ldc, A, B, C, alpha != 0.0f);
   if (rc) return rc;
-  return native_gemm_f32(transA, transB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc,
+  return native_gemm_f32(transA, transB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, dev->sms,
                          static_cast<cudaStream_t>(stream));
 }
 

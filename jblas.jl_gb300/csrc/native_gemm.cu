@@ -70,19 +70,27 @@ static int launch_simt(int ta, int tb, int64_t M, int64_t N, int64_t K, T alpha,
   return GB_OK;
 }
 
+// Tile choice: the large tiles (fewer operand loads per FMA) unless they leave SMs idle, then
+// smaller ones for more CTAs (measured at 1024^3: FP32 64x64 tiles 24 TFLOP/s against 15.5 for
+// 128x128 with 64 CTAs on 152 SMs; FP64 32x32 tiles +7%).  Every tile shape runs the same
+// per-element chain, so the choice never changes a result bit.
 int native_gemm_f64(int ta, int tb, int64_t M, int64_t N, int64_t K, double alpha, const double* A,
-                    int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc,
+                    int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc, int sms,
                     cudaStream_t s) {
   if (M == 0 || N == 0) return GB_OK;
   if (alpha == 0.0 || K == 0) return launch_scale<double>(M, N, beta, C, ldc, s);
+  if (((M + 63) / 64) * ((N + 63) / 64) < 2 * static_cast<int64_t>(sms))
+    return launch_simt<double, 32, 32, 16, 4, 4>(ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, s);
   return launch_simt<double, 64, 64, 16, 4, 4>(ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, s);
 }
 
 int native_gemm_f32(int ta, int tb, int64_t M, int64_t N, int64_t K, float alpha, const float* A,
-                    int64_t lda, const float* B, int64_t ldb, float beta, float* C, int64_t ldc,
+                    int64_t lda, const float* B, int64_t ldb, float beta, float* C, int64_t ldc, int sms,
                     cudaStream_t s) {
   if (M == 0 || N == 0) return GB_OK;
   if (alpha == 0.0f || K == 0) return launch_scale<float>(M, N, beta, C, ldc, s);
+  if (((M + 127) / 128) * ((N + 127) / 128) < static_cast<int64_t>(sms))
+    return launch_simt<float, 64, 64, 16, 4, 4>(ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, s);
   return launch_simt<float, 128, 128, 8, 8, 8>(ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, s);
 }
 
