@@ -559,18 +559,20 @@ def main():
 
     # ---------------------------------------------------------------- timed: end to end
     # Every step copies its inputs host -> device (pinned) and its result device -> host.
-    # Uploads and downloads run on their own streams (the two copy directions overlap) with
-    # double-buffered device inputs/outputs, so step i+1's uploads and step i-1's download
-    # overlap step i's compute (a serving pipeline).
+    # Uploads and downloads run on their own streams (the two copy directions overlap) into a
+    # ring of NBUF device input/output buffers: uploads run up to NBUF - 1 steps ahead of the
+    # compute and downloads trail it, so the host link's jitter (it is shared with the node's
+    # other GPUs) does not stall the compute (a serving pipeline with a queue of NBUF).
+    NBUF = 3
     barrier()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     up_stream, down_stream = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
-    A_e = [torch.empty_like(A_pin, device=dev) for _ in range(2)]
-    B_e = [torch.empty_like(B_pin, device=dev) for _ in range(2)]
-    C_e = [torch.empty((N, M), dtype=torch.float64, device=dev) for _ in range(2)]
-    up_done = [torch.cuda.Event() for _ in range(2)]
-    comp_done = [torch.cuda.Event() for _ in range(2)]
-    down_done = [torch.cuda.Event() for _ in range(2)]
+    A_e = [torch.empty_like(A_pin, device=dev) for _ in range(NBUF)]
+    B_e = [torch.empty_like(B_pin, device=dev) for _ in range(NBUF)]
+    C_e = [torch.empty((N, M), dtype=torch.float64, device=dev) for _ in range(NBUF)]
+    up_done = [torch.cuda.Event() for _ in range(NBUF)]
+    comp_done = [torch.cuda.Event() for _ in range(NBUF)]
+    down_done = [torch.cuda.Event() for _ in range(NBUF)]
     comp_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
                for _ in range(args.steps)]
     e0.record(stream)
@@ -583,9 +585,9 @@ def main():
                for _ in range(args.steps)]
 
     def upload(i):
-        b = i % 2
+        b = i % NBUF
         with torch.cuda.stream(up_stream):
-            if i >= 2:
+            if i >= NBUF:
                 up_stream.wait_event(comp_done[b])       # buffer b's previous compute is done
             up_ev[i][0].record(up_stream)
             A_e[b].copy_(A_pin, non_blocking=True)
@@ -595,14 +597,15 @@ def main():
 
     pipe_prof = gbblas.profile()
     pipe_prof.__enter__()
-    upload(0)
+    for i in range(min(NBUF - 1, args.steps)):
+        upload(i)
     for i in range(args.steps):
-        b = i % 2
-        if i + 1 < args.steps:
-            upload(i + 1)
+        b = i % NBUF
+        if i + NBUF - 1 < args.steps:
+            upload(i + NBUF - 1)
         stream.wait_event(up_done[b])
-        if i >= 2:
-            stream.wait_event(down_done[b])              # C_e[b] of step i-2 has been read
+        if i >= NBUF:
+            stream.wait_event(down_done[b])              # C_e[b] of step i - NBUF has been read
         comp_ev[i][0].record(stream)
         gbblas.gemm_(C_e[b].t(), A_e[b].t(), B_e[b].t(), mode=mode, slices=args.slices)
         comp_ev[i][1].record(stream)
@@ -736,7 +739,7 @@ def main():
             "kernel_ms_per_step": {k: v / args.steps for k, v in prof.ms.items()},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "TFLOP/s", "ms_per_step": ms_e2e,
-                    "pipeline": "double-buffered: uploads of step i+1 and download of step i overlap step i",
+                    "pipeline": "3-deep ring: uploads run up to 2 steps ahead, the download of step i overlaps step i+1",
                     "h2d_GBps": h2d_gbs, "d2h_GBps": d2h_gbs,
                     "compute_ms_in_pipeline": comp_in_pipeline,
                     "upload_ms_in_pipeline": up_in_pipeline, "download_ms_in_pipeline": down_in_pipeline,
