@@ -127,6 +127,21 @@ GB_API int gb_jmul_f64(double* D, const double* A, const double* X, int64_t M, i
 GB_API int gb_jmul_f32(float* D, const float* A, const float* X, int64_t M, int64_t N, int64_t P,
                 void* stream);
 
+/* ------------------------------------------------------------------ kernel! (pointer form) */
+/* jBLAS's pointer-level micro-kernels on device pointers, with their argument meaning.
+ * kernel!(pD, pA, pX, Kernel{Mk,Pk,stride_AD,stride_X,N}) (src/kernels.jl:212-239):
+ *   D (Mk x Pk) += A (Mk x N) * X (N x Pk), A and D with leading dimension stride_AD, X with
+ *   stride_X; per element d = fma(a_n, x_n, d) for n = 1..N in order, starting from D's value
+ *   (bit-identical to the reference's vmuladd chain).
+ * init != 0: initkernel! (src/kernels.jl:240-273): D = A * X with d = a_1 * x_1, then the same
+ *   chain (D is not read).
+ * Extensions: any Mk (the reference requires a multiple of the SIMD width, src/kernels.jl:219)
+ * and any size; N = 0 leaves D unchanged (init: D = 0). */
+GB_API int gb_kernel_f64(double* pD, const double* pA, const double* pX, int64_t Mk, int64_t Pk, int64_t stride_AD,
+                         int64_t stride_X, int64_t N, int init, void* stream);
+GB_API int gb_kernel_f32(float* pD, const float* pA, const float* pX, int64_t Mk, int64_t Pk, int64_t stride_AD,
+                         int64_t stride_X, int64_t N, int init, void* stream);
+
 /* ------------------------------------------------------------------ BLAS-3 GEMM */
 /* C = alpha*op(A)*op(B) + beta*C; op(X) = X (trans = 0) or X^T (trans = 1).
  * op(A) is M x K, op(B) is K x N, C is M x N; lda >= rows of A as stored, etc.

@@ -626,6 +626,22 @@ static int semiring_entry(Fn fn, int sr, int ta, int tb, int64_t M, int64_t N, i
   return fn(sr, ta, tb, M, N, K, A, lda, B, ldb, accumulate, C, ldc, static_cast<cudaStream_t>(stream));
 }
 
+// kernel! / initkernel! entry points: argument checks, then the onto-D chain or jmul!'s chain.
+template <typename T, typename Onto, typename Init>
+static int kernel_entry(Onto onto, Init init_fn, T* D, const T* A, const T* X, int64_t Mk, int64_t Pk,
+                        int64_t sAD, int64_t sX, int64_t N, int init, void* stream) {
+  DeviceInfo* dev = nullptr;
+  int rc = device_info(&dev);
+  if (rc) return rc;
+  if (Mk < 0 || Pk < 0 || N < 0 || (init != 0 && init != 1)) return GB_ERR_INVALID_VALUE;
+  if (sAD < (Mk > 1 ? Mk : 1) || sX < (N > 1 ? N : 1)) return GB_ERR_INVALID_VALUE;
+  if (Mk == 0 || Pk == 0) return GB_OK;
+  if (!is_device_ptr(D) || (N > 0 && (!is_device_ptr(A) || !is_device_ptr(X)))) return GB_ERR_INVALID_VALUE;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (init) return init_fn(0, 0, Mk, Pk, N, T(1), A, sAD, X, sX, T(0), D, sAD, dev->sms, s);
+  return onto(Mk, Pk, N, A, sAD, X, sX, D, sAD, dev->sms, s);
+}
+
 extern "C" {
 
 const char* gb_status_string(int status) {
@@ -738,6 +754,18 @@ int gb_gemm_f32(int transA, int transB, int64_t M, int64_t N, int64_t K, float a
   if (rc) return rc;
   return native_gemm_f32(transA, transB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, dev->sms,
                          static_cast<cudaStream_t>(stream));
+}
+
+int gb_kernel_f64(double* pD, const double* pA, const double* pX, int64_t Mk, int64_t Pk, int64_t stride_AD,
+                  int64_t stride_X, int64_t N, int init, void* stream) {
+  return kernel_entry<double>(native_kernel_onto_f64, native_gemm_f64, pD, pA, pX, Mk, Pk, stride_AD, stride_X, N,
+                              init, stream);
+}
+
+int gb_kernel_f32(float* pD, const float* pA, const float* pX, int64_t Mk, int64_t Pk, int64_t stride_AD,
+                  int64_t stride_X, int64_t N, int init, void* stream) {
+  return kernel_entry<float>(native_kernel_onto_f32, native_gemm_f32, pD, pA, pX, Mk, Pk, stride_AD, stride_X, N,
+                             init, stream);
 }
 
 int gb_gemm_adjoint_f32(int64_t M, int64_t N, int64_t K, const float* A, int64_t lda, const float* B,

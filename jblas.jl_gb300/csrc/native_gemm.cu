@@ -16,6 +16,7 @@ namespace gb {
 // jmul!'s FMA chain with the BLAS alpha/beta epilogue (beta == 0: C is not read).
 template <typename T>
 struct FmaChainOp {
+  static constexpr bool kInitFromC = false;
   static constexpr bool kPairs = false;   // the chain's order is part of its result
   T alpha, beta;
   static __device__ __forceinline__ T init() { return T(-0.0); }
@@ -23,6 +24,18 @@ struct FmaChainOp {
   __device__ __forceinline__ void store(T* c, T acc) const {
     *c = (beta == T(0)) ? alpha * acc : fma_t<T>(alpha, acc, beta * *c);
   }
+};
+
+// jBLAS's kernel! (src/kernels.jl:212-238): the chain starts from D's value,
+// d = fma(a_n, x_n, d) for n = 1..N in order, and d is stored as is.
+template <typename T>
+struct FmaOntoCOp {
+  static constexpr bool kInitFromC = true;
+  static constexpr bool kPairs = false;
+  int unused;
+  static __device__ __forceinline__ T init() { return T(0); }
+  static __device__ __forceinline__ T step(T acc, T a, T b) { return fma_t<T>(a, b, acc); }
+  __device__ __forceinline__ void store(T* c, T acc) const { *c = acc; }
 };
 
 // C = beta * C (alpha == 0 or K == 0); beta == 0 writes zeros without reading C.
@@ -68,6 +81,37 @@ static int launch_simt(int ta, int tb, int64_t M, int64_t N, int64_t K, T alpha,
 #undef GB_SIMT_CASE
   GB_CUDA_TRY(cudaGetLastError());
   return GB_OK;
+}
+
+template <typename T, int BM, int BN, int BK, int TM, int TN>
+static int launch_onto(int64_t M, int64_t N, int64_t K, const T* A, int64_t lda, const T* B, int64_t ldb, T* C,
+                       int64_t ldc, cudaStream_t s) {
+  dim3 grid;
+  if (!simt_grid<BM, BN>(M, N, &grid)) return GB_ERR_UNSUPPORTED;
+  constexpr int NT = (BM / TM) * (BN / TN);
+  const FmaOntoCOp<T> op{0};
+  GB_LAUNCH(GB_KERNEL_NATIVE_GEMM, s,
+            (simt_gemm_kernel<T, FmaOntoCOp<T>, BM, BN, BK, TM, TN, false, false><<<grid, NT, 0, s>>>(
+                M, N, K, op, A, lda, B, ldb, C, ldc)));
+  GB_CUDA_TRY(cudaGetLastError());
+  return GB_OK;
+}
+
+int native_kernel_onto_f64(int64_t M, int64_t N, int64_t K, const double* A, int64_t lda, const double* B,
+                           int64_t ldb, double* C, int64_t ldc, int sms, cudaStream_t s) {
+  if (M == 0 || N == 0 || K == 0) return GB_OK;   // an empty chain leaves D as it is
+  if (((M + 63) / 64) * ((N + 63) / 64) < 2 * static_cast<int64_t>(sms))
+    return launch_onto<double, 32, 32, 16, 4, 4>(M, N, K, A, lda, B, ldb, C, ldc, s);
+  return launch_onto<double, 64, 64, 16, 4, 4>(M, N, K, A, lda, B, ldb, C, ldc, s);
+}
+
+// FP32 always on 64x64 tiles: the 128x128 tile's 64 accumulators loaded from D exceed its
+// 128-register budget.
+int native_kernel_onto_f32(int64_t M, int64_t N, int64_t K, const float* A, int64_t lda, const float* B,
+                           int64_t ldb, float* C, int64_t ldc, int sms, cudaStream_t s) {
+  (void)sms;
+  if (M == 0 || N == 0 || K == 0) return GB_OK;
+  return launch_onto<float, 64, 64, 16, 4, 4>(M, N, K, A, lda, B, ldb, C, ldc, s);
 }
 
 // Tile choice: the large tiles (fewer operand loads per FMA) unless they leave SMs idle, then

@@ -11,6 +11,8 @@
 //   Op::init()            the accumulator before k = 1
 //   Op::step(acc, a, b)   one contraction step, applied for k = 1..K in order
 //   op.store(c, acc)      the epilogue writing one element of C
+//   Op::kInitFromC        when true the accumulator starts from C's element instead of init()
+//                         (jBLAS's kernel!, which folds A*X onto D's value)
 //   Op::kPairs, Op::step2(acc, a0, b0, a1, b1)
 //                         when kPairs, two consecutive k are folded in by one call (for
 //                         associative, exact reductions such as min / max, whose result
@@ -100,9 +102,18 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN), sizeof(T) == 4 ? 2 : 0)
 
   T acc[TM][TN];
 #pragma unroll
-  for (int i = 0; i < TM; ++i)
+  for (int i = 0; i < TM; ++i) {
+    const int64_t m = m0 + (i < VM ? ty * VM + i : BM / 2 + ty * VM + (i - VM));
 #pragma unroll
-    for (int j = 0; j < TN; ++j) acc[i][j] = Op::init();
+    for (int j = 0; j < TN; ++j) {
+      if constexpr (Op::kInitFromC) {
+        const int64_t n = n0 + (j < VN ? tx * VN + j : BN / 2 + tx * VN + (j - VN));
+        acc[i][j] = (m < M && n < N) ? C[m + n * ldc] : T(0);
+      } else {
+        acc[i][j] = Op::init();
+      }
+    }
+  }
 
   auto load_k = [&](int buf, int kk, T (&a)[TM], T (&b)[TN]) {
     const VecT<T, VM> a0 = *reinterpret_cast<const VecT<T, VM>*>(&As[buf][kk][ty * VM]);

@@ -91,6 +91,8 @@ SIGNATURES = {
                                             c_i64, ctypes.c_double, c_vp, c_i64, c_i64, c_i64, c_vp]),
     "gb_gemm_strided_batched_f32": (c_int, [c_i64, c_i64, c_i64, ctypes.c_float, c_vp, c_i64, c_i64, c_vp, c_i64,
                                             c_i64, ctypes.c_float, c_vp, c_i64, c_i64, c_i64, c_vp]),
+    "gb_kernel_f64": (c_int, [c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, c_i64, c_i64, c_int, c_vp]),
+    "gb_kernel_f32": (c_int, [c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, c_i64, c_i64, c_int, c_vp]),
     "gb_gemm_semiring_f64": (c_int, [c_int, c_int, c_int, c_i64, c_i64, c_i64, c_vp, c_i64, c_vp, c_i64, c_int,
                                      c_vp, c_i64, c_vp]),
     "gb_gemm_semiring_f32": (c_int, [c_int, c_int, c_int, c_i64, c_i64, c_i64, c_vp, c_i64, c_vp, c_i64, c_int,

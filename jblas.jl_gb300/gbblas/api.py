@@ -113,9 +113,60 @@ def gemm_(C, A, B, alpha=1.0, beta=0.0, *, mode="native", slices=0, return_bound
     return (C, bound) if return_bound else C
 
 
-def jmul_(D, A, X):
-    """jmul!(D, A, X): D = A * X with jBLAS's per-element FMA order (src/gemm.jl:244)."""
+def jmul_(D, A, X, a_prefetch=7, x_prefetch=7, a_loc=3, x_loc=3, d_loc=3):
+    """jmul!(D, A, X[, Val(Aprefetch_freq), Val(Xprefetch_freq), Val(A_loc), Val(X_loc), Val(D_loc)]):
+    D = A * X with jBLAS's per-element FMA order (src/gemm.jl:244-246).
+
+    The trailing arguments are jmul!'s software-prefetch distances and cache localities, CPU
+    cache hints; they are checked (non-negative integers, localities 0..3) and have no GPU
+    counterpart (the operands stream through shared memory)."""
+    for name, v in (("a_prefetch", a_prefetch), ("x_prefetch", x_prefetch)):
+        if not isinstance(v, int) or v < 0:
+            raise ValueError("%s must be a non-negative integer, got %r" % (name, v))
+    for name, v in (("a_loc", a_loc), ("x_loc", x_loc), ("d_loc", d_loc)):
+        if not isinstance(v, int) or not 0 <= v <= 3:
+            raise ValueError("%s must be a cache locality 0..3, got %r" % (name, v))
     return gemm_(D, A, X, 1.0, 0.0, mode="native")
+
+
+def kernel_raw(pD, pA, pX, Mk, Pk, stride_AD, stride_X, N, *, dtype, init=False, stream=None):
+    """kernel!(pD, pA, pX, Kernel{Mk,Pk,stride_AD,stride_X,N}) on device pointers (ints)
+    (src/kernels.jl:212-239): D (Mk x Pk) += A (Mk x N) * X (N x Pk), A and D with leading
+    dimension stride_AD, X with stride_X, per element d = fma(a_n, x_n, d) for n = 1..N from D's
+    value.  init=True is initkernel! (src/kernels.jl:240-273): D = A * X."""
+    name = {torch.float64: "gb_kernel_f64", torch.float32: "gb_kernel_f32"}.get(dtype)
+    if name is None:
+        raise TypeError("kernel! computes in float64 or float32, got %s" % dtype)
+    rc = getattr(_lib.lib(), name)(ctypes.c_void_p(pD), ctypes.c_void_p(pA), ctypes.c_void_p(pX), Mk, Pk,
+                                   stride_AD, stride_X, N, int(bool(init)), ctypes.c_void_p(stream))
+    check(rc, name)
+
+
+def kernel_(D, A, X, init=False):
+    """kernel!(D, A, X) on tensors: D (Mk x Pk) += A (Mk x N) * X (N x Pk) in jBLAS's chain
+    (init=True: D = A * X, initkernel!).  D and A are column-major with the same leading
+    dimension (the kernel's stride_AD), X column-major.  Returns D."""
+    dt = _dtype_of(D, A, X)
+    Mk, N = A.shape
+    N2, Pk = X.shape
+    if N2 != N or tuple(D.shape) != (Mk, Pk):
+        raise DimensionMismatch("D is %dx%d, A is %dx%d, X is %dx%d" % (*D.shape, Mk, N, N2, Pk))
+    Ds, ldd, td = _storage(D, "D", allow_copy=False)
+    As, lda, ta = _storage(A, "A", allow_copy=False)
+    Xs, ldx, tx = _storage(X, "X", allow_copy=False)
+    if td or ta or tx:
+        raise ValueError("kernel!: D, A and X must be column-major")
+    if N > 1 and Pk > 1 and lda != ldd:
+        raise ValueError("kernel!: A and D share one leading dimension (stride_AD), got %d and %d" % (lda, ldd))
+    sad = ldd if Pk > 1 else (lda if N > 1 else max(1, Mk))   # the one that is used
+    kernel_raw(Ds.data_ptr(), As.data_ptr(), Xs.data_ptr(), Mk, Pk, sad, ldx, N, dtype=dt, init=init,
+               stream=torch.cuda.current_stream(D.device).cuda_stream)
+    return D
+
+
+def initkernel_(D, A, X):
+    """initkernel!(D, A, X): D = A * X with d = a_1 x_1 first (src/kernels.jl:240-273)."""
+    return kernel_(D, A, X, init=True)
 
 
 def gemm_strided_batched_(C, A, B, alpha=1.0, beta=0.0):

@@ -4,7 +4,10 @@
 Julia front end of libgbblas (the GB300 GEMM behind jBLAS.jl's `jmul!`).  A thin `ccall`
 layer over the C ABI in `include/gbblas.h`:
 
-    jmul!(D, A, X)                 D = A * X, jBLAS's per-element FMA order (src/gemm.jl:244)
+    jmul!(D, A, X[, Val(...) x 5])  D = A * X, jBLAS's per-element FMA order (src/gemm.jl:244);
+                                   the prefetch Val hints are accepted and unused
+    kernel!(pD, pA, pX, Kernel{Mₖ,Pₖ,stride_AD,stride_X,N}())   D += A*X as jBLAS's pointer kernel
+    initkernel!(pD, pA, pX, Kernel{...}())                        D = A*X (src/kernels.jl:212-273)
     gemm!(C, A, B)                 the same call spelled as in the task (`jmul!` semantics)
     gemm!(C, A, B, α, β; mode, slices)   BLAS-3 form; mode = :native | :ozaki | :ozaki_crt
     gemm_adjoint!(dA, dB, A, B, dC)      dA = dC*B', dB = A'*dC in one launch (Float32)
@@ -101,6 +104,50 @@ function gemm!(C::AbstractMatrix{Float32}, A::AbstractMatrix{Float32}, B::Abstra
     C
 end
 
+# jmul!'s software-prefetch distances and cache localities (src/gemm.jl:244-246) are CPU cache
+# hints; accepted for drop-in use and unused on the GPU.
+jmul!(D::AbstractMatrix{T}, A::AbstractMatrix{T}, X::AbstractMatrix{T}, ::Val, hints::Val...) where {T <: Union{Float32, Float64}} =
+    jmul!(D, A, X)
+
+"""
+    Kernel{Mₖ,Pₖ,stride_AD,stride_X,N}()
+
+The micro-kernel descriptor of jBLAS's pointer kernels (src/kernel_structure.jl): an Mₖ×Pₖ tile
+of D, A and D with leading dimension stride_AD, X with stride_X, contraction length N.
+"""
+struct Kernel{Mₖ,Pₖ,stride_AD,stride_X,N} end
+
+for (T, f) in ((Float64, :gb_kernel_f64), (Float32, :gb_kernel_f32))
+    @eval begin
+        function kernel!(pD::Ptr{$T}, pA::Ptr{$T}, pX::Ptr{$T},
+                         ::Kernel{Mₖ,Pₖ,stride_AD,stride_X,N}) where {Mₖ,Pₖ,stride_AD,stride_X,N}
+            check(ccall(($(QuoteNode(f)), libgbblas), Cint,
+                        (Ptr{$T}, Ptr{$T}, Ptr{$T}, Int64, Int64, Int64, Int64, Int64, Cint, Ptr{Cvoid}),
+                        pD, pA, pX, Mₖ, Pₖ, stride_AD, stride_X, N, Cint(0), current_stream()))
+            nothing
+        end
+        function initkernel!(pD::Ptr{$T}, pA::Ptr{$T}, pX::Ptr{$T},
+                             ::Kernel{Mₖ,Pₖ,stride_AD,stride_X,N}) where {Mₖ,Pₖ,stride_AD,stride_X,N}
+            check(ccall(($(QuoteNode(f)), libgbblas), Cint,
+                        (Ptr{$T}, Ptr{$T}, Ptr{$T}, Int64, Int64, Int64, Int64, Int64, Cint, Ptr{Cvoid}),
+                        pD, pA, pX, Mₖ, Pₖ, stride_AD, stride_X, N, Cint(1), current_stream()))
+            nothing
+        end
+    end
+end
+@doc """
+    kernel!(pD, pA, pX, ::Kernel{Mₖ,Pₖ,stride_AD,stride_X,N})      D += A * X
+
+jBLAS's pointer-level micro-kernel (src/kernels.jl:212-239) on device pointers (`Ptr{T}`, e.g.
+`reinterpret(Ptr{Float64}, pointer(cuarray))`): per element d = fma(a_n, x_n, d) for n = 1..N
+starting from D's value, bit-identical to the reference.
+""" kernel!
+@doc """
+    initkernel!(pD, pA, pX, ::Kernel{Mₖ,Pₖ,stride_AD,stride_X,N})  D = A * X
+
+jBLAS's initkernel! (src/kernels.jl:240-273): d = a_1 x_1, then d = fma(a_n, x_n, d), n = 2..N.
+""" initkernel!
+
 # ------------------------------------------------------------------ mul! with transposes
 import LinearAlgebra
 using LinearAlgebra: Transpose, Adjoint
@@ -159,12 +206,6 @@ function enable_mul!(::Type{T}) where {T <: AbstractMatrix}
     nothing
 end
 
-"""
-    gemm_strided_batched!(C, A, B, α=1, β=0) -> C
-
-`C[:,:,i] = α A[:,:,i] B[:,:,i] + β C[:,:,i]` for every `i`, one launch (the batch form of
-jBLAS's `fastmul!`), per element jBLAS's FMA chain.  Arrays are column-major device arrays.
-"""
 for (T, f) in ((Float64, :gb_gemm_strided_batched_f64), (Float32, :gb_gemm_strided_batched_f32))
     @eval function gemm_strided_batched!(C::AbstractArray{$T,3}, A::AbstractArray{$T,3}, B::AbstractArray{$T,3},
                                          α::Number = one($T), β::Number = zero($T))
@@ -178,19 +219,16 @@ for (T, f) in ((Float64, :gb_gemm_strided_batched_f64), (Float32, :gb_gemm_strid
         C
     end
 end
+@doc """
+    gemm_strided_batched!(C, A, B, α=1, β=0) -> C
+
+`C[:,:,i] = α A[:,:,i] B[:,:,i] + β C[:,:,i]` for every `i`, one launch (the batch form of
+jBLAS's `fastmul!`), per element jBLAS's FMA chain.  Arrays are column-major device arrays.
+""" gemm_strided_batched!
 
 const SEMIRING = Dict(:min_plus => Cint(0), :max_plus => Cint(1), :max_min => Cint(2), :min_max => Cint(3),
                      :max_times => Cint(4))
 
-"""
-    semiring_mul!(C, A, B, semiring=:min_plus; accumulate=false) -> C
-
-`C[i,j] = ⊕_k A[i,k] ⊗ B[k,j]` (or `C[i,j] ⊕ ...` with `accumulate`) over the semiring
-`semiring` ∈ `:min_plus`, `:max_plus`, `:max_min`, `:min_max`, `:max_times` (⊕ first), the
-custom-number-type use jBLAS gives for its `Vec` fallback ("so it works with min-plus
-algebra", src/jBLAS.jl:10).  `A` and `B` may be transpose/adjoint views.  Floating point: ⊕
-ignores NaN operands and a zero result is +0.0; Int32 + and * wrap.
-"""
 for (T, f) in ((Float64, :gb_gemm_semiring_f64), (Float32, :gb_gemm_semiring_f32), (Int32, :gb_gemm_semiring_i32))
     @eval function semiring_mul!(C::AbstractMatrix{$T}, A::AbstractMatrix{$T}, B::AbstractMatrix{$T},
                                  semiring::Symbol = :min_plus; accumulate::Bool = false)
@@ -206,6 +244,15 @@ for (T, f) in ((Float64, :gb_gemm_semiring_f64), (Float32, :gb_gemm_semiring_f32
         C
     end
 end
+@doc """
+    semiring_mul!(C, A, B, semiring=:min_plus; accumulate=false) -> C
+
+`C[i,j] = ⊕_k A[i,k] ⊗ B[k,j]` (or `C[i,j] ⊕ ...` with `accumulate`) over the semiring
+`semiring` ∈ `:min_plus`, `:max_plus`, `:max_min`, `:min_max`, `:max_times` (⊕ first), the
+custom-number-type use jBLAS gives for its `Vec` fallback ("so it works with min-plus
+algebra", src/jBLAS.jl:10).  `A` and `B` may be transpose/adjoint views.  Floating point: ⊕
+ignores NaN operands and a zero result is +0.0; Int32 + and * wrap.
+""" semiring_mul!
 
 """
     gemm_adjoint!(dA, dB, A, B, dC) -> (dA, dB)

@@ -102,6 +102,31 @@ void or_jmul_f32(float* D, const float* A, const float* X, i64 M, i64 N, i64 P) 
   or_gemm_f32(0, 0, M, P, N, 1.0f, A, M, X, N, 0.0f, D, M, 1);
 }
 
+/* kernel!(pD, pA, pX, Kernel{Mk,Pk,stride_AD,stride_X,N}) (src/kernels.jl:212-238): D (Mk x Pk,
+ * leading dimension sAD) += A (Mk x N, sAD) * X (N x Pk, sX), per element
+ * d = fma(a_n, x_n, d) for n = 1..N starting from D's value (the vmuladd chain).  init:
+ * initkernel! (src/kernels.jl:240-273), d = a_1 * x_1 (rounded) first, D not read; N = 0
+ * leaves D (init: 0). */
+#define OR_KERNEL(NAME, T, FMA)                                                                     \
+  void NAME(T* D, const T* A, const T* X, i64 Mk, i64 Pk, i64 sAD, i64 sX, i64 N, int init) {      \
+    for (i64 p = 0; p < Pk; ++p)                                                                    \
+      for (i64 m = 0; m < Mk; ++m) {                                                                \
+        T d;                                                                                        \
+        i64 n0 = 0;                                                                                 \
+        if (init) {                                                                                 \
+          if (N == 0) { D[m + p * sAD] = (T)0; continue; }                                          \
+          d = A[m] * X[p * sX];                                                                     \
+          n0 = 1;                                                                                   \
+        } else {                                                                                    \
+          d = D[m + p * sAD];                                                                       \
+        }                                                                                           \
+        for (i64 n = n0; n < N; ++n) d = FMA(A[m + n * sAD], X[n + p * sX], d);                     \
+        D[m + p * sAD] = d;                                                                         \
+      }                                                                                             \
+  }
+OR_KERNEL(or_kernel_f64, double, fma)
+OR_KERNEL(or_kernel_f32, float, fmaf)
+
 /* ------------------------------------------------- register-tiled timed baseline */
 /*
  * The jmul! algorithm as the reference generates it: a rows x cols register tile

@@ -62,6 +62,8 @@ def lib():
         L.or_quad_entries.argtypes = [ctypes.c_int, ctypes.c_int, c_i64, _vp, c_i64, _vp, c_i64, c_i64, _vp,
                                       _vp, _vp, _vp, ctypes.c_int]
         L.or_fma_array.argtypes = [c_i64, _vp, _vp, _vp, _vp]
+        for nm in ("or_kernel_f64", "or_kernel_f32"):
+            getattr(L, nm).argtypes = [_vp, _vp, _vp, c_i64, c_i64, c_i64, c_i64, c_i64, ctypes.c_int]
         L.or_chain_entries_f64.argtypes = [ctypes.c_int, ctypes.c_int, c_i64, ctypes.c_double, _vp, c_i64,
                                            _vp, c_i64, ctypes.c_double, _vp, c_i64, c_i64, _vp, _vp, _vp,
                                            ctypes.c_int]
@@ -112,6 +114,19 @@ def gemm(A, B, C=None, alpha=1.0, beta=0.0, trans_a=False, trans_b=False, dtype=
 def jmul(A, X, dtype=np.float64):
     """jmul!(D, A, X) restated: D = A * X (src/gemm.jl:244)."""
     return gemm(A, X, dtype=dtype)
+
+
+def kernel_chain(D, A, X, Mk, Pk, stride_AD, stride_X, N, init=False, dtype=np.float64):
+    """jBLAS's kernel! / initkernel! on flat column-major buffers (src/kernels.jl:212-273):
+    D (Mk x Pk, leading dimension stride_AD) += A (Mk x N, stride_AD) * X (N x Pk, stride_X),
+    per element d = fma(a_n, x_n, d) for n = 1..N from D's value; init: D = A * X with
+    d = a_1 x_1 first.  Returns the new D buffer (a copy)."""
+    D = np.array(D, dtype=dtype).ravel(order="K")
+    A = np.ascontiguousarray(np.asarray(A, dtype=dtype).ravel(order="K"))
+    X = np.ascontiguousarray(np.asarray(X, dtype=dtype).ravel(order="K"))
+    fn = lib().or_kernel_f64 if np.dtype(dtype) == np.float64 else lib().or_kernel_f32
+    fn(_ptr(D), _ptr(A), _ptr(X), Mk, Pk, stride_AD, stride_X, N, int(bool(init)))
+    return D
 
 
 def jmul_tiled(A, B, nthreads=1, dtype=np.float64, out=None):
@@ -216,10 +231,11 @@ def _round_to_float(q: Fraction, bits: int) -> float:
     return sign * float(v)
 
 
-def chain_exact(A, X, bits=53):
+def chain_exact(A, X, bits=53, D0=None):
     """D = A*X with each step d = round(a*x + d) evaluated exactly (pure Python, slow).
 
     d = a1*x1 (rounded), then d = fma(ak, xk, d) for k = 2..K (src/gemm.jl:76-89,154-168).
+    With D0 (kernel!, src/kernels.jl:212-238): d starts at D0[i, j] and every k is an fma.
     Signed zeros follow IEEE: round(-0) keeps the sign of an exact zero sum as fma does."""
     A = np.asarray(A, dtype=np.float64)
     X = np.asarray(X, dtype=np.float64)
@@ -228,13 +244,17 @@ def chain_exact(A, X, bits=53):
     D = np.zeros((M, P), dtype=np.float64, order="F")
     for j in range(P):
         for i in range(M):
-            if K == 0:
+            if D0 is not None:
+                d, k_first = float(D0[i, j]), 0
+            elif K == 0:
                 D[i, j] = 0.0
                 continue
-            d = _round_to_float(Fraction(A[i, 0]) * Fraction(X[0, j]), bits)
-            if d == 0.0:
-                d = math.copysign(0.0, A[i, 0]) * math.copysign(1.0, X[0, j])
-            for k in range(1, K):
+            else:
+                d = _round_to_float(Fraction(A[i, 0]) * Fraction(X[0, j]), bits)
+                if d == 0.0:
+                    d = math.copysign(0.0, A[i, 0]) * math.copysign(1.0, X[0, j])
+                k_first = 1
+            for k in range(k_first, K):
                 exact = Fraction(A[i, k]) * Fraction(X[k, j]) + Fraction(d)
                 r = _round_to_float(exact, bits)
                 if r == 0.0:

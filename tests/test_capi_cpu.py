@@ -94,3 +94,15 @@ def test_only_the_c_abi_is_exported():
         pytest.skip("nm unavailable")
     syms = {line.split()[-1] for line in out.stdout.splitlines() if line.strip()}
     assert syms == set(declared_functions()), sorted(syms ^ set(declared_functions()))[:10]
+
+
+def test_jmul_prefetch_hints_are_validated():
+    """jmul!'s Val prefetch distances and localities are accepted and checked before any GPU work."""
+    import torch
+    D = torch.zeros(2, 2, dtype=torch.float64)
+    with pytest.raises(ValueError):
+        gbblas.jmul_(D, D, D, a_prefetch=-1)
+    with pytest.raises(ValueError):
+        gbblas.jmul_(D, D, D, a_loc=4)
+    with pytest.raises(ValueError):
+        gbblas.jmul_(D, D, D, 7, 7, 3, 3, 9)

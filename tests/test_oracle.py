@@ -253,3 +253,27 @@ def test_quad_is_near_exact_and_agrees_with_dot2():
     qt, _ = oracle.quad_entries(np.asfortranarray(A.T), np.asfortranarray(B.T), rows, cols, trans_a=True,
                                 trans_b=True)
     assert np.array_equal(qt, qhi)
+
+
+@pytest.mark.parametrize("dtype,bits", [(np.float64, 53), (np.float32, 24)])
+@pytest.mark.parametrize("init", [False, True])
+def test_kernel_chain_matches_exact_restatement(dtype, bits, init):
+    """kernel! / initkernel! on strided buffers (A and D share stride_AD) equal the exact-rational
+    chain started from D's value (kernel!) or from the rounded first product (initkernel!)."""
+    g = np.random.default_rng(23 + int(init))
+    Mk, Pk, N, sAD, sX = 7, 5, 9, 10, 12
+    Abuf = g.standard_normal(sAD * N).astype(dtype)
+    Xbuf = g.standard_normal(sX * Pk).astype(dtype)
+    Dbuf = g.standard_normal(sAD * Pk).astype(dtype)
+    Abuf[3] = -0.0
+    Dbuf[sAD + 1] = -0.0
+    out = oracle.kernel_chain(Dbuf, Abuf, Xbuf, Mk, Pk, sAD, sX, N, init=init, dtype=dtype)
+    A = Abuf.reshape(N, sAD).T[:Mk, :N].astype(np.float64)
+    X = Xbuf.reshape(Pk, sX).T[:N, :Pk].astype(np.float64)
+    D0 = Dbuf.reshape(Pk, sAD).T[:Mk, :Pk].astype(np.float64)
+    ref = oracle.chain_exact(A, X, bits=bits, D0=None if init else D0).astype(dtype)
+    got = out.reshape(Pk, sAD).T[:Mk, :Pk]
+    assert np.array_equal(got.view(np.uint64 if dtype == np.float64 else np.uint32),
+                          np.asarray(ref, order="C").view(np.uint64 if dtype == np.float64 else np.uint32))
+    # padding rows between the tiles are untouched
+    assert np.array_equal(out.reshape(Pk, sAD)[:, Mk:], Dbuf.reshape(Pk, sAD)[:, Mk:])
