@@ -129,6 +129,13 @@ def jmul_(D, A, X, a_prefetch=7, x_prefetch=7, a_loc=3, x_loc=3, d_loc=3):
     return gemm_(D, A, X, 1.0, 0.0, mode="native")
 
 
+def fastmul_(D, A, X):
+    """fastmul!(D, A, X) (src/kernels.jl:202-208): the whole small product as one tile, per element
+    d = a_1 x_1 then d = fma(a_n, x_n, d) — jmul!'s chain, so the same call.  Many such products
+    of one shape go through gemm_strided_batched_ in one launch."""
+    return gemm_(D, A, X, 1.0, 0.0, mode="native")
+
+
 def kernel_raw(pD, pA, pX, Mk, Pk, stride_AD, stride_X, N, *, dtype, init=False, stream=None):
     """kernel!(pD, pA, pX, Kernel{Mk,Pk,stride_AD,stride_X,N}) on device pointers (ints)
     (src/kernels.jl:212-239): D (Mk x Pk) += A (Mk x N) * X (N x Pk), A and D with leading

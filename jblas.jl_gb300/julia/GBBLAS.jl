@@ -6,6 +6,7 @@ layer over the C ABI in `include/gbblas.h`:
 
     jmul!(D, A, X[, Val(...) x 5])  D = A * X, jBLAS's per-element FMA order (src/gemm.jl:244);
                                    the prefetch Val hints are accepted and unused
+    fastmul!(D, A, X)              the small-matrix single-tile product (src/kernels.jl:202-208)
     kernel!(pD, pA, pX, Kernel{Mₖ,Pₖ,stride_AD,stride_X,N}())   D += A*X as jBLAS's pointer kernel
     initkernel!(pD, pA, pX, Kernel{...}())                        D = A*X (src/kernels.jl:212-273)
     gemm!(C, A, B)                 the same call spelled as in the task (`jmul!` semantics)
@@ -103,6 +104,15 @@ function gemm!(C::AbstractMatrix{Float32}, A::AbstractMatrix{Float32}, B::Abstra
                 0, 0, M, N, K, α, pointer(A), ld(A), pointer(B), ld(B), β, pointer(C), ld(C), current_stream()))
     C
 end
+
+"""
+    fastmul!(D, A, X) -> D
+
+jBLAS's single-tile product of small static matrices (src/kernels.jl:202-208): per element
+d = a_1 x_1, then d = fma(a_n, x_n, d) — jmul!'s chain, so the same call.
+"""
+fastmul!(D::AbstractMatrix{T}, A::AbstractMatrix{T}, X::AbstractMatrix{T}) where {T <: Union{Float32, Float64}} =
+    jmul!(D, A, X)
 
 # jmul!'s software-prefetch distances and cache localities (src/gemm.jl:244-246) are CPU cache
 # hints; accepted for drop-in use and unused on the GPU.

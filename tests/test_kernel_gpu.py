@@ -110,3 +110,14 @@ def test_kernel_argument_errors():
     assert L.gb_kernel_f64(p, p, p, -1, 2, 4, 4, 4, 0, st) == bad
     host = np.zeros(64)
     assert L.gb_kernel_f64(ctypes.c_void_p(host.ctypes.data), p, p, 4, 2, 4, 4, 4, 0, st) == bad
+
+
+def test_fastmul_is_jmul_chain():
+    """fastmul!(D, A, X) on a small static-size product equals the oracle's jmul! chain bit for bit."""
+    g = np.random.default_rng(12)
+    A = np.asfortranarray(g.standard_normal((8, 5)))
+    X = np.asfortranarray(g.standard_normal((5, 6)))
+    D = torch.empty((6, 8), dtype=torch.float64, device="cuda").t()
+    gbblas.fastmul_(D, torch.from_numpy(A.T.copy()).cuda().t(), torch.from_numpy(X.T.copy()).cuda().t())
+    torch.cuda.synchronize()
+    same_bits(np.ascontiguousarray(D.cpu().numpy()), np.ascontiguousarray(oracle.jmul(A, X)))
