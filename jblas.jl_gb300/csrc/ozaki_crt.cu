@@ -715,11 +715,11 @@ int crt_split(const double* X, int64_t R, int64_t K, int64_t rs, int64_t ks, con
 
 // ============================================================== reconstruction
 
-// The double nearest (ties to even) to the signed 128-bit integer hi:lo times 2^E.  Normal
-// results are assembled from the rounded 53-bit significand in integer arithmetic; results
-// outside the normal range round the significand to 53 bits (the 64-bit window keeps a
-// sticky bit, so one conversion rounds correctly) and then take one correctly rounded
-// power-of-two scaling, as ldexp(double(C'), E) does.
+// The double nearest (ties to even) to the signed 128-bit integer hi:lo times 2^E.  The top 64
+// bits from the leading one, with a sticky bit for everything below, round to 53 bits in one
+// correctly rounded u64 -> f64 conversion; a normal result then only needs its exponent moved
+// (an integer add on the bits), and results outside the normal range take one correctly
+// rounded power-of-two scaling of that double, as ldexp(double(C'), E) does.
 __device__ __forceinline__ double i128_times_pow2(uint64_t hi, uint64_t lo, int E) {
   const bool neg = static_cast<int64_t>(hi) < 0;
   if (neg) {
@@ -741,21 +741,16 @@ __device__ __forceinline__ double i128_times_pow2(uint64_t hi, uint64_t lo, int 
     sticky = false;
     lead = 63 - lz;
   }
-  uint64_t mant = top >> 11;
-  const uint64_t rest = top & 0x7FFull;
-  const bool up = rest > 0x400ull || (rest == 0x400ull && (sticky || (mant & 1ull)));
-  mant += up ? 1ull : 0ull;
-  int ex = lead + E;
-  if (mant >> 53) {
-    mant >>= 1;
-    ++ex;
-  }
-  if (ex >= -1022 && ex <= 1023) {
-    const uint64_t bits = (neg ? 0x8000000000000000ull : 0ull) | (static_cast<uint64_t>(ex + 1023) << 52) |
-                          (mant & 0x000FFFFFFFFFFFFFull);
-    return __longlong_as_double(static_cast<long long>(bits));
-  }
-  const double d = scale_pow2(__ull2double_rn(top | (sticky ? 1ull : 0ull)), lead - 63 + E);
+  // round the 64-bit window (sticky bit folded into its last place) to 53 bits in one correctly
+  // rounded conversion: a double in [2^63, 2^64]; a normal result only moves its exponent
+  const double dr = __ull2double_rn(top | (sticky ? 1ull : 0ull));
+  const long long db = __double_as_longlong(dr);
+  const int shift = lead - 63 + E;
+  const int exf = static_cast<int>(db >> 52) + shift;   // biased exponent of the result
+  if (exf >= 1 && exf <= 2046)
+    return __longlong_as_double((db + (static_cast<long long>(shift) << 52)) |
+                                (neg ? static_cast<long long>(0x8000000000000000ull) : 0ll));
+  const double d = scale_pow2(dr, shift);
   return neg ? -d : d;
 }
 
@@ -790,6 +785,7 @@ __device__ __forceinline__ void crt_combine_column(const uint8_t* __restrict__ b
   uint32_t words[NMOD];   // all loads in flight before any use
 #pragma unroll
   for (int g = 0; g < NMOD; ++g) words[g] = __ldg(reinterpret_cast<const uint32_t*>(base + g * res_plane));
+  double out[4] = {0.0, 0.0, 0.0, 0.0};
 #pragma unroll
   for (int q = 0; q < 4; ++q) {   // one element at a time: only its accumulators are live
     if (i0 + q >= M) continue;
@@ -837,7 +833,16 @@ __device__ __forceinline__ void crt_combine_column(const uint8_t* __restrict__ b
       val = alpha * val;
     else if (ab == 2)
       val = fma(alpha, val, beta * ccol[i0 + q]);
-    ccol[i0 + q] = val;
+    out[q] = val;
+  }
+  double* dst = ccol + i0;
+  if (i0 + 3 < M && (reinterpret_cast<uintptr_t>(dst) & 15) == 0) {   // two 16-byte stores
+    reinterpret_cast<double2*>(dst)[0] = make_double2(out[0], out[1]);
+    reinterpret_cast<double2*>(dst)[1] = make_double2(out[2], out[3]);
+  } else {
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      if (i0 + q < M) dst[q] = out[q];
   }
 }
 
