@@ -26,6 +26,7 @@ import json
 import os
 import statistics
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -92,7 +93,7 @@ class ClockSampler:
     def __init__(self, device_index):
         self.dev = device_index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench_%d.csv" % os.getpid())
+        self.path = os.path.join(tempfile.gettempdir(), "gbblas_clocks_%d.csv" % os.getpid())
 
     def start(self):
         try:
@@ -395,7 +396,7 @@ def workload_grouped(args):
         plan = grouped.GroupedGemm(As, Bs, Cs)
         flops = plan.flops()
         default_ms = _event_ms(plan.run, max(1, args.steps), stream)
-        cache = os.path.join(ROOT, "gpurun_out", "grouped_tuning.json")
+        cache = os.path.join(tempfile.gettempdir(), "gbblas_grouped_tuning_%d.json" % os.getpid())
         tuning, class_ms = grouped.autotune(plan, reps=3, cache=cache)
         plan.tuning = tuning
         graph = plan.capture()

@@ -70,7 +70,7 @@ static int device_info(DeviceInfo** out) {
     GB_CUDA_TRY(cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev));
     if (major != 10 || minor != 3) {
       std::snprintf(g_last_detail, sizeof(g_last_detail),
-                    "device %d is sm_%d%d; this build carries sm_103a code only", dev, major, minor);
+                    "device %d is sm_%d%d; libgbblas carries sm_103a code only", dev, major, minor);
       d.status_code = GB_ERR_NO_DEVICE;
     } else {
       cudaError_t e = cudaMalloc(&d.status, sizeof(DeviceStatus));
