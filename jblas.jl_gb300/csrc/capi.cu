@@ -165,7 +165,8 @@ int make_plane_tmap(CUtensorMap* map, const void* base, int64_t K, int64_t rows,
 // The last CRT call's plan lives on the device until someone asks for it.
 struct PendingCrtPlan {
   bool pending = false;
-  CrtDevicePlan* slot = nullptr;
+  CrtPlanRecord* record = nullptr;   // the tagged read-back copy of the call's plan
+  unsigned long long seq = 0;
   cudaEvent_t done = nullptr;
   int64_t M = 0, N = 0, kb_total = 0, k_chunk = 0;
 };
@@ -490,8 +491,9 @@ static int crt_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int64
   CrtPlan plan;   // K chunking and a schedule for up to n_ws moduli
   int rc = crt_make_plan(M, N, K, n_ws, t_fixed, &plan);
   if (rc) return rc;
-  CrtDevicePlan* slot = nullptr;
-  rc = crt_plan_slot(&slot);
+  CrtPlanRecord* record = nullptr;
+  unsigned long long seq = 0;
+  rc = crt_plan_record(&record, &seq);
   if (rc) return rc;
 
   const bool sums = (moduli == 0 || err_bound_out);
@@ -515,41 +517,51 @@ static int crt_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int64
     pp.log2m[n] = crt_log2_product(n);
     pp.tk[n] = crt_bits_for(K, n);
   }
-  void* scratch = nullptr;
-  GB_CUDA_TRY(cudaMallocFromPoolAsync(&scratch, crt_plan_scratch_bytes(), dev->pool, s));
-  rc = crt_plan_device(os.a, os.b, pp, slot, scratch, s);
-  cudaFreeAsync(scratch, s);
-  if (!rc && err_bound_out) {
-    CrtDevicePlan hp;
-    cudaError_t e = cudaMemcpyAsync(&hp, slot, sizeof(hp), cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) rc = gb_set_cuda_error(e, "ozaki crt plan");
-    else *err_bound_out = hp.bound;
-  }
-  if (rc) {
-    cudaFreeAsync(os.ws, s);
-    return rc;
-  }
-
+  // The call's workspace: its plan record (read by its kernels only), residue planes of A and
+  // B, residue-product planes and the row/column exponents.
   const int64_t mpad = (M + 255) / 256 * 256, npad = (N + 255) / 256 * 256;
+  const size_t plan_bytes = align256(sizeof(CrtDevicePlan));
   const size_t pa_bytes = align256(static_cast<size_t>(n_ws) * M * pitch * 2);
   const size_t pb_bytes = align256(static_cast<size_t>(n_ws) * N * pitch * 2);
   const size_t res_bytes = align256(static_cast<size_t>(n_ws) * mpad * npad);
   const size_t ex_bytes = align256((M + N) * sizeof(int32_t));
   char* ws = nullptr;
-  cudaError_t e = cudaMallocFromPoolAsync(reinterpret_cast<void**>(&ws), pa_bytes + pb_bytes + res_bytes + ex_bytes,
-                                          dev->pool, s);
+  cudaError_t e = cudaMallocFromPoolAsync(reinterpret_cast<void**>(&ws),
+                                          plan_bytes + pa_bytes + pb_bytes + res_bytes + ex_bytes, dev->pool, s);
   if (e != cudaSuccess) {
     cudaFreeAsync(os.ws, s);
     return gb_set_cuda_error(e, "ozaki crt workspace");
   }
-  __nv_bfloat16* pa = reinterpret_cast<__nv_bfloat16*>(ws);
-  __nv_bfloat16* pb = reinterpret_cast<__nv_bfloat16*>(ws + pa_bytes);
-  uint8_t* res = reinterpret_cast<uint8_t*>(ws + pa_bytes + pb_bytes);
-  int32_t* ea = reinterpret_cast<int32_t*>(ws + pa_bytes + pb_bytes + res_bytes);
+  CrtDevicePlan* plan_d = reinterpret_cast<CrtDevicePlan*>(ws);
+  char* wsp = ws + plan_bytes;
+  void* scratch = nullptr;
+  e = cudaMallocFromPoolAsync(&scratch, crt_plan_scratch_bytes(), dev->pool, s);
+  if (e != cudaSuccess) {
+    cudaFreeAsync(ws, s);
+    cudaFreeAsync(os.ws, s);
+    return gb_set_cuda_error(e, "ozaki crt planner scratch");
+  }
+  rc = crt_plan_device(os.a, os.b, pp, plan_d, record, seq, scratch, s);
+  cudaFreeAsync(scratch, s);
+  if (!rc && err_bound_out) {
+    CrtDevicePlan hp;
+    e = cudaMemcpyAsync(&hp, plan_d, sizeof(hp), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) rc = gb_set_cuda_error(e, "ozaki crt plan");
+    else *err_bound_out = hp.bound;
+  }
+  if (rc) {
+    cudaFreeAsync(ws, s);
+    cudaFreeAsync(os.ws, s);
+    return rc;
+  }
+  __nv_bfloat16* pa = reinterpret_cast<__nv_bfloat16*>(wsp);
+  __nv_bfloat16* pb = reinterpret_cast<__nv_bfloat16*>(wsp + pa_bytes);
+  uint8_t* res = reinterpret_cast<uint8_t*>(wsp + pa_bytes + pb_bytes);
+  int32_t* ea = reinterpret_cast<int32_t*>(wsp + pa_bytes + pb_bytes + res_bytes);
   int32_t* eb = ea + M;
-  rc = crt_split(A, M, K, a_rs, a_ks, os.a.amax_bits, slot, pa, pitch, ea, s);
-  if (!rc) rc = crt_split(B, N, K, b_rs, b_ks, os.b.amax_bits, slot, pb, pitch, eb, s);
+  rc = crt_split(A, M, K, a_rs, a_ks, os.a.amax_bits, plan_d, pa, pitch, ea, s);
+  if (!rc) rc = crt_split(B, N, K, b_rs, b_ks, os.b.amax_bits, plan_d, pb, pitch, eb, s);
   if (!rc) {
     CrtGemmArgs ga;
     ga.planes_a = pa;
@@ -572,14 +584,15 @@ static int crt_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int64
     const int64_t ctas = 2 * static_cast<int64_t>(tc_pair_tiles(M, N));
     const int64_t cap = dev->sms & ~1;
     ga.grid = static_cast<int>(ctas < cap ? ctas : cap);
-    ga.plan = slot;
+    ga.plan = plan_d;
     rc = crt_gemm_launch(ga, plan, s);
   }
   if (!rc) {
     PendingCrtPlan& pd = g_pending_crt;
     if (!pd.done && cudaEventCreateWithFlags(&pd.done, cudaEventDisableTiming) != cudaSuccess) pd.done = nullptr;
     pd.pending = pd.done && cudaEventRecord(pd.done, s) == cudaSuccess;
-    pd.slot = slot;
+    pd.record = record;
+    pd.seq = seq;
     pd.M = M;
     pd.N = N;
     pd.kb_total = plan.kb_total;
@@ -596,8 +609,14 @@ static int resolve_pending_crt_plan() {
   if (!pd.pending) return GB_OK;
   pd.pending = false;
   GB_CUDA_TRY(cudaEventSynchronize(pd.done));
-  CrtDevicePlan hp;
-  GB_CUDA_TRY(cudaMemcpy(&hp, pd.slot, sizeof(hp), cudaMemcpyDeviceToHost));
+  CrtPlanRecord rec;
+  GB_CUDA_TRY(cudaMemcpy(&rec, pd.record, sizeof(rec), cudaMemcpyDeviceToHost));
+  if (rec.seq != pd.seq) {   // CRT_PLAN_RING later calls on this device reused the record
+    std::snprintf(g_last_detail, sizeof(g_last_detail),
+                  "the plan of this thread's last CRT call was overwritten by %d later calls", CRT_PLAN_RING);
+    return GB_ERR_INVALID_VALUE;
+  }
+  const CrtDevicePlan& hp = rec.plan;
   g_last_plan.slices = hp.n;
   g_last_plan.bits = hp.t;
   g_last_plan.k_chunk = static_cast<int32_t>(pd.k_chunk);

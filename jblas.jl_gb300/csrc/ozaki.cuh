@@ -111,11 +111,17 @@ struct CrtTable {
 };
 
 // The plan of one CRT call, written on the device by the planner kernel (no host round trip)
-// and read by the split, residue-product and combine kernels.
+// into the call's own workspace and read by the split, residue-product and combine kernels.
 struct CrtDevicePlan {
   int32_t n;        // moduli
   int32_t t;        // integer bits of the scaled operands
   double bound;     // a-priori normwise error bound of the plan
+};
+// A copy of a call's plan for reading back on the host (gb_last_ozaki_plan), tagged with the
+// call's sequence number; kept in a per-device ring that no kernel reads.
+struct CrtPlanRecord {
+  CrtDevicePlan plan;
+  unsigned long long seq;
 };
 
 // Inputs of the planner besides the statistics.
@@ -148,14 +154,17 @@ int crt_bits_for(int64_t K, int n);
 int crt_make_plan(int64_t M, int64_t N, int64_t K, int n, int t, CrtPlan* plan);
 // The constant table (built once on the host).
 const CrtTable& crt_table();
-// A plan slot from the current device's ring of plan records (reused after 256 calls).
-int crt_plan_slot(CrtDevicePlan** slot);
+// A read-back record from the current device's ring (reused after CRT_PLAN_RING calls; the
+// record's tag tells whether it still holds the call `seq`).
+constexpr int CRT_PLAN_RING = 4096;
+int crt_plan_record(CrtPlanRecord** record, unsigned long long* seq);
 // Planner: from the statistics (with sums), the fewest moduli whose bound meets pp.tol (or
-// pp.n_fixed) and the widest t they allow; writes *plan on the device.  `scratch` holds
-// crt_plan_scratch_bytes() bytes of stream-ordered workspace.
+// pp.n_fixed) and the widest t they allow; writes *plan (the call's workspace) and the tagged
+// copy *record on the device.  `scratch` holds crt_plan_scratch_bytes() bytes of stream-ordered
+// workspace.
 size_t crt_plan_scratch_bytes();
 int crt_plan_device(const OzRowStats& sa, const OzRowStats& sb, const CrtPlanParams& pp, CrtDevicePlan* plan,
-                    void* scratch, cudaStream_t s);
+                    CrtPlanRecord* record, unsigned long long seq, void* scratch, cudaStream_t s);
 // Residue planes (BF16, [modulus][row][pitch], plan->n of them) and row exponents of op(X).
 int crt_split(const double* X, int64_t R, int64_t K, int64_t rs, int64_t ks, const unsigned long long* amax_bits,
               const CrtDevicePlan* plan, __nv_bfloat16* planes, int64_t pitch, int32_t* exps, cudaStream_t s);

@@ -258,15 +258,14 @@ int crt_make_plan(int64_t M, int64_t N, int64_t K, int n, int t, CrtPlan* plan) 
 
 namespace {
 struct CrtDeviceState {
-  CrtDevicePlan* ring = nullptr;
-  std::atomic<uint32_t> next{0};
+  CrtPlanRecord* ring = nullptr;
+  std::atomic<unsigned long long> next{0};
 };
-constexpr int CRT_PLAN_RING = 256;
 std::mutex g_crt_mu;
 std::vector<std::unique_ptr<CrtDeviceState>> g_crt_dev;
 }  // namespace
 
-int crt_plan_slot(CrtDevicePlan** slot) {
+int crt_plan_record(CrtPlanRecord** record, unsigned long long* seq) {
   int dev = 0;
   GB_CUDA_TRY(cudaGetDevice(&dev));
   CrtDeviceState* st = nullptr;
@@ -275,13 +274,15 @@ int crt_plan_slot(CrtDevicePlan** slot) {
     if (static_cast<int>(g_crt_dev.size()) <= dev) g_crt_dev.resize(dev + 1);
     if (!g_crt_dev[dev]) {
       auto fresh = std::make_unique<CrtDeviceState>();
-      GB_CUDA_TRY(cudaMalloc(&fresh->ring, sizeof(CrtDevicePlan) * CRT_PLAN_RING));
-      GB_CUDA_TRY(cudaMemset(fresh->ring, 0, sizeof(CrtDevicePlan) * CRT_PLAN_RING));
+      GB_CUDA_TRY(cudaMalloc(&fresh->ring, sizeof(CrtPlanRecord) * CRT_PLAN_RING));
+      GB_CUDA_TRY(cudaMemset(fresh->ring, 0xFF, sizeof(CrtPlanRecord) * CRT_PLAN_RING));   // no call's tag
       g_crt_dev[dev] = std::move(fresh);
     }
     st = g_crt_dev[dev].get();
   }
-  *slot = st->ring + (st->next.fetch_add(1) % CRT_PLAN_RING);
+  const unsigned long long k = st->next.fetch_add(1);
+  *record = st->ring + (k % CRT_PLAN_RING);
+  *seq = k;
   return GB_OK;
 }
 
@@ -355,7 +356,9 @@ __global__ void __launch_bounds__(CRT_PLAN_THREADS) crt_plan_kernel(const OzRowS
                                                                     const __grid_constant__ CrtPlanParams pp,
                                                                     int blocks_a, CrtPlanPartial* __restrict__ part,
                                                                     unsigned int* __restrict__ counter,
-                                                                    CrtDevicePlan* __restrict__ out) {
+                                                                    CrtDevicePlan* __restrict__ out,
+                                                                    CrtPlanRecord* __restrict__ record,
+                                                                    unsigned long long seq) {
   __shared__ int s_ref[CRT_PLAN_THREADS / 32], s_nf[CRT_PLAN_THREADS / 32];
   __shared__ double s_acc[4][CRT_PLAN_THREADS / 32];
   __shared__ int s_last;
@@ -365,6 +368,8 @@ __global__ void __launch_bounds__(CRT_PLAN_THREADS) crt_plan_kernel(const OzRowS
       out->n = pp.n_fixed;
       out->t = pp.t_fixed;
       out->bound = __longlong_as_double(0x7FF8000000000000ll);
+      record->plan = *out;
+      record->seq = seq;
     }
     return;
   }
@@ -512,12 +517,14 @@ __global__ void __launch_bounds__(CRT_PLAN_THREADS) crt_plan_kernel(const OzRowS
     out->n = n;
     out->t = t;
     out->bound = crt_bound_dev(nonfinite, nrm[0], nrm[1], E[0], E[1], S[0], S[1], pp.K, t);
+    record->plan = *out;
+    record->seq = seq;
     *counter = 0u;
   }
 }
 
 int crt_plan_device(const OzRowStats& sa, const OzRowStats& sb, const CrtPlanParams& pp, CrtDevicePlan* plan,
-                    void* scratch, cudaStream_t s) {
+                    CrtPlanRecord* record, unsigned long long seq, void* scratch, cudaStream_t s) {
   auto blocks_for = [](int64_t R) {
     int64_t b = (R + CRT_PLAN_THREADS - 1) / CRT_PLAN_THREADS;
     if (b > CRT_PLAN_BLOCKS) b = CRT_PLAN_BLOCKS;
@@ -529,7 +536,8 @@ int crt_plan_device(const OzRowStats& sa, const OzRowStats& sb, const CrtPlanPar
                                                           sizeof(CrtPlanPartial) * 2 * CRT_PLAN_BLOCKS);
   GB_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(unsigned int), s));
   GB_LAUNCH(GB_KERNEL_OZAKI_STATS, s,
-            (crt_plan_kernel<<<ba + bb, CRT_PLAN_THREADS, 0, s>>>(sa, sb, pp, ba, part, counter, plan)));
+            (crt_plan_kernel<<<ba + bb, CRT_PLAN_THREADS, 0, s>>>(sa, sb, pp, ba, part, counter, plan, record,
+                                                                   seq)));
   GB_CUDA_TRY(cudaGetLastError());
   return GB_OK;
 }
