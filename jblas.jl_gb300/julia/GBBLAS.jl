@@ -46,6 +46,11 @@ current_stream() = isdefined(Main, :CUDA) ? Base.unsafe_convert(Ptr{Cvoid}, Main
 
 ld(X::AbstractMatrix) = max(1, stride(X, 2))
 
+# The device address of an array as a plain `Ptr` for the C ABI: CUDA.jl's `pointer` gives a
+# `CuPtr`, which Julia does not convert to `Ptr`; both are 64-bit addresses, so the bits are
+# reinterpreted (a plain `Ptr` passes through unchanged).
+devptr(X::AbstractArray{T}) where {T} = reinterpret(Ptr{T}, pointer(X))
+
 """
     jmul!(D, A, X) -> D
 
@@ -59,7 +64,7 @@ function jmul!(D::AbstractMatrix{Float64}, A::AbstractMatrix{Float64}, X::Abstra
     check(ccall((:gb_gemm_f64, libgbblas), Cint,
                 (Cint, Cint, Int64, Int64, Int64, Cdouble, Ptr{Cdouble}, Int64, Ptr{Cdouble}, Int64, Cdouble,
                  Ptr{Cdouble}, Int64, Cint, Cint, Ptr{Cdouble}, Ptr{Cvoid}),
-                0, 0, M, P, N, 1.0, pointer(A), ld(A), pointer(X), ld(X), 0.0, pointer(D), ld(D),
+                0, 0, M, P, N, 1.0, devptr(A), ld(A), devptr(X), ld(X), 0.0, devptr(D), ld(D),
                 MODE[:native], 0, C_NULL, current_stream()))
     D
 end
@@ -69,7 +74,7 @@ function jmul!(D::AbstractMatrix{Float32}, A::AbstractMatrix{Float32}, X::Abstra
     check(ccall((:gb_gemm_f32, libgbblas), Cint,
                 (Cint, Cint, Int64, Int64, Int64, Cfloat, Ptr{Cfloat}, Int64, Ptr{Cfloat}, Int64, Cfloat,
                  Ptr{Cfloat}, Int64, Ptr{Cvoid}),
-                0, 0, M, P, N, 1f0, pointer(A), ld(A), pointer(X), ld(X), 0f0, pointer(D), ld(D),
+                0, 0, M, P, N, 1f0, devptr(A), ld(A), devptr(X), ld(X), 0f0, devptr(D), ld(D),
                 current_stream()))
     D
 end
@@ -91,7 +96,7 @@ function gemm!(C::AbstractMatrix{Float64}, A::AbstractMatrix{Float64}, B::Abstra
     check(ccall((:gb_gemm_f64, libgbblas), Cint,
                 (Cint, Cint, Int64, Int64, Int64, Cdouble, Ptr{Cdouble}, Int64, Ptr{Cdouble}, Int64, Cdouble,
                  Ptr{Cdouble}, Int64, Cint, Cint, Ptr{Cdouble}, Ptr{Cvoid}),
-                0, 0, M, N, K, α, pointer(A), ld(A), pointer(B), ld(B), β, pointer(C), ld(C),
+                0, 0, M, N, K, α, devptr(A), ld(A), devptr(B), ld(B), β, devptr(C), ld(C),
                 MODE[mode], slices, C_NULL, current_stream()))
     C
 end
@@ -101,7 +106,7 @@ function gemm!(C::AbstractMatrix{Float32}, A::AbstractMatrix{Float32}, B::Abstra
     check(ccall((:gb_gemm_f32, libgbblas), Cint,
                 (Cint, Cint, Int64, Int64, Int64, Cfloat, Ptr{Cfloat}, Int64, Ptr{Cfloat}, Int64, Cfloat,
                  Ptr{Cfloat}, Int64, Ptr{Cvoid}),
-                0, 0, M, N, K, α, pointer(A), ld(A), pointer(B), ld(B), β, pointer(C), ld(C), current_stream()))
+                0, 0, M, N, K, α, devptr(A), ld(A), devptr(B), ld(B), β, devptr(C), ld(C), current_stream()))
     C
 end
 
@@ -184,8 +189,8 @@ function mul!(C::AbstractMatrix{Float64}, A::AbstractMatrix{Float64}, B::Abstrac
     check(ccall((:gb_gemm_f64, libgbblas), Cint,
                 (Cint, Cint, Int64, Int64, Int64, Cdouble, Ptr{Cdouble}, Int64, Ptr{Cdouble}, Int64, Cdouble,
                  Ptr{Cdouble}, Int64, Cint, Cint, Ptr{Cdouble}, Ptr{Cvoid}),
-                op_flag(A), op_flag(B), M, N, K, Float64(α), pointer(As), ld(As), pointer(Bs), ld(Bs), Float64(β),
-                pointer(C), ld(C), MODE[mode], slices, C_NULL, current_stream()))
+                op_flag(A), op_flag(B), M, N, K, Float64(α), devptr(As), ld(As), devptr(Bs), ld(Bs), Float64(β),
+                devptr(C), ld(C), MODE[mode], slices, C_NULL, current_stream()))
     C
 end
 function mul!(C::AbstractMatrix{Float32}, A::AbstractMatrix{Float32}, B::AbstractMatrix{Float32},
@@ -196,8 +201,8 @@ function mul!(C::AbstractMatrix{Float32}, A::AbstractMatrix{Float32}, B::Abstrac
     check(ccall((:gb_gemm_f32, libgbblas), Cint,
                 (Cint, Cint, Int64, Int64, Int64, Cfloat, Ptr{Cfloat}, Int64, Ptr{Cfloat}, Int64, Cfloat,
                  Ptr{Cfloat}, Int64, Ptr{Cvoid}),
-                op_flag(A), op_flag(B), M, N, K, Float32(α), pointer(As), ld(As), pointer(Bs), ld(Bs), Float32(β),
-                pointer(C), ld(C), current_stream()))
+                op_flag(A), op_flag(B), M, N, K, Float32(α), devptr(As), ld(As), devptr(Bs), ld(Bs), Float32(β),
+                devptr(C), ld(C), current_stream()))
     C
 end
 
@@ -224,8 +229,8 @@ for (T, f) in ((Float64, :gb_gemm_strided_batched_f64), (Float32, :gb_gemm_strid
         check(ccall(($(QuoteNode(f)), libgbblas), Cint,
                     (Int64, Int64, Int64, $T, Ptr{$T}, Int64, Int64, Ptr{$T}, Int64, Int64, $T, Ptr{$T}, Int64, Int64,
                      Int64, Ptr{Cvoid}),
-                    M, N, K, $T(α), pointer(A), max(1, stride(A, 2)), stride(A, 3), pointer(B), max(1, stride(B, 2)),
-                    stride(B, 3), $T(β), pointer(C), max(1, stride(C, 2)), stride(C, 3), n, current_stream()))
+                    M, N, K, $T(α), devptr(A), max(1, stride(A, 2)), stride(A, 3), devptr(B), max(1, stride(B, 2)),
+                    stride(B, 3), $T(β), devptr(C), max(1, stride(C, 2)), stride(C, 3), n, current_stream()))
         C
     end
 end
@@ -249,8 +254,8 @@ for (T, f) in ((Float64, :gb_gemm_semiring_f64), (Float32, :gb_gemm_semiring_f32
         check(ccall(($(QuoteNode(f)), libgbblas), Cint,
                     (Cint, Cint, Cint, Int64, Int64, Int64, Ptr{$T}, Int64, Ptr{$T}, Int64, Cint, Ptr{$T}, Int64,
                      Ptr{Cvoid}),
-                    SEMIRING[semiring], op_flag(A), op_flag(B), M, N, K, pointer(As), ld(As), pointer(Bs), ld(Bs),
-                    Cint(accumulate), pointer(C), ld(C), current_stream()))
+                    SEMIRING[semiring], op_flag(A), op_flag(B), M, N, K, devptr(As), ld(As), devptr(Bs), ld(Bs),
+                    Cint(accumulate), devptr(C), ld(C), current_stream()))
         C
     end
 end
@@ -276,8 +281,8 @@ function gemm_adjoint!(dA::AbstractMatrix{Float32}, dB::AbstractMatrix{Float32},
     check(ccall((:gb_gemm_adjoint_f32, libgbblas), Cint,
                 (Int64, Int64, Int64, Ptr{Cfloat}, Int64, Ptr{Cfloat}, Int64, Ptr{Cfloat}, Int64, Ptr{Cfloat}, Int64,
                  Ptr{Cfloat}, Int64, Ptr{Cvoid}),
-                M, N, K, pointer(A), ld(A), pointer(B), ld(B), pointer(dC), ld(dC), pointer(dA), ld(dA),
-                pointer(dB), ld(dB), current_stream()))
+                M, N, K, devptr(A), ld(A), devptr(B), ld(B), devptr(dC), ld(dC), devptr(dA), ld(dA),
+                devptr(dB), ld(dB), current_stream()))
     dA, dB
 end
 
@@ -305,8 +310,9 @@ if Base.find_package("ChainRulesCore") !== nothing
         C = gemm(A, B)
         function gemm_pullback(ΔC)
             dC = convert(typeof(C), ChainRulesCore.unthunk(ΔC))
-            dA = gemm!(similar(A), dC, permutedims(B), 1.0, 0.0; mode = :ozaki_crt)
-            dB = gemm!(similar(B), permutedims(A), dC, 1.0, 0.0; mode = :ozaki_crt)
+            # transposes as views: the library reads them through its transpose flags, no copies
+            dA = mul!(similar(A), dC, transpose(B), 1.0, 0.0; mode = :ozaki_crt)
+            dB = mul!(similar(B), transpose(A), dC, 1.0, 0.0; mode = :ozaki_crt)
             return ChainRulesCore.NoTangent(), dA, dB
         end
         return C, gemm_pullback
