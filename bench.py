@@ -432,7 +432,7 @@ def workload_grouped(args):
                {"dtype": "f64", "results": out,
                 "roofline": {"bound": "fp64_pipe", "achieved": f64["graph_tflops"], "peak": 1.25, "unit": "TFLOP/s",
                              "frac": f64["graph_tflops"] / 1.25, "peak_source": "nominal GB300 FP64"},
-                "gpu_launches": 2 * args.steps})
+            "gpu_launches": 2 * args.steps})
     return 0
 
 
@@ -630,6 +630,23 @@ def main():
     down_in_pipeline = statistics.median(a.elapsed_time(z) for a, z in down_ev)
     copy_stream = up_stream
 
+    # the blocking host-buffer entry point (the reference's own calling pattern: host operands
+    # in, host result out, one call at a time), on the same pinned buffers
+    host_api = None
+    if rank == 0:
+        A_hv, B_hv, C_hv = A_pin.numpy().T, B_pin.numpy().T, C_pin.numpy().T   # column-major views
+        gbblas.gemm_host(C_hv, A_hv, B_hv, mode=mode, slices=args.slices)     # warm-up
+        t_calls = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            gbblas.gemm_host(C_hv, A_hv, B_hv, mode=mode, slices=args.slices)
+            t_calls.append(time.perf_counter() - t0)
+        ms_host = statistics.median(t_calls) * 1e3
+        host_api = {"value": flops / (ms_host * 1e-3) / 1e12, "unit": "TFLOP/s", "ms_per_call": ms_host,
+                    "what": "one blocking gb_gemm_f64_host call per step on pinned host buffers: upload of A "
+                            "and B, the product, download of C, no overlap between calls (median of 3, host "
+                            "wall clock)"}
+
     # the host link alone: one step's uploads and download on the copy stream, no compute
     c0, c1, c2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
     with torch.cuda.stream(copy_stream):
@@ -750,6 +767,7 @@ def main():
                     "kernel_ms_in_pipeline": {k: v / args.steps for k, v in pipe_prof.ms.items()},
                     "h2d_bytes_per_step": int(A_pin.numel() * 8 + B_pin.numel() * 8),
                     "d2h_bytes_per_step": int(C_pin.numel() * 8)},
+            "host_api": host_api,
             "gpu_launches": launches,
             "clocks": clk,
         }

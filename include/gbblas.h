@@ -175,6 +175,24 @@ GB_API int gb_gemm_f32(int transA, int transB, int64_t M, int64_t N, int64_t K, 
                 const float* A, int64_t lda, const float* B, int64_t ldb, float beta,
                 float* C, int64_t ldc, void* stream);
 
+/* ------------------------------------------------------------------ host buffers */
+/* The same products on HOST buffers, for callers whose matrices live in host memory as the
+ * reference's MMatrix operands do (pageable or pinned; device pointers work too, through
+ * unified addressing).  The call uploads op(A), op(B) (and C when beta != 0) into library
+ * workspace, runs gb_gemm_* on `stream` with the same mode and arguments, downloads C and
+ * returns once `stream` has finished: results are those of the device call, bit for bit.
+ * A bounded on-device wait that expired is reported as GB_ERR_PIPELINE_TIMEOUT (the status
+ * word is read and cleared).  gb_jmul_*_host: jmul!(D, A, X) on host MMatrix-like buffers
+ * (leading dimensions M, N, M). */
+GB_API int gb_gemm_f64_host(int transA, int transB, int64_t M, int64_t N, int64_t K, double alpha, const double* A,
+                            int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc, int mode,
+                            int slices, double* err_bound_out, void* stream);
+GB_API int gb_gemm_f32_host(int transA, int transB, int64_t M, int64_t N, int64_t K, float alpha, const float* A,
+                            int64_t lda, const float* B, int64_t ldb, float beta, float* C, int64_t ldc, void* stream);
+GB_API int gb_jmul_f64_host(double* D, const double* A, const double* X, int64_t M, int64_t N, int64_t P,
+                            void* stream);
+GB_API int gb_jmul_f32_host(float* D, const float* A, const float* X, int64_t M, int64_t N, int64_t P, void* stream);
+
 /* ------------------------------------------------------------------ grouped GEMM */
 /* One independent product C = alpha*A*B + beta*C (column-major, no transposes, device
  * pointers; alpha == 0: A, B not read; beta == 0: C not read). */

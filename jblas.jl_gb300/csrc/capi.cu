@@ -661,6 +661,53 @@ static int kernel_entry(Onto onto, Init init_fn, T* D, const T* A, const T* X, i
   return onto(Mk, Pk, N, A, sAD, X, sX, D, sAD, dev->sms, s);
 }
 
+// Host-buffer products: upload the stored operands (packed, leading dimension = rows), run the
+// device call on them, download C, synchronise, read the status word.
+template <typename T, typename DeviceCall>
+static int gemm_host(DeviceCall call, int ta, int tb, int64_t M, int64_t N, int64_t K, T alpha, const T* A,
+                     int64_t lda, const T* B, int64_t ldb, T beta, T* C, int64_t ldc, void* stream) {
+  DeviceInfo* dev = nullptr;
+  int rc = device_info(&dev);
+  if (rc) return rc;
+  if ((ta != 0 && ta != 1) || (tb != 0 && tb != 1) || M < 0 || N < 0 || K < 0) return GB_ERR_INVALID_VALUE;
+  const int64_t ra = ta ? K : M, ca = ta ? M : K, rb = tb ? N : K, cb = tb ? K : N;
+  if (lda < (ra > 1 ? ra : 1) || ldb < (rb > 1 ? rb : 1) || ldc < (M > 1 ? M : 1)) return GB_ERR_INVALID_VALUE;
+  if (M == 0 || N == 0) return GB_OK;
+  const bool need_ab = K > 0 && alpha != T(0);
+  if (!C || (need_ab && (!A || !B))) return GB_ERR_INVALID_VALUE;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const size_t sz = sizeof(T);
+  const size_t a_bytes = need_ab ? align256(static_cast<size_t>(ra) * ca * sz) : 0;
+  const size_t b_bytes = need_ab ? align256(static_cast<size_t>(rb) * cb * sz) : 0;
+  const size_t c_bytes = align256(static_cast<size_t>(M) * N * sz);
+  char* ws = nullptr;
+  cudaError_t e = cudaMallocFromPoolAsync(reinterpret_cast<void**>(&ws), a_bytes + b_bytes + c_bytes, dev->pool, s);
+  if (e != cudaSuccess) return gb_set_cuda_error(e, "host-buffer workspace");
+  T* dA = reinterpret_cast<T*>(ws);
+  T* dB = reinterpret_cast<T*>(ws + a_bytes);
+  T* dC = reinterpret_cast<T*>(ws + a_bytes + b_bytes);
+  const int64_t la = ra > 1 ? ra : 1, lb = rb > 1 ? rb : 1, lc = M > 1 ? M : 1;
+  if (need_ab) {
+    e = cudaMemcpy2DAsync(dA, la * sz, A, lda * sz, ra * sz, ca, cudaMemcpyDefault, s);
+    if (e == cudaSuccess) e = cudaMemcpy2DAsync(dB, lb * sz, B, ldb * sz, rb * sz, cb, cudaMemcpyDefault, s);
+  }
+  if (e == cudaSuccess && beta != T(0)) e = cudaMemcpy2DAsync(dC, lc * sz, C, ldc * sz, M * sz, N, cudaMemcpyDefault, s);
+  if (e != cudaSuccess) {
+    cudaFreeAsync(ws, s);
+    return gb_set_cuda_error(e, "host-buffer upload");
+  }
+  rc = call(ta, tb, M, N, K, alpha, need_ab ? dA : nullptr, la, need_ab ? dB : nullptr, lb, beta, dC, lc, stream);
+  if (!rc) {
+    e = cudaMemcpy2DAsync(C, ldc * sz, dC, lc * sz, M * sz, N, cudaMemcpyDefault, s);
+    if (e != cudaSuccess) rc = gb_set_cuda_error(e, "host-buffer download");
+  }
+  cudaFreeAsync(ws, s);
+  e = cudaStreamSynchronize(s);
+  if (!rc && e != cudaSuccess) rc = gb_set_cuda_error(e, "host-buffer call");
+  if (!rc) rc = gb_check_status(stream);
+  return rc;
+}
+
 extern "C" {
 
 const char* gb_status_string(int status) {
@@ -945,6 +992,31 @@ int gb_jmul_f64(double* D, const double* A, const double* X, int64_t M, int64_t 
 int gb_jmul_f32(float* D, const float* A, const float* X, int64_t M, int64_t N, int64_t P, void* stream) {
   return gb_gemm_f32(0, 0, M, P, N, 1.0f, A, M > 1 ? M : 1, X, N > 1 ? N : 1, 0.0f, D, M > 1 ? M : 1,
                      stream);
+}
+
+int gb_gemm_f64_host(int transA, int transB, int64_t M, int64_t N, int64_t K, double alpha, const double* A,
+                     int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc, int mode,
+                     int slices, double* err_bound_out, void* stream) {
+  auto call = [&](int ta, int tb, int64_t m, int64_t n, int64_t k, double al, const double* a, int64_t la,
+                  const double* b, int64_t lb, double be, double* c, int64_t lc, void* st) {
+    return gb_gemm_f64(ta, tb, m, n, k, al, a, la, b, lb, be, c, lc, mode, slices, err_bound_out, st);
+  };
+  return gemm_host<double>(call, transA, transB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, stream);
+}
+
+int gb_gemm_f32_host(int transA, int transB, int64_t M, int64_t N, int64_t K, float alpha, const float* A,
+                     int64_t lda, const float* B, int64_t ldb, float beta, float* C, int64_t ldc, void* stream) {
+  return gemm_host<float>(gb_gemm_f32, transA, transB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, stream);
+}
+
+int gb_jmul_f64_host(double* D, const double* A, const double* X, int64_t M, int64_t N, int64_t P, void* stream) {
+  return gb_gemm_f64_host(0, 0, M, P, N, 1.0, A, M > 1 ? M : 1, X, N > 1 ? N : 1, 0.0, D, M > 1 ? M : 1,
+                          GB_MODE_NATIVE, 0, nullptr, stream);
+}
+
+int gb_jmul_f32_host(float* D, const float* A, const float* X, int64_t M, int64_t N, int64_t P, void* stream) {
+  return gb_gemm_f32_host(0, 0, M, P, N, 1.0f, A, M > 1 ? M : 1, X, N > 1 ? N : 1, 0.0f, D, M > 1 ? M : 1,
+                          stream);
 }
 
 int gb_last_ozaki_plan(gb_ozaki_plan_t* out) {

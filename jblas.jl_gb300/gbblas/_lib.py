@@ -91,6 +91,12 @@ SIGNATURES = {
                                             c_i64, ctypes.c_double, c_vp, c_i64, c_i64, c_i64, c_vp]),
     "gb_gemm_strided_batched_f32": (c_int, [c_i64, c_i64, c_i64, ctypes.c_float, c_vp, c_i64, c_i64, c_vp, c_i64,
                                             c_i64, ctypes.c_float, c_vp, c_i64, c_i64, c_i64, c_vp]),
+    "gb_gemm_f64_host": (c_int, [c_int, c_int, c_i64, c_i64, c_i64, c_double, c_vp, c_i64, c_vp, c_i64,
+                                 c_double, c_vp, c_i64, c_int, c_int, ctypes.POINTER(c_double), c_vp]),
+    "gb_gemm_f32_host": (c_int, [c_int, c_int, c_i64, c_i64, c_i64, c_float, c_vp, c_i64, c_vp, c_i64,
+                                 c_float, c_vp, c_i64, c_vp]),
+    "gb_jmul_f64_host": (c_int, [c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, c_vp]),
+    "gb_jmul_f32_host": (c_int, [c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, c_vp]),
     "gb_kernel_f64": (c_int, [c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, c_i64, c_i64, c_int, c_vp]),
     "gb_kernel_f32": (c_int, [c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, c_i64, c_i64, c_int, c_vp]),
     "gb_gemm_semiring_f64": (c_int, [c_int, c_int, c_int, c_i64, c_i64, c_i64, c_vp, c_i64, c_vp, c_i64, c_int,

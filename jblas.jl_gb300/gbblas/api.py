@@ -113,6 +113,64 @@ def gemm_(C, A, B, alpha=1.0, beta=0.0, *, mode="native", slices=0, return_bound
     return (C, bound) if return_bound else C
 
 
+def _host_storage(X, name, out=False):
+    """(array, ld, trans) for a 2-D numpy array with a unit stride in one dimension."""
+    import numpy as np
+    if not isinstance(X, np.ndarray) or X.ndim != 2:
+        raise DimensionMismatch("%s must be a 2-D numpy array" % name)
+    if out and not X.flags.writeable:
+        raise ValueError("%s must be writable" % name)
+    r, c = X.shape
+    it = X.itemsize
+    s0, s1 = X.strides
+    if (s0 == it or r <= 1) and s1 % it == 0 and (c <= 1 or s1 // it >= max(1, r)):
+        return X, (s1 // it if c > 1 else max(1, r)), 0
+    if (s1 == it or c <= 1) and s0 % it == 0 and (r <= 1 or s0 // it >= max(1, c)):
+        return X, (s0 // it if r > 1 else max(1, c)), 1
+    raise ValueError("%s must have a unit stride in one dimension" % name)
+
+
+def gemm_host(C, A, B, alpha=1.0, beta=0.0, *, mode="native", slices=0, return_bound=False):
+    """C = alpha * A @ B + beta * C on HOST numpy arrays, in place: the blocking host-buffer call
+    (gb_gemm_f64_host / gb_gemm_f32_host uploads the operands, runs the same device product and
+    downloads C before returning).  Column-major and row-major arrays (and strided views with a
+    unit stride in one dimension) are read without copies; results equal gemm_ on device copies
+    bit for bit."""
+    import numpy as np
+    dt = C.dtype
+    if A.dtype != dt or B.dtype != dt or dt not in (np.float64, np.float32):
+        raise TypeError("gemm_host computes in float64 or float32 with one dtype, got %s, %s, %s"
+                        % (A.dtype, B.dtype, dt))
+    M, K = A.shape
+    K2, N = B.shape
+    if K2 != K or C.shape != (M, N):
+        raise DimensionMismatch("A is %dx%d, B is %dx%d, C is %dx%d" % (M, K, K2, N, *C.shape))
+    Cs, ldc, tc = _host_storage(C, "C", out=True)
+    As, lda, ta = _host_storage(A, "A")
+    Bs, ldb, tb = _host_storage(B, "B")
+    L = _lib.lib()
+    md = _MODES[mode] if isinstance(mode, str) else int(mode)
+    bound = ctypes.c_double(0.0)
+    vp = lambda X: ctypes.c_void_p(X.ctypes.data)   # noqa: E731
+    if tc == 0:
+        args = (ta, tb, M, N, K, alpha, vp(As), lda, vp(Bs), ldb, beta, vp(Cs), ldc)
+    else:   # row-major C: C^T = B^T A^T
+        args = (1 - tb, 1 - ta, N, M, K, alpha, vp(Bs), ldb, vp(As), lda, beta, vp(Cs), ldc)
+    if dt == np.float64:
+        rc = L.gb_gemm_f64_host(*args, md, int(slices), ctypes.byref(bound) if return_bound else None, None)
+        check(rc, "gb_gemm_f64_host")
+    else:
+        if md != _lib.MODE_NATIVE:
+            raise ValueError("Ozaki modes emulate float64; float32 runs natively")
+        check(L.gb_gemm_f32_host(*args, None), "gb_gemm_f32_host")
+    return (C, bound.value) if return_bound else C
+
+
+def jmul_host(D, A, X):
+    """jmul!(D, A, X) on host numpy arrays (blocking): D = A * X in jBLAS's per-element order."""
+    return gemm_host(D, A, X, 1.0, 0.0, mode="native")
+
+
 def jmul_(D, A, X, a_prefetch=7, x_prefetch=7, a_loc=3, x_loc=3, d_loc=3):
     """jmul!(D, A, X[, Val(Aprefetch_freq), Val(Xprefetch_freq), Val(A_loc), Val(X_loc), Val(D_loc)]):
     D = A * X with jBLAS's per-element FMA order (src/gemm.jl:244-246).

@@ -5,7 +5,8 @@ Julia front end of libgbblas (the GB300 GEMM behind jBLAS.jl's `jmul!`).  A thin
 layer over the C ABI in `include/gbblas.h`:
 
     jmul!(D, A, X[, Val(...) x 5])  D = A * X, jBLAS's per-element FMA order (src/gemm.jl:244);
-                                   the prefetch Val hints are accepted and unused
+                                   the prefetch Val hints are accepted and unused; host `Matrix`
+                                   operands go through the blocking host-buffer call
     fastmul!(D, A, X)              the small-matrix single-tile product (src/kernels.jl:202-208)
     kernel!(pD, pA, pX, Kernel{Mₖ,Pₖ,stride_AD,stride_X,N}())   D += A*X as jBLAS's pointer kernel
     initkernel!(pD, pA, pX, Kernel{...}())                        D = A*X (src/kernels.jl:212-273)
@@ -107,6 +108,36 @@ function gemm!(C::AbstractMatrix{Float32}, A::AbstractMatrix{Float32}, B::Abstra
                 (Cint, Cint, Int64, Int64, Int64, Cfloat, Ptr{Cfloat}, Int64, Ptr{Cfloat}, Int64, Cfloat,
                  Ptr{Cfloat}, Int64, Ptr{Cvoid}),
                 0, 0, M, N, K, α, devptr(A), ld(A), devptr(B), ld(B), β, devptr(C), ld(C), current_stream()))
+    C
+end
+
+# Host matrices (`Matrix`, the reference's own operands): the blocking host-buffer calls upload,
+# multiply on the GPU and download before returning, with the same results.
+function jmul!(D::Matrix{Float64}, A::Matrix{Float64}, X::Matrix{Float64})
+    M, N = size(A); P = size(X, 2)
+    size(X, 1) == N && size(D) == (M, P) || throw(DimensionMismatch("jmul!: $(size(D)) = $(size(A)) * $(size(X))"))
+    check(ccall((:gb_jmul_f64_host, libgbblas), Cint,
+                (Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}, Int64, Int64, Int64, Ptr{Cvoid}),
+                D, A, X, M, N, P, current_stream()))
+    D
+end
+function jmul!(D::Matrix{Float32}, A::Matrix{Float32}, X::Matrix{Float32})
+    M, N = size(A); P = size(X, 2)
+    size(X, 1) == N && size(D) == (M, P) || throw(DimensionMismatch("jmul!: $(size(D)) = $(size(A)) * $(size(X))"))
+    check(ccall((:gb_jmul_f32_host, libgbblas), Cint,
+                (Ptr{Cfloat}, Ptr{Cfloat}, Ptr{Cfloat}, Int64, Int64, Int64, Ptr{Cvoid}),
+                D, A, X, M, N, P, current_stream()))
+    D
+end
+function gemm!(C::Matrix{Float64}, A::Matrix{Float64}, B::Matrix{Float64}, α::Real, β::Real;
+               mode::Symbol = :native, slices::Integer = 0)
+    M, K = size(A); N = size(B, 2)
+    size(B, 1) == K && size(C) == (M, N) || throw(DimensionMismatch("gemm!"))
+    check(ccall((:gb_gemm_f64_host, libgbblas), Cint,
+                (Cint, Cint, Int64, Int64, Int64, Cdouble, Ptr{Cdouble}, Int64, Ptr{Cdouble}, Int64, Cdouble,
+                 Ptr{Cdouble}, Int64, Cint, Cint, Ptr{Cdouble}, Ptr{Cvoid}),
+                0, 0, M, N, K, α, A, max(1, M), B, max(1, K), β, C, max(1, M), MODE[mode], slices, C_NULL,
+                current_stream()))
     C
 end
 
