@@ -30,51 +30,40 @@ __device__ __forceinline__ void split_hi_lo(float x, uint32_t& hi_bits, uint32_t
   lo_bits = static_cast<uint32_t>(__bfloat16_as_ushort(lo));
 }
 
-// One thread = one row r of X (R x Kd view, element (r, k) at X[r*rs + k*ks]) and 16
-// consecutive k.  Writes planes[0] (hi) and planes[1] (lo), [plane][r][pitch], 32 bytes
-// per plane per thread.  RC: rows contiguous (threads along r); otherwise threads along k.
-// DUAL (rows contiguous only): also writes the transposed layout [plane][k][pitch2] + r,
-// so a matrix needed in both orientations is read once.
-template <bool RC, bool DUAL>
-__global__ void __launch_bounds__(256) split3_kernel(const float* __restrict__ X, int64_t R, int64_t Kd,
-                                                     int64_t rs, int64_t ks, __nv_bfloat16* __restrict__ planes,
-                                                     int64_t pitch, __nv_bfloat16* __restrict__ planes_t,
-                                                     int64_t pitch_t) {
-  int64_t r, kc;
-  if (RC) {
-    r = static_cast<int64_t>(blockIdx.x) * 256 + threadIdx.x;
-    kc = blockIdx.y;
-  } else {
-    kc = static_cast<int64_t>(blockIdx.x) * 256 + threadIdx.x;
-    r = blockIdx.y;
-  }
+// k contiguous or strided (element (r, k) at X[r*rs + k*ks]): one thread = one row r and 16
+// consecutive k, neighbouring threads neighbouring k; writes planes[0] (hi) and planes[1] (lo),
+// [plane][r][pitch], 32 bytes per plane per thread.  With ks == 1 the 16 values are read as four
+// 16-byte loads when aligned.
+__global__ void __launch_bounds__(256) split3_kc_kernel(const float* __restrict__ X, int64_t R, int64_t Kd,
+                                                        int64_t rs, int64_t ks, __nv_bfloat16* __restrict__ planes,
+                                                        int64_t pitch) {
+  const int64_t kc = static_cast<int64_t>(blockIdx.x) * 256 + threadIdx.x, r = blockIdx.y;
   const int64_t k0 = kc * 16;
   if (r >= R || k0 >= Kd) return;
   const int nvalid = static_cast<int>(Kd - k0 < 16 ? Kd - k0 : 16);
   const float* src = X + r * rs + k0 * ks;
+  float x[16];
+  if (ks == 1 && nvalid == 16 && (reinterpret_cast<uintptr_t>(src) & 15) == 0) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const float4 v = reinterpret_cast<const float4*>(src)[q];
+      x[4 * q] = v.x;
+      x[4 * q + 1] = v.y;
+      x[4 * q + 2] = v.z;
+      x[4 * q + 3] = v.w;
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < 16; ++j) x[j] = (j < nvalid) ? src[j * ks] : 0.0f;
+  }
   uint32_t hp[8], lp[8];
 #pragma unroll
   for (int j = 0; j < 16; j += 2) {
     uint32_t h0, l0, h1, l1;
-    const float x0 = (j < nvalid) ? src[j * ks] : 0.0f;
-    const float x1 = (j + 1 < nvalid) ? src[(j + 1) * ks] : 0.0f;
-    split_hi_lo(x0, h0, l0);
-    split_hi_lo(x1, h1, l1);
+    split_hi_lo(x[j], h0, l0);
+    split_hi_lo(x[j + 1], h1, l1);
     hp[j / 2] = h0 | (h1 << 16);
     lp[j / 2] = l0 | (l1 << 16);
-    if (DUAL) {
-      // transposed layout: row k, column r (consecutive threads: consecutive r)
-      const int64_t plane_t = Kd * pitch_t;
-      unsigned short* t = reinterpret_cast<unsigned short*>(planes_t);
-      if (j < nvalid) {
-        t[(k0 + j) * pitch_t + r] = static_cast<unsigned short>(h0);
-        t[plane_t + (k0 + j) * pitch_t + r] = static_cast<unsigned short>(l0);
-      }
-      if (j + 1 < nvalid) {
-        t[(k0 + j + 1) * pitch_t + r] = static_cast<unsigned short>(h1);
-        t[plane_t + (k0 + j + 1) * pitch_t + r] = static_cast<unsigned short>(l1);
-      }
-    }
   }
   const int64_t plane = R * pitch;
   __nv_bfloat16* dst = planes + r * pitch + k0;
@@ -85,11 +74,97 @@ __global__ void __launch_bounds__(256) split3_kernel(const float* __restrict__ X
     h4[1] = make_uint4(hp[4], hp[5], hp[6], hp[7]);
     l4[0] = make_uint4(lp[0], lp[1], lp[2], lp[3]);
     l4[1] = make_uint4(lp[4], lp[5], lp[6], lp[7]);
-  } else {
+  } else {   // unrolled with a predicate: hp / lp stay in registers
     unsigned short* d2 = reinterpret_cast<unsigned short*>(dst);
-    for (int j = 0; j < nvalid; ++j) {
-      d2[j] = static_cast<unsigned short>(hp[j / 2] >> (16 * (j & 1)));
-      d2[plane + j] = static_cast<unsigned short>(lp[j / 2] >> (16 * (j & 1)));
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      if (j < nvalid) {
+        d2[j] = static_cast<unsigned short>(hp[j / 2] >> (16 * (j & 1)));
+        d2[plane + j] = static_cast<unsigned short>(lp[j / 2] >> (16 * (j & 1)));
+      }
+    }
+  }
+}
+
+// Rows contiguous (element (r, k) at X[r + k*ks]): a CTA converts a 64 x 64 tile through shared
+// memory.  Warp w loads columns 8w..8w+7 (lanes along r: 128-byte loads); the hi/lo values go to
+// [r][k] shared tiles; each warp then stores 8 rows x 128 B of both planes, and with DUAL also
+// 8 k-rows x 128 B of the transposed planes [k][r] — whole lines in both layouts.
+template <bool DUAL>
+__global__ void __launch_bounds__(256) split3_rc_tile_kernel(const float* __restrict__ X, int64_t R, int64_t Kd,
+                                                             int64_t ks, __nv_bfloat16* __restrict__ planes,
+                                                             int64_t pitch, __nv_bfloat16* __restrict__ planes_t,
+                                                             int64_t pitch_t) {
+  __shared__ float tile[64][65];                              // [k][r]
+  __shared__ __align__(16) unsigned short hs[64][72], ls[64][72];   // [r][k], 144-byte rows
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const int64_t r0 = static_cast<int64_t>(blockIdx.x) * 64, k0 = static_cast<int64_t>(blockIdx.y) * 64;
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    const int kk = w * 8 + c;
+    const int64_t k = k0 + kk;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int rr = lane + 32 * h;
+      const int64_t r = r0 + rr;
+      tile[kk][rr] = (r < R && k < Kd) ? X[r + k * ks] : 0.0f;
+    }
+  }
+  __syncthreads();
+  const int rr = tid >> 2, kb = (tid & 3) * 16;   // this thread's row and 16-wide k chunk
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    uint32_t hb, lb;
+    split_hi_lo(tile[kb + j][rr], hb, lb);
+    hs[rr][kb + j] = static_cast<unsigned short>(hb);
+    ls[rr][kb + j] = static_cast<unsigned short>(lb);
+  }
+  __syncthreads();
+  {   // row-major planes [r][k]
+    const int64_t r = r0 + rr, k = k0 + kb;
+    if (r < R && k < Kd) {
+      const int nvalid = static_cast<int>(Kd - k < 16 ? Kd - k : 16);
+      unsigned short* dh = reinterpret_cast<unsigned short*>(planes) + r * pitch + k;
+      unsigned short* dl = dh + R * pitch;
+      if (nvalid == 16) {
+        const uint4* sh = reinterpret_cast<const uint4*>(&hs[rr][kb]);
+        const uint4* sl = reinterpret_cast<const uint4*>(&ls[rr][kb]);
+        reinterpret_cast<uint4*>(dh)[0] = sh[0];
+        reinterpret_cast<uint4*>(dh)[1] = sh[1];
+        reinterpret_cast<uint4*>(dl)[0] = sl[0];
+        reinterpret_cast<uint4*>(dl)[1] = sl[1];
+      } else {
+        for (int j = 0; j < nvalid; ++j) {
+          dh[j] = hs[rr][kb + j];
+          dl[j] = ls[rr][kb + j];
+        }
+      }
+    }
+  }
+  if (DUAL) {   // transposed planes [k][r]: this thread's k row (tid >> 2) and 16-wide r chunk
+    const int kk = tid >> 2, rb = (tid & 3) * 16;
+    const int64_t k = k0 + kk, r = r0 + rb;
+    if (k < Kd && r < R) {
+      const int nvalid = static_cast<int>(R - r < 16 ? R - r : 16);
+      unsigned short* th = reinterpret_cast<unsigned short*>(planes_t) + k * pitch_t + r;
+      unsigned short* tl = th + Kd * pitch_t;
+      if (nvalid == 16) {
+        uint32_t ph[8], pl[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          ph[i] = static_cast<uint32_t>(hs[rb + 2 * i][kk]) | (static_cast<uint32_t>(hs[rb + 2 * i + 1][kk]) << 16);
+          pl[i] = static_cast<uint32_t>(ls[rb + 2 * i][kk]) | (static_cast<uint32_t>(ls[rb + 2 * i + 1][kk]) << 16);
+        }
+        reinterpret_cast<uint4*>(th)[0] = make_uint4(ph[0], ph[1], ph[2], ph[3]);
+        reinterpret_cast<uint4*>(th)[1] = make_uint4(ph[4], ph[5], ph[6], ph[7]);
+        reinterpret_cast<uint4*>(tl)[0] = make_uint4(pl[0], pl[1], pl[2], pl[3]);
+        reinterpret_cast<uint4*>(tl)[1] = make_uint4(pl[4], pl[5], pl[6], pl[7]);
+      } else {
+        for (int i = 0; i < nvalid; ++i) {
+          th[i] = hs[rb + i][kk];
+          tl[i] = ls[rb + i][kk];
+        }
+      }
     }
   }
 }
@@ -99,19 +174,21 @@ static int split3(const float* X, int64_t R, int64_t Kd, int64_t rs, int64_t ks,
   if (R <= 0 || Kd <= 0) return GB_OK;
   const int64_t kchunks = (Kd + 15) / 16;
   if (rs == 1 || planes_t) {
-    if (kchunks > 65535) return GB_ERR_UNSUPPORTED;
-    dim3 grid(static_cast<unsigned>((R + 255) / 256), static_cast<unsigned>(kchunks));
+    if (rs != 1) return GB_ERR_UNSUPPORTED;   // the transposed layout is written from row-contiguous X
+    const int64_t ktiles = (Kd + 63) / 64;
+    if (ktiles > 65535) return GB_ERR_UNSUPPORTED;
+    dim3 grid(static_cast<unsigned>((R + 63) / 64), static_cast<unsigned>(ktiles));
     if (planes_t)
       GB_LAUNCH(GB_KERNEL_ADJOINT_SPLIT, s,
-                (split3_kernel<true, true><<<grid, 256, 0, s>>>(X, R, Kd, rs, ks, planes, pitch, planes_t, pitch_t)));
+                (split3_rc_tile_kernel<true><<<grid, 256, 0, s>>>(X, R, Kd, ks, planes, pitch, planes_t, pitch_t)));
     else
       GB_LAUNCH(GB_KERNEL_ADJOINT_SPLIT, s,
-                (split3_kernel<true, false><<<grid, 256, 0, s>>>(X, R, Kd, rs, ks, planes, pitch, nullptr, 0)));
+                (split3_rc_tile_kernel<false><<<grid, 256, 0, s>>>(X, R, Kd, ks, planes, pitch, nullptr, 0)));
   } else {
     if (R > 65535) return GB_ERR_UNSUPPORTED;
     dim3 grid(static_cast<unsigned>((kchunks + 255) / 256), static_cast<unsigned>(R));
     GB_LAUNCH(GB_KERNEL_ADJOINT_SPLIT, s,
-              (split3_kernel<false, false><<<grid, 256, 0, s>>>(X, R, Kd, rs, ks, planes, pitch, nullptr, 0)));
+              (split3_kc_kernel<<<grid, 256, 0, s>>>(X, R, Kd, rs, ks, planes, pitch)));
   }
   GB_CUDA_TRY(cudaGetLastError());
   return GB_OK;
