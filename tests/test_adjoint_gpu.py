@@ -126,3 +126,28 @@ def test_config5_full_size_fd_and_oracle(cuda):
     # normwise, for the record: well inside 2^-15
     e = np.linalg.norm(dA[rows % M, cols % K] - oracle.chain_entries(W64, B64, rows % M, cols % K, trans_b=True))
     assert e / np.linalg.norm(oracle.chain_entries(W64, B64, rows % M, cols % K, trans_b=True)) < 2.0 ** -14
+
+
+def test_leading_dimensions_larger_than_rows(cuda):
+    """A, B, dC inside larger column-major buffers and dA, dB written into padded ones: the same
+    tolerance as packed operands, and the gradients' padding rows are not written."""
+    from gpu_util import to_dev_ld
+    M, N, K = 150, 97, 133
+    g = np.random.default_rng(808)
+    A = np.asfortranarray(g.standard_normal((M, K)).astype(np.float32))
+    B = np.asfortranarray(g.standard_normal((K, N)).astype(np.float32))
+    W = np.asfortranarray(g.standard_normal((M, N)).astype(np.float32))
+    Ad, _ = to_dev_ld(A, M + 11)
+    Bd, _ = to_dev_ld(B, K + 5)
+    Wd, _ = to_dev_ld(W, M + 3)
+    dAd, dAbuf = to_dev_ld(np.zeros((M, K), np.float32), M + 9, fill=7.0)
+    dBd, dBbuf = to_dev_ld(np.zeros((K, N), np.float32), K + 2, fill=7.0)
+    gbblas.gemm_adjoint_(dAd, dBd, Ad, Bd, Wd)
+    torch.cuda.synchronize()
+    gbblas.check_device_status()
+    A64, B64, W64 = A.astype(np.float64), B.astype(np.float64), W.astype(np.float64)
+    dA_ref = oracle.gemm(W64, B64, trans_b=True)
+    dB_ref = oracle.gemm(A64, W64, trans_a=True)
+    assert np.all(np.abs(to_host(dAd) - dA_ref) <= tol_factor(N) * (np.abs(W64) @ np.abs(B64).T) + 1e-30)
+    assert np.all(np.abs(to_host(dBd) - dB_ref) <= tol_factor(M) * (np.abs(A64).T @ np.abs(W64)) + 1e-30)
+    assert np.all(to_host(dAbuf)[M:, :] == 7.0) and np.all(to_host(dBbuf)[K:, :] == 7.0)

@@ -256,3 +256,25 @@ def test_automatic_call_captures_in_a_cuda_graph(cuda):
     torch.cuda.synchronize()
     gbblas.check_device_status()
     assert_bit_equal(to_host(C_graph), to_host(C_direct))
+
+
+@pytest.mark.parametrize("tb", [0, 1])
+def test_leading_dimensions_larger_than_rows(cuda, tb):
+    """Operands inside larger column-major buffers (lda > M, ldb > rows of B as stored, ldc > M):
+    the same bits as packed operands, and C's padding rows are not written."""
+    from gpu_util import to_dev_ld
+    M, K, N = 150, 333, 97
+    g = np.random.default_rng(404 + tb)
+    A = np.asfortranarray(g.uniform(-1, 1, (M, K)) * np.ldexp(1.0, g.integers(-6, 7, (M, K))))
+    Bl = g.uniform(-1, 1, (K, N)) * np.ldexp(1.0, g.integers(-6, 7, (K, N)))
+    B = np.asfortranarray(Bl.T if tb else Bl)
+    Ad, _ = to_dev_ld(A, M + 13)
+    Bd, _ = to_dev_ld(B, B.shape[0] + 7)
+    Cd, Cbuf = to_dev_ld(np.zeros((M, N)), M + 5, fill=3.0)
+    gbblas.gemm_raw(0, tb, M, N, K, 1.0, Ad.data_ptr(), M + 13, Bd.data_ptr(), B.shape[0] + 7, 0.0,
+                    Cd.data_ptr(), M + 5, dtype=torch.float64, mode=gbblas.MODE_OZAKI_CRT, slices=15,
+                    stream=torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    gbblas.check_device_status()
+    assert_bit_equal(to_host(Cd), oracle.ozaki_crt_gemm(A, Bl, moduli=15))
+    assert np.all(to_host(Cbuf)[M:, :N] == 3.0)
