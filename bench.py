@@ -22,6 +22,7 @@ One JSON line (rank 0):
 --impl reference times that CPU port alone on the same configuration.
 """
 import argparse
+import datetime
 import json
 import os
 import statistics
@@ -86,13 +87,14 @@ def committed_traffic(workload):
 class ClockSampler:
     """nvidia-smi clock / throttle-reason samples while the timed region runs."""
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, device_index):
         self.dev = device_index
         self.proc = None
+        self.window = None   # host wall-clock (start, end) of the timed region
         self.path = os.path.join(tempfile.gettempdir(), "gbblas_clocks_%d.csv" % os.getpid())
 
     def start(self):
@@ -107,6 +109,13 @@ class ClockSampler:
             self.proc = None
         time.sleep(0.3)
 
+    def mark_start(self):
+        self.window = (time.time(), None)
+
+    def mark_end(self):
+        if self.window:
+            self.window = (self.window[0], time.time())
+
     def stop(self):
         if self.proc is None:
             return None
@@ -116,25 +125,30 @@ class ClockSampler:
         except subprocess.TimeoutExpired:
             self.proc.kill()
         self.fh.close()
-        sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        rows = []
         with open(self.path) as f:
             for line in f:
                 parts = [x.strip() for x in line.split(",")]
-                if len(parts) < 9:
+                if len(parts) < 10:
                     continue
                 try:
-                    sm.append(float(parts[1]))
-                    smax.append(float(parts[2]))
+                    ts = datetime.datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                    rows.append((ts, float(parts[2]), float(parts[3]),
+                                 {nm for nm, v in zip(names, parts[6:10]) if v.lower() == "active"}))
                 except ValueError:
                     continue
-                for nm, v in zip(names, parts[5:9]):
-                    if v.lower() == "active":
-                        reasons.add(nm)
-        if not sm:
+        if not rows:
             return None
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "samples": len(sm),
-                "reasons": sorted(reasons)}
+        scope = "whole run"
+        if self.window and self.window[1]:
+            inside = [r for r in rows if self.window[0] - 0.05 <= r[0] <= self.window[1] + 0.05]
+            if inside:
+                rows, scope = inside, "timed region"
+        sm = [r[1] for r in rows]
+        reasons = set().union(*(r[3] for r in rows))
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(r[2] for r in rows), "samples": len(rows),
+                "scope": scope, "reasons": sorted(reasons)}
 
 
 def cpu_cores():
@@ -334,6 +348,7 @@ def workload_semiring(args):
     clocks = ClockSampler(0)
     rows = []
     clocks.start()
+    clocks.mark_start()
     for dt, n in ((torch.float32, 8192), (torch.int32, 8192), (torch.float64, 4096)):
         if dt == torch.int32:
             A = torch.randint(-10**6, 10**6, (n, n), dtype=dt, device=dev).t()
@@ -358,6 +373,7 @@ def workload_semiring(args):
             rows.append({"dtype": str(dt).replace("torch.", ""), "semiring": sr, "n": n, "ms": ms,
                          "tera_mnk_per_s": n ** 3 / (ms * 1e-3) / 1e12, "sampled_bit_exact": same})
         del A, B, C
+    clocks.mark_end()
     clk = clocks.stop() or {}
     mhz = clk.get("sm_mhz") or 2070.0
     for r in rows:
@@ -545,11 +561,15 @@ def main():
     barrier()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with gbblas.profile() as prof:
+        if clocks:
+            clocks.mark_start()
         ev0.record(stream)
         for _ in range(args.steps):
             gbblas.gemm_(C_d, A_d, B_d, mode=mode, slices=args.slices)
         ev1.record(stream)
         torch.cuda.synchronize()
+        if clocks:
+            clocks.mark_end()
     barrier()
     counts1 = gbblas.launch_counts()
     clk = clocks.stop() if clocks else None
