@@ -584,7 +584,7 @@ def main():
     # ring of NBUF device input/output buffers: uploads run up to NBUF - 1 steps ahead of the
     # compute and downloads trail it, so the host link's jitter (it is shared with the node's
     # other GPUs) does not stall the compute (a serving pipeline with a queue of NBUF).
-    NBUF = 3
+    NBUF = 4
     barrier()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     up_stream, down_stream = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
@@ -780,7 +780,7 @@ def main():
             "kernel_ms_per_step": {k: v / args.steps for k, v in prof.ms.items()},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "TFLOP/s", "ms_per_step": ms_e2e,
-                    "pipeline": "3-deep ring: uploads run up to 2 steps ahead, the download of step i overlaps step i+1",
+                    "pipeline": "4-deep ring: uploads run up to 3 steps ahead, the download of step i overlaps step i+1",
                     "h2d_GBps": h2d_gbs, "d2h_GBps": d2h_gbs,
                     "compute_ms_in_pipeline": comp_in_pipeline,
                     "upload_ms_in_pipeline": up_in_pipeline, "download_ms_in_pipeline": down_in_pipeline,
