@@ -67,3 +67,52 @@ def test_short_wait_limit_crt_mode(cuda):
     torch.cuda.synchronize()
     gbblas.check_device_status()
     assert_bit_equal(to_host(C), oracle.ozaki_crt_gemm(A, B, moduli=16))
+
+
+def test_short_wait_limit_adjoint(cuda):
+    """The fused adjoint runs on the same pipeline: an expired wait is reported through the
+    status word and the next call is within its tolerance again."""
+    g = np.random.default_rng(23)
+    M, K, N = 512, 4096, 512
+    A = torch.from_numpy(g.standard_normal((K, M)).astype(np.float32)).cuda().t()
+    B = torch.from_numpy(g.standard_normal((N, K)).astype(np.float32)).cuda().t()
+    W = torch.from_numpy(g.standard_normal((N, M)).astype(np.float32)).cuda().t()
+    dA = torch.empty((K, M), dtype=torch.float32, device="cuda").t()
+    dB = torch.empty((N, K), dtype=torch.float32, device="cuda").t()
+    gbblas.check_device_status()
+    gbblas.set_wait_limit_ns(2000)
+    try:
+        gbblas.gemm_adjoint_(dA, dB, A, B, W)
+        torch.cuda.synchronize()
+    finally:
+        gbblas.set_wait_limit_ns(0)
+    with pytest.raises(gbblas.GBError) as e:
+        gbblas.check_device_status()
+    assert e.value.status == _lib.GB_ERR_PIPELINE_TIMEOUT
+    gbblas.gemm_adjoint_(dA, dB, A, B, W)
+    torch.cuda.synchronize()
+    gbblas.check_device_status()
+    ref = (W.double() @ B.double().t()).cpu().numpy()
+    bound = (2.0 ** -15 + N * 2.0 ** -24) * (W.double().abs() @ B.double().abs().t()).cpu().numpy()
+    assert np.all(np.abs(dA.double().cpu().numpy() - ref) <= bound + 1e-30)
+
+
+def test_short_wait_limit_host_buffer_call(cuda):
+    """The blocking host-buffer call returns the expired wait as its own status (it reads and
+    clears the status word), and the next call is right."""
+    g = np.random.default_rng(24)
+    M, K, N = 256, 8192, 256
+    A = np.asfortranarray(g.uniform(-1, 1, (M, K)))
+    B = np.asfortranarray(g.uniform(-1, 1, (K, N)))
+    C = np.zeros((M, N), order="F")
+    gbblas.check_device_status()
+    gbblas.set_wait_limit_ns(2000)
+    try:
+        with pytest.raises(gbblas.GBError) as e:
+            gbblas.gemm_host(C, A, B, mode="ozaki_crt", slices=16)
+    finally:
+        gbblas.set_wait_limit_ns(0)
+    assert e.value.status == _lib.GB_ERR_PIPELINE_TIMEOUT
+    gbblas.check_device_status()                      # cleared by the call itself
+    gbblas.gemm_host(C, A, B, mode="ozaki_crt", slices=16)
+    assert_bit_equal(C, oracle.ozaki_crt_gemm(A, B, moduli=16))
