@@ -59,44 +59,67 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN), sizeof(T) == 4 ? 2 : 0)
   const int64_t m0 = static_cast<int64_t>(blockIdx.x) * BM;
   const int64_t n0 = static_cast<int64_t>(blockIdx.y) * BN;
 
+  // Global-load geometry, fixed for the whole K loop.  With NT a multiple of the panel's
+  // leading extent, every load of a thread sits in one row (column) of the panel, or at one k,
+  // and its r-th element lies a fixed stride after the first: one pointer per operand,
+  // advanced by one K panel per iteration, replaces the per-element 64-bit index arithmetic.
+  // A (not transposed, A[m + k*lda]): row ml fixed, k = kA + r*(NT/BM), one row check.
+  // A (transposed,     A[k + m*lda]): k fixed,       m = mA + r*(NT/BK), one check per r.
+  // B likewise, with rows and columns exchanged.
+  static_assert(TA ? NT % BK == 0 : NT % BM == 0, "A panel: NT must tile its leading extent");
+  static_assert(TB ? NT % BN == 0 : NT % BK == 0, "B panel: NT must tile its leading extent");
+  constexpr int A_RSTEP = TA ? NT / BK : NT / BM;   // k (or m) between a thread's loads
+  constexpr int B_RSTEP = TB ? NT / BN : NT / BK;
+  const int a_lead = TA ? tid % BK : tid % BM;        // k (TA) or m within the panel
+  const int a_0 = TA ? tid / BK : tid / BM;           // first m (TA) or k
+  const int b_lead = TB ? tid % BN : tid % BK;        // n (TB) or k
+  const int b_0 = TB ? tid / BN : tid / BK;           // first k (TB) or n
+  const T* pa = TA ? A + a_lead + (m0 + a_0) * lda : A + (m0 + a_lead) + a_0 * lda;
+  const T* pb = TB ? B + (n0 + b_lead) + b_0 * ldb : B + b_lead + (n0 + b_0) * ldb;
+  const int64_t a_rs = static_cast<int64_t>(A_RSTEP) * lda;   // between a thread's loads
+  const int64_t b_rs = static_cast<int64_t>(B_RSTEP) * ldb;
+  const int64_t a_ks = TA ? BK : static_cast<int64_t>(BK) * lda;
+  const int64_t b_ks = TB ? static_cast<int64_t>(BK) * ldb : BK;
+  // Rows of A (columns of B) inside the matrix: one flag, or one bit per load.
+  uint32_t a_ok = 0, b_ok = 0;
+#pragma unroll
+  for (int r = 0; r < A_PER; ++r)
+    if (TA ? (m0 + a_0 + r * A_RSTEP < M) : (r == 0 && m0 + a_lead < M)) a_ok |= 1u << r;
+#pragma unroll
+  for (int r = 0; r < B_PER; ++r)
+    if (TB ? (r == 0 && n0 + b_lead < N) : (n0 + b_0 + r * B_RSTEP < N)) b_ok |= 1u << r;
+  if (!TA) a_ok = (a_ok & 1u) ? ~0u : 0u;   // one row of A for all loads
+  if (TB) b_ok = (b_ok & 1u) ? ~0u : 0u;    // one column of B for all loads
+
   T ra[A_PER], rb[B_PER];
 
-  auto load_tile = [&](int64_t k0) {
+  // Loads the K panel at pa / pb, of which the first kc k are inside the matrix.
+  auto load_tile = [&](int kc) {
 #pragma unroll
     for (int r = 0; r < A_PER; ++r) {
-      const int idx = tid + r * NT;
-      int ml, kl;
-      if (TA) { kl = idx % BK; ml = idx / BK; } else { ml = idx % BM; kl = idx / BM; }
-      const int64_t m = m0 + ml, k = k0 + kl;
+      const int kl = TA ? a_lead : a_0 + r * A_RSTEP;
       T v = T(0);
-      if (m < M && k < K) v = TA ? A[k + m * lda] : A[m + k * lda];
+      if (((a_ok >> r) & 1u) && kl < kc) v = pa[r * a_rs];
       ra[r] = v;
     }
 #pragma unroll
     for (int r = 0; r < B_PER; ++r) {
-      const int idx = tid + r * NT;
-      int nl, kl;
-      if (TB) { nl = idx % BN; kl = idx / BN; } else { kl = idx % BK; nl = idx / BK; }
-      const int64_t n = n0 + nl, k = k0 + kl;
+      const int kl = TB ? b_0 + r * B_RSTEP : b_lead;
       T v = T(0);
-      if (n < N && k < K) v = TB ? B[n + k * ldb] : B[k + n * ldb];
+      if (((b_ok >> r) & 1u) && kl < kc) v = pb[r * b_rs];
       rb[r] = v;
     }
   };
   auto store_tile = [&](int buf) {
 #pragma unroll
     for (int r = 0; r < A_PER; ++r) {
-      const int idx = tid + r * NT;
-      int ml, kl;
-      if (TA) { kl = idx % BK; ml = idx / BK; } else { ml = idx % BM; kl = idx / BM; }
-      As[buf][kl][ml] = ra[r];
+      if (TA) As[buf][a_lead][a_0 + r * A_RSTEP] = ra[r];
+      else As[buf][a_0 + r * A_RSTEP][a_lead] = ra[r];
     }
 #pragma unroll
     for (int r = 0; r < B_PER; ++r) {
-      const int idx = tid + r * NT;
-      int nl, kl;
-      if (TB) { nl = idx % BN; kl = idx / BN; } else { kl = idx % BK; nl = idx / BK; }
-      Bs[buf][kl][nl] = rb[r];
+      if (TB) Bs[buf][b_0 + r * B_RSTEP][b_lead] = rb[r];
+      else Bs[buf][b_lead][b_0 + r * B_RSTEP] = rb[r];
     }
   };
 
@@ -164,13 +187,17 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN), sizeof(T) == 4 ? 2 : 0)
   };
 
   if (K > 0) {
-    load_tile(0);
+    load_tile(static_cast<int>(K < BK ? K : BK));
     store_tile(0);
     __syncthreads();
     int buf = 0;
     for (int64_t k0 = 0; k0 < K; k0 += BK) {
       const bool has_next = k0 + BK < K;
-      if (has_next) load_tile(k0 + BK);
+      if (has_next) {
+        pa += a_ks;
+        pb += b_ks;
+        load_tile(static_cast<int>(K - k0 - BK < BK ? K - k0 - BK : BK));
+      }
       const int kc = static_cast<int>(K - k0 < BK ? K - k0 : BK);
       compute(buf, kc);
       if (has_next) {
