@@ -135,7 +135,7 @@ int native_gemm_f32(int ta, int tb, int64_t M, int64_t N, int64_t K, float alpha
   if (alpha == 0.0f || K == 0) return launch_scale<float>(M, N, beta, C, ldc, s);
   if (((M + 127) / 128) * ((N + 127) / 128) < static_cast<int64_t>(sms))
     return launch_simt<float, 64, 64, 16, 4, 4>(ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, s);
-  return launch_simt<float, 128, 128, 8, 8, 8>(ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, s);
+  return launch_simt<float, 128, 128, 16, 8, 8>(ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, s);
 }
 
 }  // namespace gb
