@@ -56,6 +56,35 @@ def test_gemm_bit_exact(cuda, dtype, shape, trans):
         assert_bit_equal(to_host(Cd), ref)
 
 
+# Products large enough that FP32 runs its 128 x 128 tile (16-deep K panel) and FP64 its 64 x 64
+# tile, with M and N off the tile grid, K ending inside a K panel, and every leading dimension
+# padded (NaN in A and B: a load from the padding would poison the result; C's padding must stay).
+BIG_TILE_SHAPES = [(1601, 37, 1555), (1700, 129, 1650), (1543, 16, 1675)]
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("shape", BIG_TILE_SHAPES, ids=["x".join(map(str, s)) for s in BIG_TILE_SHAPES])
+@pytest.mark.parametrize("trans", [(0, 0), (0, 1), (1, 0), (1, 1)])
+def test_gemm_large_tiles_ragged_edges(cuda, dtype, shape, trans):
+    M, K, N = shape
+    ta, tb = trans
+    g = np.random.default_rng(M + 3 * K + 7 * N + 11 * ta + 13 * tb)
+    A = np.asfortranarray(g.uniform(-1, 1, (K, M) if ta else (M, K)).astype(dtype))
+    B = np.asfortranarray(g.uniform(-1, 1, (N, K) if tb else (K, N)).astype(dtype))
+    C = np.asfortranarray(g.uniform(-1, 1, (M, N)).astype(dtype))
+    ref = oracle.gemm(A, B, C=C, alpha=1.5, beta=0.5, trans_a=bool(ta), trans_b=bool(tb), dtype=dtype)
+    lda, ldb, ldc = A.shape[0] + 5, B.shape[0] + 3, M + 2
+    Av, _ = to_dev_ld(A, lda)
+    Bv, _ = to_dev_ld(B, ldb)
+    Cv, Cbuf = to_dev_ld(C, ldc, fill=7.0)
+    gbblas.gemm_raw(ta, tb, M, N, K, 1.5, Av.data_ptr(), lda, Bv.data_ptr(), ldb, 0.5, Cv.data_ptr(), ldc,
+                    dtype=torch.float64 if dtype == np.float64 else torch.float32,
+                    stream=torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert_bit_equal(to_host(Cv), ref)
+    assert np.all(to_host(Cbuf)[M:, :] == 7.0), "rows beyond M inside the leading dimension were touched"
+
+
 def test_config1_256_cubed_uniform(cuda):
     """Plain Float64 256^3, uniform[-1,1), alpha=1, beta=0: identical to jmul!'s chain."""
     from gbblas import workloads
