@@ -280,7 +280,7 @@ def _native_sample_error(A, B, alpha, beta, dt, samples=1024):
 
 
 def workload_native(args):
-    """Config-2 sweep: native FP64 / FP32 GEMM, alpha = 1.5, beta = 0.5, uniform[-1, 1)."""
+    """Native FP64 / FP32 GEMM sweep (square 1024..16384, 16384x64x16384, 64x16384x16384), alpha = 1.5, beta = 0.5, uniform[-1, 1)."""
     import torch
     import gbblas
     dev = torch.device("cuda", 0)
@@ -394,7 +394,7 @@ def workload_semiring(args):
 
 
 def workload_grouped(args):
-    """Config 4: 4096 problems, m, n, k log-uniform in [8, 512], one persistent grouped launch in a
+    """4096 problems, m, n, k log-uniform in [8, 512], one persistent grouped launch in a
     CUDA graph with autotuned tiles, against a loop of plain per-problem launches."""
     import torch
     import gbblas
@@ -453,7 +453,7 @@ def workload_grouped(args):
 
 
 def workload_adjoint(args):
-    """Config 5: loss = sum(W .* (A*B)), A 4096x2048, B 2048x4096, W 4096x4096 N(0,1) float32:
+    """Adjoint: loss = sum(W .* (A*B)), A 4096x2048, B 2048x4096, W 4096x4096 N(0,1) float32:
     dA = W B^T and dB = A^T W in one launch (3xBF16 split, FP32 accumulation)."""
     import torch
     import gbblas

@@ -85,7 +85,7 @@ GB_API int gb_set_tc_engine(int engine);
  * slices = 0 ignores it and chooses slices and chunking together. */
 GB_API int gb_set_ozaki_min_chunks(int min_chunks);
 
-/* Returns the current device's cached workspace memory to the driver (synchronises the
+/* Returns the current device's cached workspace memory to the CUDA driver (synchronises the
  * device).  Workspace is otherwise kept between calls. */
 GB_API int gb_release_workspace(void);
 

@@ -3,7 +3,7 @@
 Compiles every ``csrc/*.cu`` translation unit in parallel with nvcc
 (``-gencode arch=compute_103a,code=sm_103a``) and links them into
 ``lib/libgbblas.so`` next to this file.  The CUDA runtime is linked statically, so
-the library only needs the driver at run time.  Symbols are hidden by default; the
+the library only needs the CUDA driver at run time.  Symbols are hidden by default; the
 header's ``GB_API`` entry points are the only exports.  Objects go to ``_build/``.
 """
 import concurrent.futures as cf

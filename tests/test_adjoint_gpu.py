@@ -81,7 +81,7 @@ def test_autograd_function_uses_the_adjoint(cuda):
     assert np.array_equal(to_host(C.detach()), ref)
 
 
-def test_config5_full_size_fd_and_oracle(cuda):
+def test_adjoint_4096x2048x4096_fd_and_oracle(cuda):
     """loss = sum(W .* (A*B)), A 4096x2048, B 2048x4096, W 4096x4096, N(0,1) float32."""
     M, K, N = 4096, 2048, 4096
     A = np.asfortranarray(workloads.normal(M, K, stream=51))

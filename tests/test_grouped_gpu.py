@@ -101,7 +101,7 @@ def test_autotune_and_cache(cuda, tmp_path):
 
 
 @pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
-def test_config4_4096_problems(cuda, dtype):
+def test_grouped_4096_loguniform_problems(cuda, dtype):
     """4096 problems, m, n, k log-uniform in [8, 512]; 128 sampled problems vs the oracle."""
     sizes = [tuple(int(x) for x in row) for row in workloads.grouped_sizes(4096)]
     g = np.random.default_rng(9)

@@ -85,7 +85,7 @@ def test_gemm_large_tiles_ragged_edges(cuda, dtype, shape, trans):
     assert np.all(to_host(Cbuf)[M:, :] == 7.0), "rows beyond M inside the leading dimension were touched"
 
 
-def test_config1_256_cubed_uniform(cuda):
+def test_jmul_256_cubed_uniform(cuda):
     """Plain Float64 256^3, uniform[-1,1), alpha=1, beta=0: identical to jmul!'s chain."""
     from gbblas import workloads
     A = workloads.uniform(256, 256, stream=1)
@@ -185,8 +185,8 @@ def test_invalid_arguments_return_status(cuda):
 
 
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
-def test_config2_1024_full_oracle(cuda, dtype):
-    """Config-2 shape 1024^3, alpha=1.5, beta=0.5: every element equals the oracle's."""
+def test_gemm_1024_cubed_full_oracle(cuda, dtype):
+    """1024^3, alpha=1.5, beta=0.5: every element equals the oracle's."""
     from gbblas import workloads
     n = 1024
     A = workloads.uniform(n, n, stream=11, dtype=dtype)
@@ -202,8 +202,8 @@ def test_config2_1024_full_oracle(cuda, dtype):
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
 @pytest.mark.parametrize("shape", [(2048, 2048, 2048), (4096, 4096, 4096), (16384, 16384, 64),
                                    (64, 16384, 16384)], ids=["2048", "4096", "tall", "wide"])
-def test_config2_sampled_entries(cuda, dtype, shape):
-    """Config-2 sweep shapes (M, K, N): 4096 sampled entries equal the oracle chain."""
+def test_gemm_large_shapes_sampled_entries(cuda, dtype, shape):
+    """Large square and tall/wide shapes (M, K, N): 4096 sampled entries equal the oracle chain."""
     from gbblas import workloads
     M, K, N = shape
     A = workloads.uniform(M, K, stream=21, dtype=dtype)

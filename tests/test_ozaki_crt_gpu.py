@@ -211,7 +211,7 @@ def test_bound_decreases_with_moduli_and_holds(cuda):
         prev = bound
 
 
-def test_config3_8192_accuracy_beats_native(cuda):
+def test_8192_cubed_accuracy_beats_native(cuda):
     """M = N = K = 8192, sign*U[1,2)*2^(e_line + e_elem) inputs, moduli chosen by the library:
     normwise error (4096 Dot2-sampled entries) below the bound and below native FP64's."""
     n = 8192

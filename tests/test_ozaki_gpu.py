@@ -165,8 +165,8 @@ def test_int8_mode_unsupported(cuda):
     assert e.value.status == gbblas._lib.GB_ERR_UNSUPPORTED
 
 
-def test_config3_8192_accuracy_beats_native(cuda):
-    """Config 3 at full size: M = N = K = 8192, sign*U[1,2)*2^(e_line + e_elem) inputs, slices
+def test_8192_cubed_accuracy_beats_native(cuda):
+    """At full size: M = N = K = 8192, sign*U[1,2)*2^(e_line + e_elem) inputs, slices
     chosen by the library; normwise error (4096 Dot2-sampled entries) below the bound and
     below the native FP64 kernel's on the same inputs."""
     n = 8192
