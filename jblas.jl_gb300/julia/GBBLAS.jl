@@ -140,6 +140,15 @@ function gemm!(C::Matrix{Float64}, A::Matrix{Float64}, B::Matrix{Float64}, α::R
                 current_stream()))
     C
 end
+function gemm!(C::Matrix{Float32}, A::Matrix{Float32}, B::Matrix{Float32}, α::Real, β::Real)
+    M, K = size(A); N = size(B, 2)
+    size(B, 1) == K && size(C) == (M, N) || throw(DimensionMismatch("gemm!"))
+    check(ccall((:gb_gemm_f32_host, libgbblas), Cint,
+                (Cint, Cint, Int64, Int64, Int64, Cfloat, Ptr{Cfloat}, Int64, Ptr{Cfloat}, Int64, Cfloat,
+                 Ptr{Cfloat}, Int64, Ptr{Cvoid}),
+                0, 0, M, N, K, α, A, max(1, M), B, max(1, K), β, C, max(1, M), current_stream()))
+    C
+end
 
 """
     fastmul!(D, A, X) -> D
