@@ -36,6 +36,15 @@ def test_every_declared_symbol_has_a_python_signature():
     assert set(declared_functions()) <= set(_lib.SIGNATURES)
 
 
+def test_julia_front_end_binds_only_declared_symbols():
+    """Every `ccall((:gb_..., libgbblas), ...)` target of the Julia front end (including the
+    symbols interpolated from `for (T, f) in ((Float64, :gb_...), ...)` loops) is in the header."""
+    src = open(os.path.join(ROOT, "jblas.jl_gb300", "julia", "GBBLAS.jl")).read()
+    bound = set(re.findall(r":(gb_[a-z0-9_]+)", src))
+    assert {"gb_gemm_f64", "gb_kernel_f64", "gb_gemm_semiring_i32", "gb_gemm_f32_host"} <= bound
+    assert bound <= set(declared_functions()), sorted(bound - set(declared_functions()))
+
+
 def test_status_strings():
     L = gbblas.lib()
     for code in range(0, -7, -1):
