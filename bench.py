@@ -57,9 +57,11 @@ def parse_args():
     p.add_argument("--no-native", action="store_true", help="skip the native FP64 comparison")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU sample")
-    p.add_argument("--workload", choices=["ozaki", "native", "grouped", "adjoint", "semiring"], default="ozaki",
-                   help="ozaki: the headline (default); native: FP64/FP32 sweep; grouped: 4096 uneven "
-                        "problems; adjoint: fused dA/dB; semiring: (min, +) and relatives")
+    p.add_argument("--workload", choices=["ozaki", "ozaki_sweep", "native", "grouped", "adjoint", "semiring"],
+                   default="ozaki",
+                   help="ozaki: the headline (default); ozaki_sweep: error and TFLOP/s by slice / moduli count; "
+                        "native: FP64/FP32 sweep; grouped: 4096 uneven problems; adjoint: fused dA/dB; "
+                        "semiring: (min, +) and relatives")
     return p.parse_args()
 
 
@@ -191,6 +193,16 @@ def componentwise_err(Cres, rows, cols, hi, lo, ab):
     return float(np.max(d[ok] / ab[ok])) if ok.any() else 0.0
 
 
+def headline_config(M, N, K, world):
+    """The workload both arms run (identical dicts): sizes, input distribution, alpha/beta."""
+    square = M == N == K
+    return {"workload": ("ozaki_fp64_gemm_%d^3" % M) if square else "ozaki_fp64_gemm_%dx%dx%d" % (M, N, K),
+            "M": M, "N": N, "K": K,
+            "distribution": "sign*U[1,2)*2^(e_line+e_elem), e_line in [-30,30] per row/col, e_elem in [-8,8]",
+            "alpha": 1.0, "beta": 0.0, "parallelism": "replicas" if world > 1 else "single",
+            "l2": "inputs larger than L2 (%d MiB per operand)" % (M * K * 8 // 2 ** 20)}
+
+
 def reference_arm(args, rank, world):
     """The reference's CPU algorithm (oracle port of jmul!) timed on the host cores."""
     if rank != 0:
@@ -217,14 +229,51 @@ def reference_arm(args, rank, world):
         "impl": "reference", "metric": METRIC, "value": v, "unit": "TFLOP/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "ozaki_fp64_gemm_%d^3" % n, "M": n, "N": n, "K": n,
-                   "distribution": "sign*U[1,2)*2^(e_line+e_elem), e_line in [-30,30], e_elem in [-8,8]",
-                   "algorithm": "jmul! FMA chain, register-tiled (oracle port; Julia reference cannot run)"},
+        "config": headline_config(n, n, n, world),
+        "algorithm": "jmul! FMA chain, register-tiled (oracle port; the Julia reference cannot run)",
         "cpu_baseline": {"value": v, "unit": "TFLOP/s", "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": v, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def pipeline_timeline(e0, up_ev, comp_ev, down_ev, nbuf, host_enqueue_ms):
+    """Per-step timeline of the end-to-end ring (ms from the start event): for each step the
+    compute stream's idle time before it and what it waited on — its upload, the previous
+    step's compute, the download that frees its ring slot, or the host (the launch arrived
+    after every dependency had finished).  Also the uploads' overlap with compute."""
+    T = lambda ev: (e0.elapsed_time(ev[0]), e0.elapsed_time(ev[1]))   # noqa: E731
+    up, comp, down = [T(x) for x in up_ev], [T(x) for x in comp_ev], [T(x) for x in down_ev]
+    steps = len(comp)
+    waited = {"upload": 0, "previous_compute": 0, "ring_download": 0, "host": 0}
+    idle, rows = [], []
+    for i in range(steps):
+        deps = {"upload": up[i][1], "previous_compute": comp[i - 1][1] if i else 0.0}
+        if i >= nbuf:
+            deps["ring_download"] = down[i - nbuf][1]
+        cause = max(deps, key=deps.get)
+        if comp[i][0] - deps[cause] > 0.05:
+            cause = "host"
+        waited[cause] += 1
+        gap = comp[i][0] - (comp[i - 1][1] if i else 0.0)
+        if i:
+            idle.append(gap)
+        rows.append({"step": i, "upload": [round(up[i][0], 3), round(up[i][1], 3)],
+                     "compute": [round(comp[i][0], 3), round(comp[i][1], 3)],
+                     "download": [round(down[i][0], 3), round(down[i][1], 3)],
+                     "compute_idle_before_ms": round(gap, 3), "waited_on": cause,
+                     "host_enqueued_ms": round(host_enqueue_ms[i], 3)})
+    # milliseconds of upload time that ran while some compute interval was active
+    overlap = 0.0
+    for a, z in up:
+        for c0, c1 in comp:
+            overlap += max(0.0, min(z, c1) - max(a, c0))
+    up_total = sum(z - a for a, z in up)
+    return {"compute_idle_ms_median": statistics.median(idle) if idle else 0.0,
+            "compute_idle_ms_total": sum(idle), "waited_on": waited,
+            "upload_overlapped_with_compute_frac": overlap / up_total if up_total else 0.0,
+            "steps": rows[:8]}
 
 
 def _event_ms(fn, steps, stream):
@@ -452,6 +501,69 @@ def workload_grouped(args):
     return 0
 
 
+def workload_ozaki_sweep(args):
+    """Emulated FP64 at 8192^3 on the sign*U[1,2)*2^(e_line+e_elem) inputs, by slice and moduli
+    count: digit slices s = 3..8 (BF16 digit products, FP32 accumulation) and the automatic s;
+    CRT moduli n = 8..16 and the automatic n; native FP64 beside them.  Per plan: TFLOP/s
+    (FP64-equivalent 2MNK over the CUDA-event step time), the a-priori bound the call returns,
+    and the normwise error against binary128 dot products on a 64 x 64 grid of outputs."""
+    import torch
+    import gbblas
+    import oracle
+    from gbblas import workloads
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev)
+    n = args.size
+    A = np.asfortranarray(workloads.ozaki_matrix(n, n, per="row", stream=1))
+    B = np.asfortranarray(workloads.ozaki_matrix(n, n, per="col", stream=2))
+    g = np.random.default_rng(77)
+    r = np.sort(g.choice(n, 64, replace=False))
+    c = np.sort(g.choice(n, 64, replace=False))
+    ii, jj = (x.ravel() for x in np.meshgrid(np.arange(64), np.arange(64), indexing="ij"))
+    hi, lo = oracle.quad_entries(np.asfortranarray(A[r, :]), np.asfortranarray(B[:, c]), ii, jj)
+    na, nb = float(np.linalg.norm(A)), float(np.linalg.norm(B))
+
+    def dev_cm(x):
+        return torch.from_numpy(np.ascontiguousarray(x.T)).to(dev).t()
+    Ad, Bd = dev_cm(A), dev_cm(B)
+    del A, B
+    C = torch.empty((n, n), dtype=torch.float64, device=dev).t()
+    rt, ct = torch.as_tensor(r, device=dev), torch.as_tensor(c, device=dev)
+    flops = 2.0 * n ** 3
+
+    def err_of():
+        got = C[rt][:, ct].cpu().numpy()[ii, jj]
+        return float(np.linalg.norm((got - hi) - lo) * np.sqrt(n * n / ii.size) / (na * nb))
+
+    rows = []
+    cases = [("native", 0)] + [("ozaki", s) for s in (3, 4, 5, 6, 7, 8, 0)] + \
+            [("ozaki_crt", m) for m in (8, 9, 10, 11, 12, 13, 14, 15, 16, 0)]
+    for mode, cnt in cases:
+        steps = 1 if mode == "native" else args.steps
+        _, bound = gbblas.gemm_(C, Ad, Bd, mode=mode, slices=cnt, return_bound=True)
+        torch.cuda.synchronize()
+        gbblas.check_device_status()
+        err = err_of()
+        plan = gbblas.last_ozaki_plan() if mode != "native" else None
+        ms = _event_ms(lambda: gbblas.gemm_(C, Ad, Bd, mode=mode, slices=cnt), steps, stream)
+        row = {"method": {"native": "native_fp64", "ozaki": "slices", "ozaki_crt": "crt"}[mode],
+               "requested": cnt if mode != "native" else None, "ms": ms,
+               "tflops": flops / (ms * 1e-3) / 1e12, "bound": bound, "normwise_err": err}
+        if plan:
+            row.update({"slices_or_moduli": plan["slices"], "bits": plan["bits"],
+                        "tensor_products": plan["products"]})
+        rows.append(row)
+    auto = [x for x in rows if x["method"] == "crt" and x["requested"] == 0][0]
+    _side_line(args, "FP64-accurate GEMM TFLOP/s by slice and moduli count, 8192^3", auto["tflops"], "TFLOP/s",
+               auto["ms"], {"workload": "ozaki_fp64_gemm_%d^3_sweep" % n, "M": n, "N": n, "K": n,
+                            "distribution": "sign*U[1,2)*2^(e_line+e_elem), e_line in [-30,30] per row/col, "
+                                            "e_elem in [-8,8]"},
+               {"dtype": "f64", "sweep": rows,
+                "error_metric": "||C - C_ref||_F / (||A||_F ||B||_F) estimated on a 64 x 64 output grid against "
+                                "binary128 dot products"})
+    return 0
+
+
 def workload_adjoint(args):
     """Adjoint: loss = sum(W .* (A*B)), A 4096x2048, B 2048x4096, W 4096x4096 N(0,1) float32:
     dA = W B^T and dB = A^T W in one launch (3xBF16 split, FP32 accumulation)."""
@@ -501,7 +613,7 @@ def main():
         if rank != 0:
             return 0
         return {"native": workload_native, "grouped": workload_grouped, "adjoint": workload_adjoint,
-                "semiring": workload_semiring}[args.workload](args)
+                "semiring": workload_semiring, "ozaki_sweep": workload_ozaki_sweep}[args.workload](args)
 
     import torch
     import gbblas
@@ -618,12 +730,15 @@ def main():
 
     pipe_prof = gbblas.profile()
     pipe_prof.__enter__()
+    host_t0 = time.perf_counter()
+    host_enqueue_ms = []
     for i in range(min(NBUF - 1, args.steps)):
         upload(i)
     for i in range(args.steps):
         b = i % NBUF
         if i + NBUF - 1 < args.steps:
             upload(i + NBUF - 1)
+        host_enqueue_ms.append((time.perf_counter() - host_t0) * 1e3)
         stream.wait_event(up_done[b])
         if i >= NBUF:
             stream.wait_event(down_done[b])              # C_e[b] of step i - NBUF has been read
@@ -648,6 +763,7 @@ def main():
     comp_in_pipeline = statistics.median(a.elapsed_time(z) for a, z in comp_ev)
     up_in_pipeline = statistics.median(a.elapsed_time(z) for a, z in up_ev)
     down_in_pipeline = statistics.median(a.elapsed_time(z) for a, z in down_ev)
+    timeline = pipeline_timeline(e0, up_ev, comp_ev, down_ev, NBUF, host_enqueue_ms)
     copy_stream = up_stream
 
     # the blocking host-buffer entry point (the reference's own calling pattern: host operands
@@ -753,18 +869,13 @@ def main():
             "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": ("ozaki_fp64_gemm_%d^3" % n) if not args.mnk else
-                       "ozaki_fp64_gemm_%dx%dx%d" % (M, N, K), "M": M, "N": N, "K": K,
-                       "distribution": "sign*U[1,2)*2^(e_line+e_elem), e_line in [-30,30] per row/col, "
-                                       "e_elem in [-8,8]",
-                       "method": args.method,
-                       **({"moduli": plan["slices"], "integer_bits": plan["bits"],
-                           "residue_products": plan["products"]} if args.method == "crt" else
-                          {"slices": plan["slices"], "bits": plan["bits"], "slice_products": plan["products"],
-                           "accumulation_groups": plan["groups"]}),
-                       "k_chunk": plan["k_chunk"], "alpha": 1.0, "beta": 0.0,
-                       "parallelism": "replicas" if world > 1 else "single",
-                       "l2": "inputs larger than L2 (512 MiB per operand)"},
+            "config": headline_config(M, N, K, world),
+            "plan": {"method": args.method,
+                     **({"moduli": plan["slices"], "integer_bits": plan["bits"],
+                         "residue_products": plan["products"]} if args.method == "crt" else
+                        {"slices": plan["slices"], "bits": plan["bits"], "slice_products": plan["products"],
+                         "accumulation_groups": plan["groups"]}),
+                     "k_chunk": plan["k_chunk"]},
             "accuracy": {"normwise_err": err_oz, "bound": bound, "componentwise_err": cerr_oz,
                          "metric": "||C - C_ref||_F / (||A||_F ||B||_F), 4096 sampled entries against "
                                    "binary128 dot products; componentwise: max |C - C_ref|_ij / (|A||B|)_ij "
@@ -785,6 +896,7 @@ def main():
                     "compute_ms_in_pipeline": comp_in_pipeline,
                     "upload_ms_in_pipeline": up_in_pipeline, "download_ms_in_pipeline": down_in_pipeline,
                     "kernel_ms_in_pipeline": {k: v / args.steps for k, v in pipe_prof.ms.items()},
+                    "timeline": timeline,
                     "h2d_bytes_per_step": int(A_pin.numel() * 8 + B_pin.numel() * 8),
                     "d2h_bytes_per_step": int(C_pin.numel() * 8)},
             "host_api": host_api,

@@ -89,8 +89,11 @@ GB_API int gb_set_ozaki_min_chunks(int min_chunks);
  * device).  Workspace is otherwise kept between calls. */
 GB_API int gb_release_workspace(void);
 
-/* Reads and clears the device-side status word written by timed-out waits
- * (synchronises `stream`). */
+/* Reads and clears the device-side status word written by timed-out waits (synchronises
+ * `stream`).  There is one status word per device, shared by every call on that device from
+ * every stream and thread: the first expired wait since the last check is reported by
+ * whichever check comes next, and the read and the clear are one atomic step, so a report is
+ * never lost between them. */
 GB_API int gb_check_status(void* stream);
 
 /* ------------------------------------------------------------------ tracing */
@@ -231,16 +234,19 @@ GB_API int gb_gemm_grouped_f32(const gb_problem_t* problems, int count, const gb
                         void* workspace, size_t workspace_bytes, void* stream);
 /* Allocation-free grouped FP64 GEMM.  No counterpart in the reference (jBLAS never
  * allocates because it only multiplies static-size arrays on the CPU).  For callers that
- * cannot allocate device memory when they multiply: code issuing work while a CUDA graph
- * capture in global mode is open (cudaMalloc is illegal there), threads that must not
- * block on the implicit device synchronisation of cudaMalloc/cudaFree, and hosts whose
- * device memory is entirely owned by another runtime.  The tile prefix sums live in a
+ * cannot allocate device memory when they multiply: threads that must not block on the
+ * implicit device synchronisation of cudaMalloc/cudaFree (a latency-bound serving loop, a
+ * callback running under another library's lock), and hosts whose device memory is
+ * entirely owned by another runtime or allocator.  The tile prefix sums live in a
  * file-scope device array of GB_GROUPED_NOALLOC_MAX + 1 int64 (512 KiB), which every GPU
  * that loads the library keeps until the process exits.  count above the maximum gives
  * GB_ERR_INVALID_VALUE.  The first call on a device looks the array's device address up
  * (cudaGetSymbolAddress, no allocation); make that first call before any stream capture.
  * Every call shares the one array: calls that overlap on the GPU (other streams, other
- * threads) race and must be serialised by the caller.  Results equal gb_gemm_grouped_f64's. */
+ * threads) race and must be serialised by the caller.  Results equal gb_gemm_grouped_f64's.
+ * A null or host `problems` table gives GB_ERR_INVALID_VALUE before anything is launched.
+ * gb_launch_counts counts its launches; the profiling timers (gb_profile_start/stop) do not
+ * time them, because timing would create CUDA events. */
 #define GB_GROUPED_NOALLOC_MAX 65536
 GB_API int gb_gemm_grouped_f64_noalloc(const gb_problem_t* problems, int count, const gb_grouped_tuning_t* tuning,
                                 void* stream);

@@ -98,6 +98,16 @@ static int device_info(DeviceInfo** out) {
   return GB_OK;
 }
 
+// Takes the device status word (code exchanged with 0) into `out`.
+__global__ void status_take_kernel(DeviceStatus* __restrict__ st, DeviceStatus* __restrict__ out) {
+  DeviceStatus r;
+  r.code = atomicExch(&st->code, 0);
+  r.where = r.code ? st->where : 0;
+  r.block = r.code ? st->block : 0;
+  r.pad = 0;
+  *out = r;
+}
+
 // Device or managed memory only: a host pointer handed to a kernel would fault.
 static bool is_device_ptr(const void* p) {
   if (p == nullptr) return false;
@@ -764,14 +774,21 @@ int gb_check_status(void* stream) {
   int rc = device_info(&dev);
   if (rc) return rc;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // Read and clear in one atomic step on the device, into a slot of this call's own: an error
+  // recorded while the check runs is either taken by it or left for the next check, never lost.
+  DeviceStatus* slot = nullptr;
+  GB_CUDA_TRY(cudaMallocFromPoolAsync(reinterpret_cast<void**>(&slot), sizeof(DeviceStatus), dev->pool, s));
+  status_take_kernel<<<1, 1, 0, s>>>(dev->status, slot);
+  cudaError_t e = cudaGetLastError();
   DeviceStatus h;
-  GB_CUDA_TRY(cudaMemcpyAsync(&h, dev->status, sizeof(h), cudaMemcpyDeviceToHost, s));
-  GB_CUDA_TRY(cudaStreamSynchronize(s));
+  std::memset(&h, 0, sizeof(h));
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&h, slot, sizeof(h), cudaMemcpyDeviceToHost, s);
+  cudaFreeAsync(slot, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return gb_set_cuda_error(e, "status check");
   if (h.code != 0) {
     std::snprintf(g_last_detail, sizeof(g_last_detail), "pipeline wait at site %d timed out in block %d",
                   h.where, h.block);
-    GB_CUDA_TRY(cudaMemsetAsync(dev->status, 0, sizeof(DeviceStatus), s));
-    GB_CUDA_TRY(cudaStreamSynchronize(s));
     return h.code;
   }
   return GB_OK;
@@ -908,6 +925,8 @@ int gb_gemm_grouped_f32(const gb_problem_t* problems, int count, const gb_groupe
 
 int gb_gemm_grouped_f64_noalloc(const gb_problem_t* problems, int count, const gb_grouped_tuning_t* tuning,
                                 void* stream) {
+  // A null or host table would fault in the prologue: reject it before any launch.
+  if (count > 0 && count <= GB_GROUPED_NOALLOC_MAX && !is_device_ptr(problems)) return GB_ERR_INVALID_VALUE;
   return grouped_f64_noalloc(problems, count, tuning, static_cast<cudaStream_t>(stream));
 }
 

@@ -9,6 +9,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 #include "../../include/gbblas.h"
 
 #if defined(__CUDA_ARCH__) && (__CUDA_ARCH__ < 1000)
@@ -335,3 +337,20 @@ __device__ __forceinline__ double scale_pow2(double x, int e) {
   } while (0)
 
 extern "C++" int gb_set_cuda_error(cudaError_t e, const char* what);
+
+namespace gb {
+// Opts a kernel into `bytes` of dynamic shared memory once per device.  The runtime loads each
+// kernel into every device's context separately and the attribute belongs to that copy, so
+// the flag is one bit per device (`done`, devices 0..63; others set it on every launch).
+// Concurrent first calls may both set it, which is harmless.
+template <typename Kernel>
+inline int opt_in_dynamic_smem(Kernel kernel, int bytes, std::atomic<unsigned long long>& done) {
+  int dev = 0;
+  GB_CUDA_TRY(cudaGetDevice(&dev));
+  const unsigned long long bit = (dev >= 0 && dev < 64) ? (1ull << dev) : 0ull;
+  if (bit && (done.load(std::memory_order_acquire) & bit)) return GB_OK;
+  GB_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  if (bit) done.fetch_or(bit, std::memory_order_release);
+  return GB_OK;
+}
+}  // namespace gb

@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -264,14 +265,29 @@ int grouped_validate_tuning(int dtype_bytes, const gb_grouped_tuning_t& t) {
   return GB_OK;
 }
 
+// Resident CTAs per SM of grouped_gemm_kernel<T>, looked up once per device (the occupancy
+// query runs against the current device's context); concurrent first calls may both query,
+// and both store the same value.
+constexpr int GROUPED_MAX_DEVICES = 64;
+
 template <typename T>
 static int grid_for(int sms) {
-  static int per_sm = 0;
-  if (!per_sm) {
+  static std::atomic<int> per_sm_of[GROUPED_MAX_DEVICES];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= GROUPED_MAX_DEVICES) {
+    cudaGetLastError();
+    dev = -1;
+  }
+  int per_sm = dev >= 0 ? per_sm_of[dev].load(std::memory_order_relaxed) : 0;
+  if (per_sm < 1) {
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, grouped_gemm_kernel<T>, GROUPED_THREADS, 0) !=
             cudaSuccess ||
-        per_sm < 1)
+        per_sm < 1) {
+      cudaGetLastError();
       per_sm = 1;
+    } else if (dev >= 0) {
+      per_sm_of[dev].store(per_sm, std::memory_order_relaxed);
+    }
   }
   return sms * per_sm;
 }
@@ -423,14 +439,16 @@ int grouped_f64_noalloc(const gb_problem_t* d_probs, int count, const gb_grouped
   rc = grouped_validate_tuning(8, t);
   if (rc) return rc;
   // The prologue rewrites offsets[0..count] on every call, so nothing needs clearing.
-  // Launched directly (not through the tracing layer, which creates CUDA events while
-  // profiling is on).
+  // Launched directly, not through the timing hooks (which create CUDA events while profiling
+  // is on); gb_launch_counts still counts both launches.
   grouped_prefix_kernel<<<1, 1024, 0, s>>>(d_probs, count, t, offsets);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return gb_set_cuda_error(e, "grouped prologue launch");
+  prof_count(GB_KERNEL_GROUPED_GEMM);
   grouped_gemm_kernel<double><<<grid_for<double>(sms), GROUPED_THREADS, 0, s>>>(d_probs, count, t, offsets);
   e = cudaGetLastError();
   if (e != cudaSuccess) return gb_set_cuda_error(e, "grouped launch");
+  prof_count(GB_KERNEL_GROUPED_GEMM);
   return GB_OK;
 }
 

@@ -5,6 +5,8 @@
 namespace gb {
 void prof_before(int kind, cudaStream_t s);
 void prof_after(int kind, cudaStream_t s);
+// Counts one launch of `kind` without timing it (no CUDA events are created or recorded).
+void prof_count(int kind);
 }  // namespace gb
 
 // Brackets one kernel launch statement with the tracing hooks.

@@ -344,24 +344,18 @@ void tc_set_engine(int e) { g_tc_engine.store(e); }
 int tc_gemm_launch(int epi, const CUtensorMap& ta0, const CUtensorMap& tb0, const CUtensorMap* ta1,
                    const CUtensorMap* tb1, const SliceSchedule& sched, const TcParams& prm, int grid,
                    int kernel_kind, cudaStream_t s) {
-  static bool attr_set[2] = {false, false};  // the attribute is per function, not per device
+  static std::atomic<unsigned long long> smem_opt_in[2];   // per kernel, one bit per device
   const CUtensorMap& a1 = ta1 ? *ta1 : ta0;
   const CUtensorMap& b1 = tb1 ? *tb1 : tb0;
   if (grid < 1) return GB_OK;
   if (epi == TC_EPI_OZAKI_F64) {
-    if (!attr_set[0]) {
-      GB_CUDA_TRY(cudaFuncSetAttribute(tc_gemm_kernel<TC_EPI_OZAKI_F64>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_BYTES));
-      attr_set[0] = true;
-    }
+    const int rc = opt_in_dynamic_smem(tc_gemm_kernel<TC_EPI_OZAKI_F64>, TC_SMEM_BYTES, smem_opt_in[0]);
+    if (rc) return rc;
     GB_LAUNCH(kernel_kind, s,
               (tc_gemm_kernel<TC_EPI_OZAKI_F64><<<grid, TC_THREADS, TC_SMEM_BYTES, s>>>(ta0, tb0, a1, b1, sched, prm)));
   } else {
-    if (!attr_set[1]) {
-      GB_CUDA_TRY(cudaFuncSetAttribute(tc_gemm_kernel<TC_EPI_F32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       TC_SMEM_BYTES));
-      attr_set[1] = true;
-    }
+    const int rc = opt_in_dynamic_smem(tc_gemm_kernel<TC_EPI_F32>, TC_SMEM_BYTES, smem_opt_in[1]);
+    if (rc) return rc;
     GB_LAUNCH(kernel_kind, s,
               (tc_gemm_kernel<TC_EPI_F32><<<grid, TC_THREADS, TC_SMEM_BYTES, s>>>(ta0, tb0, a1, b1, sched, prm)));
   }

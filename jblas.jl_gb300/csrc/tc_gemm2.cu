@@ -445,35 +445,26 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(P2Shape<EPI>::THREAD
 int tc_gemm_pair_launch(int epi, const CUtensorMap& ta0, const CUtensorMap& tb0, const CUtensorMap* ta1,
                         const CUtensorMap* tb1, const SliceSchedule& sched, const TcParams& prm, int grid,
                         int kernel_kind, cudaStream_t s) {
-  static bool attr_set[3] = {false, false, false};
+  static std::atomic<unsigned long long> smem_opt_in[3];   // per kernel, one bit per device
   const CUtensorMap& a1 = ta1 ? *ta1 : ta0;
   const CUtensorMap& b1 = tb1 ? *tb1 : tb0;
   if (grid < 2) grid = 2;
   grid &= ~1;
   if (epi == TC_EPI_OZAKI_F64) {
-    if (!attr_set[0]) {
-      GB_CUDA_TRY(cudaFuncSetAttribute(tc_gemm_pair_kernel<TC_EPI_OZAKI_F64>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, P2_SMEM_BYTES));
-      attr_set[0] = true;
-    }
+    const int rc = opt_in_dynamic_smem(tc_gemm_pair_kernel<TC_EPI_OZAKI_F64>, P2_SMEM_BYTES, smem_opt_in[0]);
+    if (rc) return rc;
     GB_LAUNCH(kernel_kind, s,
               (tc_gemm_pair_kernel<TC_EPI_OZAKI_F64><<<grid, P2Shape<TC_EPI_OZAKI_F64>::THREADS, P2_SMEM_BYTES, s>>>(ta0, tb0, a1, b1, sched,
                                                                                              prm)));
   } else if (epi == TC_EPI_CRT) {
-    if (!attr_set[2]) {
-      GB_CUDA_TRY(cudaFuncSetAttribute(tc_gemm_pair_kernel<TC_EPI_CRT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       P2_SMEM_BYTES));
-      attr_set[2] = true;
-    }
+    const int rc = opt_in_dynamic_smem(tc_gemm_pair_kernel<TC_EPI_CRT>, P2_SMEM_BYTES, smem_opt_in[2]);
+    if (rc) return rc;
     GB_LAUNCH(kernel_kind, s,
               (tc_gemm_pair_kernel<TC_EPI_CRT><<<grid, P2Shape<TC_EPI_CRT>::THREADS, P2_SMEM_BYTES, s>>>(ta0, tb0, a1, b1, sched,
                                                                                            prm)));
   } else {
-    if (!attr_set[1]) {
-      GB_CUDA_TRY(cudaFuncSetAttribute(tc_gemm_pair_kernel<TC_EPI_F32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       P2_SMEM_BYTES));
-      attr_set[1] = true;
-    }
+    const int rc = opt_in_dynamic_smem(tc_gemm_pair_kernel<TC_EPI_F32>, P2_SMEM_BYTES, smem_opt_in[1]);
+    if (rc) return rc;
     GB_LAUNCH(kernel_kind, s,
               (tc_gemm_pair_kernel<TC_EPI_F32><<<grid, P2Shape<TC_EPI_F32>::THREADS, P2_SMEM_BYTES, s>>>(ta0, tb0, a1, b1, sched, prm)));
   }

@@ -20,5 +20,9 @@ def test_reference_arm_json_line():
         assert key in d, key
     assert d["impl"] == "reference" and d["value"] > 0 and d["higher_is_better"] is True
     assert d["config"]["workload"] == "ozaki_fp64_gemm_256^3"
+    # the GPU arm prints the same config dict (its plan goes under a separate key)
+    sys.path.insert(0, ROOT)
+    import bench
+    assert d["config"] == bench.headline_config(256, 256, 256, 1)
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["value"] == d["value"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}

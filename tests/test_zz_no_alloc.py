@@ -1,7 +1,6 @@
 """The allocation-free grouped FP64 entry point (gb_gemm_grouped_f64_noalloc).
 
-Some callers cannot allocate device memory at the moment they multiply: work issued
-while a global-mode CUDA graph capture is open (cudaMalloc is illegal then), threads that
+Some callers cannot allocate device memory at the moment they multiply: threads that
 must not stall on the device synchronisation cudaMalloc/cudaFree can imply, and hosts
 whose device memory is owned by another runtime.  This entry point keeps its scratch (the
 per-problem tile prefix sums) in a fixed device array of GB_GROUPED_NOALLOC_MAX + 1
@@ -62,3 +61,24 @@ def test_noalloc_rejects_oversized_count(cuda):
                                                 ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
     assert rc == _lib.GB_ERR_INVALID_VALUE
     torch.cuda.synchronize()
+
+
+def test_noalloc_rejects_null_and_host_tables(cuda):
+    """A null table or a table in host memory is refused with GB_ERR_INVALID_VALUE before any
+    launch (a kernel given either would fault), and the next call still works."""
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    L = _lib.lib()
+    host_table = (_lib.Problem * 4)()
+    assert L.gb_gemm_grouped_f64_noalloc(None, 4, None, stream) == _lib.GB_ERR_INVALID_VALUE
+    assert L.gb_gemm_grouped_f64_noalloc(ctypes.cast(host_table, ctypes.c_void_p), 4, None,
+                                         stream) == _lib.GB_ERR_INVALID_VALUE
+    assert L.gb_gemm_grouped_f64_noalloc(None, 0, None, stream) == _lib.GB_OK
+    torch.cuda.synchronize()
+    As, Bs, Cs, Rs = _problem_set(40, 13)
+    ref_plan = grouped.GroupedGemm(As, Bs, Rs)
+    plan = grouped.GroupedGemm(As, Bs, Cs)
+    ref_plan.run(stream.value)
+    _noalloc(plan, stream.value)
+    torch.cuda.synchronize()
+    for C, R in zip(Cs, Rs):
+        assert_bit_equal(to_host(C), to_host(R))
