@@ -161,23 +161,49 @@ def cpu_cores():
 
 
 def cpu_sample(A, B, target_s, threads):
-    """Time jmul!'s register-tiled chain on a column sample of A*B; TFLOP/s and description."""
+    """Time jmul!'s register-tiled chain (the tile pick_kernel_size gives for this host's register
+    file) on a column sample of A*B; TFLOP/s, description, columns, seconds.  The sample's
+    result is checked against the scalar chain on 64 entries (the port must compute jmul!'s
+    arithmetic, not only take its time)."""
     import oracle
     n = A.shape[0]
     K = A.shape[1]
-    cols = max(6, min(B.shape[1], 48))
+    tr, tc = oracle.host_tile(np.float64)
+    cols = max(tc, min(B.shape[1], 8 * tc))
     t0 = time.perf_counter()
     oracle.jmul_tiled(A, np.asfortranarray(B[:, :cols]), nthreads=threads)
     dt = time.perf_counter() - t0
-    cols = int(min(B.shape[1], max(6, cols * target_s / max(dt, 1e-6))))
-    cols -= cols % 6 if cols > 6 else 0
+    cols = int(min(B.shape[1], max(tc, cols * target_s / max(dt, 1e-6))))
+    cols -= cols % tc
     Bs = np.asfortranarray(B[:, :cols])
     t0 = time.perf_counter()
-    oracle.jmul_tiled(A, Bs, nthreads=threads)
+    out = oracle.jmul_tiled(A, Bs, nthreads=threads)
     dt = time.perf_counter() - t0
+    g = np.random.default_rng(5)
+    ri, ci = g.integers(0, n, 64), g.integers(0, cols, 64)
+    if not np.array_equal(out[ri, ci].view(np.uint64), oracle.chain_entries(A, Bs, ri, ci).view(np.uint64)):
+        raise RuntimeError("CPU baseline result differs from jmul!'s chain")
     flops = 2.0 * n * K * cols
-    return flops / dt / 1e12, "C[:, :%d] of the %dx%dx%d product (%.3g flop), %.2f s" % (cols, n, K, B.shape[1],
-                                                                                      flops, dt), cols, dt
+    return flops / dt / 1e12, "C[:, :%d] of the %dx%dx%d product (%.3g flop), %.2f s, %dx%d register tile" % (
+        cols, n, K, B.shape[1], flops, dt, tr, tc), cols, dt
+
+
+def reference_shape_timing():
+    """jmul! at the one shape the reference publishes a time for: D 16x14 = A 16x32 * X 32x14
+    Float64, minimum 127.921 ns (test/runtests.jl:103-116, single thread).  The port on one
+    core, with this host's pick_kernel_size tile (remainder rows and columns by the scalar
+    chain) and with one 16x14 tile covering D, as the reference's benchmark kernel did."""
+    import oracle
+    g = np.random.default_rng(16)
+    A = np.asfortranarray(g.standard_normal((16, 32)))
+    X = np.asfortranarray(g.standard_normal((32, 14)))
+    flops = 2.0 * 16 * 32 * 14
+    out = {"shape": "16x32x14 (M x K x N)", "reference_min_ns": 127.921,
+           "reference_gflops": flops / 127.921}
+    for name, tile in (("host_tile", None), ("tile_16x14", (16, 14))):
+        ns = oracle.time_jmul_tiled(A, X, tile=tile)
+        out[name] = {"tile": list(tile or oracle.host_tile(np.float64)), "min_ns": ns, "gflops": flops / ns}
+    return out
 
 
 def normwise_err(Cres, A, B, rows, cols, hi, lo):
@@ -224,7 +250,9 @@ def reference_arm(args, rank, world):
     dt = (time.perf_counter() - t0) / args.steps
     flops = 2.0 * n * n * cols
     v = flops / dt / 1e12
-    sample = "each step C[:, :%d] of the %d^3 product (%.3g flop) on %d threads" % (cols, n, flops, threads)
+    tr, tc = oracle.host_tile(np.float64)
+    sample = "each step C[:, :%d] of the %d^3 product (%.3g flop) on %d threads, %dx%d register tile" % (
+        cols, n, flops, threads, tr, tc)
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "TFLOP/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
@@ -863,7 +891,8 @@ def main():
             # the reference itself is single-threaded: the same port on one core, a shorter sample
             v1, sample1, _, _ = cpu_sample(A_h, B_h, max(2.0, args.cpu_seconds / 4), 1)
             cpu = {"value": v, "unit": "TFLOP/s", "cores": threads, "kind": "port", "sample": sample,
-                   "single_core": {"value": v1, "cores": 1, "sample": sample1}}
+                   "single_core": {"value": v1, "cores": 1, "sample": sample1},
+                   "reference_shape": reference_shape_timing()}
 
         line = {
             "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,

@@ -36,6 +36,8 @@ def build(force=False, verbose=False):
            "-fno-math-errno", "-std=c11"]
     if platform.machine() in ("x86_64", "AMD64") and _cpu_has("fma") and _cpu_has("avx2"):
         cmd += ["-mfma", "-mavx2"]
+        if _cpu_has("avx512f"):
+            cmd += ["-mavx512f"]   # the 32-register file pick_kernel_size sizes the tile for
     tmp = LIB + ".tmp%d" % os.getpid()
     cmd += [SRC, "-o", tmp, "-lm"]
     if verbose:

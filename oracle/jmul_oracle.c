@@ -31,10 +31,12 @@
  *
  * Build: compiled with -ffp-contract=off so that only the explicit fma() calls fuse.
  */
+#define _POSIX_C_SOURCE 199309L   /* clock_gettime */
 #include <math.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -129,100 +131,187 @@ OR_KERNEL(or_kernel_f32, float, fmaf)
 
 /* ------------------------------------------------- register-tiled timed baseline */
 /*
- * The jmul! algorithm as the reference generates it: a rows x cols register tile
- * (src/kernel_structure.jl:76-99 pick_kernel_size), the full K reduction held in the
- * tile (src/gemm.jl:318-333), column tiles outer and row tiles inner (:313), software
- * prefetch of A `freq` columns ahead (src/memory_management.jl:204-237, default 7).
- * The tile here is 8 x 6 doubles (16 x 6 floats), the shape pick_kernel_size gives for
- * 32 registers of 4 lanes; remainder tiles use the scalar chain.  Per element the
- * operation order equals chain_f64, so results are bit-identical to or_gemm_f64.
- * Threads split the column tiles (the reference is single-threaded; nthreads = 1 is
- * the faithful configuration).
+ * The jmul! algorithm as the reference generates it: a TR x TC register tile whose shape
+ * pick_kernel_size chooses for the host's register file (src/kernel_structure.jl:76-99,
+ * restated by or_pick_kernel_size below and by oracle.pick_kernel_size), the full K
+ * reduction held in the tile (src/gemm.jl:318-333), column tiles outer and row tiles inner
+ * (:313), software prefetch of A `freq` = 7 columns ahead (src/memory_management.jl:204-237).
+ * Remainder rows and columns, which jmul! leaves unwritten (src/gemm.jl:340-345), use the
+ * scalar chain here.  Per element the operation order equals chain_f64, so results are
+ * bit-identical to or_gemm_f64 whatever the tile.  Threads split the column tiles (the
+ * reference is single-threaded; nthreads = 1 is the faithful configuration).
+ *
+ * Tiles instantiated (rows x cols): f64 40x5 (AVX-512: 8 lanes, 32 registers), 12x4 (AVX2:
+ * 4 lanes, 16 registers), 10x5 (128-bit NEON: 2 lanes, 32 registers), 20x5 (4 lanes, 32
+ * registers), 16x14 (the one tile of the reference's 16x32x14 benchmark, test/runtests.jl:103-116),
+ * 8x6; f32 80x5, 24x4, 20x5, 40x5, 16x14.
  */
-#define TMR 8
-#define TNR 6
-#define TMR32 16
-
-void or_jmul_tiled_f64(i64 M, i64 N, i64 K, const double* A, i64 lda, const double* B, i64 ldb,
-                       double* C, i64 ldc, int nthreads) {
-  const i64 col_chunks = N / TNR, row_chunks = M / TMR;
-#ifdef _OPENMP
-#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads > 0 ? nthreads : 1)
+/* SIMD width of the host's register file (bytes), the vector type of the tile's columns. */
+#if defined(__AVX512F__)
+#define OR_VB 64
+#elif defined(__AVX2__)
+#define OR_VB 32
+#else
+#define OR_VB 16
 #endif
-  for (i64 cc = 0; cc < col_chunks; ++cc) {
-    for (i64 rc = 0; rc < row_chunks; ++rc) {
-      const double* pa = A + rc * TMR;
-      const double* pb = B + cc * TNR * ldb;
-      double acc[TNR][TMR];
-      if (K == 0) {
-        for (int c = 0; c < TNR; ++c) for (int r = 0; r < TMR; ++r) acc[c][r] = 0.0;
-      } else {
-        for (int c = 0; c < TNR; ++c) {
-          const double x = pb[c * ldb];
-          for (int r = 0; r < TMR; ++r) acc[c][r] = pa[r] * x;
-        }
-        for (i64 k = 1; k < K; ++k) {
-          const double* ak = pa + k * lda;
-          __builtin_prefetch(ak + 7 * lda, 0, 3);
-          double av[TMR];
-          for (int r = 0; r < TMR; ++r) av[r] = ak[r];
-          for (int c = 0; c < TNR; ++c) {
-            const double x = pb[k + c * ldb];
-            for (int r = 0; r < TMR; ++r) acc[c][r] = fma(av[r], x, acc[c][r]);
-          }
-        }
-      }
-      for (int c = 0; c < TNR; ++c)
-        for (int r = 0; r < TMR; ++r) C[rc * TMR + r + (cc * TNR + c) * ldc] = acc[c][r];
-    }
-    for (i64 i = row_chunks * TMR; i < M; ++i)
-      for (int c = 0; c < TNR; ++c)
-        C[i + (cc * TNR + c) * ldc] = chain_f64(0, 0, i, cc * TNR + c, K, A, lda, B, ldb);
+typedef double or_vd __attribute__((vector_size(OR_VB)));
+typedef float or_vf __attribute__((vector_size(OR_VB)));
+
+/* One TR x TC tile over the whole K (src/gemm.jl:318-333).  When TR is a multiple of the SIMD
+ * width the tile's columns are held as GCC vectors (portable vector extensions, no intrinsics)
+ * so that the accumulators stay in registers as the reference's Vec tiles do; acc + a * x is
+ * contracted to one fused multiply-add (fp-contract=fast is enabled for these functions only,
+ * and no other product meets an add in them), the first step a plain rounded product.  The
+ * bit-exact tests against the scalar chain check that every step fused.  Other tiles use
+ * scalar fma() loops. */
+#define OR_TILED(NAME, T, VT, FMA, TR, TC)                                                          \
+  __attribute__((optimize("fp-contract=fast"))) static void NAME##_tile(                          \
+      i64 K, const T* pa, i64 lda, const T* pb, i64 ldb, T* pc, i64 ldc) {                          \
+    enum { L = OR_VB / (int)sizeof(T), NV = ((TR) % (OR_VB / (int)sizeof(T)) == 0) ? (TR) / (OR_VB / (int)sizeof(T)) : 0 }; \
+    if (NV > 0 && K > 0) {                                                                          \
+      VT acc[TC][NV > 0 ? NV : 1];                                                                  \
+      _Pragma("GCC unroll 32")                                                                      \
+      for (int c = 0; c < (TC); ++c) {                                                              \
+        const VT x = (VT){0} + pb[c * ldb];                                                         \
+        _Pragma("GCC unroll 32")                                                                    \
+        for (int v = 0; v < NV; ++v) {                                                              \
+          VT a;                                                                                     \
+          memcpy(&a, pa + v * L, sizeof(a));                                                        \
+          acc[c][v] = a * x;                                                                        \
+        }                                                                                           \
+      }                                                                                             \
+      for (i64 k = 1; k < K; ++k) {                                                                 \
+        const T* ak = pa + k * lda;                                                                 \
+        __builtin_prefetch(ak + 7 * lda, 0, 3);                                                     \
+        VT av[NV > 0 ? NV : 1];                                                                     \
+        _Pragma("GCC unroll 32")                                                                    \
+        for (int v = 0; v < NV; ++v) memcpy(&av[v], ak + v * L, sizeof(VT));                        \
+        _Pragma("GCC unroll 32")                                                                    \
+        for (int c = 0; c < (TC); ++c) {                                                            \
+          const VT x = (VT){0} + pb[k + c * ldb];                                                   \
+          _Pragma("GCC unroll 32")                                                                  \
+          for (int v = 0; v < NV; ++v) acc[c][v] = acc[c][v] + av[v] * x;                           \
+        }                                                                                           \
+      }                                                                                             \
+      _Pragma("GCC unroll 32")                                                                      \
+      for (int c = 0; c < (TC); ++c)                                                                \
+        _Pragma("GCC unroll 32")                                                                    \
+        for (int v = 0; v < NV; ++v) memcpy(pc + v * L + c * ldc, &acc[c][v], sizeof(VT));          \
+      return;                                                                                       \
+    }                                                                                               \
+    T acc[TC][TR];                                                                                  \
+    if (K == 0) {                                                                                   \
+      for (int c = 0; c < (TC); ++c) for (int r = 0; r < (TR); ++r) acc[c][r] = (T)0;               \
+    } else {                                                                                        \
+      for (int c = 0; c < (TC); ++c) {                                                              \
+        const T x = pb[c * ldb];                                                                    \
+        for (int r = 0; r < (TR); ++r) acc[c][r] = pa[r] * x;                                       \
+      }                                                                                             \
+      for (i64 k = 1; k < K; ++k) {                                                                 \
+        const T* ak = pa + k * lda;                                                                 \
+        __builtin_prefetch(ak + 7 * lda, 0, 3);                                                     \
+        T av[TR];                                                                                   \
+        for (int r = 0; r < (TR); ++r) av[r] = ak[r];                                               \
+        for (int c = 0; c < (TC); ++c) {                                                            \
+          const T x = pb[k + c * ldb];                                                              \
+          for (int r = 0; r < (TR); ++r) acc[c][r] = FMA(av[r], x, acc[c][r]);                      \
+        }                                                                                           \
+      }                                                                                             \
+    }                                                                                               \
+    for (int c = 0; c < (TC); ++c)                                                                  \
+      for (int r = 0; r < (TR); ++r) pc[r + c * ldc] = acc[c][r];                                   \
+  }                                                                                                 \
+  static void NAME(i64 M, i64 N, i64 K, const T* A, i64 lda, const T* B, i64 ldb, T* C, i64 ldc,    \
+                   int nthreads, T (*chain)(int, int, i64, i64, i64, const T*, i64, const T*, i64)) {  \
+    const i64 col_chunks = N / (TC), row_chunks = M / (TR);                                         \
+    /* one thread: no parallel region (its fork/join costs more than a small product) */            \
+    _Pragma("omp parallel for schedule(dynamic, 1) num_threads(nthreads > 1 ? nthreads : 1) if(nthreads > 1)") \
+    for (i64 cc = 0; cc < col_chunks; ++cc) {                                                       \
+      for (i64 rc = 0; rc < row_chunks; ++rc)                                                       \
+        NAME##_tile(K, A + rc * (TR), lda, B + cc * (TC) * ldb, ldb, C + rc * (TR) + cc * (TC) * ldc, ldc); \
+      for (i64 i = row_chunks * (TR); i < M; ++i)                                                   \
+        for (int c = 0; c < (TC); ++c)                                                              \
+          C[i + (cc * (TC) + c) * ldc] = chain(0, 0, i, cc * (TC) + c, K, A, lda, B, ldb);          \
+    }                                                                                               \
+    for (i64 j = col_chunks * (TC); j < N; ++j)                                                     \
+      for (i64 i = 0; i < M; ++i) C[i + j * ldc] = chain(0, 0, i, j, K, A, lda, B, ldb);            \
+    (void)nthreads;                                                                                 \
   }
-  for (i64 j = col_chunks * TNR; j < N; ++j)
-    for (i64 i = 0; i < M; ++i) C[i + j * ldc] = chain_f64(0, 0, i, j, K, A, lda, B, ldb);
-  (void)nthreads;
+
+OR_TILED(tiled_f64_40x5, double, or_vd, fma, 40, 5)
+OR_TILED(tiled_f64_12x4, double, or_vd, fma, 12, 4)
+OR_TILED(tiled_f64_10x5, double, or_vd, fma, 10, 5)
+OR_TILED(tiled_f64_20x5, double, or_vd, fma, 20, 5)
+OR_TILED(tiled_f64_16x14, double, or_vd, fma, 16, 14)
+OR_TILED(tiled_f64_8x6, double, or_vd, fma, 8, 6)
+OR_TILED(tiled_f32_80x5, float, or_vf, fmaf, 80, 5)
+OR_TILED(tiled_f32_24x4, float, or_vf, fmaf, 24, 4)
+OR_TILED(tiled_f32_20x5, float, or_vf, fmaf, 20, 5)
+OR_TILED(tiled_f32_40x5, float, or_vf, fmaf, 40, 5)
+OR_TILED(tiled_f32_16x14, float, or_vf, fmaf, 16, 14)
+
+/* pick_kernel_size (src/kernel_structure.jl:76-99) for elements of t_size bytes in a file of
+ * reg_count registers of reg_bytes: grow the rows one register of A at a time (a_loads), give
+ * the tile the columns the remaining registers hold (one register kept for the broadcast of
+ * X), and stop when the tile's elements per loaded register stop increasing.  Returns the
+ * elements per register; rows and cols of the tile through the pointers. */
+int or_pick_kernel_size(int t_size, int reg_bytes, int reg_count, int* rows, int* cols) {
+  const int epr = reg_bytes / t_size;
+  const int lines = (epr * reg_count + epr - 1) / epr;
+  int best_r = 0, best_c = 0;
+  double best = -1.0 / 0.0;
+  for (int a = 1; a <= lines; ++a) {
+    const int r = a * epr, c = (reg_count - a - 1) / a;
+    const double ratio = (double)(r * c) / (double)(c + a);
+    if (ratio < best) break;
+    best = ratio;
+    best_r = r;
+    best_c = c;
+  }
+  *rows = best_r;
+  *cols = best_c;
+  return epr;
 }
 
-void or_jmul_tiled_f32(i64 M, i64 N, i64 K, const float* A, i64 lda, const float* B, i64 ldb,
-                       float* C, i64 ldc, int nthreads) {
-  const i64 col_chunks = N / TNR, row_chunks = M / TMR32;
-#ifdef _OPENMP
-#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads > 0 ? nthreads : 1)
-#endif
-  for (i64 cc = 0; cc < col_chunks; ++cc) {
-    for (i64 rc = 0; rc < row_chunks; ++rc) {
-      const float* pa = A + rc * TMR32;
-      const float* pb = B + cc * TNR * ldb;
-      float acc[TNR][TMR32];
-      if (K == 0) {
-        for (int c = 0; c < TNR; ++c) for (int r = 0; r < TMR32; ++r) acc[c][r] = 0.0f;
-      } else {
-        for (int c = 0; c < TNR; ++c) {
-          const float x = pb[c * ldb];
-          for (int r = 0; r < TMR32; ++r) acc[c][r] = pa[r] * x;
-        }
-        for (i64 k = 1; k < K; ++k) {
-          const float* ak = pa + k * lda;
-          __builtin_prefetch(ak + 7 * lda, 0, 3);
-          float av[TMR32];
-          for (int r = 0; r < TMR32; ++r) av[r] = ak[r];
-          for (int c = 0; c < TNR; ++c) {
-            const float x = pb[k + c * ldb];
-            for (int r = 0; r < TMR32; ++r) acc[c][r] = fmaf(av[r], x, acc[c][r]);
-          }
-        }
-      }
-      for (int c = 0; c < TNR; ++c)
-        for (int r = 0; r < TMR32; ++r) C[rc * TMR32 + r + (cc * TNR + c) * ldc] = acc[c][r];
-    }
-    for (i64 i = row_chunks * TMR32; i < M; ++i)
-      for (int c = 0; c < TNR; ++c)
-        C[i + (cc * TNR + c) * ldc] = chain_f32(0, 0, i, cc * TNR + c, K, A, lda, B, ldb);
+/* Tiled jmul! with a TR x TC tile chosen by the caller; returns -1 for a tile that is not
+ * instantiated (nothing is written then). */
+int or_jmul_tiled_rc_f64(int tr, int tc, i64 M, i64 N, i64 K, const double* A, i64 lda, const double* B, i64 ldb,
+                         double* C, i64 ldc, int nthreads) {
+#define OR_CASE(R, C_, FN) \
+  if (tr == (R) && tc == (C_)) { FN(M, N, K, A, lda, B, ldb, C, ldc, nthreads, chain_f64); return 0; }
+  OR_CASE(40, 5, tiled_f64_40x5) OR_CASE(12, 4, tiled_f64_12x4) OR_CASE(10, 5, tiled_f64_10x5)
+  OR_CASE(20, 5, tiled_f64_20x5) OR_CASE(16, 14, tiled_f64_16x14) OR_CASE(8, 6, tiled_f64_8x6)
+#undef OR_CASE
+  return -1;
+}
+
+int or_jmul_tiled_rc_f32(int tr, int tc, i64 M, i64 N, i64 K, const float* A, i64 lda, const float* B, i64 ldb,
+                         float* C, i64 ldc, int nthreads) {
+#define OR_CASE(R, C_, FN) \
+  if (tr == (R) && tc == (C_)) { FN(M, N, K, A, lda, B, ldb, C, ldc, nthreads, chain_f32); return 0; }
+  OR_CASE(80, 5, tiled_f32_80x5) OR_CASE(24, 4, tiled_f32_24x4) OR_CASE(20, 5, tiled_f32_20x5)
+  OR_CASE(40, 5, tiled_f32_40x5) OR_CASE(16, 14, tiled_f32_16x14)
+#undef OR_CASE
+  return -1;
+}
+
+/* Minimum time in ns of one single-threaded tiled jmul! call (M x N x K, f64, tile tr x tc),
+ * over `batches` batches of `reps` back-to-back calls on the same operands (the statistic
+ * BenchmarkTools reports as the minimum; test/runtests.jl:111-116).  -1 for a tile that is
+ * not instantiated. */
+double or_time_jmul_tiled_f64(int tr, int tc, i64 M, i64 N, i64 K, const double* A, const double* B, double* C,
+                              int reps, int batches) {
+  double best = -1.0;
+  for (int b = 0; b < batches; ++b) {
+    struct timespec t0, t1;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    for (int r = 0; r < reps; ++r)
+      if (or_jmul_tiled_rc_f64(tr, tc, M, N, K, A, M, B, K, C, M, 1)) return -1.0;
+    clock_gettime(CLOCK_MONOTONIC, &t1);
+    const double ns = ((double)(t1.tv_sec - t0.tv_sec) * 1e9 + (double)(t1.tv_nsec - t0.tv_nsec)) / reps;
+    if (best < 0 || ns < best) best = ns;
   }
-  for (i64 j = col_chunks * TNR; j < N; ++j)
-    for (i64 i = 0; i < M; ++i) C[i + j * ldc] = chain_f32(0, 0, i, j, K, A, lda, B, ldb);
-  (void)nthreads;
+  return best;
 }
 
 /* ------------------------------------------------------------ near-exact sampled dots */

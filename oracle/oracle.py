@@ -54,9 +54,15 @@ def lib():
                                   c_i64, _vp, c_i64, ctypes.c_double, _vp, c_i64, ctypes.c_int]
         L.or_gemm_f32.argtypes = [ctypes.c_int, ctypes.c_int, c_i64, c_i64, c_i64, ctypes.c_float, _vp,
                                   c_i64, _vp, c_i64, ctypes.c_float, _vp, c_i64, ctypes.c_int]
-        for nm in ("or_jmul_tiled_f64", "or_jmul_tiled_f32"):
-            getattr(L, nm).argtypes = [c_i64, c_i64, c_i64, _vp, c_i64, _vp, c_i64, _vp, c_i64,
-                                       ctypes.c_int]
+        for nm in ("or_jmul_tiled_rc_f64", "or_jmul_tiled_rc_f32"):
+            getattr(L, nm).argtypes = [ctypes.c_int, ctypes.c_int, c_i64, c_i64, c_i64, _vp, c_i64, _vp, c_i64,
+                                       _vp, c_i64, ctypes.c_int]
+            getattr(L, nm).restype = ctypes.c_int
+        L.or_pick_kernel_size.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _vp]
+        L.or_pick_kernel_size.restype = ctypes.c_int
+        L.or_time_jmul_tiled_f64.argtypes = [ctypes.c_int, ctypes.c_int, c_i64, c_i64, c_i64, _vp, _vp, _vp,
+                                             ctypes.c_int, ctypes.c_int]
+        L.or_time_jmul_tiled_f64.restype = ctypes.c_double
         L.or_dot2_entries.argtypes = [ctypes.c_int, ctypes.c_int, c_i64, _vp, c_i64, _vp, c_i64, c_i64,
                                       _vp, _vp, _vp, _vp, _vp, ctypes.c_int]
         L.or_quad_entries.argtypes = [ctypes.c_int, ctypes.c_int, c_i64, _vp, c_i64, _vp, c_i64, c_i64, _vp,
@@ -129,17 +135,83 @@ def kernel_chain(D, A, X, Mk, Pk, stride_AD, stride_X, N, init=False, dtype=np.f
     return D
 
 
-def jmul_tiled(A, B, nthreads=1, dtype=np.float64, out=None):
-    """The timed CPU baseline: jmul!'s register-tiled loop nest (same results as jmul)."""
+def pick_kernel_size(t_size, register_size, register_count):
+    """jBLAS's micro-tile choice (src/kernel_structure.jl:76-99) restated: (elements per
+    register, rows, cols) for elements of t_size bytes in register_count registers of
+    register_size bytes.  Rows grow one register of A at a time; the tile gets the columns
+    that the remaining registers hold beside one X broadcast register, (count - a - 1) // a;
+    the search stops at the first shape whose elements per loaded register (rows * cols /
+    (cols + a)) falls below the previous one's."""
+    epr = register_size // t_size
+    lines = -(-(epr * register_count) // epr)
+    best, rows, cols = -math.inf, 0, 0
+    for a in range(1, lines + 1):
+        r, c = a * epr, (register_count - a - 1) // a
+        ratio = (r * c) / (c + a)
+        if ratio < best:
+            break
+        best, rows, cols = ratio, r, c
+    return epr, rows, cols
+
+
+def host_register_file():
+    """(register bytes, register count) of this host's SIMD file, as the reference's build
+    script reads them (deps/build.jl:3-4: simdbytes(), 32 registers with AVX-512F else 16):
+    x86-64 AVX-512F 64 x 32, AVX2 32 x 16, SSE 16 x 16; AArch64 NEON (and 128-bit SVE) 16 x 32."""
+    import platform
+    if platform.machine() in ("x86_64", "AMD64"):
+        flags = set()
+        try:
+            with open("/proc/cpuinfo") as f:
+                for line in f:
+                    if line.startswith("flags"):
+                        flags = set(line.split())
+                        break
+        except OSError:
+            pass
+        if "avx512f" in flags:
+            return 64, 32
+        if "avx2" in flags:
+            return 32, 16
+        return 16, 16
+    return 16, 32
+
+
+def host_tile(dtype=np.float64):
+    """(rows, cols) of the register tile pick_kernel_size gives on this host."""
+    _, r, c = pick_kernel_size(np.dtype(dtype).itemsize, *host_register_file())
+    return r, c
+
+
+def jmul_tiled(A, B, nthreads=1, dtype=np.float64, out=None, tile=None):
+    """The timed CPU baseline: jmul!'s register-tiled loop nest (same results as jmul) with the
+    register tile pick_kernel_size gives for this host (or `tile` = (rows, cols))."""
     A, lda = _colmajor(A, dtype)
     B, ldb = _colmajor(B, dtype)
     M, K = A.shape
     N = B.shape[1]
     if out is None:
         out = np.empty((M, N), dtype=dtype, order="F")
-    fn = lib().or_jmul_tiled_f64 if dtype == np.float64 else lib().or_jmul_tiled_f32
-    fn(M, N, K, _ptr(A), lda, _ptr(B), ldb, _ptr(out), max(1, M), int(nthreads))
+    tr, tc = tile or host_tile(dtype)
+    fn = lib().or_jmul_tiled_rc_f64 if np.dtype(dtype) == np.float64 else lib().or_jmul_tiled_rc_f32
+    if fn(tr, tc, M, N, K, _ptr(A), lda, _ptr(B), ldb, _ptr(out), max(1, M), int(nthreads)) != 0:
+        raise ValueError("no %dx%d register tile for %s" % (tr, tc, np.dtype(dtype).name))
     return out
+
+
+def time_jmul_tiled(A, B, tile=None, reps=2000, batches=50):
+    """Minimum time (ns) of one single-threaded float64 jmul_tiled call on A (M x K) and B (K x N),
+    over `batches` batches of `reps` calls (BenchmarkTools' minimum, test/runtests.jl:111-116)."""
+    A, _ = _colmajor(A, np.float64)
+    B, _ = _colmajor(B, np.float64)
+    M, K = A.shape
+    N = B.shape[1]
+    C = np.empty((M, N), order="F")
+    tr, tc = tile or host_tile(np.float64)
+    ns = lib().or_time_jmul_tiled_f64(tr, tc, M, N, K, _ptr(A), _ptr(B), _ptr(C), int(reps), int(batches))
+    if ns < 0:
+        raise ValueError("no %dx%d float64 register tile" % (tr, tc))
+    return ns
 
 
 def chain_entries(A, B, rows, cols, C=None, alpha=1.0, beta=0.0, trans_a=False, trans_b=False,

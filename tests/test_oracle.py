@@ -31,17 +31,61 @@ def test_exact_chain_reproduces_a_fixture():
     np.testing.assert_array_equal(D, z["D"])
 
 
+TILES = {np.float64: [(40, 5), (12, 4), (10, 5), (20, 5), (16, 14), (8, 6)],
+         np.float32: [(80, 5), (24, 4), (20, 5), (40, 5), (16, 14)]}
+
+
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
 @pytest.mark.parametrize("shape", [(1, 1, 1), (7, 5, 3), (41, 17, 13), (64, 64, 64), (130, 70, 33)])
 @pytest.mark.parametrize("nthreads", [1, 4])
 def test_tiled_baseline_equals_chain(dtype, shape, nthreads):
+    """Every instantiated register tile (and the host's own) gives jmul!'s chain bit for bit."""
     M, K, N = shape
     g = np.random.default_rng(5)
     A = np.asfortranarray(g.uniform(-1, 1, (M, K)).astype(dtype))
     B = np.asfortranarray(g.uniform(-1, 1, (K, N)).astype(dtype))
     ref = oracle.gemm(A, B, dtype=dtype)
-    got = oracle.jmul_tiled(A, B, nthreads=nthreads, dtype=dtype)
-    np.testing.assert_array_equal(got, ref)
+    for tile in [None] + TILES[dtype]:
+        got = oracle.jmul_tiled(A, B, nthreads=nthreads, dtype=dtype, tile=tile)
+        np.testing.assert_array_equal(got, ref)
+
+
+# (t_size, register bytes, register count) -> (elements per register, rows, cols)
+PICK_KERNEL_SIZE = [
+    ((8, 64, 32), (8, 40, 5)),    # AVX-512, Float64
+    ((4, 64, 32), (16, 80, 5)),   # AVX-512, Float32
+    ((8, 32, 16), (4, 12, 4)),    # AVX2, Float64
+    ((4, 32, 16), (8, 24, 4)),    # AVX2, Float32
+    ((8, 16, 32), (2, 10, 5)),    # 128-bit NEON (32 registers), Float64
+    ((4, 16, 32), (4, 20, 5)),    # 128-bit NEON, Float32
+    ((8, 32, 32), (4, 20, 5)),    # 32 registers of 4 Float64 lanes
+]
+
+
+@pytest.mark.parametrize("args,expect", PICK_KERNEL_SIZE, ids=["avx512_f64", "avx512_f32", "avx2_f64",
+                                                              "avx2_f32", "neon_f64", "neon_f32", "32x4_f64"])
+def test_pick_kernel_size_restatement(args, expect):
+    """The greedy search of src/kernel_structure.jl:76-99, in Python and in the C oracle."""
+    assert oracle.pick_kernel_size(*args) == expect
+    import ctypes
+    r, c = ctypes.c_int(0), ctypes.c_int(0)
+    epr = oracle.lib().or_pick_kernel_size(*args, ctypes.byref(r), ctypes.byref(c))
+    assert (epr, r.value, c.value) == expect
+
+
+def test_host_tile_is_instantiated():
+    for dt in (np.float64, np.float32):
+        assert oracle.host_tile(dt) in TILES[dt]
+
+
+def test_time_jmul_tiled_reference_shape():
+    """The timing helper runs the reference's benchmark shape (D 16x14 = A 16x32 * X 32x14)."""
+    g = np.random.default_rng(8)
+    A = np.asfortranarray(g.standard_normal((16, 32)))
+    X = np.asfortranarray(g.standard_normal((32, 14)))
+    for tile in (None, (16, 14)):
+        ns = oracle.time_jmul_tiled(A, X, tile=tile, reps=100, batches=3)
+        assert 0 < ns < 1e7
 
 
 def test_chain_entries_equals_full_oracle():
