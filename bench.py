@@ -57,10 +57,11 @@ def parse_args():
     p.add_argument("--no-native", action="store_true", help="skip the native FP64 comparison")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU sample")
-    p.add_argument("--workload", choices=["ozaki", "ozaki_sweep", "native", "grouped", "adjoint", "semiring"],
+    p.add_argument("--workload", choices=["ozaki", "ozaki_sweep", "native", "f32_tc", "grouped", "adjoint",
+                                          "semiring"],
                    default="ozaki",
                    help="ozaki: the headline (default); ozaki_sweep: error and TFLOP/s by slice / moduli count; "
-                        "native: FP64/FP32 sweep; grouped: 4096 uneven problems; adjoint: fused dA/dB; "
+                        "native: FP64/FP32 sweep; f32_tc: FP32 on tensor cores; grouped: 4096 uneven problems; adjoint: fused dA/dB; "
                         "semiring: (min, +) and relatives")
     return p.parse_args()
 
@@ -592,6 +593,59 @@ def workload_ozaki_sweep(args):
     return 0
 
 
+def workload_f32_tc(args):
+    """FP32 GEMM at 8192^3 on N(0,1) inputs: the tensor-core term modes (BF16X3: 3 BF16 products,
+    BF16X6: 6) beside the bit-exact native FP32 mode; TFLOP/s (useful 2MNK flops), componentwise
+    error max |C - C_ref| / (|A||B|) on a 64 x 64 output grid against Dot2, and the MMA kernel's
+    BF16 tensor rate (products x 2MNK over its CUDA-event time) against the measured peak."""
+    import torch
+    import gbblas
+    import oracle
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev)
+    n = args.size
+    gen = torch.Generator(device=dev).manual_seed(8192)
+    A = torch.randn((n, n), generator=gen, dtype=torch.float32, device=dev).t()
+    B = torch.randn((n, n), generator=gen, dtype=torch.float32, device=dev).t()
+    C = torch.empty((n, n), dtype=torch.float32, device=dev).t()
+    g = np.random.default_rng(9)
+    r = np.sort(g.choice(n, 64, replace=False))
+    c = np.sort(g.choice(n, 64, replace=False))
+    rt, ct = torch.as_tensor(r, device=dev), torch.as_tensor(c, device=dev)
+    ii, jj = (x.ravel() for x in np.meshgrid(np.arange(64), np.arange(64), indexing="ij"))
+    hi, lo, ab = oracle.dot2_entries(np.asfortranarray(A[rt].double().cpu().numpy()),
+                                     np.asfortranarray(B[:, ct].double().cpu().numpy()), ii, jj)
+    peaks, src = load_peaks()
+    flops = 2.0 * n ** 3
+    rows = []
+    for mode, products in (("native", 0), ("bf16x3", 3), ("bf16x6", 6)):
+        steps = max(1, min(args.steps, 3)) if mode == "native" else args.steps
+        for _ in range(max(1, args.warmup if mode != "native" else 1)):
+            gbblas.gemm_(C, A, B, mode=mode)
+        torch.cuda.synchronize()
+        got = C[rt][:, ct].double().cpu().numpy()[ii, jj]
+        err = float(np.max(np.abs((got - hi) - lo) / ab))
+        with gbblas.profile() as prof:
+            ms = _event_ms(lambda: gbblas.gemm_(C, A, B, mode=mode), steps, stream)
+        row = {"mode": mode, "ms": ms, "tflops": flops / (ms * 1e-3) / 1e12, "componentwise_err": err,
+               "kernel_ms_per_step": {k: v / steps for k, v in prof.ms.items()}}
+        if products:
+            mma_ms = prof.ms.get("f32_mma", float("nan")) / max(1, prof.launches.get("f32_mma", 1))
+            tensor = products * 2.0 * n * n * (-(-n // 64) * 64)
+            row["roofline"] = {"bound": "tensor", "achieved": tensor / (mma_ms * 1e-3) / 1e12,
+                               "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
+                               "frac": tensor / (mma_ms * 1e-3) / 1e12 / peaks["bf16_tflops"],
+                               "peak_source": "%s bf16_tflops" % src, "kernel": "f32_mma", "ms_per_launch": mma_ms}
+        rows.append(row)
+    head = [x for x in rows if x["mode"] == "bf16x6"][0]
+    _side_line(args, "FP32 GEMM TFLOP/s on tensor cores (BF16 term products), 8192^3", head["tflops"], "TFLOP/s",
+               head["ms"], {"workload": "f32_gemm_%d^3" % n, "M": n, "N": n, "K": n, "inputs": "N(0,1)",
+                            "alpha": 1.0, "beta": 0.0},
+               {"dtype": "f32", "modes": rows, "roofline": head["roofline"],
+                "error_metric": "max |C - C_ref|_ij / (|A||B|)_ij on a 64 x 64 output grid against Dot2"})
+    return 0
+
+
 def workload_adjoint(args):
     """Adjoint: loss = sum(W .* (A*B)), A 4096x2048, B 2048x4096, W 4096x4096 N(0,1) float32:
     dA = W B^T and dB = A^T W in one launch (3xBF16 split, FP32 accumulation)."""
@@ -641,7 +695,8 @@ def main():
         if rank != 0:
             return 0
         return {"native": workload_native, "grouped": workload_grouped, "adjoint": workload_adjoint,
-                "semiring": workload_semiring, "ozaki_sweep": workload_ozaki_sweep}[args.workload](args)
+                "semiring": workload_semiring, "ozaki_sweep": workload_ozaki_sweep,
+                "f32_tc": workload_f32_tc}[args.workload](args)
 
     import torch
     import gbblas
@@ -734,54 +789,61 @@ def main():
     up_done = [torch.cuda.Event() for _ in range(NBUF)]
     comp_done = [torch.cuda.Event() for _ in range(NBUF)]
     down_done = [torch.cuda.Event() for _ in range(NBUF)]
-    comp_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-               for _ in range(args.steps)]
-    e0.record(stream)
-    up_stream.wait_stream(stream)
-    down_stream.wait_stream(stream)
 
-    up_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-             for _ in range(args.steps)]
-    down_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-               for _ in range(args.steps)]
+    def run_pipeline(steps):
+        """Enqueues `steps` pipelined steps; returns their (start, end) event pairs per stage
+        and the host time at which each step's compute was enqueued."""
+        up_ev, comp_ev, down_ev = ([(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                                    for _ in range(steps)] for _ in range(3))
+        up_stream.wait_stream(stream)
+        down_stream.wait_stream(stream)
 
-    def upload(i):
-        b = i % NBUF
-        with torch.cuda.stream(up_stream):
+        def upload(i):
+            b = i % NBUF
+            with torch.cuda.stream(up_stream):
+                if i >= NBUF:
+                    up_stream.wait_event(comp_done[b])       # buffer b's previous compute is done
+                up_ev[i][0].record(up_stream)
+                A_e[b].copy_(A_pin, non_blocking=True)
+                B_e[b].copy_(B_pin, non_blocking=True)
+                up_ev[i][1].record(up_stream)
+                up_done[b].record(up_stream)
+
+        host_t0 = time.perf_counter()
+        host_enqueue_ms = []
+        for i in range(min(NBUF - 1, steps)):
+            upload(i)
+        for i in range(steps):
+            b = i % NBUF
+            if i + NBUF - 1 < steps:
+                upload(i + NBUF - 1)
+            host_enqueue_ms.append((time.perf_counter() - host_t0) * 1e3)
+            stream.wait_event(up_done[b])
             if i >= NBUF:
-                up_stream.wait_event(comp_done[b])       # buffer b's previous compute is done
-            up_ev[i][0].record(up_stream)
-            A_e[b].copy_(A_pin, non_blocking=True)
-            B_e[b].copy_(B_pin, non_blocking=True)
-            up_ev[i][1].record(up_stream)
-            up_done[b].record(up_stream)
+                stream.wait_event(down_done[b])              # C_e[b] of step i - NBUF has been read
+            comp_ev[i][0].record(stream)
+            gbblas.gemm_(C_e[b].t(), A_e[b].t(), B_e[b].t(), mode=mode, slices=args.slices)
+            comp_ev[i][1].record(stream)
+            comp_done[b].record(stream)
+            with torch.cuda.stream(down_stream):
+                down_stream.wait_event(comp_done[b])
+                down_ev[i][0].record(down_stream)
+                C_pin.copy_(C_e[b], non_blocking=True)
+                down_ev[i][1].record(down_stream)
+                down_done[b].record(down_stream)
+        stream.wait_stream(up_stream)
+        stream.wait_stream(down_stream)
+        return up_ev, comp_ev, down_ev, host_enqueue_ms
 
+    # warm-up: the same pipeline, untimed (the ring buffers' first copies are slow: the first
+    # upload into a fresh device buffer measured 55 ms instead of 5 ms)
+    run_pipeline(max(args.warmup, NBUF))
+    torch.cuda.synchronize()
+    barrier()
     pipe_prof = gbblas.profile()
     pipe_prof.__enter__()
-    host_t0 = time.perf_counter()
-    host_enqueue_ms = []
-    for i in range(min(NBUF - 1, args.steps)):
-        upload(i)
-    for i in range(args.steps):
-        b = i % NBUF
-        if i + NBUF - 1 < args.steps:
-            upload(i + NBUF - 1)
-        host_enqueue_ms.append((time.perf_counter() - host_t0) * 1e3)
-        stream.wait_event(up_done[b])
-        if i >= NBUF:
-            stream.wait_event(down_done[b])              # C_e[b] of step i - NBUF has been read
-        comp_ev[i][0].record(stream)
-        gbblas.gemm_(C_e[b].t(), A_e[b].t(), B_e[b].t(), mode=mode, slices=args.slices)
-        comp_ev[i][1].record(stream)
-        comp_done[b].record(stream)
-        with torch.cuda.stream(down_stream):
-            down_stream.wait_event(comp_done[b])
-            down_ev[i][0].record(down_stream)
-            C_pin.copy_(C_e[b], non_blocking=True)
-            down_ev[i][1].record(down_stream)
-            down_done[b].record(down_stream)
-    stream.wait_stream(up_stream)
-    stream.wait_stream(down_stream)
+    e0.record(stream)
+    up_ev, comp_ev, down_ev, host_enqueue_ms = run_pipeline(args.steps)
     e1.record(stream)
     torch.cuda.synchronize()
     pipe_prof.__exit__(None, None, None)
@@ -920,7 +982,9 @@ def main():
             "kernel_ms_per_step": {k: v / args.steps for k, v in prof.ms.items()},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "TFLOP/s", "ms_per_step": ms_e2e,
-                    "pipeline": "4-deep ring: uploads run up to 3 steps ahead, the download of step i overlaps step i+1",
+                    "pipeline": "4-deep ring: uploads run up to 3 steps ahead, the download of step i overlaps step "
+                                "i+1; the timed steps start with an empty pipeline (the first upload and the last "
+                                "download are not overlapped), after an untimed warm-up pass of the same pipeline",
                     "h2d_GBps": h2d_gbs, "d2h_GBps": d2h_gbs,
                     "compute_ms_in_pipeline": comp_in_pipeline,
                     "upload_ms_in_pipeline": up_in_pipeline, "download_ms_in_pipeline": down_in_pipeline,

@@ -52,13 +52,15 @@ typedef enum {
   GB_ERR_NO_DEVICE = -6        /* no usable sm_103 device is current */
 } gb_status_t;
 
-/* Arithmetic mode of gb_gemm_f64. */
+/* Arithmetic mode of gb_gemm_f64 (NATIVE, OZAKI_*) and gb_gemm_f32_ex (NATIVE, BF16X*). */
 typedef enum {
   GB_MODE_NATIVE = 0,     /* FP64 FMA chain on the CUDA cores, jBLAS's per-element order */
   GB_MODE_OZAKI_BF16 = 1, /* FP64-accurate emulation: BF16 slices on tcgen05, exact FP32 sums */
   GB_MODE_OZAKI_INT8 = 2, /* INT8 slices: GB_ERR_UNSUPPORTED on sm_103a (no tcgen05 kind::i8) */
-  GB_MODE_OZAKI_CRT = 3   /* FP64-accurate emulation: exact integer product from BF16 residues
+  GB_MODE_OZAKI_CRT = 3,  /* FP64-accurate emulation: exact integer product from BF16 residues
                              modulo pairwise coprime moduli (Chinese remainder theorem) */
+  GB_MODE_BF16X3 = 4,     /* FP32 on tcgen05: two BF16 terms per value, three term products */
+  GB_MODE_BF16X6 = 5      /* FP32 on tcgen05: three BF16 terms per value, six term products */
 } gb_mode_t;
 
 GB_API const char* gb_status_string(int status);
@@ -109,6 +111,8 @@ typedef enum {
   GB_KERNEL_ADJOINT_MMA = 7,
   GB_KERNEL_OZAKI_COMBINE = 8,   /* CRT reconstruction of the residue products */
   GB_KERNEL_SEMIRING_GEMM = 9,
+  GB_KERNEL_F32_SPLIT = 10,      /* BF16 term planes of gb_gemm_f32_ex's tensor-core modes */
+  GB_KERNEL_F32_MMA = 11,        /* their term products on tcgen05 */
   GB_KERNEL_KINDS = 16
 } gb_kernel_kind_t;
 GB_API const char* gb_kernel_kind_name(int kind);
@@ -177,6 +181,20 @@ GB_API int gb_gemm_f64(int transA, int transB, int64_t M, int64_t N, int64_t K, 
 GB_API int gb_gemm_f32(int transA, int transB, int64_t M, int64_t N, int64_t K, float alpha,
                 const float* A, int64_t lda, const float* B, int64_t ldb, float beta,
                 float* C, int64_t ldc, void* stream);
+/* gb_gemm_f32 with an arithmetic mode (gb_gemm_f32 is mode GB_MODE_NATIVE: the jmul! FMA chain,
+ * bit for bit).  The tensor-core modes have no reference counterpart; they give up jmul!'s
+ * per-element order for tcgen05 throughput.  Every FP32 value is split into BF16 terms
+ * (t_0 = bf16(x), t_1 = bf16(x - t_0), t_2 = bf16(x - t_0 - t_1)) and the term products with
+ * p + q below the term count are accumulated in FP32 on the tensor cores:
+ *   GB_MODE_BF16X3  2 terms, 3 products; per element |C - C_exact| <= about
+ *                   (2^-15 + K 2^-24) |alpha| (|op(A)| |op(B)|)_ij  (+ beta C rounding)
+ *   GB_MODE_BF16X6  3 terms, 6 products; about (2^-21 + K 2^-24) |alpha| (|op(A)| |op(B)|)_ij,
+ *                   FP32-level accuracy
+ * Workspace (the term planes, (terms) x (M + N) x K BF16) comes from the library pool.  Other
+ * modes give GB_ERR_INVALID_VALUE.  Arguments, transposes, alpha/beta rules as gb_gemm_f32. */
+GB_API int gb_gemm_f32_ex(int transA, int transB, int64_t M, int64_t N, int64_t K, float alpha,
+                          const float* A, int64_t lda, const float* B, int64_t ldb, float beta,
+                          float* C, int64_t ldc, int mode, void* stream);
 
 /* ------------------------------------------------------------------ host buffers */
 /* The same products on HOST buffers, for callers whose matrices live in host memory as the

@@ -22,21 +22,28 @@
 
 namespace gb {
 
-__device__ __forceinline__ void split_hi_lo(float x, uint32_t& hi_bits, uint32_t& lo_bits) {
-  const __nv_bfloat16 hi = __float2bfloat16_rn(x);
-  const float r = x - __bfloat162float(hi);
-  const __nv_bfloat16 lo = __float2bfloat16_rn(r);
-  hi_bits = static_cast<uint32_t>(__bfloat16_as_ushort(hi));
-  lo_bits = static_cast<uint32_t>(__bfloat16_as_ushort(lo));
+// x = t_0 + t_1 (+ t_2) in BF16 terms: t_0 = bf16(x), t_1 = bf16(x - t_0), t_2 = bf16(x - t_0 - t_1).
+// Each difference is exact in FP32 (it keeps the lower bits of x), so with three terms the sum is
+// x exactly (24 = 3 x 8 significand bits, barring underflow); with two, |x - t_0 - t_1| <= 2^-17 |x|.
+template <int NT>
+__device__ __forceinline__ void split_terms(float x, uint32_t (&t)[NT]) {
+  float r = x;
+#pragma unroll
+  for (int i = 0; i < NT; ++i) {
+    const __nv_bfloat16 b = __float2bfloat16_rn(r);
+    t[i] = static_cast<uint32_t>(__bfloat16_as_ushort(b));
+    r -= __bfloat162float(b);
+  }
 }
 
 // k contiguous or strided (element (r, k) at X[r*rs + k*ks]): one thread = one row r and 16
-// consecutive k, neighbouring threads neighbouring k; writes planes[0] (hi) and planes[1] (lo),
-// [plane][r][pitch], 32 bytes per plane per thread.  With ks == 1 the 16 values are read as four
+// consecutive k, neighbouring threads neighbouring k; writes the NT term planes
+// [term][r][pitch], 32 bytes per plane per thread.  With ks == 1 the 16 values are read as four
 // 16-byte loads when aligned.
-__global__ void __launch_bounds__(256) split3_kc_kernel(const float* __restrict__ X, int64_t R, int64_t Kd,
-                                                        int64_t rs, int64_t ks, __nv_bfloat16* __restrict__ planes,
-                                                        int64_t pitch) {
+template <int NT>
+__global__ void __launch_bounds__(256) split_kc_kernel(const float* __restrict__ X, int64_t R, int64_t Kd,
+                                                       int64_t rs, int64_t ks, __nv_bfloat16* __restrict__ planes,
+                                                       int64_t pitch, int64_t plane) {
   const int64_t kc = static_cast<int64_t>(blockIdx.x) * 256 + threadIdx.x, r = blockIdx.y;
   const int64_t k0 = kc * 16;
   if (r >= R || k0 >= Kd) return;
@@ -56,47 +63,47 @@ __global__ void __launch_bounds__(256) split3_kc_kernel(const float* __restrict_
 #pragma unroll
     for (int j = 0; j < 16; ++j) x[j] = (j < nvalid) ? src[j * ks] : 0.0f;
   }
-  uint32_t hp[8], lp[8];
+  uint32_t packed[NT][8];
 #pragma unroll
   for (int j = 0; j < 16; j += 2) {
-    uint32_t h0, l0, h1, l1;
-    split_hi_lo(x[j], h0, l0);
-    split_hi_lo(x[j + 1], h1, l1);
-    hp[j / 2] = h0 | (h1 << 16);
-    lp[j / 2] = l0 | (l1 << 16);
+    uint32_t t0[NT], t1[NT];
+    split_terms<NT>(x[j], t0);
+    split_terms<NT>(x[j + 1], t1);
+#pragma unroll
+    for (int i = 0; i < NT; ++i) packed[i][j / 2] = t0[i] | (t1[i] << 16);
   }
-  const int64_t plane = R * pitch;
   __nv_bfloat16* dst = planes + r * pitch + k0;
   if (nvalid == 16) {
-    uint4* h4 = reinterpret_cast<uint4*>(dst);
-    uint4* l4 = reinterpret_cast<uint4*>(dst + plane);
-    h4[0] = make_uint4(hp[0], hp[1], hp[2], hp[3]);
-    h4[1] = make_uint4(hp[4], hp[5], hp[6], hp[7]);
-    l4[0] = make_uint4(lp[0], lp[1], lp[2], lp[3]);
-    l4[1] = make_uint4(lp[4], lp[5], lp[6], lp[7]);
-  } else {   // unrolled with a predicate: hp / lp stay in registers
+#pragma unroll
+    for (int i = 0; i < NT; ++i) {
+      uint4* d4 = reinterpret_cast<uint4*>(dst + i * plane);
+      d4[0] = make_uint4(packed[i][0], packed[i][1], packed[i][2], packed[i][3]);
+      d4[1] = make_uint4(packed[i][4], packed[i][5], packed[i][6], packed[i][7]);
+    }
+  } else {   // unrolled with a predicate: the packed terms stay in registers
     unsigned short* d2 = reinterpret_cast<unsigned short*>(dst);
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
       if (j < nvalid) {
-        d2[j] = static_cast<unsigned short>(hp[j / 2] >> (16 * (j & 1)));
-        d2[plane + j] = static_cast<unsigned short>(lp[j / 2] >> (16 * (j & 1)));
+#pragma unroll
+        for (int i = 0; i < NT; ++i)
+          d2[i * plane + j] = static_cast<unsigned short>(packed[i][j / 2] >> (16 * (j & 1)));
       }
     }
   }
 }
 
 // Rows contiguous (element (r, k) at X[r + k*ks]): a CTA converts a 64 x 64 tile through shared
-// memory.  Warp w loads columns 8w..8w+7 (lanes along r: 128-byte loads); the hi/lo values go to
-// [r][k] shared tiles; each warp then stores 8 rows x 128 B of both planes, and with DUAL also
+// memory.  Warp w loads columns 8w..8w+7 (lanes along r: 128-byte loads); the terms go to
+// [r][k] shared tiles; each warp then stores 8 rows x 128 B of every plane, and with DUAL also
 // 8 k-rows x 128 B of the transposed planes [k][r] — whole lines in both layouts.
-template <bool DUAL>
-__global__ void __launch_bounds__(256) split3_rc_tile_kernel(const float* __restrict__ X, int64_t R, int64_t Kd,
-                                                             int64_t ks, __nv_bfloat16* __restrict__ planes,
-                                                             int64_t pitch, __nv_bfloat16* __restrict__ planes_t,
-                                                             int64_t pitch_t) {
-  __shared__ float tile[64][65];                              // [k][r]
-  __shared__ __align__(16) unsigned short hs[64][72], ls[64][72];   // [r][k], 144-byte rows
+template <int NT, bool DUAL>
+__global__ void __launch_bounds__(256) split_rc_tile_kernel(const float* __restrict__ X, int64_t R, int64_t Kd,
+                                                            int64_t ks, __nv_bfloat16* __restrict__ planes,
+                                                            int64_t pitch, __nv_bfloat16* __restrict__ planes_t,
+                                                            int64_t pitch_t) {
+  __shared__ float tile[64][65];                                 // [k][r]
+  __shared__ __align__(16) unsigned short ts[NT][64][72];       // [term][r][k], 144-byte rows
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   const int64_t r0 = static_cast<int64_t>(blockIdx.x) * 64, k0 = static_cast<int64_t>(blockIdx.y) * 64;
 #pragma unroll
@@ -114,29 +121,25 @@ __global__ void __launch_bounds__(256) split3_rc_tile_kernel(const float* __rest
   const int rr = tid >> 2, kb = (tid & 3) * 16;   // this thread's row and 16-wide k chunk
 #pragma unroll
   for (int j = 0; j < 16; ++j) {
-    uint32_t hb, lb;
-    split_hi_lo(tile[kb + j][rr], hb, lb);
-    hs[rr][kb + j] = static_cast<unsigned short>(hb);
-    ls[rr][kb + j] = static_cast<unsigned short>(lb);
+    uint32_t t[NT];
+    split_terms<NT>(tile[kb + j][rr], t);
+#pragma unroll
+    for (int i = 0; i < NT; ++i) ts[i][rr][kb + j] = static_cast<unsigned short>(t[i]);
   }
   __syncthreads();
   {   // row-major planes [r][k]
     const int64_t r = r0 + rr, k = k0 + kb;
     if (r < R && k < Kd) {
       const int nvalid = static_cast<int>(Kd - k < 16 ? Kd - k : 16);
-      unsigned short* dh = reinterpret_cast<unsigned short*>(planes) + r * pitch + k;
-      unsigned short* dl = dh + R * pitch;
-      if (nvalid == 16) {
-        const uint4* sh = reinterpret_cast<const uint4*>(&hs[rr][kb]);
-        const uint4* sl = reinterpret_cast<const uint4*>(&ls[rr][kb]);
-        reinterpret_cast<uint4*>(dh)[0] = sh[0];
-        reinterpret_cast<uint4*>(dh)[1] = sh[1];
-        reinterpret_cast<uint4*>(dl)[0] = sl[0];
-        reinterpret_cast<uint4*>(dl)[1] = sl[1];
-      } else {
-        for (int j = 0; j < nvalid; ++j) {
-          dh[j] = hs[rr][kb + j];
-          dl[j] = ls[rr][kb + j];
+#pragma unroll
+      for (int i = 0; i < NT; ++i) {
+        unsigned short* d = reinterpret_cast<unsigned short*>(planes) + (i * R + r) * pitch + k;
+        if (nvalid == 16) {
+          const uint4* src = reinterpret_cast<const uint4*>(&ts[i][rr][kb]);
+          reinterpret_cast<uint4*>(d)[0] = src[0];
+          reinterpret_cast<uint4*>(d)[1] = src[1];
+        } else {
+          for (int j = 0; j < nvalid; ++j) d[j] = ts[i][rr][kb + j];
         }
       }
     }
@@ -146,49 +149,62 @@ __global__ void __launch_bounds__(256) split3_rc_tile_kernel(const float* __rest
     const int64_t k = k0 + kk, r = r0 + rb;
     if (k < Kd && r < R) {
       const int nvalid = static_cast<int>(R - r < 16 ? R - r : 16);
-      unsigned short* th = reinterpret_cast<unsigned short*>(planes_t) + k * pitch_t + r;
-      unsigned short* tl = th + Kd * pitch_t;
-      if (nvalid == 16) {
-        uint32_t ph[8], pl[8];
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          ph[i] = static_cast<uint32_t>(hs[rb + 2 * i][kk]) | (static_cast<uint32_t>(hs[rb + 2 * i + 1][kk]) << 16);
-          pl[i] = static_cast<uint32_t>(ls[rb + 2 * i][kk]) | (static_cast<uint32_t>(ls[rb + 2 * i + 1][kk]) << 16);
-        }
-        reinterpret_cast<uint4*>(th)[0] = make_uint4(ph[0], ph[1], ph[2], ph[3]);
-        reinterpret_cast<uint4*>(th)[1] = make_uint4(ph[4], ph[5], ph[6], ph[7]);
-        reinterpret_cast<uint4*>(tl)[0] = make_uint4(pl[0], pl[1], pl[2], pl[3]);
-        reinterpret_cast<uint4*>(tl)[1] = make_uint4(pl[4], pl[5], pl[6], pl[7]);
-      } else {
-        for (int i = 0; i < nvalid; ++i) {
-          th[i] = hs[rb + i][kk];
-          tl[i] = ls[rb + i][kk];
+      for (int i = 0; i < NT; ++i) {
+        unsigned short* d = reinterpret_cast<unsigned short*>(planes_t) + (i * Kd + k) * pitch_t + r;
+        if (nvalid == 16) {
+          uint32_t p[8];
+#pragma unroll
+          for (int q = 0; q < 8; ++q)
+            p[q] = static_cast<uint32_t>(ts[i][rb + 2 * q][kk]) | (static_cast<uint32_t>(ts[i][rb + 2 * q + 1][kk]) << 16);
+          reinterpret_cast<uint4*>(d)[0] = make_uint4(p[0], p[1], p[2], p[3]);
+          reinterpret_cast<uint4*>(d)[1] = make_uint4(p[4], p[5], p[6], p[7]);
+        } else {
+          for (int q = 0; q < nvalid; ++q) d[q] = ts[i][rb + q][kk];
         }
       }
     }
   }
 }
 
-static int split3(const float* X, int64_t R, int64_t Kd, int64_t rs, int64_t ks, __nv_bfloat16* planes,
-                  int64_t pitch, __nv_bfloat16* planes_t, int64_t pitch_t, cudaStream_t s) {
+// BF16 term planes of the R x Kd operand whose element (r, k) is X[r*rs + k*ks]: planes
+// [term][r][pitch] (and with planes_t, from the same read, [term][k][pitch_t]; rows contiguous
+// only).  nterms = 2 or 3.
+int split_bf16_terms(const float* X, int64_t R, int64_t Kd, int64_t rs, int64_t ks, int nterms,
+                     __nv_bfloat16* planes, int64_t pitch, __nv_bfloat16* planes_t, int64_t pitch_t, int kind,
+                     cudaStream_t s) {
   if (R <= 0 || Kd <= 0) return GB_OK;
-  const int64_t kchunks = (Kd + 15) / 16;
+  if (nterms != 2 && nterms != 3) return GB_ERR_INVALID_VALUE;
   if (rs == 1 || planes_t) {
     if (rs != 1) return GB_ERR_UNSUPPORTED;   // the transposed layout is written from row-contiguous X
     const int64_t ktiles = (Kd + 63) / 64;
-    if (ktiles > 65535) return GB_ERR_UNSUPPORTED;
+    if (ktiles > 65535 || (R + 63) / 64 > 0x7FFFFFFF) return GB_ERR_UNSUPPORTED;
     dim3 grid(static_cast<unsigned>((R + 63) / 64), static_cast<unsigned>(ktiles));
-    if (planes_t)
-      GB_LAUNCH(GB_KERNEL_ADJOINT_SPLIT, s,
-                (split3_rc_tile_kernel<true><<<grid, 256, 0, s>>>(X, R, Kd, ks, planes, pitch, planes_t, pitch_t)));
+    if (planes_t && nterms == 2)
+      GB_LAUNCH(kind, s, (split_rc_tile_kernel<2, true><<<grid, 256, 0, s>>>(X, R, Kd, ks, planes, pitch, planes_t,
+                                                                               pitch_t)));
+    else if (planes_t)
+      GB_LAUNCH(kind, s, (split_rc_tile_kernel<3, true><<<grid, 256, 0, s>>>(X, R, Kd, ks, planes, pitch, planes_t,
+                                                                               pitch_t)));
+    else if (nterms == 2)
+      GB_LAUNCH(kind, s, (split_rc_tile_kernel<2, false><<<grid, 256, 0, s>>>(X, R, Kd, ks, planes, pitch, nullptr,
+                                                                                0)));
     else
-      GB_LAUNCH(GB_KERNEL_ADJOINT_SPLIT, s,
-                (split3_rc_tile_kernel<false><<<grid, 256, 0, s>>>(X, R, Kd, ks, planes, pitch, nullptr, 0)));
+      GB_LAUNCH(kind, s, (split_rc_tile_kernel<3, false><<<grid, 256, 0, s>>>(X, R, Kd, ks, planes, pitch, nullptr,
+                                                                                0)));
   } else {
-    if (R > 65535) return GB_ERR_UNSUPPORTED;
-    dim3 grid(static_cast<unsigned>((kchunks + 255) / 256), static_cast<unsigned>(R));
-    GB_LAUNCH(GB_KERNEL_ADJOINT_SPLIT, s,
-              (split3_kc_kernel<<<grid, 256, 0, s>>>(X, R, Kd, rs, ks, planes, pitch)));
+    const int64_t kchunks = (Kd + 15) / 16;
+    const int64_t plane = R * pitch;
+    for (int64_t r0 = 0; r0 < R; r0 += 65535) {   // rows beyond the grid's y range: bands
+      const int64_t rb = (R - r0 < 65535) ? R - r0 : 65535;
+      dim3 grid(static_cast<unsigned>((kchunks + 255) / 256), static_cast<unsigned>(rb));
+      if (nterms == 2)
+        GB_LAUNCH(kind, s, (split_kc_kernel<2><<<grid, 256, 0, s>>>(X + r0 * rs, rb, Kd, rs, ks, planes + r0 * pitch,
+                                                                    pitch, plane)));
+      else
+        GB_LAUNCH(kind, s, (split_kc_kernel<3><<<grid, 256, 0, s>>>(X + r0 * rs, rb, Kd, rs, ks, planes + r0 * pitch,
+                                                                    pitch, plane)));
+    }
   }
   GB_CUDA_TRY(cudaGetLastError());
   return GB_OK;
@@ -232,11 +248,11 @@ int adjoint_f32(int64_t M, int64_t N, int64_t K, const float* A, int64_t lda, co
   __nv_bfloat16* P4 = reinterpret_cast<__nv_bfloat16*>(w);                      // dC [p][j][i]
 
   // dC (M x N, column-major): rows i contiguous -> [p][i][j] and, from the same read, [p][j][i]
-  int rc = split3(dC, M, N, 1, lddc, P1, pN, P4, pM, s);
+  int rc = split_bf16_terms(dC, M, N, 1, lddc, 2, P1, pN, P4, pM, GB_KERNEL_ADJOINT_SPLIT, s);
   // B (K x N): rows k contiguous -> [p][k][j]
-  if (!rc) rc = split3(B, K, N, 1, ldb, P2, pN, nullptr, 0, s);
+  if (!rc) rc = split_bf16_terms(B, K, N, 1, ldb, 2, P2, pN, nullptr, 0, GB_KERNEL_ADJOINT_SPLIT, s);
   // A^T rows k (contraction over i, contiguous in memory) -> [p][k][i]
-  if (!rc) rc = split3(A, K, M, lda, 1, P3, pM, nullptr, 0, s);
+  if (!rc) rc = split_bf16_terms(A, K, M, lda, 1, 2, P3, pM, nullptr, 0, GB_KERNEL_ADJOINT_SPLIT, s);
   if (rc) return rc;
 
   CUtensorMap ta0, tb0, ta1, tb1;

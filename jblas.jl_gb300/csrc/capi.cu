@@ -24,6 +24,10 @@
 #include "tc_gemm.cuh"
 
 namespace gb {
+size_t gemm_f32_tc_workspace_bytes(int64_t M, int64_t N, int64_t K, int nterms);
+int gemm_f32_tc(int ta, int tb, int64_t M, int64_t N, int64_t K, float alpha, const float* A, int64_t lda,
+                const float* B, int64_t ldb, float beta, float* C, int64_t ldc, int nterms, void* ws, int sms,
+                DeviceStatus* status, uint64_t wait_limit_ns, cudaStream_t s);
 size_t adjoint_workspace_bytes(int64_t M, int64_t N, int64_t K);
 int adjoint_f32(int64_t M, int64_t N, int64_t K, const float* A, int64_t lda, const float* B, int64_t ldb,
                 const float* dC, int64_t lddc, float* dA, int64_t ldda, float* dB, int64_t lddb, void* ws,
@@ -837,6 +841,29 @@ int gb_gemm_f32(int transA, int transB, int64_t M, int64_t N, int64_t K, float a
   if (rc) return rc;
   return native_gemm_f32(transA, transB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, dev->sms,
                          static_cast<cudaStream_t>(stream));
+}
+
+int gb_gemm_f32_ex(int transA, int transB, int64_t M, int64_t N, int64_t K, float alpha, const float* A,
+                   int64_t lda, const float* B, int64_t ldb, float beta, float* C, int64_t ldc, int mode,
+                   void* stream) {
+  if (mode != GB_MODE_NATIVE && mode != GB_MODE_BF16X3 && mode != GB_MODE_BF16X6) return GB_ERR_INVALID_VALUE;
+  DeviceInfo* dev = nullptr;
+  int rc = device_info(&dev);
+  if (rc) return rc;
+  rc = check_gemm_args(transA, transB, M, N, K, lda, ldb, ldc, A, B, C, alpha != 0.0f);
+  if (rc) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // no product to form (alpha = 0, K = 0): C = beta C exactly as the native mode does it
+  if (mode == GB_MODE_NATIVE || M == 0 || N == 0 || K == 0 || alpha == 0.0f)
+    return native_gemm_f32(transA, transB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, dev->sms, s);
+  if (tc_pair_tiles(M, N) > 0x7FFFFFFF / 2 || tc_tiles(M, N) > 0x7FFFFFFF / 2) return GB_ERR_UNSUPPORTED;
+  const int nterms = (mode == GB_MODE_BF16X3) ? 2 : 3;
+  void* ws = nullptr;
+  GB_CUDA_TRY(cudaMallocFromPoolAsync(&ws, gemm_f32_tc_workspace_bytes(M, N, K, nterms), dev->pool, s));
+  rc = gemm_f32_tc(transA, transB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, nterms, ws, dev->sms, dev->status,
+                   g_wait_limit_ns.load(), s);
+  cudaFreeAsync(ws, s);
+  return rc;
 }
 
 int gb_kernel_f64(double* pD, const double* pA, const double* pX, int64_t Mk, int64_t Pk, int64_t stride_AD,

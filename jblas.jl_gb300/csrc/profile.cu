@@ -70,7 +70,7 @@ const char* gb_kernel_kind_name(int kind) {
   static const char* names[GB_KERNEL_KINDS] = {
       "ozaki_stats", "ozaki_split", "ozaki_slice_mma", "native_gemm", "scale_c",
       "grouped_gemm", "adjoint_split", "adjoint_mma", "ozaki_combine", "semiring_gemm",
-      "reserved10", "reserved11", "reserved12", "reserved13", "reserved14", "reserved15"};
+      "f32_split", "f32_mma", "reserved12", "reserved13", "reserved14", "reserved15"};
   if (kind < 0 || kind >= GB_KERNEL_KINDS) return "unknown";
   return names[kind];
 }

@@ -21,6 +21,8 @@ MODE_NATIVE = 0
 MODE_OZAKI_BF16 = 1
 MODE_OZAKI_INT8 = 2
 MODE_OZAKI_CRT = 3
+MODE_BF16X3 = 4
+MODE_BF16X6 = 5
 
 SEMIRINGS = {"min_plus": 0, "max_plus": 1, "max_min": 2, "min_max": 3, "max_times": 4}
 
@@ -79,6 +81,8 @@ SIGNATURES = {
                             c_double, c_vp, c_i64, c_int, c_int, ctypes.POINTER(c_double), c_vp]),
     "gb_gemm_f32": (c_int, [c_int, c_int, c_i64, c_i64, c_i64, c_float, c_vp, c_i64, c_vp, c_i64,
                             c_float, c_vp, c_i64, c_vp]),
+    "gb_gemm_f32_ex": (c_int, [c_int, c_int, c_i64, c_i64, c_i64, c_float, c_vp, c_i64, c_vp, c_i64,
+                               c_float, c_vp, c_i64, c_int, c_vp]),
     "gb_plan_ozaki": (c_int, [c_i64, c_i64, c_i64, c_int, ctypes.POINTER(OzakiPlan)]),
     "gb_plan_ozaki_crt": (c_int, [c_i64, c_i64, c_i64, c_int, ctypes.POINTER(OzakiPlan)]),
     "gb_gemm_adjoint_f32": (c_int, [c_i64, c_i64, c_i64, c_vp, c_i64, c_vp, c_i64, c_vp, c_i64, c_vp, c_i64,

@@ -69,23 +69,30 @@ def gemm_raw(transA, transB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, *, dt
                            int(slices), ctypes.byref(bound) if want_bound else None, st)
         check(rc, "gb_gemm_f64")
         return bound.value if want_bound else None
-    if mode != _lib.MODE_NATIVE:
-        raise ValueError("Ozaki modes emulate float64; float32 runs natively")
-    rc = L.gb_gemm_f32(int(transA), int(transB), M, N, K, float(alpha), ctypes.c_void_p(A), lda,
-                       ctypes.c_void_p(B), ldb, float(beta), ctypes.c_void_p(C), ldc, st)
-    check(rc, "gb_gemm_f32")
+    if mode in (_lib.MODE_OZAKI_BF16, _lib.MODE_OZAKI_INT8, _lib.MODE_OZAKI_CRT):
+        raise ValueError("Ozaki modes emulate float64; float32 runs natively or in a BF16 term mode")
+    if mode == _lib.MODE_NATIVE:
+        rc = L.gb_gemm_f32(int(transA), int(transB), M, N, K, float(alpha), ctypes.c_void_p(A), lda,
+                           ctypes.c_void_p(B), ldb, float(beta), ctypes.c_void_p(C), ldc, st)
+        check(rc, "gb_gemm_f32")
+    else:
+        rc = L.gb_gemm_f32_ex(int(transA), int(transB), M, N, K, float(alpha), ctypes.c_void_p(A), lda,
+                              ctypes.c_void_p(B), ldb, float(beta), ctypes.c_void_p(C), ldc, int(mode), st)
+        check(rc, "gb_gemm_f32_ex")
     return None
 
 
 _MODES = {"native": _lib.MODE_NATIVE, "ozaki": _lib.MODE_OZAKI_BF16,
           "ozaki_bf16": _lib.MODE_OZAKI_BF16, "ozaki_int8": _lib.MODE_OZAKI_INT8,
-          "ozaki_crt": _lib.MODE_OZAKI_CRT}
+          "ozaki_crt": _lib.MODE_OZAKI_CRT, "bf16x3": _lib.MODE_BF16X3, "bf16x6": _lib.MODE_BF16X6}
 
 
 def gemm_(C, A, B, alpha=1.0, beta=0.0, *, mode="native", slices=0, return_bound=False):
     """C = alpha * A @ B + beta * C in place; A (M x K), B (K x N), C (M x N).
 
-    mode "native": the jmul! FMA chain (bit-identical to the oracle); "ozaki": FP64
+    mode "native": the jmul! FMA chain (bit-identical to the oracle); "bf16x3" / "bf16x6"
+    (float32 only): BF16 term products on the tensor cores (2 terms, 3 products / 3 terms, 6
+    products; componentwise error about (2^-15 / 2^-21 + K 2^-24) |A||B|); "ozaki": FP64
     emulation on BF16 tensor cores by digit slices (float64 only; slices = 0 picks the
     count for the library tolerance); "ozaki_crt": FP64 emulation by residue products
     and the Chinese remainder theorem (slices = number of moduli, 0 = automatic).  With return_bound the a-priori normwise error bound is
