@@ -383,13 +383,16 @@ def workload_native(args):
                          "tflops": 2.0 * M * N * K / (ms * 1e-3) / 1e12, **err})
             del A, B, C
     f64 = [r for r in rows if r["dtype"] == "float64" and r["M"] == r["N"] == r["K"] == 8192][0]
+    pk = gbblas.measure_fma_peaks()
+    for r in rows:
+        r["frac_of_measured_pipe"] = r["tflops"] / pk["fp64_tflops" if r["dtype"] == "float64" else "fp32_tflops"]
     _side_line(args, "native FP64 GEMM TFLOP/s (CUDA cores, jmul! FMA order)", f64["tflops"], "TFLOP/s",
                f64["ms"], {"workload": "native_gemm_sweep", "alpha": 1.5, "beta": 0.5,
                            "headline_shape": "f64 8192^3"},
-               {"dtype": "f64", "sweep": rows,
-                "roofline": {"bound": "fp64_pipe", "achieved": f64["tflops"], "peak": 1.25, "unit": "TFLOP/s",
-                             "frac": f64["tflops"] / 1.25, "peak_source": "nominal GB300 FP64 (not in the measured "
-                                                                           "peaks file)"}})
+               {"dtype": "f64", "sweep": rows, "fma_peaks": pk,
+                "roofline": {"bound": "fp64_pipe", "achieved": f64["tflops"], "peak": pk["fp64_tflops"],
+                             "unit": "TFLOP/s", "frac": f64["tflops"] / pk["fp64_tflops"],
+                             "peak_source": "measured DFMA register loop (gb_measure_fma_peaks)"}})
     return 0
 
 
@@ -520,12 +523,15 @@ def workload_grouped(args):
         del g2
         del As, Bs, Cs, plan, graph
     f64 = out["float64"]
+    pk = gbblas.measure_fma_peaks()
+    out["float32"]["frac_of_measured_fp32_pipe"] = out["float32"]["graph_tflops"] / pk["fp32_tflops"]
     _side_line(args, "grouped FP64 GEMM TFLOP/s, 4096 uneven problems, one persistent launch in a CUDA graph",
                f64["graph_tflops"], "TFLOP/s", f64["graph_ms"],
                {"workload": "grouped_4096_loguniform_8_512", "count": 4096, "alpha": 1.0, "beta": 0.0},
-               {"dtype": "f64", "results": out,
-                "roofline": {"bound": "fp64_pipe", "achieved": f64["graph_tflops"], "peak": 1.25, "unit": "TFLOP/s",
-                             "frac": f64["graph_tflops"] / 1.25, "peak_source": "nominal GB300 FP64"},
+               {"dtype": "f64", "results": out, "fma_peaks": pk,
+                "roofline": {"bound": "fp64_pipe", "achieved": f64["graph_tflops"], "peak": pk["fp64_tflops"],
+                             "unit": "TFLOP/s", "frac": f64["graph_tflops"] / pk["fp64_tflops"],
+                             "peak_source": "measured DFMA register loop (gb_measure_fma_peaks)"},
             "gpu_launches": 2 * args.steps})
     return 0
 
@@ -839,17 +845,31 @@ def main():
     # upload into a fresh device buffer measured 55 ms instead of 5 ms)
     run_pipeline(max(args.warmup, NBUF))
     torch.cuda.synchronize()
-    barrier()
-    pipe_prof = gbblas.profile()
-    pipe_prof.__enter__()
-    e0.record(stream)
-    up_ev, comp_ev, down_ev, host_enqueue_ms = run_pipeline(args.steps)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    pipe_prof.__exit__(None, None, None)
-    barrier()
-    ms_e2e = max_over_ranks(e0.elapsed_time(e1) / args.steps)
+    # Three timed windows of `steps` steps each; the window with the median time is reported, all
+    # three beside it.  The host link is shared with the node's other GPUs: single copies were
+    # seen to take 20-95 ms instead of 3-5 ms when other traffic ran, which one window of 20
+    # steps cannot absorb and a median of windows does not hide (all windows are in the line).
+    windows = []
+    for _ in range(3):
+        barrier()
+        pipe_prof = gbblas.profile()
+        pipe_prof.__enter__()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        up_ev, comp_ev, down_ev, host_enqueue_ms = run_pipeline(args.steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        pipe_prof.__exit__(None, None, None)
+        barrier()
+        windows.append({"ms": max_over_ranks(e0.elapsed_time(e1) / args.steps), "prof": pipe_prof,
+                        "ev": (e0, up_ev, comp_ev, down_ev, host_enqueue_ms)})
+    order = sorted(range(3), key=lambda w: windows[w]["ms"])
+    med = windows[order[1]]
+    ms_e2e = med["ms"]
+    pipe_prof = med["prof"]
+    e0, up_ev, comp_ev, down_ev, host_enqueue_ms = med["ev"]
     e2e_value = world * flops / (ms_e2e * 1e-3) / 1e12
+    e2e_windows = [world * flops / (w["ms"] * 1e-3) / 1e12 for w in windows]
     comp_in_pipeline = statistics.median(a.elapsed_time(z) for a, z in comp_ev)
     up_in_pipeline = statistics.median(a.elapsed_time(z) for a, z in up_ev)
     down_in_pipeline = statistics.median(a.elapsed_time(z) for a, z in down_ev)
@@ -943,7 +963,10 @@ def main():
             C_nat = np.asfortranarray(Cn.cpu().numpy())
             err_nat = normwise_err(C_nat, A_h, B_h, rows, cols, hi, lo)
             cerr_nat = componentwise_err(C_nat, rows, cols, hi, lo, ab)
+            pk = gbblas.measure_fma_peaks()
             native = {"tflops": flops / (nat_ms * 1e-3) / 1e12, "ms": nat_ms, "normwise_err": err_nat,
+                      "fp64_pipe_tflops_measured": pk["fp64_tflops"],
+                      "frac_of_measured_fp64": flops / (nat_ms * 1e-3) / 1e12 / pk["fp64_tflops"],
                       "componentwise_err": cerr_nat,
                       "ozaki_speedup": (flops / (ms_step * 1e-3) / 1e12) / (flops / (nat_ms * 1e-3) / 1e12)}
         cpu = None
@@ -989,7 +1012,8 @@ def main():
                     "compute_ms_in_pipeline": comp_in_pipeline,
                     "upload_ms_in_pipeline": up_in_pipeline, "download_ms_in_pipeline": down_in_pipeline,
                     "kernel_ms_in_pipeline": {k: v / args.steps for k, v in pipe_prof.ms.items()},
-                    "timeline": timeline,
+                    "timeline": timeline, "windows_tflops": e2e_windows,
+                    "windows": "median of 3 timed windows of `steps` steps (all three listed)",
                     "h2d_bytes_per_step": int(A_pin.numel() * 8 + B_pin.numel() * 8),
                     "d2h_bytes_per_step": int(C_pin.numel() * 8)},
             "host_api": host_api,

@@ -87,6 +87,12 @@ GB_API int gb_set_tc_engine(int engine);
  * slices = 0 ignores it and chooses slices and chunking together. */
 GB_API int gb_set_ozaki_min_chunks(int min_chunks);
 
+/* Measured FMA-pipe peaks of the current device in TFLOP/s (either pointer may be NULL): a
+ * register-only loop of independent FMA chains on every SM, FP64 (DFMA) and FP32 (FFMA), timed
+ * with CUDA events.  The CUDA-core counterpart of jBLAS's machine constants (deps/build.jl:26-34);
+ * it takes a few milliseconds and synchronises the device. */
+GB_API int gb_measure_fma_peaks(double* fp64_tflops, double* fp32_tflops);
+
 /* Returns the current device's cached workspace memory to the CUDA driver (synchronises the
  * device).  Workspace is otherwise kept between calls. */
 GB_API int gb_release_workspace(void);

@@ -24,6 +24,7 @@
 #include "tc_gemm.cuh"
 
 namespace gb {
+int measure_fma_peaks(int sms, double* fp64_tflops, double* fp32_tflops);
 size_t gemm_f32_tc_workspace_bytes(int64_t M, int64_t N, int64_t K, int nterms);
 int gemm_f32_tc(int ta, int tb, int64_t M, int64_t N, int64_t K, float alpha, const float* A, int64_t lda,
                 const float* B, int64_t ldb, float beta, float* C, int64_t ldc, int nterms, void* ws, int sms,
@@ -750,6 +751,13 @@ int gb_set_ozaki_tolerance(double tol) {
   if (tol > 0.0) std::memcpy(&b, &tol, sizeof(b));
   g_ozaki_tol_bits.store(b);
   return GB_OK;
+}
+
+int gb_measure_fma_peaks(double* fp64_tflops, double* fp32_tflops) {
+  DeviceInfo* dev = nullptr;
+  int rc = device_info(&dev);
+  if (rc) return rc;
+  return measure_fma_peaks(dev->sms, fp64_tflops, fp32_tflops);
 }
 
 int gb_release_workspace(void) {

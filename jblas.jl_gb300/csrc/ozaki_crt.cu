@@ -648,53 +648,42 @@ __global__ void __launch_bounds__(256) crt_split_kc_kernel(const double* __restr
   for (int g = 0; g < nmod; ++g) store_residues(out0 + g * plane_stride, crt_residues8(d, mod, g), nvalid);
 }
 
-// Rows contiguous: a CTA converts a 32-row x 64-k tile.  Warp w loads columns 8w..8w+7 of the
-// tile (lane = row: 256 contiguous bytes per load) into shared memory and computes the
-// residues of row `lane`, k 8w..8w+7; per modulus the residues pass through a padded shared
-// tile (double buffered) so that each warp stores 4 rows x 128 B, whole lines of the plane.
-// Bank spread: 16-byte accesses at word 36 row + 4 chunk touch each bank 4 times per warp
-// (the minimum for 512 B).
+// Rows contiguous (element (r, k) at X[r + k ks]): warp w of a CTA owns rows 4w..4w+3 of a
+// 32-row x 64-k tile; lane l takes row 4w + l / 8 and the 8 consecutive k of chunk l % 8.  Each
+// of its 8 loads is one 8-byte element, and a warp's load instruction reads 8 whole 32-byte
+// sectors (4 rows of one column, 8 columns); per modulus a warp stores 4 rows x 128 bytes of
+// the plane, whole lines.  No shared memory and no barriers: the residue work of one modulus
+// overlaps the stores of the previous one.
 __global__ void __launch_bounds__(256) crt_split_rc_kernel(const double* __restrict__ X, int64_t R, int64_t K,
                                                            int64_t ks, const unsigned long long* __restrict__ amax_bits,
                                                            __nv_bfloat16* __restrict__ planes, int64_t pitch,
                                                            int32_t* __restrict__ exps,
                                                            const __grid_constant__ CrtModuli mod,
                                                            const CrtDevicePlan* __restrict__ plan) {
-  __shared__ double tile[64][33];
-  __shared__ __align__(16) uint32_t otile[2][32][36];   // 32 rows x (64 BF16 = 32 words, + 4 words pad)
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int64_t r0 = static_cast<int64_t>(blockIdx.x) * 32, kb = static_cast<int64_t>(blockIdx.y) * 64;
-  const int64_t r = r0 + lane;
-#pragma unroll
-  for (int c = 0; c < 8; ++c) {
-    const int64_t k = kb + w * 8 + c;
-    tile[w * 8 + c][lane] = (r < R && k < K) ? X[r + k * ks] : 0.0;
-  }
-  __syncthreads();
+  const int64_t r = static_cast<int64_t>(blockIdx.x) * 32 + 4 * w + (lane >> 3);
+  const int64_t k0 = static_cast<int64_t>(blockIdx.y) * 64 + 8 * (lane & 7);
+  if (r >= R || k0 >= K) return;
   const int nmod = plan->n, tbits = plan->t;
-  const int e = r < R ? row_exponent(amax_bits[r]) : 0;
-  if (r < R && kb == 0 && w == 0) exps[r] = e;
+  const int e = row_exponent(amax_bits[r]);
+  if (k0 == 0) exps[r] = e;
   const bool nonfinite = (e == OZ_EXP_NONFINITE);
+  const int nvalid = static_cast<int>(K - k0 < 8 ? K - k0 : 8);
+  const double* src = X + r + k0 * ks;
+  double x[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) x[j] = (j < nvalid) ? src[j * ks] : 0.0;
   float d[5][8];
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
     float dj[5];
-    crt_digits(tile[w * 8 + j][lane], e, tbits, nonfinite, dj);
+    crt_digits(x[j], e, tbits, nonfinite, dj);
 #pragma unroll
     for (int l = 0; l < 5; ++l) d[l][j] = dj[l];
   }
-  // store mapping: warp w owns tile rows 4w..4w+3; lane -> row 4w + lane / 8, 16-byte chunk lane % 8
-  const int orow = 4 * w + (lane >> 3), ochunk = lane & 7;
-  const int64_t gr = r0 + orow, gk = kb + ochunk * 8;
-  const int nvalid = gr < R && gk < K ? static_cast<int>(K - gk < 8 ? K - gk : 8) : 0;
-  __nv_bfloat16* gout = planes + gr * pitch + gk;
+  __nv_bfloat16* out0 = planes + r * pitch + k0;
   const int64_t plane_stride = R * pitch;
-  for (int g = 0; g < nmod; ++g) {
-    *reinterpret_cast<uint4*>(&otile[g & 1][lane][w * 4]) = crt_residues8(d, mod, g);
-    __syncthreads();   // buffer g & 1 is rewritten two moduli later, after the next barrier
-    const uint4 v = *reinterpret_cast<const uint4*>(&otile[g & 1][orow][ochunk * 4]);
-    if (nvalid > 0) store_residues(gout + g * plane_stride, v, nvalid);
-  }
+  for (int g = 0; g < nmod; ++g) store_residues(out0 + g * plane_stride, crt_residues8(d, mod, g), nvalid);
 }
 
 int crt_split(const double* X, int64_t R, int64_t K, int64_t rs, int64_t ks, const unsigned long long* amax_bits,

@@ -81,6 +81,7 @@ SIGNATURES = {
                             c_double, c_vp, c_i64, c_int, c_int, ctypes.POINTER(c_double), c_vp]),
     "gb_gemm_f32": (c_int, [c_int, c_int, c_i64, c_i64, c_i64, c_float, c_vp, c_i64, c_vp, c_i64,
                             c_float, c_vp, c_i64, c_vp]),
+    "gb_measure_fma_peaks": (c_int, [ctypes.POINTER(c_double), ctypes.POINTER(c_double)]),
     "gb_gemm_f32_ex": (c_int, [c_int, c_int, c_i64, c_i64, c_i64, c_float, c_vp, c_i64, c_vp, c_i64,
                                c_float, c_vp, c_i64, c_int, c_vp]),
     "gb_plan_ozaki": (c_int, [c_i64, c_i64, c_i64, c_int, ctypes.POINTER(OzakiPlan)]),

@@ -359,6 +359,14 @@ def set_ozaki_min_chunks(n):
     check(_lib.lib().gb_set_ozaki_min_chunks(int(n)), "gb_set_ozaki_min_chunks")
 
 
+def measure_fma_peaks():
+    """{"fp64_tflops", "fp32_tflops"}: the current GPU's FMA-pipe peaks, measured by a
+    register-only loop (gb_measure_fma_peaks; synchronises the device)."""
+    d64, d32 = ctypes.c_double(0.0), ctypes.c_double(0.0)
+    check(_lib.lib().gb_measure_fma_peaks(ctypes.byref(d64), ctypes.byref(d32)), "gb_measure_fma_peaks")
+    return {"fp64_tflops": d64.value, "fp32_tflops": d32.value}
+
+
 def set_tc_engine(engine):
     """Tensor-core engine: 0 automatic, 1 single-CTA 128x256 tiles, 2 CTA pairs (256x256)."""
     check(_lib.lib().gb_set_tc_engine(int(engine)), "gb_set_tc_engine")

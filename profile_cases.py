@@ -1,6 +1,6 @@
 """Small single-kernel cases for profiling each gbblas kernel family under ncu.
 
-    python -m gbblas.profile_cases <case>        (run from jblas.jl_gb300/, or with it on sys.path)
+    python profile_cases.py <case>        (from the repository root, after building the library)
 
 Each case runs one warm-up call and one measured call of the library on seeded inputs
 sized for a quick capture (inputs larger than L2 where the kernel streams memory, a few GB
@@ -16,13 +16,17 @@ cases:
   grouped_f32    the same problems in FP32 (tuned configuration of the bench)
   adjoint        gb_gemm_adjoint_f32, A 4096 x 2048, B 2048 x 4096
   semiring_f32   gb_gemm_semiring_f32 (min, +), 4096^3
+  f32_bf16x3     gb_gemm_f32_ex BF16X3 (term split, 3 term products), 4096^3
+  f32_bf16x6     gb_gemm_f32_ex BF16X6 (term split, 6 term products), 4096^3
 """
+import os
 import sys
 
 import numpy as np
 import torch
 
-from . import api, grouped, workloads
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "jblas.jl_gb300"))
+from gbblas import api, grouped, workloads  # noqa: E402
 
 
 def _dev_cm(x):
@@ -40,11 +44,11 @@ def _timed(fn):
     return e0.elapsed_time(e1)
 
 
-def case_native(dtype, n):
+def case_native(dtype, n, mode="native"):
     A = (torch.rand((n, n), dtype=dtype, device="cuda") * 2 - 1).t()
     B = (torch.rand((n, n), dtype=dtype, device="cuda") * 2 - 1).t()
     C = torch.empty((n, n), dtype=dtype, device="cuda").t()
-    return _timed(lambda: api.gemm_(C, A, B))
+    return _timed(lambda: api.gemm_(C, A, B, mode=mode))
 
 
 def case_ozaki():
@@ -102,6 +106,8 @@ CASES = {
     "grouped_f32": lambda: case_grouped(torch.float32, [0, 0, 1, 1, 3, 5]),
     "adjoint": case_adjoint,
     "semiring_f32": case_semiring,
+    "f32_bf16x3": lambda: case_native(torch.float32, 4096, "bf16x3"),
+    "f32_bf16x6": lambda: case_native(torch.float32, 4096, "bf16x6"),
 }
 
 
