@@ -75,11 +75,49 @@ GB_API int gb_set_wait_limit_ns(uint64_t ns);
  * the default 2^-50. */
 GB_API int gb_set_ozaki_tolerance(double tol);
 
-/* Tensor-core engine for the Ozaki slice-mode and adjoint products: 0 = automatic (CTA
- * pairs), 1 = one CTA per 128 x 256 tile, 2 = CTA pairs on 256 x 256 tiles (tcgen05
- * cta_group::2, half of B per SM).  Ozaki results are identical under both engines.  The
- * CRT mode always runs on CTA pairs. */
+/* Engine override for the tensor-core products (slices, FP32 term modes, adjoint): 0 = the
+ * engine of the tuning table (gb_set_tc_tuning; CTA pairs by default), 1 = one CTA per
+ * 128 x 256 tile, 2 = CTA pairs on 256 x 256 tiles (tcgen05 cta_group::2, half of B per SM).
+ * Ozaki results are identical under both engines.  The CRT mode always runs on CTA pairs. */
 GB_API int gb_set_tc_engine(int engine);
+
+/* ------------------------------------------------------------------ tensor-core tuning */
+/* Launch configuration of the tensor-core engine per kind of product and output-size class:
+ * the GPU counterpart of jBLAS's micro-tile choice and block options (pick_kernel_size,
+ * src/kernel_structure.jl:76-99; BLASOptions, src/blas_options.jl:2-7), chosen by measurement
+ * (gb_autotune_tc) instead of a register-count formula.
+ *   engine     1 = one CTA per 128 x 256 output tile (tcgen05 cta_group::1),
+ *              2 = a CTA pair per 256 x 256 tile (cta_group::2, each SM loads half of B);
+ *              the CRT mode runs on pairs only
+ *   band       output-tile rows per band of the tile raster (1..64; tiles of a band share their
+ *              A rows in L2)
+ *   tma_store  FP32 outputs (GB_TC_F32, GB_TC_ADJOINT) on the pair engine: 1 = C staged in
+ *              shared memory and written by TMA stores (beta = 0), 0 = direct stores
+ * Size classes by max(M, N): 0 up to 2048, 1 up to 8192, 2 beyond.  gb_set_tc_engine, when set,
+ * overrides the engine of every kind. */
+typedef enum { GB_TC_OZAKI_SLICES = 0, GB_TC_OZAKI_CRT = 1, GB_TC_F32 = 2, GB_TC_ADJOINT = 3, GB_TC_KINDS = 4 } gb_tc_kind_t;
+#define GB_TC_SIZE_CLASSES 3
+typedef struct {
+  int32_t engine;
+  int32_t band;
+  int32_t tma_store;
+  int32_t reserved;   /* 0 */
+} gb_tc_tuning_t;
+GB_API int gb_tc_size_class(int64_t M, int64_t N);
+GB_API int gb_tc_default_tuning(int kind, gb_tc_tuning_t* out);
+GB_API int gb_get_tc_tuning(int kind, int size_class, gb_tc_tuning_t* out);
+/* Installs a tuning (NULL = the default) for later calls of that kind and class; an invalid
+ * combination gives GB_ERR_INVALID_VALUE. */
+GB_API int gb_set_tc_tuning(int kind, int size_class, const gb_tc_tuning_t* tuning);
+/* Times every candidate (engines, bands 2..32 pair tiles / 4..64 single tiles, TMA stores where
+ * they apply) on seeded synthetic M x N x K operands of the kind (slices: 8 digit slices; CRT:
+ * 15 moduli; FP32: BF16X3) with `reps` timed calls after a warm-up, and returns the fastest in
+ * `out` (best_ms: its time per call; may be NULL).  The installed tuning is left as it was; the
+ * caller installs the result with gb_set_tc_tuning.  Allocates its operands, synchronises
+ * `stream`, and changes the engine override and the class's tuning while it runs: make no other
+ * tensor-core calls meanwhile. */
+GB_API int gb_autotune_tc(int kind, int64_t M, int64_t N, int64_t K, int reps, gb_tc_tuning_t* out, float* best_ms,
+                          void* stream);
 
 /* K chunking used by OZAKI calls with an explicit slice count: K is cut into at least
  * `min_chunks` exact accumulation chunks (shorter chunks allow wider digits, at the cost

@@ -262,10 +262,13 @@ int adjoint_f32(int64_t M, int64_t N, int64_t K, const float* A, int64_t lda, co
   if (!rc) rc = make_plane_tmap(&tb1, P4, M, N, 2, pM, TC_BN);
   if (rc) return rc;
 
-  const bool pair = tc_use_pair();
+  const int64_t big = M > N ? (M > K ? M : K) : (N > K ? N : K);
+  const TcTuning tune = tc_tuning_for(TC_KIND_ADJOINT, big, big);
+  const bool pair = tune.engine == 2;
   const int64_t tbm = pair ? 256 : TC_BM, tbn = pair ? 256 : TC_BN;
   TcParams prm;
   std::memset(&prm, 0, sizeof(prm));
+  prm.band = tune.band;
   TcProblem& P = prm.prob[0];   // dA (M x K), contraction N
   P.M = M; P.N = K; P.K = N;
   P.tiles_m = static_cast<int32_t>((M + tbm - 1) / tbm);
@@ -296,9 +299,13 @@ int adjoint_f32(int64_t M, int64_t N, int64_t K, const float* A, int64_t lda, co
     rc = make_plane_tmap(&tb0h, P2, N, K, 2, pN, 128);
     if (!rc) rc = make_plane_tmap(&tb1h, P4, M, N, 2, pM, 128);
     if (rc) return rc;
+    CUtensorMap tc0, tc1;
+    prm.c_tma = (tune.tma_store && make_c_tmap_f32(&tc0, dA, M, K, ldda) && make_c_tmap_f32(&tc1, dB, K, N, lddb))
+                    ? 1 : 0;
     const int64_t ctas = 2 * static_cast<int64_t>(prm.total_tiles), cap = sms & ~1;
     return tc_gemm_pair_launch(TC_EPI_F32, ta0, tb0h, &ta1, &tb1h, sched, prm,
-                               static_cast<int>(ctas < cap ? ctas : cap), GB_KERNEL_ADJOINT_MMA, s);
+                               static_cast<int>(ctas < cap ? ctas : cap), GB_KERNEL_ADJOINT_MMA, s,
+                               prm.c_tma ? &tc0 : nullptr, prm.c_tma ? &tc1 : nullptr);
   }
   const int grid = prm.total_tiles < sms ? prm.total_tiles : sms;
   return tc_gemm_launch(TC_EPI_F32, ta0, tb0, &ta1, &tb1, sched, prm, grid, GB_KERNEL_ADJOINT_MMA, s);

@@ -25,6 +25,7 @@
 
 namespace gb {
 int measure_fma_peaks(int sms, double* fp64_tflops, double* fp32_tflops);
+int tc_autotune(int kind, int64_t M, int64_t N, int64_t K, int reps, TcTuning* out, float* best_ms, cudaStream_t s);
 size_t gemm_f32_tc_workspace_bytes(int64_t M, int64_t N, int64_t K, int nterms);
 int gemm_f32_tc(int ta, int tb, int64_t M, int64_t N, int64_t K, float alpha, const float* A, int64_t lda,
                 const float* B, int64_t ldb, float beta, float* C, int64_t ldc, int nterms, void* ws, int sms,
@@ -175,6 +176,19 @@ int make_plane_tmap(CUtensorMap* map, const void* base, int64_t K, int64_t rows,
     return GB_ERR_CUDA;
   }
   return GB_OK;
+}
+
+bool make_c_tmap_f32(CUtensorMap* map, const void* C, int64_t M, int64_t N, int64_t ldc) {
+  auto fn = encode_fn();
+  if (!fn || !C || M < 1 || N < 1 || (reinterpret_cast<uintptr_t>(C) & 15) || (ldc & 3)) return false;
+  if (M > 0x7FFFFFFF || N > 0x7FFFFFFF || ldc * 4 >= (int64_t(1) << 40)) return false;
+  cuuint64_t dims[2] = {static_cast<cuuint64_t>(M), static_cast<cuuint64_t>(N)};
+  cuuint64_t strides[1] = {static_cast<cuuint64_t>(ldc * 4)};
+  cuuint32_t box[2] = {32u, 32u};
+  cuuint32_t estr[2] = {1u, 1u};
+  return fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(C), dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 // The last CRT call's plan lives on the device until someone asks for it.
@@ -435,7 +449,8 @@ static int ozaki_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int
   g_last_plan.products = plan.products;
   g_last_plan.groups = plan.groups;
   g_last_plan.flops_tensor = plan.flops_tensor;
-  const int grid = oz_grid_for(dev->sms, M, N);
+  const TcTuning tune = tc_tuning_for(TC_KIND_SLICES, M, N);
+  const int grid = oz_grid_for(dev->sms, M, N, tune.engine);
   const size_t pa_bytes = align256(static_cast<size_t>(s_use) * M * pitch * 2);
   const size_t pb_bytes = align256(static_cast<size_t>(s_use) * N * pitch * 2);
   const size_t ex_bytes = align256((M + N) * sizeof(int32_t));
@@ -476,6 +491,8 @@ static int ozaki_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int
     ga.status = dev->status;
     ga.wait_limit_ns = g_wait_limit_ns.load();
     ga.grid = grid;
+    ga.engine = tune.engine;
+    ga.band = tune.band;
     rc = oz_gemm_launch(ga, plan, s);
   }
   cudaFreeAsync(ws, s);
@@ -600,6 +617,7 @@ static int crt_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int64
     const int64_t cap = dev->sms & ~1;
     ga.grid = static_cast<int>(ctas < cap ? ctas : cap);
     ga.plan = plan_d;
+    ga.band = tc_tuning_for(TC_KIND_CRT, M, N).band;
     rc = crt_gemm_launch(ga, plan, s);
   }
   if (!rc) {
@@ -750,6 +768,49 @@ int gb_set_ozaki_tolerance(double tol) {
   uint64_t b = 0;
   if (tol > 0.0) std::memcpy(&b, &tol, sizeof(b));
   g_ozaki_tol_bits.store(b);
+  return GB_OK;
+}
+
+static_assert(sizeof(gb_tc_tuning_t) == sizeof(TcTuning), "tuning layouts");
+
+int gb_tc_size_class(int64_t M, int64_t N) {
+  if (M < 0 || N < 0) return GB_ERR_INVALID_VALUE;
+  return tc_tune_class(M, N);
+}
+
+int gb_tc_default_tuning(int kind, gb_tc_tuning_t* out) {
+  if (!out || kind < 0 || kind >= GB_TC_KINDS) return GB_ERR_INVALID_VALUE;
+  const TcTuning t = tc_default_tuning(kind);
+  std::memcpy(out, &t, sizeof(t));
+  return GB_OK;
+}
+
+int gb_get_tc_tuning(int kind, int size_class, gb_tc_tuning_t* out) {
+  if (!out || kind < 0 || kind >= GB_TC_KINDS || size_class < 0 || size_class >= GB_TC_SIZE_CLASSES)
+    return GB_ERR_INVALID_VALUE;
+  const TcTuning t = tc_get_tuning(kind, size_class);
+  std::memcpy(out, &t, sizeof(t));
+  return GB_OK;
+}
+
+int gb_set_tc_tuning(int kind, int size_class, const gb_tc_tuning_t* tuning) {
+  if (!tuning) return tc_set_tuning(kind, size_class, nullptr);
+  TcTuning t;
+  std::memcpy(&t, tuning, sizeof(t));
+  if (t.reserved != 0) return GB_ERR_INVALID_VALUE;
+  return tc_set_tuning(kind, size_class, &t);
+}
+
+int gb_autotune_tc(int kind, int64_t M, int64_t N, int64_t K, int reps, gb_tc_tuning_t* out, float* best_ms,
+                   void* stream) {
+  if (!out) return GB_ERR_INVALID_VALUE;
+  DeviceInfo* dev = nullptr;
+  int rc = device_info(&dev);
+  if (rc) return rc;
+  TcTuning t;
+  rc = tc_autotune(kind, M, N, K, reps, &t, best_ms, static_cast<cudaStream_t>(stream));
+  if (rc) return rc;
+  std::memcpy(out, &t, sizeof(t));
   return GB_OK;
 }
 

@@ -66,7 +66,8 @@ int gemm_f32_tc(int ta, int tb, int64_t M, int64_t N, int64_t K, float alpha, co
   if (!rc)
     rc = split_bf16_terms(B, N, K, tb ? 1 : ldb, tb ? ldb : 1, nterms, PB, pk, nullptr, 0, GB_KERNEL_F32_SPLIT, s);
   if (rc) return rc;
-  const bool pair = tc_use_pair();
+  const TcTuning tune = tc_tuning_for(TC_KIND_F32, M, N);
+  const bool pair = tune.engine == 2;
   CUtensorMap tmap_a, tmap_b;
   rc = make_plane_tmap(&tmap_a, PA, K, M, nterms, pk, TC_BM);
   if (!rc) rc = make_plane_tmap(&tmap_b, PB, K, N, nterms, pk, pair ? 128 : TC_BN);
@@ -74,6 +75,7 @@ int gemm_f32_tc(int ta, int tb, int64_t M, int64_t N, int64_t K, float alpha, co
   const int64_t tbm = pair ? 256 : TC_BM, tbn = pair ? 256 : TC_BN;
   TcParams prm;
   std::memset(&prm, 0, sizeof(prm));
+  prm.band = tune.band;
   TcProblem& P = prm.prob[0];
   P.M = M;
   P.N = N;
@@ -94,9 +96,12 @@ int gemm_f32_tc(int ta, int tb, int64_t M, int64_t N, int64_t K, float alpha, co
   SliceSchedule sched;
   term_schedule(sched, nterms, P.kb_total);
   if (pair) {
+    CUtensorMap tmap_c;
+    prm.c_tma = (tune.tma_store && beta == 0.0f && make_c_tmap_f32(&tmap_c, C, M, N, ldc)) ? 1 : 0;
     const int64_t ctas = 2 * static_cast<int64_t>(prm.total_tiles), cap = sms & ~1;
     return tc_gemm_pair_launch(TC_EPI_F32, tmap_a, tmap_b, nullptr, nullptr, sched, prm,
-                               static_cast<int>(ctas < cap ? ctas : cap), GB_KERNEL_F32_MMA, s);
+                               static_cast<int>(ctas < cap ? ctas : cap), GB_KERNEL_F32_MMA, s,
+                               prm.c_tma ? &tmap_c : nullptr, nullptr);
   }
   const int grid = prm.total_tiles < sms ? prm.total_tiles : sms;
   return tc_gemm_launch(TC_EPI_F32, tmap_a, tmap_b, nullptr, nullptr, sched, prm, grid, GB_KERNEL_F32_MMA, s);

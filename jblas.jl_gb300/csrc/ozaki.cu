@@ -618,9 +618,10 @@ int oz_gemm_launch(const OzGemmArgs& a, const OzPlan& plan, cudaStream_t s) {
   if (rc) return rc;
   rc = make_plane_tmap(&tb, a.planes_b, a.K, a.N, a.slices, a.pitch, TC_BN);
   if (rc) return rc;
-  const bool pair = tc_use_pair();
+  const bool pair = a.engine == 2;
   TcParams prm;
   std::memset(&prm, 0, sizeof(prm));
+  prm.band = a.band;
   TcProblem& P = prm.prob[0];
   P.M = a.M;
   P.N = a.N;
@@ -652,8 +653,8 @@ int oz_gemm_launch(const OzGemmArgs& a, const OzPlan& plan, cudaStream_t s) {
                         GB_KERNEL_OZAKI_SLICE_MMA, s);
 }
 
-int oz_grid_for(int sms, int64_t M, int64_t N) {
-  if (tc_use_pair()) {
+int oz_grid_for(int sms, int64_t M, int64_t N, int engine) {
+  if (engine == 2) {
     const int64_t ctas = 2 * static_cast<int64_t>(tc_pair_tiles(M, N));
     const int64_t cap = sms & ~1;
     return static_cast<int>(ctas < cap ? ctas : cap);

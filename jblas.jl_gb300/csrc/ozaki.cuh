@@ -71,10 +71,12 @@ struct OzGemmArgs {
   DeviceStatus* status;
   uint64_t wait_limit_ns;
   int grid;
+  int engine;             // 1 = one CTA per 128 x 256 tile, 2 = CTA pairs on 256 x 256 tiles
+  int band;               // tile rows per L2 band of the raster
 };
 int oz_gemm_launch(const OzGemmArgs& a, const OzPlan& plan, cudaStream_t s);
 // Persistent grid size: one CTA per SM, at most one per output tile.
-int oz_grid_for(int sms, int64_t M, int64_t N);
+int oz_grid_for(int sms, int64_t M, int64_t N, int engine);
 
 // ---------------------------------------------------------------- CRT mode (ozaki_crt.cu)
 // Constants of the CRT mode, fixed by the moduli table; passed by value to the kernels.
@@ -186,6 +188,7 @@ struct CrtGemmArgs {
   uint64_t wait_limit_ns;
   int grid;               // even (CTA pairs)
   const CrtDevicePlan* plan;
+  int band;               // pair-tile rows per L2 band of the raster
 };
 // Residue products on the CTA-pair engine, then the CRT reconstruction into C.  `plan`
 // (host) gives the K chunking and a schedule for up to plan.n moduli; the kernels run

@@ -902,6 +902,7 @@ int crt_gemm_launch(const CrtGemmArgs& a, const CrtPlan& plan, cudaStream_t s) {
   prm.res_ld = a.res_ld;
   prm.res_plane = a.res_plane;
   prm.dev_ngroups = &a.plan->n;
+  prm.band = a.band;
   for (int g = 0; g < plan.n; ++g) {
     prm.crt_p[g] = crt_table().mod.pf[g];
     prm.crt_inv[g] = crt_table().mod.pinv[g];

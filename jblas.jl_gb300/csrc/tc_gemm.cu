@@ -31,10 +31,9 @@ constexpr int EXP_NONFINITE = 0x7FFFFFFF;
 // independent of the caller's, so that TMEM and shared memory are never released early.
 constexpr uint64_t TC_CLEANUP_WAIT_NS = 2000000000ull;
 
-// Tile raster: bands of 16 row tiles, column tiles inside a band (keeps the concurrently
+// Tile raster: bands of GM row tiles (16 by default), column tiles inside a band (keeps the concurrently
 // active A and B panels of one plane pair inside L2).
-__device__ __forceinline__ void tile_coords(int t, int tiles_m, int tiles_n, int& tm, int& tn) {
-  constexpr int GM = 16;
+__device__ __forceinline__ void tile_coords(int t, int tiles_m, int tiles_n, int GM, int& tm, int& tn) {
   const int band = t / (GM * tiles_n);
   const int in_band = t - band * GM * tiles_n;
   const int band_rows = min(GM, tiles_m - band * GM);
@@ -119,7 +118,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         const CUtensorMap* ta = pr ? &tmap_a1 : &tmap_a0;
         const CUtensorMap* tb = pr ? &tmap_b1 : &tmap_b0;
         int tm, tn;
-        tile_coords(t - P.tile_begin, P.tiles_m, P.tiles_n, tm, tn);
+        tile_coords(t - P.tile_begin, P.tiles_m, P.tiles_n, prm.band, tm, tn);
         const int m0 = tm * TC_BM, n0 = tn * TC_BN;
         for (int g = 0; g < G && ok; ++g) {
           for (int c = 0; c < P.nchunks && ok; ++c) {
@@ -232,7 +231,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       const int pr = problem_of(prm, t);
       const TcProblem& P = prm.prob[pr];
       int tm, tn;
-      tile_coords(t - P.tile_begin, P.tiles_m, P.tiles_n, tm, tn);
+      tile_coords(t - P.tile_begin, P.tiles_m, P.tiles_n, prm.band, tm, tn);
       const int64_t row = static_cast<int64_t>(tm) * TC_BM + row_l;
       const int64_t n0 = static_cast<int64_t>(tn) * TC_BN;
       const bool row_ok = row < P.M;

@@ -73,7 +73,32 @@ struct TcParams {
   float crt_inv[TC_MAX_MODULI];
   const int32_t* dev_ngroups;   // when set, the number of schedule groups to run (read on the device)
   float crt_psi[TC_MAX_MODULI][TC_MAX_MODULI];   // [n - 1][g]: multiplier of the final residue
+  int32_t band;         // output-tile rows per band of the tile raster (L2 reuse of the A rows)
+  int32_t c_tma;        // TC_EPI_F32: 1 = C written by TMA stores from shared memory (beta = 0)
 };
+
+// ---------------------------------------------------------------- tuning (pick_kernel_size)
+// Launch configuration of the engine per kind of product and output-size class, the
+// GPU-side counterpart of jBLAS's micro-tile choice and block options
+// (src/kernel_structure.jl:76-99, src/blas_options.jl:2-7): engine (1 = one CTA per 128 x 256
+// tile, cta_group::1; 2 = a CTA pair per 256 x 256 tile, cta_group::2), band (output-tile rows
+// of the L2 band of the tile raster) and, for FP32 outputs, TMA stores of C.
+enum TcKind { TC_KIND_SLICES = 0, TC_KIND_CRT = 1, TC_KIND_F32 = 2, TC_KIND_ADJOINT = 3, TC_KINDS = 4 };
+constexpr int TC_TUNE_CLASSES = 3;   // by max(M, N): <= 2048, <= 8192, larger
+struct TcTuning {
+  int32_t engine;
+  int32_t band;
+  int32_t tma_store;
+  int32_t reserved;
+};
+int tc_tune_class(int64_t M, int64_t N);
+TcTuning tc_default_tuning(int kind);
+int tc_validate_tuning(int kind, const TcTuning& t);
+// The tuning a call of this kind and output size uses (gb_set_tc_engine, when set, overrides
+// the engine).
+TcTuning tc_tuning_for(int kind, int64_t M, int64_t N);
+int tc_set_tuning(int kind, int cls, const TcTuning* t);   // t = nullptr: the default
+TcTuning tc_get_tuning(int kind, int cls);
 
 // Tensor maps for problem 0 and (optionally) problem 1; box 64 x 128 for A, 64 x 256 for B.
 int tc_gemm_launch(int epi, const CUtensorMap& ta0, const CUtensorMap& tb0, const CUtensorMap* ta1,
@@ -82,19 +107,24 @@ int tc_gemm_launch(int epi, const CUtensorMap& ta0, const CUtensorMap& tb0, cons
 
 // CTA-pair form (tc_gemm2.cu): 256 x 256 tiles on two SMs; TcProblem tile counts and
 // tile_begin are in 256 x 256 units, grid is even.
+// tc0 / tc1: FP32 C maps of problems 0 / 1 (make_c_tmap_f32), read when prm.c_tma is set.
 int tc_gemm_pair_launch(int epi, const CUtensorMap& ta0, const CUtensorMap& tb0, const CUtensorMap* ta1,
                         const CUtensorMap* tb1, const SliceSchedule& sched, const TcParams& prm, int grid,
-                        int kernel_kind, cudaStream_t s);
+                        int kernel_kind, cudaStream_t s, const CUtensorMap* tc0 = nullptr,
+                        const CUtensorMap* tc1 = nullptr);
 
-// Engine selection: 0 = automatic (CTA pairs), 1 = single-CTA 128 x 256 tiles, 2 = CTA pairs.
+// Engine override: 0 = the tuning's engine, 1 = single-CTA 128 x 256 tiles, 2 = CTA pairs.
 int tc_engine_setting();
 void tc_set_engine(int e);
-inline bool tc_use_pair() { return tc_engine_setting() != 1; }
 
 // 3-D BF16 tensor map {K, rows, planes} over [planes][rows][pitch], box 64 x box_rows x 1,
 // 128-byte swizzle (defined in capi.cu).
 int make_plane_tmap(CUtensorMap* map, const void* base, int64_t K, int64_t rows, int64_t slices,
                     int64_t pitch, int box_rows);
+// 2-D FP32 tensor map over a column-major M x N matrix C (leading dimension ldc), box 32 x 32,
+// for the TMA-store epilogue.  false when C's layout does not allow one (base not 16-byte
+// aligned, ldc not a multiple of 4, sizes beyond the map's range); the caller then stores directly.
+bool make_c_tmap_f32(CUtensorMap* map, const void* C, int64_t M, int64_t N, int64_t ldc);
 
 inline int tc_pair_tiles(int64_t M, int64_t N) {
   return static_cast<int>(((M + 255) / 256) * ((N + 255) / 256));

@@ -38,12 +38,19 @@ constexpr int P2_B_BYTES = 128 * TC_BK * 2;     // 16 KB: this CTA's half of B
 constexpr int P2_STAGE_BYTES = P2_A_BYTES + P2_B_BYTES;
 constexpr int P2_TMEM_COLS = 512;
 constexpr int P2_SMEM_BYTES = P2_STAGES * P2_STAGE_BYTES + 1024 + 256;
+// TC_EPI_F32 with TMA stores: behind the stages and a 1 KB barrier block, one 32 x 32 FP32 box
+// of C per epilogue warp (8 warps x 4 KB), in the tensor map's own layout (rows fastest): a warp
+// writes 32 consecutive floats per column, so the staging is conflict-free without a swizzle.
+constexpr int P2_CSTAGE_OFF = P2_STAGES * P2_STAGE_BYTES + 1024;
+constexpr int P2_CSTAGE_BYTES = 8 * 32 * 32 * 4;
+constexpr int P2_SMEM_BYTES_F32 = 1024 + P2_CSTAGE_OFF + P2_CSTAGE_BYTES;
+static_assert(P2_SMEM_BYTES_F32 <= 232448, "shared memory per CTA");
 
 constexpr int P2_EXP_NONFINITE = 0x7FFFFFFF;
 constexpr uint64_t P2_CLEANUP_WAIT_NS = 2000000000ull;
 
-__device__ __forceinline__ void p2_tile_coords(int t, int tiles_m, int tiles_n, int& tm, int& tn) {
-  constexpr int GM = 8;   // bands of 8 pair tiles (2048 rows)
+__device__ __forceinline__ void p2_tile_coords(int t, int tiles_m, int tiles_n, int GM, int& tm, int& tn) {
+  // bands of GM pair tiles (GM x 256 rows; 8 by default), column tiles inside a band
   const int band = t / (GM * tiles_n);
   const int in_band = t - band * GM * tiles_n;
   const int band_rows = min(GM, tiles_m - band * GM);
@@ -85,6 +92,7 @@ template <int EPI>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(P2Shape<EPI>::THREADS, 1)
     tc_gemm_pair_kernel(const __grid_constant__ CUtensorMap tmap_a0, const __grid_constant__ CUtensorMap tmap_b0,
                         const __grid_constant__ CUtensorMap tmap_a1, const __grid_constant__ CUtensorMap tmap_b1,
+                        const __grid_constant__ CUtensorMap tmap_c0, const __grid_constant__ CUtensorMap tmap_c1,
                         const __grid_constant__ SliceSchedule sched, const __grid_constant__ TcParams prm) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -151,7 +159,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(P2Shape<EPI>::THREAD
         const CUtensorMap* ta = pr ? &tmap_a1 : &tmap_a0;
         const CUtensorMap* tb = pr ? &tmap_b1 : &tmap_b0;
         int tm, tn;
-        p2_tile_coords(t - P.tile_begin, P.tiles_m, P.tiles_n, tm, tn);
+        p2_tile_coords(t - P.tile_begin, P.tiles_m, P.tiles_n, prm.band, tm, tn);
         const int m0 = tm * 256 + 128 * static_cast<int>(rank);
         const int n0 = tn * 256 + 128 * static_cast<int>(rank);
         for (int g = g0; g < g1 && ok; ++g) {
@@ -270,7 +278,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(P2Shape<EPI>::THREAD
       const int pr = p2_problem_of(prm, t);
       const TcProblem& P = prm.prob[pr];
       int tm, tn;
-      p2_tile_coords(t - P.tile_begin, P.tiles_m, P.tiles_n, tm, tn);
+      p2_tile_coords(t - P.tile_begin, P.tiles_m, P.tiles_n, prm.band, tm, tn);
       const int64_t row = static_cast<int64_t>(tm) * 256 + 128 * static_cast<int>(rank) + row_l;
       const int64_t n0 = static_cast<int64_t>(tn) * 256;
       const bool row_ok = row < P.M;
@@ -366,6 +374,24 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(P2Shape<EPI>::THREAD
             tc_wait_ld();
             const int64_t colb = n0 + cb;
             if (EPI == TC_EPI_F32) {
+              if (prm.c_tma && beta == 0.0) {
+                // C through shared memory and a TMA store of the warp's 32 x 32 box (rows and
+                // columns outside C are clipped by the copy); the box buffer is reused once the
+                // previous store of this warp has read it
+                float* cbuf = reinterpret_cast<float*>(smem + P2_CSTAGE_OFF + (warp - 2) * 4096);
+                const float fa = static_cast<float>(alpha);
+                if (lane == 0) bulk_wait_read_all();
+                __syncwarp();
+#pragma unroll
+                for (int j = 0; j < 32; ++j) cbuf[j * 32 + lane] = fa * __uint_as_float(v[j]);
+                fence_proxy_async_smem();
+                __syncwarp();
+                if (lane == 0) {
+                  tma_store_2d(pr ? &tmap_c1 : &tmap_c0, cbuf, static_cast<int>(row - lane), static_cast<int>(colb));
+                  bulk_commit_group();
+                }
+                continue;
+              }
               if (row_ok) {
                 float* __restrict__ crow = static_cast<float*>(P.C) + row + colb * P.ldc;
                 const float fa = static_cast<float>(alpha), fb = static_cast<float>(beta);
@@ -432,6 +458,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(P2Shape<EPI>::THREAD
     }
   }
 
+  if (EPI == TC_EPI_F32 && prm.c_tma && warp >= 2 && lane == 0) bulk_wait_all();   // C stores done
   tc_fence_before();
   __syncthreads();
   cluster_sync_all();   // neither CTA releases TMEM or exits while its peer still works
@@ -444,29 +471,31 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(P2Shape<EPI>::THREAD
 
 int tc_gemm_pair_launch(int epi, const CUtensorMap& ta0, const CUtensorMap& tb0, const CUtensorMap* ta1,
                         const CUtensorMap* tb1, const SliceSchedule& sched, const TcParams& prm, int grid,
-                        int kernel_kind, cudaStream_t s) {
+                        int kernel_kind, cudaStream_t s, const CUtensorMap* tc0, const CUtensorMap* tc1) {
   static std::atomic<unsigned long long> smem_opt_in[3];   // per kernel, one bit per device
   const CUtensorMap& a1 = ta1 ? *ta1 : ta0;
   const CUtensorMap& b1 = tb1 ? *tb1 : tb0;
+  // C maps are read only when prm.c_tma is set (TC_EPI_F32); otherwise any map fills the slots
+  const CUtensorMap& c0 = tc0 ? *tc0 : ta0;
+  const CUtensorMap& c1 = tc1 ? *tc1 : c0;
+  if (prm.c_tma && (epi != TC_EPI_F32 || !tc0 || (prm.nprob == 2 && !tc1))) return GB_ERR_INVALID_VALUE;
   if (grid < 2) grid = 2;
   grid &= ~1;
   if (epi == TC_EPI_OZAKI_F64) {
     const int rc = opt_in_dynamic_smem(tc_gemm_pair_kernel<TC_EPI_OZAKI_F64>, P2_SMEM_BYTES, smem_opt_in[0]);
     if (rc) return rc;
     GB_LAUNCH(kernel_kind, s,
-              (tc_gemm_pair_kernel<TC_EPI_OZAKI_F64><<<grid, P2Shape<TC_EPI_OZAKI_F64>::THREADS, P2_SMEM_BYTES, s>>>(ta0, tb0, a1, b1, sched,
-                                                                                             prm)));
+              (tc_gemm_pair_kernel<TC_EPI_OZAKI_F64><<<grid, P2Shape<TC_EPI_OZAKI_F64>::THREADS, P2_SMEM_BYTES, s>>>(ta0, tb0, a1, b1, c0, c1, sched, prm)));
   } else if (epi == TC_EPI_CRT) {
     const int rc = opt_in_dynamic_smem(tc_gemm_pair_kernel<TC_EPI_CRT>, P2_SMEM_BYTES, smem_opt_in[2]);
     if (rc) return rc;
     GB_LAUNCH(kernel_kind, s,
-              (tc_gemm_pair_kernel<TC_EPI_CRT><<<grid, P2Shape<TC_EPI_CRT>::THREADS, P2_SMEM_BYTES, s>>>(ta0, tb0, a1, b1, sched,
-                                                                                           prm)));
+              (tc_gemm_pair_kernel<TC_EPI_CRT><<<grid, P2Shape<TC_EPI_CRT>::THREADS, P2_SMEM_BYTES, s>>>(ta0, tb0, a1, b1, c0, c1, sched, prm)));
   } else {
-    const int rc = opt_in_dynamic_smem(tc_gemm_pair_kernel<TC_EPI_F32>, P2_SMEM_BYTES, smem_opt_in[1]);
+    const int rc = opt_in_dynamic_smem(tc_gemm_pair_kernel<TC_EPI_F32>, P2_SMEM_BYTES_F32, smem_opt_in[1]);
     if (rc) return rc;
     GB_LAUNCH(kernel_kind, s,
-              (tc_gemm_pair_kernel<TC_EPI_F32><<<grid, P2Shape<TC_EPI_F32>::THREADS, P2_SMEM_BYTES, s>>>(ta0, tb0, a1, b1, sched, prm)));
+              (tc_gemm_pair_kernel<TC_EPI_F32><<<grid, P2Shape<TC_EPI_F32>::THREADS, P2_SMEM_BYTES_F32, s>>>(ta0, tb0, a1, b1, c0, c1, sched, prm)));
   }
   GB_CUDA_TRY(cudaGetLastError());
   return GB_OK;

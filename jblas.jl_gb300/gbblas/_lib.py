@@ -50,6 +50,23 @@ class Problem(ctypes.Structure):
                 ("alpha", ctypes.c_double), ("beta", ctypes.c_double)]
 
 
+TC_KINDS = {"ozaki_slices": 0, "ozaki_crt": 1, "f32": 2, "adjoint": 3}
+TC_SIZE_CLASSES = 3
+
+
+class TcTuning(ctypes.Structure):
+    """gb_tc_tuning_t: tensor-core engine, L2 band and TMA-store choice of one kind and size class."""
+    _fields_ = [("engine", ctypes.c_int32), ("band", ctypes.c_int32), ("tma_store", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+    def as_dict(self):
+        return {"engine": self.engine, "band": self.band, "tma_store": self.tma_store}
+
+    @classmethod
+    def from_dict(cls, d):
+        return cls(int(d["engine"]), int(d["band"]), int(d.get("tma_store", 0)), 0)
+
+
 class Tuning(ctypes.Structure):
     """gb_grouped_tuning_t: tile configuration per size class."""
     _fields_ = [("config", ctypes.c_int32 * GROUPED_CLASSES)]
@@ -82,6 +99,12 @@ SIGNATURES = {
     "gb_gemm_f32": (c_int, [c_int, c_int, c_i64, c_i64, c_i64, c_float, c_vp, c_i64, c_vp, c_i64,
                             c_float, c_vp, c_i64, c_vp]),
     "gb_measure_fma_peaks": (c_int, [ctypes.POINTER(c_double), ctypes.POINTER(c_double)]),
+    "gb_tc_size_class": (c_int, [c_i64, c_i64]),
+    "gb_tc_default_tuning": (c_int, [c_int, ctypes.POINTER(TcTuning)]),
+    "gb_get_tc_tuning": (c_int, [c_int, c_int, ctypes.POINTER(TcTuning)]),
+    "gb_set_tc_tuning": (c_int, [c_int, c_int, ctypes.POINTER(TcTuning)]),
+    "gb_autotune_tc": (c_int, [c_int, c_i64, c_i64, c_i64, c_int, ctypes.POINTER(TcTuning),
+                               ctypes.POINTER(c_float), c_vp]),
     "gb_gemm_f32_ex": (c_int, [c_int, c_int, c_i64, c_i64, c_i64, c_float, c_vp, c_i64, c_vp, c_i64,
                                c_float, c_vp, c_i64, c_int, c_vp]),
     "gb_plan_ozaki": (c_int, [c_i64, c_i64, c_i64, c_int, ctypes.POINTER(OzakiPlan)]),

@@ -11,7 +11,8 @@ layer over the C ABI in `include/gbblas.h`:
     kernel!(pD, pA, pX, Kernel{Mₖ,Pₖ,stride_AD,stride_X,N}())   D += A*X as jBLAS's pointer kernel
     initkernel!(pD, pA, pX, Kernel{...}())                        D = A*X (src/kernels.jl:212-273)
     gemm!(C, A, B)                 the same call spelled as in the task (`jmul!` semantics)
-    gemm!(C, A, B, α, β; mode, slices)   BLAS-3 form; mode = :native | :ozaki | :ozaki_crt
+    gemm!(C, A, B, α, β; mode, slices)   BLAS-3 form; mode = :native | :ozaki | :ozaki_crt (Float64),
+                                         :native | :bf16x3 | :bf16x6 (Float32)
     gemm_adjoint!(dA, dB, A, B, dC)      dA = dC*B', dB = A'*dC in one launch (Float32)
     mul!(C, A, B, α, β; mode, slices)    LinearAlgebra.mul! semantics, A and B may be
                                          transpose/adjoint views (real element types)
@@ -31,7 +32,7 @@ const libgbblas = get(ENV, "GBBLAS_LIB", joinpath(@__DIR__, "..", "lib", "libgbb
 
 const GB_OK = Cint(0)
 const MODE = Dict(:native => Cint(0), :ozaki => Cint(1), :ozaki_bf16 => Cint(1), :ozaki_int8 => Cint(2),
-                  :ozaki_crt => Cint(3))
+                  :ozaki_crt => Cint(3), :bf16x3 => Cint(4), :bf16x6 => Cint(5))
 
 struct GBError <: Exception
     status::Cint
@@ -101,13 +102,17 @@ function gemm!(C::AbstractMatrix{Float64}, A::AbstractMatrix{Float64}, B::Abstra
                 MODE[mode], slices, C_NULL, current_stream()))
     C
 end
-function gemm!(C::AbstractMatrix{Float32}, A::AbstractMatrix{Float32}, B::AbstractMatrix{Float32}, α::Real, β::Real)
+# Float32: mode = :native (jmul!'s FMA chain, bit for bit) or :bf16x3 / :bf16x6 (BF16 term
+# products on the tensor cores, gb_gemm_f32_ex).
+function gemm!(C::AbstractMatrix{Float32}, A::AbstractMatrix{Float32}, B::AbstractMatrix{Float32}, α::Real, β::Real;
+               mode::Symbol = :native)
     M, K = size(A); N = size(B, 2)
     size(B, 1) == K && size(C) == (M, N) || throw(DimensionMismatch("gemm!"))
-    check(ccall((:gb_gemm_f32, libgbblas), Cint,
+    check(ccall((:gb_gemm_f32_ex, libgbblas), Cint,
                 (Cint, Cint, Int64, Int64, Int64, Cfloat, Ptr{Cfloat}, Int64, Ptr{Cfloat}, Int64, Cfloat,
-                 Ptr{Cfloat}, Int64, Ptr{Cvoid}),
-                0, 0, M, N, K, α, devptr(A), ld(A), devptr(B), ld(B), β, devptr(C), ld(C), current_stream()))
+                 Ptr{Cfloat}, Int64, Cint, Ptr{Cvoid}),
+                0, 0, M, N, K, α, devptr(A), ld(A), devptr(B), ld(B), β, devptr(C), ld(C), MODE[mode],
+                current_stream()))
     C
 end
 
@@ -219,7 +224,7 @@ storage(X::Wrapped{<:Real}) = parent(X)
 `C = α op(A) op(B) + β C` with LinearAlgebra's argument meaning, on device matrices; `A`
 and `B` may be `transpose`/`adjoint` views (passed to the library as transpose flags, the
 data is not copied).  Float64 accepts `mode` (`:native`, `:ozaki`, `:ozaki_crt`), Float32
-runs natively.
+`:native`, `:bf16x3` or `:bf16x6`.
 """
 function mul!(C::AbstractMatrix{Float64}, A::AbstractMatrix{Float64}, B::AbstractMatrix{Float64},
               α::Number = true, β::Number = false; mode::Symbol = :native, slices::Integer = 0)
@@ -234,15 +239,15 @@ function mul!(C::AbstractMatrix{Float64}, A::AbstractMatrix{Float64}, B::Abstrac
     C
 end
 function mul!(C::AbstractMatrix{Float32}, A::AbstractMatrix{Float32}, B::AbstractMatrix{Float32},
-              α::Number = true, β::Number = false)
+              α::Number = true, β::Number = false; mode::Symbol = :native)
     M, K = size(A); N = size(B, 2)
     size(B, 1) == K && size(C) == (M, N) || throw(DimensionMismatch("mul!: $(size(C)) = $(size(A)) * $(size(B))"))
     As, Bs = storage(A), storage(B)
-    check(ccall((:gb_gemm_f32, libgbblas), Cint,
+    check(ccall((:gb_gemm_f32_ex, libgbblas), Cint,
                 (Cint, Cint, Int64, Int64, Int64, Cfloat, Ptr{Cfloat}, Int64, Ptr{Cfloat}, Int64, Cfloat,
-                 Ptr{Cfloat}, Int64, Ptr{Cvoid}),
+                 Ptr{Cfloat}, Int64, Cint, Ptr{Cvoid}),
                 op_flag(A), op_flag(B), M, N, K, Float32(α), devptr(As), ld(As), devptr(Bs), ld(Bs), Float32(β),
-                devptr(C), ld(C), current_stream()))
+                devptr(C), ld(C), MODE[mode], current_stream()))
     C
 end
 

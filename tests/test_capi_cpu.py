@@ -115,3 +115,34 @@ def test_jmul_prefetch_hints_are_validated():
         gbblas.jmul_(D, D, D, a_loc=4)
     with pytest.raises(ValueError):
         gbblas.jmul_(D, D, D, 7, 7, 3, 3, 9)
+
+
+def test_tc_tuning_table_roundtrip_and_validation():
+    """The tensor-core tuning table (no GPU work): defaults, set/get per kind and size class,
+    invalid combinations refused, NULL restoring the default."""
+    import ctypes
+    from gbblas import _lib, tuning
+    L = _lib.lib()
+    assert [tuning.size_class(m, n) for m, n in ((1, 1), (2048, 100), (2049, 5), (8192, 8192), (8193, 1))] == \
+        [0, 0, 1, 1, 2]
+    for kind in _lib.TC_KINDS:
+        d = tuning.default_tuning(kind)
+        assert (d.engine, d.band, d.tma_store) == (2, 8, 0)
+        for cls in range(_lib.TC_SIZE_CLASSES):
+            assert tuning.get_tuning(kind, cls).as_dict() == d.as_dict()
+    tuning.set_tuning("f32", 1, {"engine": 2, "band": 16, "tma_store": 1})
+    assert tuning.get_tuning("f32", 1).as_dict() == {"engine": 2, "band": 16, "tma_store": 1}
+    assert tuning.get_tuning("f32", 0).as_dict()["band"] == 8
+    bad = [("ozaki_crt", {"engine": 1, "band": 8}), ("f32", {"engine": 3, "band": 8}),
+           ("f32", {"engine": 2, "band": 0}), ("f32", {"engine": 2, "band": 65}),
+           ("ozaki_slices", {"engine": 2, "band": 8, "tma_store": 1}),
+           ("adjoint", {"engine": 1, "band": 8, "tma_store": 1})]
+    for kind, d in bad:
+        t = _lib.TcTuning.from_dict(d)
+        assert L.gb_set_tc_tuning(_lib.TC_KINDS[kind], 0, ctypes.byref(t)) == _lib.GB_ERR_INVALID_VALUE, (kind, d)
+    t = _lib.TcTuning(2, 8, 0, 1)   # reserved must be 0
+    assert L.gb_set_tc_tuning(2, 0, ctypes.byref(t)) == _lib.GB_ERR_INVALID_VALUE
+    assert L.gb_set_tc_tuning(9, 0, None) == _lib.GB_ERR_INVALID_VALUE
+    assert L.gb_set_tc_tuning(2, 3, None) == _lib.GB_ERR_INVALID_VALUE
+    tuning.set_tuning("f32", 1, None)
+    assert tuning.get_tuning("f32", 1).as_dict() == tuning.default_tuning("f32").as_dict()

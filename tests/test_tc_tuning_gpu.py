@@ -1,0 +1,139 @@
+"""The tensor-core tuning table changes how products are scheduled and stored, never their values.
+
+  * digit slices and CRT residues are exact integer sums in FP32, so every engine and band gives
+    the restatement's bits;
+  * FP32 term modes and the adjoint accumulate in the same order whatever the band or the store
+    path, so TMA stores of C give the bits of direct stores (ragged shapes included), and a C
+    whose layout a TMA map cannot describe (unaligned leading dimension) falls back to direct
+    stores;
+  * gb_autotune_tc returns a valid tuning, the JSON cache round-trips and installs it.
+"""
+import json
+
+import numpy as np
+import pytest
+import torch
+
+import gbblas
+from gbblas import tuning
+import oracle
+from gpu_util import assert_bit_equal, to_dev, to_dev_ld, to_host
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture
+def restore_tuning(cuda):
+    yield
+    for kind in ("ozaki_slices", "ozaki_crt", "f32", "adjoint"):
+        for cls in range(3):
+            tuning.set_tuning(kind, cls, None)
+    gbblas.set_tc_engine(0)
+
+
+CANDIDATES = [{"engine": 2, "band": 1}, {"engine": 2, "band": 3}, {"engine": 2, "band": 64},
+              {"engine": 1, "band": 1}, {"engine": 1, "band": 5}, {"engine": 1, "band": 64}]
+
+
+@pytest.mark.parametrize("cand", CANDIDATES, ids=["p1", "p3", "p64", "s1", "s5", "s64"])
+def test_slices_bit_exact_under_every_engine_and_band(restore_tuning, cand):
+    M, K, N = 700, 300, 1100   # several bands and a ragged last band
+    g = np.random.default_rng(5)
+    A = np.asfortranarray(g.uniform(-1, 1, (M, K)) * np.ldexp(1.0, g.integers(-6, 7, (M, K))))
+    B = np.asfortranarray(g.uniform(-1, 1, (K, N)))
+    tuning.set_tuning("ozaki_slices", tuning.size_class(M, N), cand)
+    Cd = to_dev(np.zeros((M, N)))
+    gbblas.gemm_(Cd, to_dev(A), to_dev(B), mode="ozaki", slices=5)
+    torch.cuda.synchronize()
+    gbblas.check_device_status()
+    assert_bit_equal(to_host(Cd), oracle.ozaki_gemm(A, B, slices=5))
+
+
+@pytest.mark.parametrize("band", [1, 2, 5, 64])
+def test_crt_bit_exact_under_every_band(restore_tuning, band):
+    M, K, N = 900, 257, 700
+    g = np.random.default_rng(6 + band)
+    A = np.asfortranarray(g.uniform(-1, 1, (M, K)) * np.ldexp(1.0, g.integers(-6, 7, (M, K))))
+    B = np.asfortranarray(g.uniform(-1, 1, (K, N)))
+    tuning.set_tuning("ozaki_crt", tuning.size_class(M, N), {"engine": 2, "band": band})
+    Cd = to_dev(np.zeros((M, N)))
+    gbblas.gemm_(Cd, to_dev(A), to_dev(B), mode="ozaki_crt", slices=12)
+    torch.cuda.synchronize()
+    gbblas.check_device_status()
+    assert_bit_equal(to_host(Cd), oracle.ozaki_crt_gemm(A, B, moduli=12))
+
+
+SHAPES = [(1, 1, 1), (33, 70, 17), (300, 257, 130), (513, 96, 1000), (1024, 512, 768)]
+
+
+@pytest.mark.parametrize("mode", ["bf16x3", "bf16x6"])
+@pytest.mark.parametrize("shape", SHAPES, ids=["x".join(map(str, s)) for s in SHAPES])
+def test_f32_tma_store_equals_direct_stores(restore_tuning, mode, shape):
+    M, K, N = shape
+    g = np.random.default_rng(M + K + N)
+    A, B = to_dev(g.standard_normal((M, K)).astype(np.float32)), to_dev(g.standard_normal((K, N)).astype(np.float32))
+    cls = tuning.size_class(M, N)
+    out = []
+    for tma, band in ((0, 8), (1, 8), (1, 3)):
+        tuning.set_tuning("f32", cls, {"engine": 2, "band": band, "tma_store": tma})
+        Cd = to_dev(np.full((M, N), np.nan, np.float32))
+        gbblas.gemm_(Cd, A, B, 1.25, 0.0, mode=mode)
+        torch.cuda.synchronize()
+        gbblas.check_device_status()
+        out.append(to_host(Cd))
+    assert_bit_equal(out[1], out[0])
+    assert_bit_equal(out[2], out[0])
+    assert not np.isnan(out[0]).any()
+
+
+def test_f32_tma_store_padding_untouched_and_unaligned_fallback(restore_tuning):
+    """C inside a larger buffer: rows between M and ldc keep their contents; ldc = M + 1 (not a
+    multiple of 4) cannot be a TMA map and takes the direct stores, with the same bits."""
+    M, K, N = 130, 200, 90
+    g = np.random.default_rng(12)
+    A, B = to_dev(g.standard_normal((M, K)).astype(np.float32)), to_dev(g.standard_normal((K, N)).astype(np.float32))
+    tuning.set_tuning("f32", 0, {"engine": 2, "band": 8, "tma_store": 1})
+    results = []
+    for ld in (M + 6, M + 1):   # ld = 136 (TMA-capable), 131 (not)
+        Cd, buf = to_dev_ld(np.zeros((M, N), np.float32), ld, fill=7.0)
+        gbblas.gemm_(Cd, A, B, mode="bf16x3")
+        torch.cuda.synchronize()
+        gbblas.check_device_status()
+        assert np.all(to_host(buf)[M:, :N] == 7.0)
+        results.append(to_host(Cd))
+    assert_bit_equal(results[0], results[1])
+
+
+def test_adjoint_tma_store_equals_direct_stores(restore_tuning):
+    M, N, K = 300, 513, 129
+    g = np.random.default_rng(21)
+    A = to_dev(g.standard_normal((M, K)).astype(np.float32))
+    B = to_dev(g.standard_normal((K, N)).astype(np.float32))
+    W = to_dev(g.standard_normal((M, N)).astype(np.float32))
+    cls = tuning.size_class(max(M, N, K), max(M, N, K))
+    got = []
+    for tma in (0, 1):
+        tuning.set_tuning("adjoint", cls, {"engine": 2, "band": 8, "tma_store": tma})
+        dA = torch.full((K, M), float("nan"), dtype=torch.float32, device="cuda").t()
+        dB = torch.full((N, K), float("nan"), dtype=torch.float32, device="cuda").t()
+        gbblas.gemm_adjoint_(dA, dB, A, B, W)
+        torch.cuda.synchronize()
+        gbblas.check_device_status()
+        got.append((to_host(dA), to_host(dB)))
+    assert_bit_equal(got[1][0], got[0][0])
+    assert_bit_equal(got[1][1], got[0][1])
+
+
+def test_autotune_and_cache_roundtrip(restore_tuning, tmp_path):
+    cache = str(tmp_path / "tc_tuning.json")
+    t, ms = tuning.autotune("f32", 1024, 1024, 512, reps=1, cache=cache)
+    assert t.engine in (1, 2) and 1 <= t.band <= 64 and t.tma_store in (0, 1) and ms > 0
+    assert tuning.get_tuning("f32", 0).as_dict() == t.as_dict()   # installed
+    with open(cache) as f:
+        data = json.load(f)
+    assert len(data) == 1 and list(data.values())[0]["tuning"] == t.as_dict()
+    tuning.set_tuning("f32", 0, None)
+    assert tuning.load_cache(cache) == 1
+    assert tuning.get_tuning("f32", 0).as_dict() == t.as_dict()
+    t2, _ = tuning.autotune("ozaki_crt", 512, 512, 256, reps=1, cache=cache)
+    assert t2.engine == 2
