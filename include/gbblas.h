@@ -272,10 +272,14 @@ typedef struct {
 
 /* Tile configuration per size class.  Classes by max(m, n): <=16, <=32, <=64, <=128,
  * <=256, >256.  Configurations (rows x cols of a C tile, 256 threads each):
- *   0: 16x16  1: 32x32  2: 64x32  3: 64x64  4: 128x64 (f32 only)  5: 128x128 (f32 only)
+ *   0: 16x16  1: 32x32  2: 64x32  3: 64x64                     (f64 and f32)
+ *   4: 128x64  5: 128x128  6: 32x64  7: 64x128  8: 128x32  9: 32x128   (f32 only)
+ *   GB_GROUPED_AUTO: chosen per problem from its m, n and k by a cost model (padding of the
+ *   tiles against the FMA efficiency of their register tiles; the FP32 default)
  * This replaces jBLAS's fixed BLASOptions(m_k, p_k) (src/blas_options.jl:2-7). */
 #define GB_GROUPED_CLASSES 6
-#define GB_GROUPED_CONFIGS 6
+#define GB_GROUPED_CONFIGS 10
+#define GB_GROUPED_AUTO 31
 typedef struct {
   int32_t config[GB_GROUPED_CLASSES];
 } gb_grouped_tuning_t;

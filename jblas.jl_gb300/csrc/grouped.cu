@@ -23,25 +23,56 @@
 #include "gb_common.cuh"
 #include "grouped.cuh"
 #include "profile.cuh"
+#include "simt_gemm.cuh"
 
 namespace gb {
 
 struct TileCfg {
   int bm, bn, bk, tm, tn;
 };
-// Every configuration runs on 256 threads: (bm / tm) * (bn / tn) == 256.
+// Every configuration runs on 256 threads: (bm / tm) * (bn / tn) == 256.  0-3 serve both
+// element types; 4-9 (FP32 only) are the larger and rectangular tiles of the FP32 tile loop.
 __host__ __device__ constexpr TileCfg tile_cfg(int c) {
   return c == 0 ? TileCfg{16, 16, 16, 1, 1}
        : c == 1 ? TileCfg{32, 32, 16, 2, 2}
        : c == 2 ? TileCfg{64, 32, 16, 4, 2}
        : c == 3 ? TileCfg{64, 64, 16, 4, 4}
-       : c == 4 ? TileCfg{128, 64, 8, 8, 4}
-                : TileCfg{128, 128, 8, 8, 8};
+       : c == 4 ? TileCfg{128, 64, 16, 8, 4}
+       : c == 5 ? TileCfg{128, 128, 16, 8, 8}
+       : c == 6 ? TileCfg{32, 64, 16, 2, 4}
+       : c == 7 ? TileCfg{64, 128, 16, 4, 8}
+       : c == 8 ? TileCfg{128, 32, 16, 8, 2}
+                : TileCfg{32, 128, 16, 2, 8};
 }
+constexpr int GROUPED_CONFIGS_F64 = 4;
+constexpr int GROUPED_CONFIGS_F32 = 10;
 
 __host__ __device__ inline int size_class(int64_t m, int64_t n) {
   const int64_t d = m > n ? m : n;
   return d <= 16 ? 0 : d <= 32 ? 1 : d <= 64 ? 2 : d <= 128 ? 3 : d <= 256 ? 4 : 5;
+}
+
+// Per-problem choice (GB_GROUPED_AUTO): the configuration with the least modelled time
+//   tiles x (bm bn max(k, 1) / eff(tm tn) + overhead)
+// where eff is the measured FMA efficiency of a register tile of tm x tn elements per thread
+// relative to the 8 x 8 tile, and overhead the fixed cost of one tile (its first panel's load
+// latency, index set-up and epilogue) in the same units.  Padding rows and columns of a tile
+// cost as much as real ones, so tall and wide problems take rectangular tiles.
+__host__ __device__ inline int auto_config(int64_t m, int64_t n, int64_t k, int nconfigs) {
+  float best = 3.4e38f;
+  int arg = 0;
+  for (int c = 0; c < nconfigs; ++c) {
+    const TileCfg t = tile_cfg(c);
+    const int e = t.tm * t.tn;
+    const float eff = e >= 64 ? 1.0f : e >= 32 ? 0.9f : e >= 16 ? 0.75f : e >= 8 ? 0.55f : e >= 4 ? 0.35f : 0.1f;
+    const float tiles = static_cast<float>((m + t.bm - 1) / t.bm) * static_cast<float>((n + t.bn - 1) / t.bn);
+    const float cost = tiles * (static_cast<float>(t.bm * t.bn) * static_cast<float>(k > 1 ? k : 1) / eff + 32768.0f);
+    if (cost < best) {
+      best = cost;
+      arg = c;
+    }
+  }
+  return arg;
 }
 
 // tuning.config[cls] without a dynamically indexed (local-memory) array
@@ -52,6 +83,12 @@ __device__ __forceinline__ int config_of(const gb_grouped_tuning_t& t, int cls) 
   return v;
 }
 
+// The configuration one problem runs under (the table's, or the per-problem choice).
+template <int NCFG>
+__host__ __device__ inline int problem_config(int table_cfg, int64_t m, int64_t n, int64_t k) {
+  return table_cfg == GB_GROUPED_AUTO ? auto_config(m, n, k, NCFG) : table_cfg;
+}
+
 template <typename T>
 __device__ __forceinline__ T fmad(T a, T b, T c);
 template <>
@@ -60,8 +97,23 @@ template <>
 __device__ __forceinline__ float fmad<float>(float a, float b, float c) { return fmaf(a, b, c); }
 
 constexpr int GROUPED_THREADS = 256;
-// largest As + Bs of any configuration (bytes): 16 x 64 + 16 x (64 + 1) FP64 words
-constexpr int GROUPED_SMEM = (16 * 64 + 16 * 65) * 8;
+// largest shared memory of any tile routine (bytes): the double-buffered 128 x 128 x 16 FP32
+// panels of the SIMT mainloop (the FP64 16 x 64 + 16 x 65 panels take 16.5 KB)
+constexpr int GROUPED_SMEM = SimtSmem<float, 128, 128, 16>::ELEMS * 4;
+static_assert(GROUPED_SMEM >= (16 * 64 + 16 * 65) * 8, "FP64 tile panels");
+
+// jmul!'s FMA chain with the alpha/beta epilogue of the grouped call (alpha != 0 here).
+template <typename T>
+struct GroupedChainOp {
+  static constexpr bool kInitFromC = false;
+  static constexpr bool kPairs = false;
+  T alpha, beta;
+  static __device__ __forceinline__ T init() { return T(-0.0); }
+  static __device__ __forceinline__ T step(T acc, T a, T b) { return fma_t<T>(a, b, acc); }
+  __device__ __forceinline__ void store(T* c, T acc) const {
+    *c = (beta == T(0)) ? alpha * acc : fma_t<T>(alpha, acc, beta * *c);
+  }
+};
 
 // One BM x BN tile of problem `p` (column-major, no transposes).  Per element the FMA chain
 // runs k = 0..K-1 in order from -0.0 (equal to jmul!'s a1*x1 first step, bit for bit).
@@ -172,10 +224,30 @@ __device__ __forceinline__ void grouped_tile(const gb_problem_t& p, int tm, int 
   }
 }
 
+// alpha = 0: C = beta C on one bm x bn tile (beta = 0 writes zeros without reading C; A and B
+// are not read), as jBLAS's alpha/beta extension of gb_gemm_* defines it.
+template <typename T>
+__device__ __forceinline__ void scale_tile(const gb_problem_t& p, int64_t m0, int64_t n0, int bm, int bn) {
+  T* __restrict__ C = static_cast<T*>(p.C);
+  const T beta = static_cast<T>(p.beta);
+  for (int e = threadIdx.x; e < bm * bn; e += GROUPED_THREADS) {
+    const int64_t m = m0 + e % bm, n = n0 + e / bm;
+    if (m < p.m && n < p.n) {
+      T* c = &C[m + n * p.ldc];
+      *c = (beta == T(0)) ? T(0) : beta * *c;
+    }
+  }
+}
+
 // Prologue: tiles per problem under the tuning table, exclusive prefix sum into
 // offsets[0..count]; one block, each thread scans a contiguous chunk.
+__device__ __forceinline__ int prologue_config(const gb_grouped_tuning_t& tuning, const gb_problem_t& p, bool f32) {
+  const int c = config_of(tuning, size_class(p.m, p.n));
+  return f32 ? problem_config<GROUPED_CONFIGS_F32>(c, p.m, p.n, p.k) : problem_config<GROUPED_CONFIGS_F64>(c, p.m, p.n, p.k);
+}
+
 __global__ void __launch_bounds__(1024) grouped_prefix_kernel(const gb_problem_t* __restrict__ probs, int count,
-                                                              gb_grouped_tuning_t tuning,
+                                                              gb_grouped_tuning_t tuning, bool f32,
                                                               long long* __restrict__ offsets) {
   __shared__ long long part[1024];
   const int t = threadIdx.x;
@@ -184,7 +256,7 @@ __global__ void __launch_bounds__(1024) grouped_prefix_kernel(const gb_problem_t
   long long sum = 0;
   for (int i = b; i < e; ++i) {
     const gb_problem_t& p = probs[i];
-    const TileCfg c = tile_cfg(config_of(tuning, size_class(p.m, p.n)));
+    const TileCfg c = tile_cfg(prologue_config(tuning, p, f32));
     const long long tiles = (p.m <= 0 || p.n <= 0) ? 0 : ((p.m + c.bm - 1) / c.bm) * ((p.n + c.bn - 1) / c.bn);
     sum += tiles;
   }
@@ -200,7 +272,7 @@ __global__ void __launch_bounds__(1024) grouped_prefix_kernel(const gb_problem_t
   for (int i = b; i < e; ++i) {
     offsets[i] = run;
     const gb_problem_t& p = probs[i];
-    const TileCfg c = tile_cfg(config_of(tuning, size_class(p.m, p.n)));
+    const TileCfg c = tile_cfg(prologue_config(tuning, p, f32));
     run += (p.m <= 0 || p.n <= 0) ? 0 : ((p.m + c.bm - 1) / c.bm) * ((p.n + c.bn - 1) / c.bn);
   }
   if (t == 1023) offsets[count] = part[1023];
@@ -220,12 +292,12 @@ __global__ void __launch_bounds__(GROUPED_THREADS, 2) grouped_gemm_kernel(const 
       if (offsets[mid] <= w) lo = mid; else hi = mid - 1;
     }
     const gb_problem_t p = probs[lo];
-    const int cfg = config_of(tuning, size_class(p.m, p.n));
+    const int cfg = prologue_config(tuning, p, sizeof(T) == 4);
     const TileCfg c = tile_cfg(cfg);
     const long long local = w - offsets[lo];
     const int tiles_m = static_cast<int>((p.m + c.bm - 1) / c.bm);
     const int tm = static_cast<int>(local % tiles_m), tn = static_cast<int>(local / tiles_m);
-    if (sizeof(T) == 8) {
+    if constexpr (sizeof(T) == 8) {
       // FP64 runs at the DFMA rate whatever the tile: the small configurations keep the
       // register count (and so the resident CTAs per SM) low.
       switch (cfg) {
@@ -234,15 +306,35 @@ __global__ void __launch_bounds__(GROUPED_THREADS, 2) grouped_gemm_kernel(const 
         case 2: grouped_tile<T, 64, 32, 16, 4, 2>(p, tm, tn, smem); break;
         default: grouped_tile<T, 64, 64, 16, 4, 4>(p, tm, tn, smem); break;
       }
+    } else if (cfg == 0) {
+      grouped_tile<T, 16, 16, 16, 1, 1>(p, tm, tn, smem);   // one element a thread
+    } else if ((__double_as_longlong(p.alpha) & 0x7FFFFFFFFFFFFFFFll) == 0) {
+      scale_tile<T>(p, static_cast<int64_t>(tm) * c.bm, static_cast<int64_t>(tn) * c.bn, c.bm, c.bn);
     } else {
+      // FP32 register tiles of two or more rows and columns: the double-buffered SIMT mainloop
+      // of the native GEMM (simt_gemm.cuh) on this problem's tile
+      const GroupedChainOp<T> op{static_cast<T>(p.alpha), static_cast<T>(p.beta)};
+      const T* A = static_cast<const T*>(p.A);
+      const T* B = static_cast<const T*>(p.B);
+      T* C = static_cast<T*>(p.C);
+      T* sm = reinterpret_cast<T*>(smem);
+      const int64_t m0 = static_cast<int64_t>(tm) * c.bm, n0 = static_cast<int64_t>(tn) * c.bn;
+#define GB_GTILE(BM_, BN_, TM_, TN_)                                                                      \
+  simt_tile<T, GroupedChainOp<T>, BM_, BN_, 16, TM_, TN_, false, false>(p.m, p.n, p.k, op, A, p.lda, B, p.ldb, C, \
+                                                                       p.ldc, m0, n0, sm)
       switch (cfg) {
-        case 0: grouped_tile<T, 16, 16, 16, 1, 1>(p, tm, tn, smem); break;
-        case 1: grouped_tile<T, 32, 32, 16, 2, 2>(p, tm, tn, smem); break;
-        case 2: grouped_tile<T, 64, 32, 16, 4, 2>(p, tm, tn, smem); break;
-        case 3: grouped_tile<T, 64, 64, 16, 4, 4>(p, tm, tn, smem); break;
-        case 4: grouped_tile<T, 128, 64, 8, 8, 4>(p, tm, tn, smem); break;
-        default: grouped_tile<T, 128, 128, 8, 8, 8>(p, tm, tn, smem); break;
+        case 1: GB_GTILE(32, 32, 2, 2); break;
+        case 2: GB_GTILE(64, 32, 4, 2); break;
+        case 3: GB_GTILE(64, 64, 4, 4); break;
+        case 4: GB_GTILE(128, 64, 8, 4); break;
+        case 5: GB_GTILE(128, 128, 8, 8); break;
+        case 6: GB_GTILE(32, 64, 2, 4); break;
+        case 7: GB_GTILE(64, 128, 4, 8); break;
+        case 8: GB_GTILE(128, 32, 8, 2); break;
+        default: GB_GTILE(32, 128, 2, 8); break;
       }
+#undef GB_GTILE
+      __syncthreads();   // the next tile reuses the shared panels
     }
   }
 }
@@ -251,17 +343,18 @@ gb_grouped_tuning_t grouped_default_tuning(int dtype_bytes) {
   gb_grouped_tuning_t t;
   std::memset(&t, 0, sizeof(t));
   // classes: <=16, <=32, <=64, <=128, <=256, >256
+  // FP32: the per-problem choice in every class (rectangular tiles for tall and wide problems)
   const int f64[GB_GROUPED_CLASSES] = {0, 1, 2, 3, 3, 3};
-  const int f32[GB_GROUPED_CLASSES] = {0, 1, 3, 3, 4, 5};
-  for (int c = 0; c < GB_GROUPED_CLASSES; ++c) t.config[c] = dtype_bytes == 8 ? f64[c] : f32[c];
+  for (int c = 0; c < GB_GROUPED_CLASSES; ++c) t.config[c] = dtype_bytes == 8 ? f64[c] : GB_GROUPED_AUTO;
   return t;
 }
 
-int grouped_configs(int dtype_bytes) { return dtype_bytes == 8 ? 4 : GB_GROUPED_CONFIGS; }
+int grouped_configs(int dtype_bytes) { return dtype_bytes == 8 ? GROUPED_CONFIGS_F64 : GROUPED_CONFIGS_F32; }
 
 int grouped_validate_tuning(int dtype_bytes, const gb_grouped_tuning_t& t) {
   for (int c = 0; c < GB_GROUPED_CLASSES; ++c)
-    if (t.config[c] < 0 || t.config[c] >= grouped_configs(dtype_bytes)) return GB_ERR_INVALID_VALUE;
+    if (t.config[c] != GB_GROUPED_AUTO && (t.config[c] < 0 || t.config[c] >= grouped_configs(dtype_bytes)))
+      return GB_ERR_INVALID_VALUE;
   return GB_OK;
 }
 
@@ -296,7 +389,7 @@ int grouped_launch(int dtype_bytes, const gb_problem_t* d_probs, int count, cons
                    long long* d_offsets, int sms, cudaStream_t s) {
   if (count <= 0) return GB_OK;
   GB_LAUNCH(GB_KERNEL_GROUPED_GEMM, s,
-            (grouped_prefix_kernel<<<1, 1024, 0, s>>>(d_probs, count, tuning, d_offsets)));
+            (grouped_prefix_kernel<<<1, 1024, 0, s>>>(d_probs, count, tuning, dtype_bytes == 4, d_offsets)));
   if (dtype_bytes == 8) {
     const int grid = grid_for<double>(sms);
     GB_LAUNCH(GB_KERNEL_GROUPED_GEMM, s,
@@ -352,7 +445,8 @@ int grouped_autotune(int dtype_bytes, const gb_problem_t* h_probs, int count, in
       break;
     }
     float best_ms = 1e30f;
-    for (int cfg = 0; cfg < grouped_configs(dtype_bytes); ++cfg) {
+    for (int ci = 0; ci <= grouped_configs(dtype_bytes); ++ci) {
+      const int cfg = (ci == grouped_configs(dtype_bytes)) ? GB_GROUPED_AUTO : ci;
       gb_grouped_tuning_t t = best;
       t.config[c] = cfg;
       rc = grouped_launch(dtype_bytes, d_sub, static_cast<int>(v.size()), t, d_off, sms, s);   // warm-up
@@ -441,7 +535,7 @@ int grouped_f64_noalloc(const gb_problem_t* d_probs, int count, const gb_grouped
   // The prologue rewrites offsets[0..count] on every call, so nothing needs clearing.
   // Launched directly, not through the timing hooks (which create CUDA events while profiling
   // is on); gb_launch_counts still counts both launches.
-  grouped_prefix_kernel<<<1, 1024, 0, s>>>(d_probs, count, t, offsets);
+  grouped_prefix_kernel<<<1, 1024, 0, s>>>(d_probs, count, t, false, offsets);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return gb_set_cuda_error(e, "grouped prologue launch");
   prof_count(GB_KERNEL_GROUPED_GEMM);

@@ -36,28 +36,36 @@ __device__ __forceinline__ double fma_t<double>(double a, double b, double c) { 
 template <>
 __device__ __forceinline__ float fma_t<float>(float a, float b, float c) { return fmaf(a, b, c); }
 
-// Tile configuration: BM x BN CTA tile, BK K-panel, TM x TN per thread split in two
-// halves of VM (VN) contiguous rows (columns) to allow vector shared-memory reads.
-// 4-byte elements: two CTAs per SM (at most 128 registers a thread for 256 threads);
-// 8-byte elements: no residency bound (0), which leaves ptxas its own register choice.
+// Shared memory of one tile: double-buffered BK x BM and BK x BN panels, rows padded by 16
+// bytes (transposing stores hit distinct banks, vector reads stay aligned).
+template <typename T, int BM, int BN, int BK>
+struct SimtSmem {
+  static constexpr int PAD = 16 / static_cast<int>(sizeof(T));
+  static constexpr int A_ELEMS = 2 * BK * (BM + PAD);
+  static constexpr int ELEMS = A_ELEMS + 2 * BK * (BN + PAD);
+};
+
+// One BM x BN tile of C at (m0, n0), computed by the NT = (BM / TM) * (BN / TN) threads of the
+// CTA in `smem` (SimtSmem<T, BM, BN, BK>::ELEMS elements, 16-byte aligned).  TM x TN per thread,
+// split in two halves of VM (VN) contiguous rows (columns) to allow vector shared-memory reads.
+// The last shared-memory reads are not followed by a barrier: a caller that runs another tile in
+// the same shared memory synchronises first.
 template <typename T, typename Op, int BM, int BN, int BK, int TM, int TN, bool TA, bool TB>
-__global__ void __launch_bounds__((BM / TM) * (BN / TN), sizeof(T) == 4 ? 2 : 0)
-    simt_gemm_kernel(int64_t M, int64_t N, int64_t K, Op op, const T* __restrict__ A, int64_t lda,
-                     const T* __restrict__ B, int64_t ldb, T* __restrict__ C, int64_t ldc) {
+__device__ __forceinline__ void simt_tile(int64_t M, int64_t N, int64_t K, const Op& op, const T* __restrict__ A,
+                                          int64_t lda, const T* __restrict__ B, int64_t ldb, T* __restrict__ C,
+                                          int64_t ldc, int64_t m0, int64_t n0, T* smem) {
   constexpr int NT = (BM / TM) * (BN / TN);
   constexpr int VM = TM / 2, VN = TN / 2;
   constexpr int A_PER = (BM * BK) / NT, B_PER = (BK * BN) / NT;
   static_assert((BM * BK) % NT == 0 && (BK * BN) % NT == 0, "tile/thread mismatch");
+  static_assert(TM % 2 == 0 && TN % 2 == 0, "two halves per thread tile");
 
-  // Rows padded by 16 bytes: transposing stores hit distinct banks, vector reads stay aligned.
-  constexpr int PAD = 16 / static_cast<int>(sizeof(T));
-  __shared__ __align__(16) T As[2][BK][BM + PAD];
-  __shared__ __align__(16) T Bs[2][BK][BN + PAD];
+  constexpr int PAD = SimtSmem<T, BM, BN, BK>::PAD;
+  T (*As)[BK][BM + PAD] = reinterpret_cast<T (*)[BK][BM + PAD]>(smem);
+  T (*Bs)[BK][BN + PAD] = reinterpret_cast<T (*)[BK][BN + PAD]>(smem + SimtSmem<T, BM, BN, BK>::A_ELEMS);
 
   const int tid = threadIdx.x;
   const int tx = tid % (BN / TN), ty = tid / (BN / TN);
-  const int64_t m0 = static_cast<int64_t>(blockIdx.x) * BM;
-  const int64_t n0 = static_cast<int64_t>(blockIdx.y) * BN;
 
   // Global-load geometry, fixed for the whole K loop.  With NT a multiple of the panel's
   // leading extent, every load of a thread sits in one row (column) of the panel, or at one k,
@@ -219,6 +227,19 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN), sizeof(T) == 4 ? 2 : 0)
       op.store(&C[m + n * ldc], acc[i][j]);
     }
   }
+}
+
+// The tile above as a kernel: CTA (x, y) computes the tile at (x BM, y BN).
+// 4-byte elements: two CTAs per SM (at most 128 registers a thread for 256 threads);
+// 8-byte elements: no residency bound (0), which leaves ptxas its own register choice.
+template <typename T, typename Op, int BM, int BN, int BK, int TM, int TN, bool TA, bool TB>
+__global__ void __launch_bounds__((BM / TM) * (BN / TN), sizeof(T) == 4 ? 2 : 0)
+    simt_gemm_kernel(int64_t M, int64_t N, int64_t K, Op op, const T* __restrict__ A, int64_t lda,
+                     const T* __restrict__ B, int64_t ldb, T* __restrict__ C, int64_t ldc) {
+  __shared__ __align__(16) T smem[SimtSmem<T, BM, BN, BK>::ELEMS];
+  simt_tile<T, Op, BM, BN, BK, TM, TN, TA, TB>(M, N, K, op, A, lda, B, ldb, C, ldc,
+                                               static_cast<int64_t>(blockIdx.x) * BM,
+                                               static_cast<int64_t>(blockIdx.y) * BN, smem);
 }
 
 // Grid of the kernel above for an M x N output; false when it does not fit a launch.

@@ -18,9 +18,11 @@ from . import _lib
 from ._lib import check
 
 CLASSES = 6
-CONFIGS = 6
+CONFIGS = 10
+AUTO = 31   # GB_GROUPED_AUTO: tile configuration chosen per problem by the library's cost model
 CLASS_LIMITS = (16, 32, 64, 128, 256)   # max(m, n) upper bounds of classes 0..4; 5 is larger
-CONFIG_TILES = {0: (16, 16), 1: (32, 32), 2: (64, 32), 3: (64, 64), 4: (128, 64), 5: (128, 128)}
+CONFIG_TILES = {0: (16, 16), 1: (32, 32), 2: (64, 32), 3: (64, 64), 4: (128, 64), 5: (128, 128),
+                6: (32, 64), 7: (64, 128), 8: (128, 32), 9: (32, 128), AUTO: "per problem"}
 
 
 Problem = _lib.Problem

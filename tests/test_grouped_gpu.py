@@ -53,21 +53,25 @@ def test_bit_exact_default_tuning(cuda, dtype):
 
 @pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
 def test_every_configuration_bit_exact(cuda, dtype):
+    """Every tile configuration (and the per-problem choice) gives jmul!'s chain bit for bit,
+    with alpha/beta (including alpha = 0: C = beta C without reading A and B)."""
     g = np.random.default_rng(2)
-    sizes = [tuple(int(x) for x in g.integers(1, 200, 3)) for _ in range(24)]
-    nconf = 4 if dtype == torch.float64 else 6
-    for cfg in range(nconf):
-        hA, hB, hC, As, Bs, Cs = make_problems(sizes, dtype, 3 + cfg)
-        plan = grouped.GroupedGemm(As, Bs, Cs, alpha=1.0, beta=0.0,
+    sizes = [tuple(int(x) for x in g.integers(1, 300, 3)) for _ in range(24)] + [(300, 5, 40), (5, 300, 40)]
+    nconf = 4 if dtype == torch.float64 else grouped.CONFIGS
+    alphas = [1.0] * (len(sizes) - 2) + [0.0, 1.5]
+    betas = [0.0] * (len(sizes) - 3) + [0.5, 0.5, -0.25]
+    for cfg in list(range(nconf)) + [grouped.AUTO]:
+        hA, hB, hC, As, Bs, Cs = make_problems(sizes, dtype, 3 + (cfg % 16))
+        plan = grouped.GroupedGemm(As, Bs, Cs, alpha=alphas, beta=betas,
                                    tuning=grouped.Tuning.from_list([cfg] * grouped.CLASSES))
         plan.run()
-        check_all(hA, hB, hC, Cs, dtype, [1.0] * len(sizes), [0.0] * len(sizes))
+        check_all(hA, hB, hC, Cs, dtype, alphas, betas)
 
 
 def test_invalid_tuning_rejected(cuda):
     hA, hB, hC, As, Bs, Cs = make_problems([(8, 8, 8)], torch.float64, 4)
     plan = grouped.GroupedGemm(As, Bs, Cs, tuning=grouped.Tuning.from_list([5] * grouped.CLASSES))
-    with pytest.raises(gbblas.GBError) as e:     # configurations 4 and 5 are float32 only
+    with pytest.raises(gbblas.GBError) as e:     # configurations 4 to 9 are float32 only
         plan.run()
     assert e.value.status == _lib.GB_ERR_INVALID_VALUE
 
