@@ -74,13 +74,16 @@ def load_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
 
 
-def committed_traffic(workload):
-    """DRAM bytes per launch of the slice-product kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "ozaki_slice_mma_%s.txt" % workload)
+def committed_traffic(method, n):
+    """DRAM bytes per launch of the tensor-core product kernel from the committed ncu summary: the
+    4096 x 4096 x 8192 capture scaled to n^3 by the pair tiles one launch processes (only n = 8192
+    is recorded there)."""
+    name = {"crt": "ozaki_crt_launch_list_4096x4096x8192.md", "slices": "ozaki_slices_launch_list_4096x4096x8192.md"}
+    path = os.path.join(ROOT, "profiles", name.get(method, ""))
     try:
         with open(path) as f:
             for line in f:
-                if line.startswith("dram_bytes_per_launch_full_size:"):
+                if line.startswith("dram_bytes_per_launch_scaled_%d:" % n):
                     return float(line.split(":", 1)[1].split()[0])
     except OSError:
         pass
@@ -624,6 +627,21 @@ def workload_f32_tc(args):
     peaks, src = load_peaks()
     flops = 2.0 * n ** 3
     rows = []
+    from gbblas import tuning
+    cls = tuning.size_class(n, n)
+    # the FP32 epilogue's two store paths, same bits: direct stores and TMA stores of C
+    epilogue = {}
+    for mode in ("bf16x3", "bf16x6"):
+        for tma in (0, 1):
+            tuning.set_tuning("f32", cls, {"engine": 2, "band": 8, "tma_store": tma})
+            gbblas.gemm_(C, A, B, mode=mode)
+            torch.cuda.synchronize()
+            with gbblas.profile() as prof:
+                ms_t = _event_ms(lambda: gbblas.gemm_(C, A, B, mode=mode), args.steps, stream)
+            epilogue["%s_%s" % (mode, "tma_store" if tma else "direct")] = {
+                "ms": ms_t, "mma_ms": prof.ms.get("f32_mma", float("nan")) / max(1, prof.launches.get("f32_mma", 1))}
+    tuning.set_tuning("f32", cls, None)
+    tuned, tuned_ms = tuning.autotune("f32", n, n, n, reps=3, install=False)
     for mode, products in (("native", 0), ("bf16x3", 3), ("bf16x6", 6)):
         steps = max(1, min(args.steps, 3)) if mode == "native" else args.steps
         for _ in range(max(1, args.warmup if mode != "native" else 1)):
@@ -647,7 +665,8 @@ def workload_f32_tc(args):
     _side_line(args, "FP32 GEMM TFLOP/s on tensor cores (BF16 term products), 8192^3", head["tflops"], "TFLOP/s",
                head["ms"], {"workload": "f32_gemm_%d^3" % n, "M": n, "N": n, "K": n, "inputs": "N(0,1)",
                             "alpha": 1.0, "beta": 0.0},
-               {"dtype": "f32", "modes": rows, "roofline": head["roofline"],
+               {"dtype": "f32", "modes": rows, "roofline": head["roofline"], "epilogue_store_paths": epilogue,
+                "autotuned": {"tuning": tuned.as_dict(), "ms_bf16x3": tuned_ms},
                 "error_metric": "max |C - C_ref|_ij / (|A||B|)_ij on a 64 x 64 output grid against Dot2"})
     return 0
 
@@ -669,11 +688,19 @@ def workload_adjoint(args):
     W = dev_cm(workloads.normal(M, N, stream=53))
     dA = torch.empty((K, M), dtype=torch.float32, device=dev).t()
     dB = torch.empty((N, K), dtype=torch.float32, device=dev).t()
-    for _ in range(args.warmup):
-        gbblas.gemm_adjoint_(dA, dB, A, B, W)
-    torch.cuda.synchronize()
-    with gbblas.profile() as prof:
-        ms = _event_ms(lambda: gbblas.gemm_adjoint_(dA, dB, A, B, W), args.steps, stream)
+    from gbblas import tuning
+    cls = tuning.size_class(M, M)
+    store_paths = {}
+    for tma in (1, 0):   # the default (direct stores) last: its profile is the reported one
+        tuning.set_tuning("adjoint", cls, {"engine": 2, "band": 8, "tma_store": tma})
+        for _ in range(args.warmup):
+            gbblas.gemm_adjoint_(dA, dB, A, B, W)
+        torch.cuda.synchronize()
+        with gbblas.profile() as prof:
+            ms = _event_ms(lambda: gbblas.gemm_adjoint_(dA, dB, A, B, W), args.steps, stream)
+        store_paths["tma_store" if tma else "direct"] = {
+            "ms": ms, "mma_ms": prof.ms.get("adjoint_mma", float("nan")) / max(1, prof.launches.get("adjoint_mma", 1))}
+    tuning.set_tuning("adjoint", cls, None)
     useful = 2 * 2.0 * M * N * K
     tensor = 3 * useful
     mma_ms = prof.ms.get("adjoint_mma", float("nan")) / max(1, prof.launches.get("adjoint_mma", 1))
@@ -683,6 +710,7 @@ def workload_adjoint(args):
                "TFLOP/s", ms, {"workload": "adjoint_4096x2048x4096_f32", "M": M, "K": K, "N": N,
                                 "split": "3xBF16, FP32 accumulation"},
                {"dtype": "f32", "kernel_ms_per_step": {k: v / args.steps for k, v in prof.ms.items()},
+                "epilogue_store_paths": store_paths,
                 "roofline": {"bound": "tensor", "achieved": achieved, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
                              "frac": achieved / peaks["bf16_tflops"], "peak_source": "%s bf16_tflops" % src,
                              "work": "BF16 tensor flops = 3 products x 2 outputs x 2*M*N*K"}})
@@ -907,6 +935,12 @@ def main():
     d2h_gbs = C_pin.numel() * 8 / (c1.elapsed_time(c2) * 1e-3) / 1e9
 
     plan = gbblas.last_ozaki_plan()   # the plan the automatic choice used
+    crt_tuned = None
+    if rank == 0 and args.method == "crt" and not args.mnk:
+        from gbblas import tuning
+        t_best, t_ms = tuning.autotune("ozaki_crt", M, N, K, reps=2, install=False)
+        crt_tuned = {"tuning": t_best.as_dict(), "ms_15_moduli": t_ms,
+                     "default": tuning.get_tuning("ozaki_crt", tuning.size_class(M, N)).as_dict()}
     alt = None
     if not args.no_alt:
         # the other emulation method on the same inputs (automatic plan), for comparison
@@ -935,7 +969,7 @@ def main():
         timed_s = ms_step * args.steps / 1e3
         peak_key = "bf16_tflops_sustained" if timed_s >= 1.0 else "bf16_tflops"
         achieved = plan["flops_tensor"] / (mma_ms * 1e-3) / 1e12
-        traffic = committed_traffic("%s_%d" % (args.method, n)) if not args.mnk else None
+        traffic = committed_traffic(args.method, n) if not args.mnk else None
 
         # ------------------------------------------------------------ accuracy and native
         import oracle
@@ -997,11 +1031,14 @@ def main():
             "native_fp64": native,
             "roofline": {"bound": "tensor", "achieved": achieved, "peak": peaks[peak_key], "unit": "TFLOP/s",
                          "frac": achieved / peaks[peak_key], "traffic": traffic,
+                         "traffic_source": "ncu dram__bytes_read.sum + write.sum of a 4096x4096x8192 launch "
+                                           "scaled by 4x the pair tiles (profiles/, a lower bound at 8192^3)",
                          "kernel": "ozaki_slice_mma", "ms_per_launch": mma_ms,
                          "peak_source": "%s %s" % (peak_src, peak_key),
                          "work": "BF16 tensor flops per launch = %s * 2*M*N*ceil(K/64)*64"
                                  % ("moduli" if args.method == "crt" else "slice_products")},
             "other_method": alt,
+            "tc_autotune": crt_tuned,
             "kernel_ms_per_step": {k: v / args.steps for k, v in prof.ms.items()},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "TFLOP/s", "ms_per_step": ms_e2e,

@@ -82,7 +82,8 @@ int oz_grid_for(int sms, int64_t M, int64_t N, int engine);
 // Constants of the CRT mode, fixed by the moduli table; passed by value to the kernels.
 struct CrtModuli {                  // per modulus g (independent of how many a call uses)
   uint32_t p[TC_MAX_MODULI];        // the moduli (pairwise coprime, <= 253)
-  float climb[TC_MAX_MODULI][4];    // split: 2^(13 (l + 1)) mod p, l = 0..3
+  float climb4[TC_MAX_MODULI][3];   // split, t <= 52: 2^(14 (l + 1)) mod p in (-p/2, p/2], l = 0..2
+  float climb5[TC_MAX_MODULI][4];   // split, t > 52: 2^(13 (l + 1)) mod p, l = 0..3
   float pf[TC_MAX_MODULI];          // p as a float
   float pinv[TC_MAX_MODULI];        // fl32(1 / p)
 };

@@ -168,10 +168,16 @@ CrtTable build_table() {
     md.p[g] = p;
     md.pf[g] = static_cast<float>(p);
     md.pinv[g] = 1.0f / static_cast<float>(p);
-    uint64_t pw = 1;   // 2^(13 (l + 1)) mod p
+    uint64_t pw = 1;   // 2^(14 (l + 1)) mod p, taken in (-p/2, p/2]
+    for (int l = 0; l < 3; ++l) {
+      pw = (pw << 14) % p;
+      md.climb4[g][l] = static_cast<float>(2 * pw > p ? static_cast<int64_t>(pw) - static_cast<int64_t>(p)
+                                                      : static_cast<int64_t>(pw));
+    }
+    pw = 1;   // 2^(13 (l + 1)) mod p
     for (int l = 0; l < 4; ++l) {
       pw = (pw << 13) % p;
-      md.climb[g][l] = static_cast<float>(pw);
+      md.climb5[g][l] = static_cast<float>(pw);
     }
   }
   for (int n = 1; n <= TC_MAX_MODULI; ++n) {
@@ -564,30 +570,45 @@ __device__ __forceinline__ uint64_t crt_fixed_point(double x, int e, int SB) {
   return (bits >> 63) ? 0ull - mag : mag;
 }
 
-// Balanced digits of Y = round-half-away(x 2^(t - e)) (|Y| <= 2^t, t <= 62):
-// Y = sum_{l<4} d_l 2^(13 l) + d_4 2^52 with d_0..d_3 in [-4096, 4095] and |d_4| <= 1024, as
-// exact FP32 values.  Y + BAL (BAL = 4096 (1 + 2^13 + 2^26 + 2^39)) has the low digits + 4096
-// in its four 13-bit fields and d_4 in its signed top 12 bits.
-__device__ __forceinline__ void crt_digits(double x, int e, int tbits, bool nonfinite, float (&d)[5]) {
-  constexpr float DBIAS = 8388608.0f + 4096.0f;
-  constexpr unsigned long long BAL = 4096ull * (1ull + (1ull << 13) + (1ull << 26) + (1ull << 39));
+// Balanced digits of Y = round-half-away(x 2^(t - e)) (|Y| <= 2^t), as exact FP32 values.
+//   ND = 4 (t <= 52): Y = d_0 + d_1 2^14 + d_2 2^28 + d_3 2^42, d_0..d_2 in [-8192, 8191],
+//        |d_3| <= 1024: the fields of Y + 8192 (1 + 2^14 + 2^28) and its signed top bits
+//   ND = 5 (t <= 62): Y = sum_{l<4} d_l 2^(13 l) + d_4 2^52, d_0..d_3 in [-4096, 4095],
+//        |d_4| <= 1024: the fields of Y + 4096 (1 + 2^13 + 2^26 + 2^39) and its top bits
+template <int ND>
+__device__ __forceinline__ void crt_digits(double x, int e, int tbits, bool nonfinite, float (&d)[ND]) {
+  constexpr int W = (ND == 4) ? 14 : 13;
+  constexpr uint32_t MASK = (1u << W) - 1u, H = 1u << (W - 1);
+  constexpr float DBIAS = 8388608.0f + static_cast<float>(H);
+  constexpr unsigned long long BAL = (ND == 4) ? 8192ull * (1ull + (1ull << 14) + (1ull << 28))
+                                               : 4096ull * (1ull + (1ull << 13) + (1ull << 26) + (1ull << 39));
   const uint64_t u = (nonfinite ? 0ull : crt_fixed_point(x, e, tbits + 1)) + BAL;
+  const uint32_t lo = static_cast<uint32_t>(u), hi = static_cast<uint32_t>(u >> 32);
 #pragma unroll
-  for (int l = 0; l < 4; ++l)
-    d[l] = __uint_as_float(0x4B000000u | (static_cast<uint32_t>(u >> (13 * l)) & 0x1FFFu)) - DBIAS;
-  const uint32_t top = static_cast<uint32_t>(static_cast<int64_t>(u) >> 52) + 4096u;
-  d[4] = __uint_as_float(0x4B000000u | (top & 0x1FFFu)) - DBIAS;
+  for (int l = 0; l < ND - 1; ++l) {
+    const int sh = W * l;
+    const uint32_t field = (sh < 32 ? __funnelshift_r(lo, hi, sh) : hi >> (sh - 32)) & MASK;
+    d[l] = __uint_as_float(0x4B000000u | field) - DBIAS;
+  }
+  const uint32_t top = static_cast<uint32_t>(static_cast<int32_t>(hi) >> (W * (ND - 1) - 32)) + H;
+  d[ND - 1] = __uint_as_float(0x4B000000u | (top & MASK)) - DBIAS;
 }
 
 // Residues of 8 elements (digits d[.][j]) modulo p, packed as BF16 pairs.  Per element
-//   s = d_0 + sum_{l>=1} d_l (2^(13 l) mod p)     |s| <= 4096 (1 + 3 * 252) + 1024 * 252 < 2^22,
-//                                                 exact in FP32 (four FMAs)
-//   r = s - p rint(s / p)                         |r| <= p/2 + 1/2, so |r| <= 127
+//   s = d_0 + sum_{l>=1} d_l c_l     ND = 4: c_l = 2^(14 l) mod p in (-p/2, p/2],
+//                                      |s| <= 8192 (1 + 2 * 126) + 1024 * 126 < 2^22;
+//                                    ND = 5: c_l = 2^(13 l) mod p in [0, p),
+//                                      |s| <= 4096 (1 + 3 * 252) + 1024 * 252 < 2^22;
+//                                    exact in FP32 (ND - 1 FMAs)
+//   r = s - p rint(s / p)            |r| <= p/2 + 1/2, so |r| <= 127
 // all on the FMA pipe; r has at most 7 significant bits, so its BF16 is the upper half of its
 // FP32 bits.
-__device__ __forceinline__ uint4 crt_residues8(const float (&d)[5][8], const CrtModuli& mod, int g) {
+template <int ND>
+__device__ __forceinline__ uint4 crt_residues8(const float (&d)[ND][8], const CrtModuli& mod, int g) {
   constexpr float MAGIC = 12582912.0f;   // 1.5 * 2^23: x + MAGIC - MAGIC = rint(x), |x| < 2^22
-  const float c1 = mod.climb[g][0], c2 = mod.climb[g][1], c3 = mod.climb[g][2], c4 = mod.climb[g][3];
+  float c[ND - 1];
+#pragma unroll
+  for (int l = 0; l < ND - 1; ++l) c[l] = (ND == 4) ? mod.climb4[g][l] : mod.climb5[g][l];
   const float pf = mod.pf[g], inv = mod.pinv[g];
   uint32_t packed[4];
 #pragma unroll
@@ -595,10 +616,9 @@ __device__ __forceinline__ uint4 crt_residues8(const float (&d)[5][8], const Crt
     float rr[2];
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
-      float sj = fmaf(d[1][j + h], c1, d[0][j + h]);
-      sj = fmaf(d[2][j + h], c2, sj);
-      sj = fmaf(d[3][j + h], c3, sj);
-      sj = fmaf(d[4][j + h], c4, sj);
+      float sj = d[0][j + h];
+#pragma unroll
+      for (int l = 1; l < ND; ++l) sj = fmaf(d[l][j + h], c[l - 1], sj);
       const float q = fmaf(sj, inv, MAGIC) - MAGIC;
       rr[h] = fmaf(-pf, q, sj);
     }
@@ -615,6 +635,22 @@ __device__ __forceinline__ void store_residues(__nv_bfloat16* dst, uint4 v, int 
     unsigned short* d2 = reinterpret_cast<unsigned short*>(dst);
     for (int j = 0; j < nvalid; ++j) d2[j] = static_cast<unsigned short>(w[j / 2] >> (16 * (j & 1)));
   }
+}
+
+// Digits and residue planes of 8 consecutive k of one row: plane g at out0 + g * plane_stride.
+template <int ND>
+__device__ __forceinline__ void crt_split8(const double (&x)[8], int e, int tbits, bool nonfinite, int nmod,
+                                           const CrtModuli& mod, __nv_bfloat16* out0, int64_t plane_stride,
+                                           int nvalid) {
+  float d[ND][8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    float dj[ND];
+    crt_digits<ND>(x[j], e, tbits, nonfinite, dj);
+#pragma unroll
+    for (int l = 0; l < ND; ++l) d[l][j] = dj[l];
+  }
+  for (int g = 0; g < nmod; ++g) store_residues(out0 + g * plane_stride, crt_residues8<ND>(d, mod, g), nvalid);
 }
 
 // k contiguous: one thread = one row and 8 consecutive k, neighbouring threads neighbouring k
@@ -635,17 +671,13 @@ __global__ void __launch_bounds__(256) crt_split_kc_kernel(const double* __restr
   const bool nonfinite = (e == OZ_EXP_NONFINITE);
   const int nvalid = static_cast<int>(K - k0 < 8 ? K - k0 : 8);
   const double* src = X + r * rs + k0 * ks;
-  float d[5][8];
+  double x[8];
 #pragma unroll
-  for (int j = 0; j < 8; ++j) {
-    float dj[5];
-    crt_digits((j < nvalid) ? src[j * ks] : 0.0, e, tbits, nonfinite, dj);
-#pragma unroll
-    for (int l = 0; l < 5; ++l) d[l][j] = dj[l];
-  }
+  for (int j = 0; j < 8; ++j) x[j] = (j < nvalid) ? src[j * ks] : 0.0;
   __nv_bfloat16* out0 = planes + r * pitch + k0;
   const int64_t plane_stride = R * pitch;
-  for (int g = 0; g < nmod; ++g) store_residues(out0 + g * plane_stride, crt_residues8(d, mod, g), nvalid);
+  if (tbits <= 52) crt_split8<4>(x, e, tbits, nonfinite, nmod, mod, out0, plane_stride, nvalid);
+  else crt_split8<5>(x, e, tbits, nonfinite, nmod, mod, out0, plane_stride, nvalid);
 }
 
 // Rows contiguous (element (r, k) at X[r + k ks]): warp w of a CTA owns rows 4w..4w+3 of a
@@ -673,17 +705,10 @@ __global__ void __launch_bounds__(256) crt_split_rc_kernel(const double* __restr
   double x[8];
 #pragma unroll
   for (int j = 0; j < 8; ++j) x[j] = (j < nvalid) ? src[j * ks] : 0.0;
-  float d[5][8];
-#pragma unroll
-  for (int j = 0; j < 8; ++j) {
-    float dj[5];
-    crt_digits(x[j], e, tbits, nonfinite, dj);
-#pragma unroll
-    for (int l = 0; l < 5; ++l) d[l][j] = dj[l];
-  }
   __nv_bfloat16* out0 = planes + r * pitch + k0;
   const int64_t plane_stride = R * pitch;
-  for (int g = 0; g < nmod; ++g) store_residues(out0 + g * plane_stride, crt_residues8(d, mod, g), nvalid);
+  if (tbits <= 52) crt_split8<4>(x, e, tbits, nonfinite, nmod, mod, out0, plane_stride, nvalid);
+  else crt_split8<5>(x, e, tbits, nonfinite, nmod, mod, out0, plane_stride, nvalid);
 }
 
 int crt_split(const double* X, int64_t R, int64_t K, int64_t rs, int64_t ks, const unsigned long long* amax_bits,

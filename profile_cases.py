@@ -12,6 +12,7 @@ cases:
   ozaki          gb_gemm_f64 OZAKI (stats, split, slice products), 4096 x 4096 x 8192
   ozaki_crt      gb_gemm_f64 OZAKI_CRT, 15 moduli (stats, residue split, residue products,
                  CRT combine), 4096 x 4096 x 8192
+  ozaki_crt_auto the same with the automatic plan (statistics with the planner's sums)
   grouped_f64    gb_gemm_grouped_f64, 4096 problems with m, n, k log-uniform in [8, 512]
   grouped_f32    the same problems in FP32 (tuned configuration of the bench)
   adjoint        gb_gemm_adjoint_f32, A 4096 x 2048, B 2048 x 4096
@@ -59,12 +60,12 @@ def case_ozaki():
     return _timed(lambda: api.gemm_(C, A, B, mode="ozaki", slices=10))
 
 
-def case_ozaki_crt():
+def case_ozaki_crt(moduli=15):
     M, N, K = 4096, 4096, 8192
     A = _dev_cm(workloads.ozaki_matrix(M, K, per="row", stream=1))
     B = _dev_cm(workloads.ozaki_matrix(K, N, per="col", stream=2))
     C = torch.empty((N, M), dtype=torch.float64, device="cuda").t()
-    return _timed(lambda: api.gemm_(C, A, B, mode="ozaki_crt", slices=15))
+    return _timed(lambda: api.gemm_(C, A, B, mode="ozaki_crt", slices=moduli))
 
 
 def case_grouped(dtype=torch.float64, tuning=None):
@@ -102,6 +103,7 @@ CASES = {
     "native_f32": lambda: case_native(torch.float32, 4096),
     "ozaki": case_ozaki,
     "ozaki_crt": case_ozaki_crt,
+    "ozaki_crt_auto": lambda: case_ozaki_crt(0),
     "grouped_f64": case_grouped,
     "grouped_f32": lambda: case_grouped(torch.float32, [0, 0, 1, 1, 3, 5]),
     "adjoint": case_adjoint,
