@@ -14,7 +14,7 @@ cases:
                  CRT combine), 4096 x 4096 x 8192
   ozaki_crt_auto the same with the automatic plan (statistics with the planner's sums)
   grouped_f64    gb_gemm_grouped_f64, 4096 problems with m, n, k log-uniform in [8, 512]
-  grouped_f32    the same problems in FP32 (tuned configuration of the bench)
+  grouped_f32    the same problems in FP32 (default configuration: tiles chosen per problem)
   adjoint        gb_gemm_adjoint_f32, A 4096 x 2048, B 2048 x 4096
   semiring_f32   gb_gemm_semiring_f32 (min, +), 4096^3
   f32_bf16x3     gb_gemm_f32_ex BF16X3 (term split, 3 term products), 4096^3
@@ -105,7 +105,7 @@ CASES = {
     "ozaki_crt": case_ozaki_crt,
     "ozaki_crt_auto": lambda: case_ozaki_crt(0),
     "grouped_f64": case_grouped,
-    "grouped_f32": lambda: case_grouped(torch.float32, [0, 0, 1, 1, 3, 5]),
+    "grouped_f32": lambda: case_grouped(torch.float32),
     "adjoint": case_adjoint,
     "semiring_f32": case_semiring,
     "f32_bf16x3": lambda: case_native(torch.float32, 4096, "bf16x3"),
