@@ -139,7 +139,8 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const void* tmap, uint64_
 }
 
 // 2-D tiled store shared -> global (bulk-group completion): the box at coordinates {c0, c1}
-// of the tensor map; parts of the box outside the tensor are not written.
+// of the tensor map.  Callers store boxes that lie wholly inside the tensor (a box crossing the
+// innermost dimension's end was seen to write up to the next 16-byte boundary).
 __device__ __forceinline__ void tma_store_2d(const void* tmap, const void* src, int c0, int c1) {
   asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%2, %3}], [%1];" ::"l"(
                    reinterpret_cast<uint64_t>(tmap)),

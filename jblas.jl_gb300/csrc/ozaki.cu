@@ -315,16 +315,26 @@ __global__ void __launch_bounds__(256) stats_kc2_kernel(const double* __restrict
   const int64_t K2 = K / 2;
   RunStats rs_;
   int64_t k = lane;
-  for (; k + 96 < K2; k += 128) {
-    const ulonglong2 b0 = row[k], b1 = row[k + 32], b2 = row[k + 64], b3 = row[k + 96];
-    rs_.add(b0.x, SUMS);
-    rs_.add(b0.y, SUMS);
-    rs_.add(b1.x, SUMS);
-    rs_.add(b1.y, SUMS);
-    rs_.add(b2.x, SUMS);
-    rs_.add(b2.y, SUMS);
-    rs_.add(b3.x, SUMS);
-    rs_.add(b3.y, SUMS);
+  // software-pipelined: the next four 16-byte loads are in flight while the current four are
+  // folded in (the data-dependent branches of the running statistics would otherwise keep the
+  // compiler from hoisting them)
+  if (k + 96 < K2) {
+    ulonglong2 b[4] = {row[k], row[k + 32], row[k + 64], row[k + 96]};
+    for (; k + 128 + 96 < K2; k += 128) {
+      const ulonglong2 n[4] = {row[k + 128], row[k + 160], row[k + 192], row[k + 224]};
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        rs_.add(b[q].x, SUMS);
+        rs_.add(b[q].y, SUMS);
+        b[q] = n[q];
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      rs_.add(b[q].x, SUMS);
+      rs_.add(b[q].y, SUMS);
+    }
+    k += 128;
   }
   for (; k < K2; k += 32) {
     const ulonglong2 b = row[k];
@@ -375,17 +385,25 @@ __global__ void __launch_bounds__(256) stats_rc2_kernel(const double* __restrict
   if (r < R) {
     const int64_t h = r >> 1, hs = ks >> 1;   // pair index of (r, k): (r + k ks) / 2
     int64_t k = k0 + tk;
-    for (; k + 24 < k1; k += 32) {
-      const ulonglong2 b0 = Xb[h + k * hs], b1 = Xb[h + (k + 8) * hs];
-      const ulonglong2 b2 = Xb[h + (k + 16) * hs], b3 = Xb[h + (k + 24) * hs];
-      s0.add(b0.x, SUMS);
-      s1.add(b0.y, SUMS);
-      s0.add(b1.x, SUMS);
-      s1.add(b1.y, SUMS);
-      s0.add(b2.x, SUMS);
-      s1.add(b2.y, SUMS);
-      s0.add(b3.x, SUMS);
-      s1.add(b3.y, SUMS);
+    // software-pipelined as in stats_kc2_kernel
+    if (k + 24 < k1) {
+      ulonglong2 b[4] = {Xb[h + k * hs], Xb[h + (k + 8) * hs], Xb[h + (k + 16) * hs], Xb[h + (k + 24) * hs]};
+      for (; k + 32 + 24 < k1; k += 32) {
+        const ulonglong2 n[4] = {Xb[h + (k + 32) * hs], Xb[h + (k + 40) * hs], Xb[h + (k + 48) * hs],
+                                 Xb[h + (k + 56) * hs]};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          s0.add(b[q].x, SUMS);
+          s1.add(b[q].y, SUMS);
+          b[q] = n[q];
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        s0.add(b[q].x, SUMS);
+        s1.add(b[q].y, SUMS);
+      }
+      k += 32;
     }
     for (; k < k1; k += 8) {
       const ulonglong2 b = Xb[h + k * hs];

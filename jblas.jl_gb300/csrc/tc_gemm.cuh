@@ -122,7 +122,7 @@ void tc_set_engine(int e);
 int make_plane_tmap(CUtensorMap* map, const void* base, int64_t K, int64_t rows, int64_t slices,
                     int64_t pitch, int box_rows);
 // 2-D FP32 tensor map over a column-major M x N matrix C (leading dimension ldc), box 32 x 32,
-// for the TMA-store epilogue.  false when C's layout does not allow one (base not 16-byte
+// for the TMA-store epilogue (which stores only boxes lying wholly inside C).  false when C's layout does not allow one (base not 16-byte
 // aligned, ldc not a multiple of 4, sizes beyond the map's range); the caller then stores directly.
 bool make_c_tmap_f32(CUtensorMap* map, const void* C, int64_t M, int64_t N, int64_t ldc);
 

@@ -374,10 +374,12 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(P2Shape<EPI>::THREAD
             tc_wait_ld();
             const int64_t colb = n0 + cb;
             if (EPI == TC_EPI_F32) {
-              if (prm.c_tma && beta == 0.0) {
-                // C through shared memory and a TMA store of the warp's 32 x 32 box (rows and
-                // columns outside C are clipped by the copy); the box buffer is reused once the
-                // previous store of this warp has read it
+              if (prm.c_tma && beta == 0.0 && row - lane + 32 <= P.M && colb + 32 <= P.N) {
+                // C through shared memory and a TMA store of the warp's 32 x 32 box; boxes that
+                // reach past C's last row or column take the direct stores below (measured: a
+                // store box that crosses the last row was not clipped at the row but at the next
+                // 16-byte boundary, writing rows of the caller's padding).  The box buffer is
+                // reused once the previous store of this warp has read it.
                 float* cbuf = reinterpret_cast<float*>(smem + P2_CSTAGE_OFF + (warp - 2) * 4096);
                 const float fa = static_cast<float>(alpha);
                 if (lane == 0) bulk_wait_read_all();
