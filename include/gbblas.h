@@ -285,7 +285,8 @@ typedef struct {
 } gb_grouped_tuning_t;
 
 GB_API int gb_grouped_default_tuning(int dtype_bytes, gb_grouped_tuning_t* out);
-/* Device workspace a grouped call over `count` problems needs (prefix sums of tiles). */
+/* Device workspace a grouped call over `count` problems needs (tile prefix sums and the schedule
+ * order: 8 (count + 1 + (count + 1) / 2) bytes). */
 GB_API size_t gb_grouped_workspace_size(int count);
 /* All `count` products (table `problems` in DEVICE memory) in one persistent launch after
  * a prologue that counts tiles per problem.  tuning NULL = defaults.  workspace NULL =
@@ -303,9 +304,9 @@ GB_API int gb_gemm_grouped_f32(const gb_problem_t* problems, int count, const gb
  * cannot allocate device memory when they multiply: threads that must not block on the
  * implicit device synchronisation of cudaMalloc/cudaFree (a latency-bound serving loop, a
  * callback running under another library's lock), and hosts whose device memory is
- * entirely owned by another runtime or allocator.  The tile prefix sums live in a
- * file-scope device array of GB_GROUPED_NOALLOC_MAX + 1 int64 (512 KiB), which every GPU
- * that loads the library keeps until the process exits.  count above the maximum gives
+ * entirely owned by another runtime or allocator.  The call's scratch (tile prefix sums and the
+ * order in which the problems are scheduled) lives in a file-scope device array of 98,305
+ * int64 (768 KiB), which every GPU that loads the library keeps until the process exits.  count above the maximum gives
  * GB_ERR_INVALID_VALUE.  The first call on a device looks the array's device address up
  * (cudaGetSymbolAddress, no allocation); make that first call before any stream capture.
  * Every call shares the one array: calls that overlap on the GPU (other streams, other

@@ -239,27 +239,63 @@ __device__ __forceinline__ void scale_tile(const gb_problem_t& p, int64_t m0, in
   }
 }
 
-// Prologue: tiles per problem under the tuning table, exclusive prefix sum into
-// offsets[0..count]; one block, each thread scans a contiguous chunk.
 __device__ __forceinline__ int prologue_config(const gb_grouped_tuning_t& tuning, const gb_problem_t& p, bool f32) {
   const int c = config_of(tuning, size_class(p.m, p.n));
   return f32 ? problem_config<GROUPED_CONFIGS_F32>(c, p.m, p.n, p.k) : problem_config<GROUPED_CONFIGS_F64>(c, p.m, p.n, p.k);
 }
 
+// Workspace of a call over `count` problems (int64 words): the tile prefix sums in schedule
+// order offsets[0..count], then the schedule order (count int32 problem indices).
+__host__ __device__ inline long long* grouped_order_words(long long* ws, int count) { return ws + count + 1; }
+
+// Prologue (one block): the schedule orders the problems by the work of one of their tiles
+// (tile rows x tile columns x k, in 32 power-of-two buckets, heaviest first), so that the CTAs,
+// striding over the schedule, take tiles of similar length side by side and the short ones
+// fill the tail; it writes the order and the exclusive prefix sums of the tiles in that order.
+// The order inside a bucket depends on timing, which changes no result (each tile is
+// independent).
 __global__ void __launch_bounds__(1024) grouped_prefix_kernel(const gb_problem_t* __restrict__ probs, int count,
                                                               gb_grouped_tuning_t tuning, bool f32,
-                                                              long long* __restrict__ offsets) {
+                                                              long long* __restrict__ ws) {
   __shared__ long long part[1024];
+  __shared__ int hist[32], start[32];
+  long long* offsets = ws;
+  int* order = reinterpret_cast<int*>(grouped_order_words(ws, count));
   const int t = threadIdx.x;
+  if (t < 32) hist[t] = 0;
+  __syncthreads();
+  auto bucket_of = [&](const gb_problem_t& p, const TileCfg& c) {
+    const long long w = static_cast<long long>(c.bm) * c.bn * (p.k > 1 ? p.k : 1);
+    const int lg = 63 - __clzll(w);                 // w >= 1
+    return 31 - (lg > 31 ? 31 : lg);                 // heavy first
+  };
+  for (int i = t; i < count; i += 1024) {
+    const gb_problem_t& p = probs[i];
+    atomicAdd(&hist[bucket_of(p, tile_cfg(prologue_config(tuning, p, f32)))], 1);
+  }
+  __syncthreads();
+  if (t == 0) {
+    int run = 0;
+    for (int b = 0; b < 32; ++b) {
+      start[b] = run;
+      run += hist[b];
+    }
+  }
+  __syncthreads();
+  for (int i = t; i < count; i += 1024) {
+    const gb_problem_t& p = probs[i];
+    order[atomicAdd(&start[bucket_of(p, tile_cfg(prologue_config(tuning, p, f32)))], 1)] = i;
+  }
+  __syncthreads();
   const int per = (count + 1023) / 1024;
   const int b = t * per, e = min(count, b + per);
-  long long sum = 0;
-  for (int i = b; i < e; ++i) {
-    const gb_problem_t& p = probs[i];
+  auto tiles_of = [&](int pos) -> long long {
+    const gb_problem_t& p = probs[order[pos]];
     const TileCfg c = tile_cfg(prologue_config(tuning, p, f32));
-    const long long tiles = (p.m <= 0 || p.n <= 0) ? 0 : ((p.m + c.bm - 1) / c.bm) * ((p.n + c.bn - 1) / c.bn);
-    sum += tiles;
-  }
+    return (p.m <= 0 || p.n <= 0) ? 0 : ((p.m + c.bm - 1) / c.bm) * ((p.n + c.bn - 1) / c.bn);
+  };
+  long long sum = 0;
+  for (int i = b; i < e; ++i) sum += tiles_of(i);
   part[t] = sum;
   __syncthreads();
   for (int off = 1; off < 1024; off <<= 1) {   // inclusive Hillis-Steele scan of the parts
@@ -271,27 +307,28 @@ __global__ void __launch_bounds__(1024) grouped_prefix_kernel(const gb_problem_t
   long long run = (t == 0) ? 0 : part[t - 1];
   for (int i = b; i < e; ++i) {
     offsets[i] = run;
-    const gb_problem_t& p = probs[i];
-    const TileCfg c = tile_cfg(prologue_config(tuning, p, f32));
-    run += (p.m <= 0 || p.n <= 0) ? 0 : ((p.m + c.bm - 1) / c.bm) * ((p.n + c.bn - 1) / c.bn);
+    run += tiles_of(i);
   }
   if (t == 1023) offsets[count] = part[1023];
 }
 
+// Persistent tile loop: CTA b takes tiles b, b + grid, ... of the schedule.
 template <typename T>
 __global__ void __launch_bounds__(GROUPED_THREADS, 2) grouped_gemm_kernel(const gb_problem_t* __restrict__ probs,
                                                                        int count, gb_grouped_tuning_t tuning,
-                                                                       const long long* __restrict__ offsets) {
+                                                                       long long* __restrict__ ws) {
   __shared__ __align__(16) unsigned char smem[GROUPED_SMEM];
+  const long long* offsets = ws;
+  const int* order = reinterpret_cast<const int*>(grouped_order_words(ws, count));
   const long long total = offsets[count];
   for (long long w = blockIdx.x; w < total; w += gridDim.x) {
-    // problem index: last p with offsets[p] <= w (problems with no tiles share offsets)
+    // schedule position: last pos with offsets[pos] <= w (problems with no tiles share offsets)
     int lo = 0, hi = count - 1;
     while (lo < hi) {
       const int mid = (lo + hi + 1) >> 1;
       if (offsets[mid] <= w) lo = mid; else hi = mid - 1;
     }
-    const gb_problem_t p = probs[lo];
+    const gb_problem_t p = probs[order[lo]];
     const int cfg = prologue_config(tuning, p, sizeof(T) == 4);
     const TileCfg c = tile_cfg(cfg);
     const long long local = w - offsets[lo];
@@ -319,19 +356,19 @@ __global__ void __launch_bounds__(GROUPED_THREADS, 2) grouped_gemm_kernel(const 
       T* C = static_cast<T*>(p.C);
       T* sm = reinterpret_cast<T*>(smem);
       const int64_t m0 = static_cast<int64_t>(tm) * c.bm, n0 = static_cast<int64_t>(tn) * c.bn;
-#define GB_GTILE(BM_, BN_, TM_, TN_)                                                                      \
-  simt_tile<T, GroupedChainOp<T>, BM_, BN_, 16, TM_, TN_, false, false>(p.m, p.n, p.k, op, A, p.lda, B, p.ldb, C, \
-                                                                       p.ldc, m0, n0, sm)
+#define GB_GTILE(BM_, BN_, BK_, TM_, TN_)                                                                    \
+  simt_tile<T, GroupedChainOp<T>, BM_, BN_, BK_, TM_, TN_, false, false>(p.m, p.n, p.k, op, A, p.lda, B, p.ldb, C, \
+                                                                        p.ldc, m0, n0, sm)
       switch (cfg) {
-        case 1: GB_GTILE(32, 32, 2, 2); break;
-        case 2: GB_GTILE(64, 32, 4, 2); break;
-        case 3: GB_GTILE(64, 64, 4, 4); break;
-        case 4: GB_GTILE(128, 64, 8, 4); break;
-        case 5: GB_GTILE(128, 128, 8, 8); break;
-        case 6: GB_GTILE(32, 64, 2, 4); break;
-        case 7: GB_GTILE(64, 128, 4, 8); break;
-        case 8: GB_GTILE(128, 32, 8, 2); break;
-        default: GB_GTILE(32, 128, 2, 8); break;
+        case 1: GB_GTILE(32, 32, 16, 2, 2); break;
+        case 2: GB_GTILE(64, 32, 16, 4, 2); break;
+        case 3: GB_GTILE(64, 64, 16, 4, 4); break;
+        case 4: GB_GTILE(128, 64, 16, 8, 4); break;
+        case 5: GB_GTILE(128, 128, 16, 8, 8); break;
+        case 6: GB_GTILE(32, 64, 16, 2, 4); break;
+        case 7: GB_GTILE(64, 128, 16, 4, 8); break;
+        case 8: GB_GTILE(128, 32, 16, 8, 2); break;
+        default: GB_GTILE(32, 128, 16, 2, 8); break;
       }
 #undef GB_GTILE
       __syncthreads();   // the next tile reuses the shared panels
@@ -404,7 +441,8 @@ int grouped_launch(int dtype_bytes, const gb_problem_t* d_probs, int count, cons
 }
 
 size_t grouped_workspace_bytes(int count) {
-  return (static_cast<size_t>(count) + 1) * sizeof(long long);
+  // prefix sums (count + 1), the order (count int32 in (count + 1) / 2 words)
+  return (static_cast<size_t>(count) + 1 + (static_cast<size_t>(count) + 1) / 2) * sizeof(long long);
 }
 
 // Autotuner: for every size class present, time each configuration on that class's
@@ -426,7 +464,7 @@ int grouped_autotune(int dtype_bytes, const gb_problem_t* h_probs, int count, in
   long long* d_off = nullptr;
   GB_CUDA_TRY(cudaMallocFromPoolAsync(&scratch, max_c * dtype_bytes, pool, s));
   GB_CUDA_TRY(cudaMallocFromPoolAsync(reinterpret_cast<void**>(&d_sub), sizeof(gb_problem_t) * (count + 1), pool, s));
-  GB_CUDA_TRY(cudaMallocFromPoolAsync(reinterpret_cast<void**>(&d_off), sizeof(long long) * (count + 1), pool, s));
+  GB_CUDA_TRY(cudaMallocFromPoolAsync(reinterpret_cast<void**>(&d_off), grouped_workspace_bytes(count), pool, s));
   cudaEvent_t e0, e1;
   GB_CUDA_TRY(cudaEventCreate(&e0));
   GB_CUDA_TRY(cudaEventCreate(&e1));
@@ -489,7 +527,9 @@ namespace gb {
 constexpr int GROUPED_NOALLOC_MAX = GB_GROUPED_NOALLOC_MAX;
 constexpr int NOALLOC_MAX_DEVICES = 64;
 
-static __device__ __align__(256) long long g_noalloc_offsets[GROUPED_NOALLOC_MAX + 1];
+// int64 words of grouped_workspace_bytes(GROUPED_NOALLOC_MAX): 98,305 (768 KiB)
+constexpr int GROUPED_NOALLOC_WORDS = GROUPED_NOALLOC_MAX + 1 + (GROUPED_NOALLOC_MAX + 1) / 2;
+static __device__ __align__(256) long long g_noalloc_offsets[GROUPED_NOALLOC_WORDS];
 
 // Device address of g_noalloc_offsets per device.  In host code the symbol names a host
 // stand-in, so the address is looked up once per device (with that device current) and
@@ -532,7 +572,8 @@ int grouped_f64_noalloc(const gb_problem_t* d_probs, int count, const gb_grouped
   const gb_grouped_tuning_t t = tuning ? *tuning : grouped_default_tuning(8);
   rc = grouped_validate_tuning(8, t);
   if (rc) return rc;
-  // The prologue rewrites offsets[0..count] on every call, so nothing needs clearing.
+  // The prologue rewrites the prefix sums and the order on every call, so nothing needs
+  // clearing.
   // Launched directly, not through the timing hooks (which create CUDA events while profiling
   // is on); gb_launch_counts still counts both launches.
   grouped_prefix_kernel<<<1, 1024, 0, s>>>(d_probs, count, t, false, offsets);

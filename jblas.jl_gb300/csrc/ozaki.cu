@@ -176,7 +176,22 @@ struct RunStats {
   __device__ __forceinline__ void add(unsigned long long bits, bool sums) {
     const unsigned long long a = bits & 0x7FFFFFFFFFFFFFFFull;
     mx = a > mx ? a : mx;
-    if (!sums || a == 0) return;
+    if (!sums) return;
+    // Fast path: a normal element whose exponent field does not exceed the running one
+    // (e > -2000 once an element has been seen; e = field - 1022 for a normal maximum).  Its
+    // scaled value |x| 2^-e truncated to FP32 takes the exponent field - e - 896 and the top 23
+    // fraction bits; below FP32's normal range it is 0, as in scaled_f32_trunc.
+    const uint32_t hi = static_cast<uint32_t>(a >> 32);
+    const int field = static_cast<int>(hi >> 20);
+    if (field != 0 && field != 0x7FF && field - 1022 <= e) {
+      const int fe = field - e - 896;   // (field - 1023) - e + 127
+      const uint32_t frac = __funnelshift_r(static_cast<uint32_t>(a), hi, 29) & 0x7FFFFFu;
+      const float f = fe >= 1 ? __uint_as_float((static_cast<uint32_t>(fe) << 23) | frac) : 0.0f;
+      sa += f;
+      sq = fmaf(f, f, sq);
+      return;
+    }
+    if (a == 0) return;
     const int ea = exp_of_abits(a);
     if (ea == OZ_EXP_NONFINITE) {
       nonfinite = true;
