@@ -314,8 +314,7 @@ __global__ void __launch_bounds__(1024) grouped_prefix_kernel(const gb_problem_t
 
 // Persistent tile loop: CTA b takes tiles b, b + grid, ... of the schedule.
 template <typename T>
-__global__ void __launch_bounds__(GROUPED_THREADS, sizeof(T) == 4 ? 3 : 2)
-    grouped_gemm_kernel(const gb_problem_t* __restrict__ probs,
+__global__ void __launch_bounds__(GROUPED_THREADS, 2) grouped_gemm_kernel(const gb_problem_t* __restrict__ probs,
                                                                        int count, gb_grouped_tuning_t tuning,
                                                                        long long* __restrict__ ws) {
   __shared__ __align__(16) unsigned char smem[GROUPED_SMEM];
@@ -364,20 +363,12 @@ __global__ void __launch_bounds__(GROUPED_THREADS, sizeof(T) == 4 ? 3 : 2)
         case 1: GB_GTILE(32, 32, 16, 2, 2); break;
         case 2: GB_GTILE(64, 32, 16, 4, 2); break;
         case 3: GB_GTILE(64, 64, 16, 4, 4); break;
-        case 4: GB_GTILE(128, 64, 8, 8, 4); break;
-        case 5:   // 128 x 128 as two 128 x 64 halves: the register budget of three CTAs per SM
-          GB_GTILE(128, 64, 8, 8, 4);
-          __syncthreads();
-          {
-            const int64_t n1 = n0 + 64;
-            simt_tile<T, GroupedChainOp<T>, 128, 64, 8, 8, 4, false, false>(p.m, p.n, p.k, op, A, p.lda, B, p.ldb,
-                                                                            C, p.ldc, m0, n1, sm);
-          }
-          break;
+        case 4: GB_GTILE(128, 64, 16, 8, 4); break;
+        case 5: GB_GTILE(128, 128, 16, 8, 8); break;
         case 6: GB_GTILE(32, 64, 16, 2, 4); break;
-        case 7: GB_GTILE(64, 128, 8, 4, 8); break;
-        case 8: GB_GTILE(128, 32, 8, 8, 2); break;
-        default: GB_GTILE(32, 128, 8, 2, 8); break;
+        case 7: GB_GTILE(64, 128, 16, 4, 8); break;
+        case 8: GB_GTILE(128, 32, 16, 8, 2); break;
+        default: GB_GTILE(32, 128, 16, 2, 8); break;
       }
 #undef GB_GTILE
       __syncthreads();   // the next tile reuses the shared panels
