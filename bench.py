@@ -964,12 +964,17 @@ def main():
         del C_alt
     line = None
     if rank == 0:
+        # a CRT call in column panels launches the residue products once per panel: the
+        # algorithmic work and the DRAM traffic of one launch are the call's divided by that
+        launches_per_call = max(1, round(prof.launches.get("ozaki_slice_mma", args.steps) / args.steps))
         mma_ms = prof.ms.get("ozaki_slice_mma", float("nan")) / max(1, prof.launches.get("ozaki_slice_mma", 1))
         peaks, peak_src = load_peaks()
         timed_s = ms_step * args.steps / 1e3
         peak_key = "bf16_tflops_sustained" if timed_s >= 1.0 else "bf16_tflops"
-        achieved = plan["flops_tensor"] / (mma_ms * 1e-3) / 1e12
+        achieved = plan["flops_tensor"] / launches_per_call / (mma_ms * 1e-3) / 1e12
         traffic = committed_traffic(args.method, n) if not args.mnk else None
+        if traffic is not None:
+            traffic /= launches_per_call
 
         # ------------------------------------------------------------ accuracy and native
         import oracle
@@ -1032,14 +1037,19 @@ def main():
             "roofline": {"bound": "tensor", "achieved": achieved, "peak": peaks[peak_key], "unit": "TFLOP/s",
                          "frac": achieved / peaks[peak_key], "traffic": traffic,
                          "traffic_source": "ncu dram__bytes_read.sum + write.sum of a 4096x4096x8192 launch "
-                                           "scaled by 4x the pair tiles (profiles/, a lower bound at 8192^3)",
+                                           "scaled by the pair tiles one launch processes (profiles/, a lower "
+                                           "bound at 8192^3)",
                          "kernel": "ozaki_slice_mma", "ms_per_launch": mma_ms,
+                         "launches_per_call": launches_per_call,
                          "peak_source": "%s %s" % (peak_src, peak_key),
-                         "work": "BF16 tensor flops per launch = %s * 2*M*N*ceil(K/64)*64"
+                         "work": "BF16 tensor flops per launch = %s * 2*M*N*ceil(K/64)*64 / launches_per_call"
                                  % ("moduli" if args.method == "crt" else "slice_products")},
             "other_method": alt,
             "tc_autotune": crt_tuned,
             "kernel_ms_per_step": {k: v / args.steps for k, v in prof.ms.items()},
+            "kernel_ms_note": ("CUDA-event time of each kernel kind per step; with column panels the split of "
+                               "the next panel and the reconstruction of the previous one run beside the "
+                               "residue products, so the kinds can sum to more than ms_per_step"),
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "TFLOP/s", "ms_per_step": ms_e2e,
                     "pipeline": "4-deep ring: uploads run up to 3 steps ahead, the download of step i overlaps step "

@@ -93,6 +93,11 @@ GB_API int gb_set_tc_engine(int engine);
  *              A rows in L2)
  *   tma_store  FP32 outputs (GB_TC_F32, GB_TC_ADJOINT) on the pair engine: 1 = C staged in
  *              shared memory and written by TMA stores (beta = 0), 0 = direct stores
+ *   panels     GB_TC_OZAKI_CRT only (0 elsewhere): C's columns in this many panels (0 or 1 = one;
+ *              at most 4, and at most one per 256 columns); the residue products of panel p
+ *              run on a high-priority stream of the library while the caller's stream splits
+ *              panel p + 1 of B and reconstructs panel p - 1 of C.  Under stream capture a
+ *              call uses one panel.  Results do not depend on it.
  * Size classes by max(M, N): 0 up to 2048, 1 up to 8192, 2 beyond.  gb_set_tc_engine, when set,
  * overrides the engine of every kind. */
 typedef enum { GB_TC_OZAKI_SLICES = 0, GB_TC_OZAKI_CRT = 1, GB_TC_F32 = 2, GB_TC_ADJOINT = 3, GB_TC_KINDS = 4 } gb_tc_kind_t;
@@ -101,10 +106,10 @@ typedef struct {
   int32_t engine;
   int32_t band;
   int32_t tma_store;
-  int32_t reserved;   /* 0 */
+  int32_t panels;
 } gb_tc_tuning_t;
 GB_API int gb_tc_size_class(int64_t M, int64_t N);
-GB_API int gb_tc_default_tuning(int kind, gb_tc_tuning_t* out);
+GB_API int gb_tc_default_tuning(int kind, int size_class, gb_tc_tuning_t* out);
 GB_API int gb_get_tc_tuning(int kind, int size_class, gb_tc_tuning_t* out);
 /* Installs a tuning (NULL = the default) for later calls of that kind and class; an invalid
  * combination gives GB_ERR_INVALID_VALUE. */

@@ -13,6 +13,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <vector>
 
@@ -51,15 +52,59 @@ static std::atomic<uint64_t> g_wait_limit_ns{4000000000ull};
 static std::atomic<uint64_t> g_ozaki_tol_bits{0};
 static std::atomic<int> g_ozaki_min_chunks{1};
 
+// A high-priority stream with the events that fork a call's work onto it and join it back:
+// a CRT call runs its residue products there while its own stream splits the next column panel
+// and reconstructs the previous one.  One call holds a lane at a time.
+struct Lane {
+  static constexpr int EVENTS = 2 * TC_MAX_PANELS + 1;   // fork and join per panel, one for errors
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[EVENTS] = {};
+};
+
 struct DeviceInfo {
   bool init = false;
   int status_code = GB_OK;
   int sms = 0;
   DeviceStatus* status = nullptr;  // device-side status word
   cudaMemPool_t pool = nullptr;    // workspace pool, memory kept across calls
+  std::mutex lane_mu;
+  std::vector<Lane*> free_lanes;   // created on demand, kept until exit
 };
 static std::mutex g_dev_mu;
-static std::vector<DeviceInfo> g_devs;
+// One entry per device ordinal; entries are never moved, so a DeviceInfo* stays valid while
+// other threads set up further devices.
+static std::vector<std::unique_ptr<DeviceInfo>> g_devs;
+
+// A lane of the current device (created on first need), or nullptr when none can be made;
+// the call gives it back with give_lane once its work is enqueued.
+static Lane* take_lane(DeviceInfo* d) {
+  {
+    std::lock_guard<std::mutex> lk(d->lane_mu);
+    if (!d->free_lanes.empty()) {
+      Lane* l = d->free_lanes.back();
+      d->free_lanes.pop_back();
+      return l;
+    }
+  }
+  std::unique_ptr<Lane> l(new Lane);
+  int least = 0, greatest = 0;
+  if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) return nullptr;
+  if (cudaStreamCreateWithPriority(&l->stream, cudaStreamNonBlocking, greatest) != cudaSuccess) return nullptr;
+  for (int i = 0; i < Lane::EVENTS; ++i) {
+    if (cudaEventCreateWithFlags(&l->ev[i], cudaEventDisableTiming) != cudaSuccess) {
+      for (int j = 0; j < i; ++j) cudaEventDestroy(l->ev[j]);
+      cudaStreamDestroy(l->stream);
+      return nullptr;
+    }
+  }
+  return l.release();
+}
+
+static void give_lane(DeviceInfo* d, Lane* l) {
+  if (!l) return;
+  std::lock_guard<std::mutex> lk(d->lane_mu);
+  d->free_lanes.push_back(l);
+}
 
 // Per-device setup: architecture check, SM count, status word.
 static int device_info(DeviceInfo** out) {
@@ -67,7 +112,8 @@ static int device_info(DeviceInfo** out) {
   GB_CUDA_TRY(cudaGetDevice(&dev));
   std::lock_guard<std::mutex> lk(g_dev_mu);
   if (static_cast<int>(g_devs.size()) <= dev) g_devs.resize(dev + 1);
-  DeviceInfo& d = g_devs[dev];
+  if (!g_devs[dev]) g_devs[dev].reset(new DeviceInfo);
+  DeviceInfo& d = *g_devs[dev];
   if (!d.init) {
     d.init = true;
     int major = 0, minor = 0;
@@ -155,7 +201,9 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 }
 
 int make_plane_tmap(CUtensorMap* map, const void* base, int64_t K, int64_t rows, int64_t slices,
-                    int64_t pitch, int box_rows) {
+                    int64_t pitch, int box_rows, int64_t plane_rows) {
+  if (plane_rows == 0) plane_rows = rows;
+  if (plane_rows < rows) return GB_ERR_INVALID_VALUE;
   auto fn = encode_fn();
   if (!fn) {
     std::snprintf(g_last_detail, sizeof(g_last_detail), "cuTensorMapEncodeTiled unavailable");
@@ -164,7 +212,7 @@ int make_plane_tmap(CUtensorMap* map, const void* base, int64_t K, int64_t rows,
   cuuint64_t dims[3] = {static_cast<cuuint64_t>(K), static_cast<cuuint64_t>(rows),
                         static_cast<cuuint64_t>(slices)};
   cuuint64_t strides[2] = {static_cast<cuuint64_t>(pitch * 2),
-                           static_cast<cuuint64_t>(rows * pitch * 2)};
+                           static_cast<cuuint64_t>(plane_rows * pitch * 2)};
   cuuint32_t box[3] = {64u, static_cast<cuuint32_t>(box_rows), 1u};
   cuuint32_t estr[3] = {1u, 1u, 1u};
   CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides, box,
@@ -592,33 +640,93 @@ static int crt_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int64
   uint8_t* res = reinterpret_cast<uint8_t*>(wsp + pa_bytes + pb_bytes);
   int32_t* ea = reinterpret_cast<int32_t*>(wsp + pa_bytes + pb_bytes + res_bytes);
   int32_t* eb = ea + M;
-  rc = crt_split(A, M, K, a_rs, a_ks, os.a.amax_bits, plan_d, pa, pitch, ea, s);
-  if (!rc) rc = crt_split(B, N, K, b_rs, b_ks, os.b.amax_bits, plan_d, pb, pitch, eb, s);
-  if (!rc) {
-    CrtGemmArgs ga;
-    ga.planes_a = pa;
-    ga.planes_b = pb;
-    ga.pitch = pitch;
-    ga.M = M;
-    ga.N = N;
-    ga.K = K;
-    ga.ea = ea;
-    ga.eb = eb;
-    ga.alpha = alpha;
-    ga.beta = beta;
-    ga.C = C;
-    ga.ldc = ldc;
-    ga.res = res;
-    ga.res_ld = mpad;
-    ga.res_plane = mpad * npad;
-    ga.status = dev->status;
-    ga.wait_limit_ns = g_wait_limit_ns.load();
-    const int64_t ctas = 2 * static_cast<int64_t>(tc_pair_tiles(M, N));
+  CrtGemmArgs ga;
+  ga.planes_a = pa;
+  ga.planes_b = pb;
+  ga.pitch = pitch;
+  ga.M = M;
+  ga.N = N;
+  ga.K = K;
+  ga.ea = ea;
+  ga.eb = eb;
+  ga.alpha = alpha;
+  ga.beta = beta;
+  ga.C = C;
+  ga.ldc = ldc;
+  ga.res = res;
+  ga.res_ld = mpad;
+  ga.res_plane = mpad * npad;
+  ga.status = dev->status;
+  ga.wait_limit_ns = g_wait_limit_ns.load();
+  ga.plan = plan_d;
+  const TcTuning tune = tc_tuning_for(TC_KIND_CRT, M, N);
+  ga.band = tune.band;
+  ga.b_plane_rows = N;
+  auto grid_for = [&](int64_t n) {
+    const int64_t ctas = 2 * static_cast<int64_t>(tc_pair_tiles(M, n));
     const int64_t cap = dev->sms & ~1;
-    ga.grid = static_cast<int>(ctas < cap ? ctas : cap);
-    ga.plan = plan_d;
-    ga.band = tc_tuning_for(TC_KIND_CRT, M, N).band;
-    rc = crt_gemm_launch(ga, plan, s);
+    return static_cast<int>(ctas < cap ? ctas : cap);
+  };
+  // Column panels: the residue products of panel p run on a high-priority lane while this
+  // stream splits panel p + 1 of B and reconstructs panel p - 1 of C, on the SMs' spare
+  // registers and issue slots beside the tensor-core kernel.  One panel (the plain sequence
+  // on this stream) when the tuning asks for one and under stream capture; at most one panel
+  // per 256 columns.
+  const int64_t tiles_n = (N + 255) / 256;
+  int panels = tune.panels < 1 ? 1 : tune.panels;
+  if (panels > TC_MAX_PANELS) panels = TC_MAX_PANELS;
+  if (panels > tiles_n) panels = static_cast<int>(tiles_n);
+  cudaStreamCaptureStatus cap_status = cudaStreamCaptureStatusNone;
+  Lane* lane = nullptr;
+  if (panels > 1 && cudaStreamIsCapturing(s, &cap_status) == cudaSuccess && cap_status == cudaStreamCaptureStatusNone)
+    lane = take_lane(dev);
+  rc = crt_split(A, M, K, a_rs, a_ks, os.a.amax_bits, plan_d, pa, pitch, M, ea, s);
+  if (!lane) {
+    if (!rc) rc = crt_split(B, N, K, b_rs, b_ks, os.b.amax_bits, plan_d, pb, pitch, N, eb, s);
+    if (!rc) {
+      ga.grid = grid_for(N);
+      rc = crt_mma_launch(ga, plan, s);
+    }
+    if (!rc) rc = crt_combine_launch(ga, s);
+  } else {
+    // panel boundaries on whole 256-column tiles
+    int64_t n0[TC_MAX_PANELS + 1];
+    for (int p = 0; p <= panels; ++p) {
+      const int64_t c = tiles_n * p / panels * 256;
+      n0[p] = c < N ? c : N;
+    }
+    auto panel_args = [&](int p) {
+      CrtGemmArgs g = ga;
+      g.N = n0[p + 1] - n0[p];
+      g.planes_b = pb + n0[p] * pitch;
+      g.eb = eb + n0[p];
+      g.C = C + n0[p] * ldc;
+      g.res = res + n0[p] * mpad;
+      g.grid = grid_for(g.N);
+      return g;
+    };
+    cudaStream_t hs = lane->stream;
+    auto cu = [&](cudaError_t e) {
+      if (e != cudaSuccess && !rc) rc = gb_set_cuda_error(e, "ozaki crt panel pipeline");
+    };
+    for (int p = 0; p < panels && !rc; ++p) {
+      rc = crt_split(B + n0[p] * b_rs, n0[p + 1] - n0[p], K, b_rs, b_ks, os.b.amax_bits + n0[p], plan_d,
+                     pb + n0[p] * pitch, pitch, N, eb + n0[p], s);
+      if (!rc) cu(cudaEventRecord(lane->ev[2 * p], s));
+      if (!rc) cu(cudaStreamWaitEvent(hs, lane->ev[2 * p], 0));
+      if (!rc) rc = crt_mma_launch(panel_args(p), plan, hs);
+      if (!rc) cu(cudaEventRecord(lane->ev[2 * p + 1], hs));
+    }
+    for (int p = 0; p < panels && !rc; ++p) {
+      cu(cudaStreamWaitEvent(s, lane->ev[2 * p + 1], 0));
+      if (!rc) rc = crt_combine_launch(panel_args(p), s);
+    }
+    if (rc) {
+      // join whatever reached the lane before the error, so the workspace is freed after it
+      if (cudaEventRecord(lane->ev[Lane::EVENTS - 1], hs) == cudaSuccess)
+        cudaStreamWaitEvent(s, lane->ev[Lane::EVENTS - 1], 0);
+    }
+    give_lane(dev, lane);
   }
   if (!rc) {
     PendingCrtPlan& pd = g_pending_crt;
@@ -778,9 +886,10 @@ int gb_tc_size_class(int64_t M, int64_t N) {
   return tc_tune_class(M, N);
 }
 
-int gb_tc_default_tuning(int kind, gb_tc_tuning_t* out) {
-  if (!out || kind < 0 || kind >= GB_TC_KINDS) return GB_ERR_INVALID_VALUE;
-  const TcTuning t = tc_default_tuning(kind);
+int gb_tc_default_tuning(int kind, int size_class, gb_tc_tuning_t* out) {
+  if (!out || kind < 0 || kind >= GB_TC_KINDS || size_class < 0 || size_class >= GB_TC_SIZE_CLASSES)
+    return GB_ERR_INVALID_VALUE;
+  const TcTuning t = tc_default_tuning(kind, size_class);
   std::memcpy(out, &t, sizeof(t));
   return GB_OK;
 }
@@ -797,7 +906,6 @@ int gb_set_tc_tuning(int kind, int size_class, const gb_tc_tuning_t* tuning) {
   if (!tuning) return tc_set_tuning(kind, size_class, nullptr);
   TcTuning t;
   std::memcpy(&t, tuning, sizeof(t));
-  if (t.reserved != 0) return GB_ERR_INVALID_VALUE;
   return tc_set_tuning(kind, size_class, &t);
 }
 

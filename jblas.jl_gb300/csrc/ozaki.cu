@@ -576,7 +576,7 @@ __global__ void __launch_bounds__(256) split_kernel(const double* __restrict__ X
                                                     int64_t rs, int64_t ks,
                                                     const unsigned long long* __restrict__ amax_bits,
                                                     int slices, int bits, __nv_bfloat16* __restrict__ planes,
-                                                    int64_t pitch, int32_t* __restrict__ exps) {
+                                                    int64_t pitch, int64_t plane_stride, int32_t* __restrict__ exps) {
   int64_t r, kc;
   if (RC) {
     r = static_cast<int64_t>(blockIdx.x) * 256 + threadIdx.x;
@@ -595,13 +595,14 @@ __global__ void __launch_bounds__(256) split_kernel(const double* __restrict__ X
 #pragma unroll
   for (int j = 0; j < 16; ++j) x[j] = (j < nvalid) ? src[j * ks] : 0.0;
   __nv_bfloat16* out0 = planes + r * pitch + k0;
-  const int64_t plane_stride = R * pitch;
   split_16<Word>(x, e, slices, bits, out0, plane_stride, nvalid);
 }
 
-int oz_split(const double* X, int64_t R, int64_t K, int64_t rs, int64_t ks,
-             const unsigned long long* amax_bits, int slices, int bits, __nv_bfloat16* planes,
-             int64_t pitch, int32_t* exps, cudaStream_t s) {
+// Rows [0, R) of X; plane_stride = the element distance between consecutive digit planes (the
+// planes of the whole operand: its rows times the pitch, also for a band of its rows).
+static int oz_split_rows(const double* X, int64_t R, int64_t K, int64_t rs, int64_t ks,
+                         const unsigned long long* amax_bits, int slices, int bits, __nv_bfloat16* planes,
+                         int64_t pitch, int64_t plane_stride, int32_t* exps, cudaStream_t s) {
   if (R <= 0 || K <= 0) return GB_OK;
   const int64_t kchunks = (K + 15) / 16;
   const bool wide = slices * bits > 62;
@@ -612,19 +613,20 @@ int oz_split(const double* X, int64_t R, int64_t K, int64_t rs, int64_t ks,
     if (wide)
       GB_LAUNCH(GB_KERNEL_OZAKI_SPLIT, s,
                 (split_kernel<true, unsigned __int128><<<grid, 256, 0, s>>>(X, R, K, rs, ks, amax_bits, slices,
-                                                                             bits, planes, pitch, exps)));
+                                                                             bits, planes, pitch, plane_stride,
+                                                                             exps)));
     else
       GB_LAUNCH(GB_KERNEL_OZAKI_SPLIT, s,
                 (split_kernel<true, uint64_t><<<grid, 256, 0, s>>>(X, R, K, rs, ks, amax_bits, slices, bits,
-                                                                    planes, pitch, exps)));
+                                                                    planes, pitch, plane_stride, exps)));
   } else {
     const int64_t gx = (kchunks + 255) / 256;
     if (R > 65535) {
-      // rows beyond the grid's y range: launch in row bands
+      // rows beyond the grid's y range: launch in row bands (same planes, same plane stride)
       for (int64_t r0 = 0; r0 < R; r0 += 65535) {
         const int64_t rb = (R - r0 < 65535) ? R - r0 : 65535;
-        int rc = oz_split(X + r0 * rs, rb, K, rs, ks, amax_bits + r0, slices, bits, planes + r0 * pitch,
-                          pitch, exps + r0, s);
+        int rc = oz_split_rows(X + r0 * rs, rb, K, rs, ks, amax_bits + r0, slices, bits, planes + r0 * pitch,
+                               pitch, plane_stride, exps + r0, s);
         if (rc) return rc;
       }
       return GB_OK;
@@ -633,14 +635,21 @@ int oz_split(const double* X, int64_t R, int64_t K, int64_t rs, int64_t ks,
     if (wide)
       GB_LAUNCH(GB_KERNEL_OZAKI_SPLIT, s,
                 (split_kernel<false, unsigned __int128><<<grid, 256, 0, s>>>(X, R, K, rs, ks, amax_bits, slices,
-                                                                              bits, planes, pitch, exps)));
+                                                                              bits, planes, pitch, plane_stride,
+                                                                              exps)));
     else
       GB_LAUNCH(GB_KERNEL_OZAKI_SPLIT, s,
                 (split_kernel<false, uint64_t><<<grid, 256, 0, s>>>(X, R, K, rs, ks, amax_bits, slices, bits,
-                                                                     planes, pitch, exps)));
+                                                                     planes, pitch, plane_stride, exps)));
   }
   GB_CUDA_TRY(cudaGetLastError());
   return GB_OK;
+}
+
+int oz_split(const double* X, int64_t R, int64_t K, int64_t rs, int64_t ks,
+             const unsigned long long* amax_bits, int slices, int bits, __nv_bfloat16* planes,
+             int64_t pitch, int32_t* exps, cudaStream_t s) {
+  return oz_split_rows(X, R, K, rs, ks, amax_bits, slices, bits, planes, pitch, R * pitch, exps, s);
 }
 
 // ============================================================== slice products

@@ -168,9 +168,12 @@ int crt_plan_record(CrtPlanRecord** record, unsigned long long* seq);
 size_t crt_plan_scratch_bytes();
 int crt_plan_device(const OzRowStats& sa, const OzRowStats& sb, const CrtPlanParams& pp, CrtDevicePlan* plan,
                     CrtPlanRecord* record, unsigned long long seq, void* scratch, cudaStream_t s);
-// Residue planes (BF16, [modulus][row][pitch], plan->n of them) and row exponents of op(X).
+// Residue planes (BF16, [modulus][row][pitch], plan->n of them) and row exponents of rows
+// [0, R) of op(X); the planes belong to an operand of plane_rows >= R rows (a band of rows
+// passes X, amax_bits, planes and exps offset to its first row, and the operand's row count).
 int crt_split(const double* X, int64_t R, int64_t K, int64_t rs, int64_t ks, const unsigned long long* amax_bits,
-              const CrtDevicePlan* plan, __nv_bfloat16* planes, int64_t pitch, int32_t* exps, cudaStream_t s);
+              const CrtDevicePlan* plan, __nv_bfloat16* planes, int64_t pitch, int64_t plane_rows, int32_t* exps,
+              cudaStream_t s);
 
 struct CrtGemmArgs {
   const void* planes_a;   // [n][M][pitch] bf16
@@ -190,11 +193,15 @@ struct CrtGemmArgs {
   int grid;               // even (CTA pairs)
   const CrtDevicePlan* plan;
   int band;               // pair-tile rows per L2 band of the raster
+  int64_t b_plane_rows;   // rows of the operand whose planes planes_b points into (>= N; a panel
+                          // of columns passes planes_b at its first row)
 };
-// Residue products on the CTA-pair engine, then the CRT reconstruction into C.  `plan`
-// (host) gives the K chunking and a schedule for up to plan.n moduli; the kernels run
-// the device plan's n <= plan.n.
-int crt_gemm_launch(const CrtGemmArgs& a, const CrtPlan& plan, cudaStream_t s);
+// Residue products on the CTA-pair engine (crt_mma_launch), then the CRT reconstruction into C
+// (crt_combine_launch).  `plan` (host) gives the K chunking and a schedule for up to plan.n
+// moduli; the kernels run the device plan's n <= plan.n.  A panel of C's columns passes
+// planes_b, eb, C and res offset to its first column (a multiple of 256) and N = its width.
+int crt_mma_launch(const CrtGemmArgs& a, const CrtPlan& plan, cudaStream_t s);
+int crt_combine_launch(const CrtGemmArgs& a, cudaStream_t s);
 
 
 }  // namespace gb

@@ -471,21 +471,28 @@ __global__ void __launch_bounds__(CRT_PLAN_THREADS) crt_plan_kernel(const OzRowS
   __syncthreads();
   if (!s_last || threadIdx.x >= 32) return;
   __threadfence();
-  // last block, warp 0: combine the partials of each operand in block order (every lane the
-  // same), then lane c - 1 evaluates c moduli and a ballot picks the fewest that pass
+  // last block, warp 0: combine the partials of each operand (lane l takes blocks l, l + 32, ...;
+  // butterfly reductions leave the same sums in every lane), then lane c - 1 evaluates c moduli
+  // and a ballot picks the fewest that pass
   double nrm[2], E[2], S[2], smx[2];
   int nonfinite = 0;
 #pragma unroll
   for (int op = 0; op < 2; ++op) {
     const int b0 = op ? blocks_a : 0, b1 = op ? static_cast<int>(gridDim.x) : blocks_a;
-    int gref = -1100;
-    for (int b = b0; b < b1; ++b) {
+    int gref = -1100, nfl = 0;
+    for (int b = b0 + lane; b < b1; b += 32) {
       const CrtPlanPartial& q = part[b];
-      nonfinite |= q.nonfinite;
+      nfl |= q.nonfinite;
       if (q.any && q.ref > gref) gref = q.ref;
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      gref = max(gref, __shfl_xor_sync(0xffffffffu, gref, o));
+      nfl |= __shfl_xor_sync(0xffffffffu, nfl, o);
+    }
+    nonfinite |= nfl;
     double ae2 = 0.0, as2 = 0.0, an2 = 0.0, amx = 0.0;
-    for (int b = b0; b < b1; ++b) {
+    for (int b = b0 + lane; b < b1; b += 32) {
       const CrtPlanPartial& q = part[b];
       if (!q.any) continue;
       const double f = pow2_or_zero(2 * (q.ref - gref));
@@ -494,6 +501,11 @@ __global__ void __launch_bounds__(CRT_PLAN_THREADS) crt_plan_kernel(const OzRowS
       an2 += q.n2 * f;
       amx = fmax(amx, q.smax);
     }
+    ae2 = warp_sum(ae2);
+    as2 = warp_sum(as2);
+    an2 = warp_sum(an2);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) amx = fmax(amx, __shfl_xor_sync(0xffffffffu, amx, o));
     nrm[op] = sqrt(an2);
     E[op] = sqrt(ae2);
     S[op] = sqrt(as2);
@@ -650,6 +662,21 @@ __device__ __forceinline__ void crt_split8(const double (&x)[8], int e, int tbit
 #pragma unroll
     for (int l = 0; l < ND; ++l) d[l][j] = dj[l];
   }
+  // The moduli counts automatic plans pick for FP64 data (t = 52) run a straight loop whose
+  // table constants are immediate operands; other counts loop over the planes.
+  if (ND == 4) {
+    switch (nmod) {
+#define GB_CRT_SPLIT_CASE(n)                                                                          \
+  case n: {                                                                                           \
+    _Pragma("unroll") for (int g = 0; g < n; ++g)                                                     \
+        store_residues(out0 + g * plane_stride, crt_residues8<ND>(d, mod, g), nvalid);                \
+    return;                                                                                           \
+  }
+      GB_CRT_SPLIT_CASE(14) GB_CRT_SPLIT_CASE(15) GB_CRT_SPLIT_CASE(16)
+#undef GB_CRT_SPLIT_CASE
+      default: break;
+    }
+  }
   for (int g = 0; g < nmod; ++g) store_residues(out0 + g * plane_stride, crt_residues8<ND>(d, mod, g), nvalid);
 }
 
@@ -659,7 +686,7 @@ __global__ void __launch_bounds__(256) crt_split_kc_kernel(const double* __restr
                                                            int64_t rs, int64_t ks,
                                                            const unsigned long long* __restrict__ amax_bits,
                                                            __nv_bfloat16* __restrict__ planes, int64_t pitch,
-                                                           int32_t* __restrict__ exps,
+                                                           int64_t plane_stride, int32_t* __restrict__ exps,
                                                            const __grid_constant__ CrtModuli mod,
                                                            const CrtDevicePlan* __restrict__ plan) {
   const int64_t kc = static_cast<int64_t>(blockIdx.x) * 256 + threadIdx.x, r = blockIdx.y;
@@ -675,7 +702,6 @@ __global__ void __launch_bounds__(256) crt_split_kc_kernel(const double* __restr
 #pragma unroll
   for (int j = 0; j < 8; ++j) x[j] = (j < nvalid) ? src[j * ks] : 0.0;
   __nv_bfloat16* out0 = planes + r * pitch + k0;
-  const int64_t plane_stride = R * pitch;
   if (tbits <= 52) crt_split8<4>(x, e, tbits, nonfinite, nmod, mod, out0, plane_stride, nvalid);
   else crt_split8<5>(x, e, tbits, nonfinite, nmod, mod, out0, plane_stride, nvalid);
 }
@@ -689,7 +715,7 @@ __global__ void __launch_bounds__(256) crt_split_kc_kernel(const double* __restr
 __global__ void __launch_bounds__(256) crt_split_rc_kernel(const double* __restrict__ X, int64_t R, int64_t K,
                                                            int64_t ks, const unsigned long long* __restrict__ amax_bits,
                                                            __nv_bfloat16* __restrict__ planes, int64_t pitch,
-                                                           int32_t* __restrict__ exps,
+                                                           int64_t plane_stride, int32_t* __restrict__ exps,
                                                            const __grid_constant__ CrtModuli mod,
                                                            const CrtDevicePlan* __restrict__ plan) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -706,21 +732,24 @@ __global__ void __launch_bounds__(256) crt_split_rc_kernel(const double* __restr
 #pragma unroll
   for (int j = 0; j < 8; ++j) x[j] = (j < nvalid) ? src[j * ks] : 0.0;
   __nv_bfloat16* out0 = planes + r * pitch + k0;
-  const int64_t plane_stride = R * pitch;
   if (tbits <= 52) crt_split8<4>(x, e, tbits, nonfinite, nmod, mod, out0, plane_stride, nvalid);
   else crt_split8<5>(x, e, tbits, nonfinite, nmod, mod, out0, plane_stride, nvalid);
 }
 
 int crt_split(const double* X, int64_t R, int64_t K, int64_t rs, int64_t ks, const unsigned long long* amax_bits,
-              const CrtDevicePlan* plan, __nv_bfloat16* planes, int64_t pitch, int32_t* exps, cudaStream_t s) {
+              const CrtDevicePlan* plan, __nv_bfloat16* planes, int64_t pitch, int64_t plane_rows, int32_t* exps,
+              cudaStream_t s) {
   const CrtModuli& mod = crt_table().mod;
   if (R <= 0 || K <= 0) return GB_OK;
+  if (plane_rows < R) return GB_ERR_INVALID_VALUE;
+  const int64_t plane_stride = plane_rows * pitch;   // modulus planes of the whole operand
   if (rs == 1 && R > 1) {
     const int64_t gy = (K + 63) / 64;
     if (gy > 65535 || (R + 31) / 32 > 0x7FFFFFFF) return GB_ERR_UNSUPPORTED;
     dim3 grid(static_cast<unsigned>((R + 31) / 32), static_cast<unsigned>(gy));
     GB_LAUNCH(GB_KERNEL_OZAKI_SPLIT, s,
-              (crt_split_rc_kernel<<<grid, 256, 0, s>>>(X, R, K, ks, amax_bits, planes, pitch, exps, mod, plan)));
+              (crt_split_rc_kernel<<<grid, 256, 0, s>>>(X, R, K, ks, amax_bits, planes, pitch, plane_stride, exps,
+                                                        mod, plan)));
   } else {
     const int64_t kchunks = (K + 7) / 8;
     for (int64_t r0 = 0; r0 < R; r0 += 65535) {   // rows beyond the grid's y range: bands
@@ -728,7 +757,8 @@ int crt_split(const double* X, int64_t R, int64_t K, int64_t rs, int64_t ks, con
       dim3 grid(static_cast<unsigned>((kchunks + 255) / 256), static_cast<unsigned>(rb));
       GB_LAUNCH(GB_KERNEL_OZAKI_SPLIT, s,
                 (crt_split_kc_kernel<<<grid, 256, 0, s>>>(X + r0 * rs, rb, K, rs, ks, amax_bits + r0,
-                                                          planes + r0 * pitch, pitch, exps + r0, mod, plan)));
+                                                          planes + r0 * pitch, pitch, plane_stride, exps + r0, mod,
+                                                          plan)));
     }
   }
   GB_CUDA_TRY(cudaGetLastError());
@@ -738,8 +768,8 @@ int crt_split(const double* X, int64_t R, int64_t K, int64_t rs, int64_t ks, con
 // ============================================================== reconstruction
 
 // The double nearest (ties to even) to the signed 128-bit integer hi:lo times 2^E.  The top 64
-// bits from the leading one, with a sticky bit for everything below, round to 53 bits in one
-// correctly rounded u64 -> f64 conversion; a normal result then only needs its exponent moved
+// bits from the leading one, with a sticky bit for everything below, round to 53 bits (ties to
+// even, in integer arithmetic); a normal result then only needs its exponent moved
 // (an integer add on the bits), and results outside the normal range take one correctly
 // rounded power-of-two scaling of that double, as ldexp(double(C'), E) does.
 __device__ __forceinline__ double i128_times_pow2(uint64_t hi, uint64_t lo, int E) {
@@ -763,16 +793,20 @@ __device__ __forceinline__ double i128_times_pow2(uint64_t hi, uint64_t lo, int 
     sticky = false;
     lead = 63 - lz;
   }
-  // round the 64-bit window (sticky bit folded into its last place) to 53 bits in one correctly
-  // rounded conversion: a double in [2^63, 2^64]; a normal result only moves its exponent
-  const double dr = __ull2double_rn(top | (sticky ? 1ull : 0ull));
-  const long long db = __double_as_longlong(dr);
+  // round the 64-bit window (sticky bit folded into its last place) to 53 bits, ties to even, by
+  // integer operations (GB300's FP64 pipe, which a u64 -> f64 conversion would use, is narrow):
+  // the bits of a double in [2^63, 2^64] are (1085 << 52) + the rounded 53-bit significand,
+  // whose carry out of bit 52 (a window rounded up to 2^64) lands in the exponent field.
+  const uint64_t win = top | (sticky ? 1ull : 0ull);
+  const uint64_t mant = win >> 11;
+  const uint32_t below = static_cast<uint32_t>(win) & 0x7FFu;
+  const long long db = (1085ll << 52) + static_cast<long long>(mant + ((below + (mant & 1u)) > 0x400u ? 1u : 0u));
   const int shift = lead - 63 + E;
   const int exf = static_cast<int>(db >> 52) + shift;   // biased exponent of the result
   if (exf >= 1 && exf <= 2046)
     return __longlong_as_double((db + (static_cast<long long>(shift) << 52)) |
                                 (neg ? static_cast<long long>(0x8000000000000000ull) : 0ll));
-  const double d = scale_pow2(dr, shift);
+  const double d = scale_pow2(__longlong_as_double(db), shift);
   return neg ? -d : d;
 }
 
@@ -901,12 +935,12 @@ __global__ void __launch_bounds__(256) crt_combine_kernel(const uint8_t* __restr
 
 // ============================================================== driver
 
-int crt_gemm_launch(const CrtGemmArgs& a, const CrtPlan& plan, cudaStream_t s) {
+int crt_mma_launch(const CrtGemmArgs& a, const CrtPlan& plan, cudaStream_t s) {
   CUtensorMap ta, tb;
   // maps and schedule cover plan.n planes; the kernels run the device plan's n of them
   int rc = make_plane_tmap(&ta, a.planes_a, a.K, a.M, plan.n, a.pitch, 128);
   if (rc) return rc;
-  rc = make_plane_tmap(&tb, a.planes_b, a.K, a.N, plan.n, a.pitch, 128);
+  rc = make_plane_tmap(&tb, a.planes_b, a.K, a.N, plan.n, a.pitch, 128, a.b_plane_rows ? a.b_plane_rows : a.N);
   if (rc) return rc;
   TcParams prm;
   std::memset(&prm, 0, sizeof(prm));
@@ -934,8 +968,11 @@ int crt_gemm_launch(const CrtGemmArgs& a, const CrtPlan& plan, cudaStream_t s) {
   }
   for (int n = 1; n <= plan.n; ++n)
     for (int g = 0; g < n; ++g) prm.crt_psi[n - 1][g] = crt_table().rec[n - 1].psi[g];
-  rc = tc_gemm_pair_launch(TC_EPI_CRT, ta, tb, nullptr, nullptr, plan.sched, prm, a.grid, GB_KERNEL_OZAKI_SLICE_MMA, s);
-  if (rc) return rc;
+  return tc_gemm_pair_launch(TC_EPI_CRT, ta, tb, nullptr, nullptr, plan.sched, prm, a.grid, GB_KERNEL_OZAKI_SLICE_MMA,
+                             s);
+}
+
+int crt_combine_launch(const CrtGemmArgs& a, cudaStream_t s) {
   const int64_t bx = (a.M + 1023) / 1024;
   const int64_t by = a.N < 65535 ? a.N : 65535;
   if (bx > 0x7FFFFFFF) return GB_ERR_UNSUPPORTED;

@@ -89,10 +89,11 @@ struct TcTuning {
   int32_t engine;
   int32_t band;
   int32_t tma_store;
-  int32_t reserved;
+  int32_t panels;   // CRT: column panels pipelined against the residue products (0/1 = one)
 };
 int tc_tune_class(int64_t M, int64_t N);
-TcTuning tc_default_tuning(int kind);
+constexpr int TC_MAX_PANELS = 4;   // CRT column panels
+TcTuning tc_default_tuning(int kind, int cls);
 int tc_validate_tuning(int kind, const TcTuning& t);
 // The tuning a call of this kind and output size uses (gb_set_tc_engine, when set, overrides
 // the engine).
@@ -117,10 +118,11 @@ int tc_gemm_pair_launch(int epi, const CUtensorMap& ta0, const CUtensorMap& tb0,
 int tc_engine_setting();
 void tc_set_engine(int e);
 
-// 3-D BF16 tensor map {K, rows, planes} over [planes][rows][pitch], box 64 x box_rows x 1,
-// 128-byte swizzle (defined in capi.cu).
+// 3-D BF16 tensor map {K, rows, planes} over [planes][plane_rows][pitch] (plane_rows = 0: rows;
+// a band of rows passes base at its first row and the planes' full row count), box
+// 64 x box_rows x 1, 128-byte swizzle (defined in capi.cu).
 int make_plane_tmap(CUtensorMap* map, const void* base, int64_t K, int64_t rows, int64_t slices,
-                    int64_t pitch, int box_rows);
+                    int64_t pitch, int box_rows, int64_t plane_rows = 0);
 // 2-D FP32 tensor map over a column-major M x N matrix C (leading dimension ldc), box 32 x 32,
 // for the TMA-store epilogue (which stores only boxes lying wholly inside C).  false when C's layout does not allow one (base not 16-byte
 // aligned, ldc not a multiple of 4, sizes beyond the map's range); the caller then stores directly.

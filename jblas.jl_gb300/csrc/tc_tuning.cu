@@ -18,7 +18,7 @@ TcTuning g_tune[TC_KINDS][TC_TUNE_CLASSES];
 void init_locked() {
   if (g_tune_init) return;
   for (int k = 0; k < TC_KINDS; ++k)
-    for (int c = 0; c < TC_TUNE_CLASSES; ++c) g_tune[k][c] = tc_default_tuning(k);
+    for (int c = 0; c < TC_TUNE_CLASSES; ++c) g_tune[k][c] = tc_default_tuning(k, c);
   g_tune_init = true;
 }
 }  // namespace
@@ -29,14 +29,14 @@ int tc_tune_class(int64_t M, int64_t N) {
 }
 
 // Defaults measured on GB300: CTA pairs (per-SM operand traffic halved, 95-100% of the BF16
-// peak against 75% for one CTA per tile), bands of 8 pair tiles (2048 rows), direct stores.
-TcTuning tc_default_tuning(int kind) {
-  (void)kind;
+// peak against 75% for one CTA per tile), bands of 8 pair tiles (2048 rows), direct stores;
+// CRT products wider than 2048 columns in two column panels.
+TcTuning tc_default_tuning(int kind, int cls) {
   TcTuning t;
   t.engine = 2;
   t.band = 8;
   t.tma_store = 0;
-  t.reserved = 0;
+  t.panels = (kind == TC_KIND_CRT && cls > 0) ? 2 : 0;
   return t;
 }
 
@@ -48,6 +48,7 @@ int tc_validate_tuning(int kind, const TcTuning& t) {
   if (t.tma_store != 0 && t.tma_store != 1) return GB_ERR_INVALID_VALUE;
   if (t.tma_store && kind != TC_KIND_F32 && kind != TC_KIND_ADJOINT) return GB_ERR_INVALID_VALUE;
   if (t.tma_store && t.engine != 2) return GB_ERR_INVALID_VALUE;   // TMA-store epilogue: pair engine
+  if (t.panels < 0 || t.panels > TC_MAX_PANELS || (t.panels > 1 && kind != TC_KIND_CRT)) return GB_ERR_INVALID_VALUE;
   return GB_OK;
 }
 
@@ -73,7 +74,7 @@ TcTuning tc_tuning_for(int kind, int64_t M, int64_t N) {
 
 int tc_set_tuning(int kind, int cls, const TcTuning* t) {
   if (kind < 0 || kind >= TC_KINDS || cls < 0 || cls >= TC_TUNE_CLASSES) return GB_ERR_INVALID_VALUE;
-  const TcTuning v = t ? *t : tc_default_tuning(kind);
+  const TcTuning v = t ? *t : tc_default_tuning(kind, cls);
   const int rc = tc_validate_tuning(kind, v);
   if (rc) return rc;
   std::lock_guard<std::mutex> lk(g_tune_mu);
@@ -171,13 +172,15 @@ int tc_autotune(int kind, int64_t M, int64_t N, int64_t K, int reps, TcTuning* o
     if (kind == TC_KIND_CRT && engine == 1) continue;
     for (int bi = 0; bi < 5 && !rc; ++bi) {
       const int band = (engine == 2 ? 2 : 4) << bi;   // 2..32 pair tiles, 4..64 single tiles
-      for (int tma = 0; tma <= 1 && !rc; ++tma) {
-        if (tma && (engine != 2 || (kind != TC_KIND_F32 && kind != TC_KIND_ADJOINT))) continue;
+      // the second option: TMA stores of C (FP32 outputs on pairs) or column panels (CRT: 1..4)
+      const int nopt = (kind == TC_KIND_CRT) ? TC_MAX_PANELS
+                       : (engine == 2 && (kind == TC_KIND_F32 || kind == TC_KIND_ADJOINT)) ? 2 : 1;
+      for (int opt = 0; opt < nopt && !rc; ++opt) {
         TcTuning t;
         t.engine = engine;
         t.band = band;
-        t.tma_store = tma;
-        t.reserved = 0;
+        t.tma_store = (kind == TC_KIND_CRT) ? 0 : opt;
+        t.panels = (kind == TC_KIND_CRT) ? opt + 1 : 0;
         rc = tc_set_tuning(kind, cls, &t);
         if (!rc) rc = call();   // warm-up
         if (rc) break;

@@ -55,16 +55,17 @@ TC_SIZE_CLASSES = 3
 
 
 class TcTuning(ctypes.Structure):
-    """gb_tc_tuning_t: tensor-core engine, L2 band and TMA-store choice of one kind and size class."""
+    """gb_tc_tuning_t: tensor-core engine, L2 band, TMA-store choice and (CRT) column panels of
+    one kind and size class."""
     _fields_ = [("engine", ctypes.c_int32), ("band", ctypes.c_int32), ("tma_store", ctypes.c_int32),
-                ("reserved", ctypes.c_int32)]
+                ("panels", ctypes.c_int32)]
 
     def as_dict(self):
-        return {"engine": self.engine, "band": self.band, "tma_store": self.tma_store}
+        return {"engine": self.engine, "band": self.band, "tma_store": self.tma_store, "panels": self.panels}
 
     @classmethod
     def from_dict(cls, d):
-        return cls(int(d["engine"]), int(d["band"]), int(d.get("tma_store", 0)), 0)
+        return cls(int(d["engine"]), int(d["band"]), int(d.get("tma_store", 0)), int(d.get("panels", 0)))
 
 
 class Tuning(ctypes.Structure):
@@ -100,7 +101,7 @@ SIGNATURES = {
                             c_float, c_vp, c_i64, c_vp]),
     "gb_measure_fma_peaks": (c_int, [ctypes.POINTER(c_double), ctypes.POINTER(c_double)]),
     "gb_tc_size_class": (c_int, [c_i64, c_i64]),
-    "gb_tc_default_tuning": (c_int, [c_int, ctypes.POINTER(TcTuning)]),
+    "gb_tc_default_tuning": (c_int, [c_int, c_int, ctypes.POINTER(TcTuning)]),
     "gb_get_tc_tuning": (c_int, [c_int, c_int, ctypes.POINTER(TcTuning)]),
     "gb_set_tc_tuning": (c_int, [c_int, c_int, ctypes.POINTER(TcTuning)]),
     "gb_autotune_tc": (c_int, [c_int, c_i64, c_i64, c_i64, c_int, ctypes.POINTER(TcTuning),

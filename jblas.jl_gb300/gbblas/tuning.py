@@ -30,9 +30,9 @@ def size_class(M, N):
     return rc
 
 
-def default_tuning(kind):
+def default_tuning(kind, cls=1):
     t = TcTuning()
-    check(_lib.lib().gb_tc_default_tuning(_kind(kind), ctypes.byref(t)), "gb_tc_default_tuning")
+    check(_lib.lib().gb_tc_default_tuning(_kind(kind), int(cls), ctypes.byref(t)), "gb_tc_default_tuning")
     return t
 
 

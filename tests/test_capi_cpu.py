@@ -126,23 +126,31 @@ def test_tc_tuning_table_roundtrip_and_validation():
     assert [tuning.size_class(m, n) for m, n in ((1, 1), (2048, 100), (2049, 5), (8192, 8192), (8193, 1))] == \
         [0, 0, 1, 1, 2]
     for kind in _lib.TC_KINDS:
-        d = tuning.default_tuning(kind)
-        assert (d.engine, d.band, d.tma_store) == (2, 8, 0)
         for cls in range(_lib.TC_SIZE_CLASSES):
+            d = tuning.default_tuning(kind, cls)
+            # CRT products above 2048 columns default to two column panels
+            panels = 2 if (kind == "ozaki_crt" and cls > 0) else 0
+            assert (d.engine, d.band, d.tma_store, d.panels) == (2, 8, 0, panels)
             assert tuning.get_tuning(kind, cls).as_dict() == d.as_dict()
     tuning.set_tuning("f32", 1, {"engine": 2, "band": 16, "tma_store": 1})
-    assert tuning.get_tuning("f32", 1).as_dict() == {"engine": 2, "band": 16, "tma_store": 1}
+    assert tuning.get_tuning("f32", 1).as_dict() == {"engine": 2, "band": 16, "tma_store": 1, "panels": 0}
     assert tuning.get_tuning("f32", 0).as_dict()["band"] == 8
+    tuning.set_tuning("ozaki_crt", 2, {"engine": 2, "band": 4, "panels": 4})
+    assert tuning.get_tuning("ozaki_crt", 2).as_dict() == {"engine": 2, "band": 4, "tma_store": 0, "panels": 4}
     bad = [("ozaki_crt", {"engine": 1, "band": 8}), ("f32", {"engine": 3, "band": 8}),
            ("f32", {"engine": 2, "band": 0}), ("f32", {"engine": 2, "band": 65}),
            ("ozaki_slices", {"engine": 2, "band": 8, "tma_store": 1}),
-           ("adjoint", {"engine": 1, "band": 8, "tma_store": 1})]
+           ("adjoint", {"engine": 1, "band": 8, "tma_store": 1}),
+           ("ozaki_crt", {"engine": 2, "band": 8, "panels": 5}), ("ozaki_crt", {"engine": 2, "band": 8, "panels": -1}),
+           ("f32", {"engine": 2, "band": 8, "panels": 2}), ("ozaki_slices", {"engine": 2, "band": 8, "panels": 2})]
     for kind, d in bad:
         t = _lib.TcTuning.from_dict(d)
         assert L.gb_set_tc_tuning(_lib.TC_KINDS[kind], 0, ctypes.byref(t)) == _lib.GB_ERR_INVALID_VALUE, (kind, d)
-    t = _lib.TcTuning(2, 8, 0, 1)   # reserved must be 0
-    assert L.gb_set_tc_tuning(2, 0, ctypes.byref(t)) == _lib.GB_ERR_INVALID_VALUE
     assert L.gb_set_tc_tuning(9, 0, None) == _lib.GB_ERR_INVALID_VALUE
     assert L.gb_set_tc_tuning(2, 3, None) == _lib.GB_ERR_INVALID_VALUE
+    t = _lib.TcTuning()
+    assert L.gb_tc_default_tuning(1, 3, ctypes.byref(t)) == _lib.GB_ERR_INVALID_VALUE
     tuning.set_tuning("f32", 1, None)
-    assert tuning.get_tuning("f32", 1).as_dict() == tuning.default_tuning("f32").as_dict()
+    tuning.set_tuning("ozaki_crt", 2, None)
+    assert tuning.get_tuning("f32", 1).as_dict() == tuning.default_tuning("f32", 1).as_dict()
+    assert tuning.get_tuning("ozaki_crt", 2).as_dict() == tuning.default_tuning("ozaki_crt", 2).as_dict()

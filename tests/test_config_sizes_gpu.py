@@ -134,3 +134,35 @@ def test_crt_8192_moduli_sweep(ozaki_8192):
             prev = bound
         else:
             assert bound <= 2.0 ** -50
+
+
+@pytest.mark.parametrize("panels", [1, 2])
+@pytest.mark.parametrize("mode", ["ozaki_crt", "ozaki"])
+def test_k_contiguous_operand_beyond_65535_rows(cuda, mode, panels):
+    """B with 66000 columns stored k-contiguous: its digit or residue planes are written by row
+    bands of at most 65535 rows (the grid's y limit), all into the planes of the whole operand.
+    Columns on both sides of every band edge and of the CRT panel edge match the restatement
+    bit for bit."""
+    from gbblas import tuning
+    M, K, N = 64, 64, 66000
+    g = np.random.default_rng(123 + panels)
+    A = np.asfortranarray(g.uniform(-1, 1, (M, K)) * np.ldexp(1.0, g.integers(-6, 7, (M, K))))
+    B = np.asfortranarray(g.uniform(-1, 1, (K, N)) * np.ldexp(1.0, g.integers(-6, 7, (K, N))))
+    cls = tuning.size_class(M, N)
+    try:
+        if mode == "ozaki_crt":
+            tuning.set_tuning("ozaki_crt", cls, {"engine": 2, "band": 8, "panels": panels})
+        elif panels > 1:
+            pytest.skip("column panels are a CRT option")
+        Cd = to_dev(np.zeros((M, N)))
+        gbblas.gemm_(Cd, to_dev(A), to_dev(B), mode=mode, slices=12 if mode == "ozaki_crt" else 5)
+        torch.cuda.synchronize()
+        gbblas.check_device_status()
+    finally:
+        tuning.set_tuning("ozaki_crt", cls, None)
+    edges = [0, 1, 32767, 32768, 33023, 33024, 65534, 65535, 65536, 65999]
+    cols = np.unique(np.concatenate([edges, g.choice(N, 22, replace=False)]))
+    got = Cd[:, torch.from_numpy(cols).to(Cd.device)].cpu().numpy()
+    Bs = np.asfortranarray(B[:, cols])
+    ref = (oracle.ozaki_crt_gemm(A, Bs, moduli=12) if mode == "ozaki_crt" else oracle.ozaki_gemm(A, Bs, slices=5))
+    assert_bit_equal(np.asfortranarray(got), ref)

@@ -1,7 +1,7 @@
 """The tensor-core tuning table changes how products are scheduled and stored, never their values.
 
-  * digit slices and CRT residues are exact integer sums in FP32, so every engine and band gives
-    the restatement's bits;
+  * digit slices and CRT residues are exact integer sums in FP32, so every engine, band and
+    (CRT) number of column panels gives the restatement's bits;
   * FP32 term modes and the adjoint accumulate in the same order whatever the band or the store
     path, so TMA stores of C give the bits of direct stores (ragged shapes included), and a C
     whose layout a TMA map cannot describe (unaligned leading dimension) falls back to direct
@@ -15,7 +15,7 @@ import pytest
 import torch
 
 import gbblas
-from gbblas import tuning
+from gbblas import tuning, workloads
 import oracle
 from gpu_util import assert_bit_equal, to_dev, to_dev_ld, to_host
 
@@ -61,6 +61,46 @@ def test_crt_bit_exact_under_every_band(restore_tuning, band):
     torch.cuda.synchronize()
     gbblas.check_device_status()
     assert_bit_equal(to_host(Cd), oracle.ozaki_crt_gemm(A, B, moduli=12))
+
+
+def _crt_raw(A, B_phys, tb, N, C0, alpha, beta, moduli):
+    M, K = A.shape
+    Ad, Bd, Cd = to_dev(A), to_dev(B_phys), to_dev(C0)
+    bound = gbblas.gemm_raw(0, tb, M, N, K, alpha, Ad.data_ptr(), M, Bd.data_ptr(), B_phys.shape[0], beta,
+                            Cd.data_ptr(), M, dtype=torch.float64, mode=gbblas.MODE_OZAKI_CRT, slices=moduli,
+                            stream=torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    gbblas.check_device_status()
+    return to_host(Cd), bound
+
+
+@pytest.mark.parametrize("panels", [1, 2, 3, 4])
+@pytest.mark.parametrize("tb", [0, 1], ids=["B_k_contiguous", "B_rows_contiguous"])
+def test_crt_bit_exact_under_every_panel_count(restore_tuning, panels, tb):
+    """Column panels: the residue products of each panel run on the library's high-priority
+    stream while the caller's stream splits the next panel of B and reconstructs the previous
+    panel of C.  Every panel count gives the restatement's bits, with B stored k-contiguous or
+    rows-contiguous, alpha and beta, and a last panel narrower than the others (1100 columns =
+    five 256-column tiles)."""
+    M, K, N = 700, 257, 1100
+    g = np.random.default_rng(40 + panels + 5 * tb)
+    A = np.asfortranarray(g.uniform(-1, 1, (M, K)) * np.ldexp(1.0, g.integers(-6, 7, (M, K))))
+    Bl = g.uniform(-1, 1, (K, N)) * np.ldexp(1.0, g.integers(-6, 7, (K, N)))
+    C0 = np.asfortranarray(g.uniform(-1, 1, (M, N)))
+    tuning.set_tuning("ozaki_crt", tuning.size_class(M, N), {"engine": 2, "band": 8, "panels": panels})
+    got, _ = _crt_raw(A, np.asfortranarray(Bl.T if tb else Bl), tb, N, C0, 1.5, 0.5, 13)
+    assert_bit_equal(got, oracle.ozaki_crt_gemm(A, Bl, C=C0, alpha=1.5, beta=0.5, moduli=13))
+
+
+def test_crt_panels_with_automatic_plan(restore_tuning):
+    """The automatic plan (moduli chosen on the device) read by every panel's kernels."""
+    M, K, N = 512, 300, 1024
+    A = np.asfortranarray(workloads.ozaki_matrix(M, K, per="row", stream=71))
+    B = np.asfortranarray(workloads.ozaki_matrix(K, N, per="col", stream=72))
+    tuning.set_tuning("ozaki_crt", tuning.size_class(M, N), {"engine": 2, "band": 2, "panels": 3})
+    got, _ = _crt_raw(A, B, 0, N, np.zeros((M, N)), 1.0, 0.0, 0)
+    plan = gbblas.last_ozaki_plan()
+    assert_bit_equal(got, oracle.ozaki_crt_gemm(A, B, moduli=plan["slices"], bits=plan["bits"]))
 
 
 SHAPES = [(1, 1, 1), (33, 70, 17), (300, 257, 130), (513, 96, 1000), (1024, 512, 768)]
