@@ -12,7 +12,10 @@ cases:
   ozaki          gb_gemm_f64 OZAKI (stats, split, slice products), 4096 x 4096 x 8192
   ozaki_crt      gb_gemm_f64 OZAKI_CRT, 15 moduli (stats, residue split, residue products,
                  CRT combine), 4096 x 4096 x 8192
+                 in two column panels (the default tuning at this size)
   ozaki_crt_auto the same with the automatic plan (statistics with the planner's sums)
+  ozaki_crt_1panel, ozaki_crt_auto_1panel
+                 the same in one panel: every kernel once per call, on the caller's stream
   grouped_f64    gb_gemm_grouped_f64, 4096 problems with m, n, k log-uniform in [8, 512]
   grouped_f32    the same problems in FP32 (default configuration: tiles chosen per problem)
   adjoint        gb_gemm_adjoint_f32, A 4096 x 2048, B 2048 x 4096
@@ -27,7 +30,7 @@ import numpy as np
 import torch
 
 sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "jblas.jl_gb300"))
-from gbblas import api, grouped, workloads  # noqa: E402
+from gbblas import api, grouped, tuning, workloads  # noqa: E402
 
 
 def _dev_cm(x):
@@ -60,11 +63,15 @@ def case_ozaki():
     return _timed(lambda: api.gemm_(C, A, B, mode="ozaki", slices=10))
 
 
-def case_ozaki_crt(moduli=15):
+def case_ozaki_crt(moduli=15, panels=None):
+    """panels: column panels of the call (None = the tuning table's default, 2 at this size;
+    1 = every kernel once per call, on the caller's stream)."""
     M, N, K = 4096, 4096, 8192
     A = _dev_cm(workloads.ozaki_matrix(M, K, per="row", stream=1))
     B = _dev_cm(workloads.ozaki_matrix(K, N, per="col", stream=2))
     C = torch.empty((N, M), dtype=torch.float64, device="cuda").t()
+    if panels is not None:
+        tuning.set_tuning("ozaki_crt", tuning.size_class(M, N), {"engine": 2, "band": 8, "panels": panels})
     return _timed(lambda: api.gemm_(C, A, B, mode="ozaki_crt", slices=moduli))
 
 
@@ -104,6 +111,8 @@ CASES = {
     "ozaki": case_ozaki,
     "ozaki_crt": case_ozaki_crt,
     "ozaki_crt_auto": lambda: case_ozaki_crt(0),
+    "ozaki_crt_1panel": lambda: case_ozaki_crt(15, panels=1),
+    "ozaki_crt_auto_1panel": lambda: case_ozaki_crt(0, panels=1),
     "grouped_f64": case_grouped,
     "grouped_f32": lambda: case_grouped(torch.float32),
     "adjoint": case_adjoint,
