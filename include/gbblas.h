@@ -93,11 +93,12 @@ GB_API int gb_set_tc_engine(int engine);
  *              A rows in L2)
  *   tma_store  FP32 outputs (GB_TC_F32, GB_TC_ADJOINT) on the pair engine: 1 = C staged in
  *              shared memory and written by TMA stores (beta = 0), 0 = direct stores
- *   panels     GB_TC_OZAKI_CRT only (0 elsewhere): C's columns in this many panels (0 or 1 = one;
- *              at most 4, and at most one per 256 columns); the residue products of panel p
- *              run on a high-priority stream of the library while the caller's stream splits
- *              panel p + 1 of B and reconstructs panel p - 1 of C.  Under stream capture a
- *              call uses one panel.  Results do not depend on it.
+ *   panels     GB_TC_OZAKI_CRT only (0 elsewhere): C in blocks — 0 or 1: one; 2, 3: column
+ *              panels; 4: 2 x 2 blocks (column panels when M <= 256); at most one per 256
+ *              columns.  The residue products of block b run on a high-priority stream of the
+ *              library while the caller's stream splits the operand panels of block b + 1 and
+ *              reconstructs block b - 1.  Under stream capture a call uses one block.
+ *              Results do not depend on it.
  * Size classes by max(M, N): 0 up to 2048, 1 up to 8192, 2 beyond.  gb_set_tc_engine, when set,
  * overrides the engine of every kind. */
 typedef enum { GB_TC_OZAKI_SLICES = 0, GB_TC_OZAKI_CRT = 1, GB_TC_F32 = 2, GB_TC_ADJOINT = 3, GB_TC_KINDS = 4 } gb_tc_kind_t;

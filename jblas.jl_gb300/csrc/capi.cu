@@ -661,6 +661,7 @@ static int crt_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int64
   ga.plan = plan_d;
   const TcTuning tune = tc_tuning_for(TC_KIND_CRT, M, N);
   ga.band = tune.band;
+  ga.a_plane_rows = M;
   ga.b_plane_rows = N;
   auto grid_for = [&](int64_t n) {
     const int64_t ctas = 2 * static_cast<int64_t>(tc_pair_tiles(M, n));
@@ -680,8 +681,8 @@ static int crt_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int64
   Lane* lane = nullptr;
   if (panels > 1 && cudaStreamIsCapturing(s, &cap_status) == cudaSuccess && cap_status == cudaStreamCaptureStatusNone)
     lane = take_lane(dev);
-  rc = crt_split(A, M, K, a_rs, a_ks, os.a.amax_bits, plan_d, pa, pitch, M, ea, s);
   if (!lane) {
+    rc = crt_split(A, M, K, a_rs, a_ks, os.a.amax_bits, plan_d, pa, pitch, M, ea, s);
     if (!rc) rc = crt_split(B, N, K, b_rs, b_ks, os.b.amax_bits, plan_d, pb, pitch, N, eb, s);
     if (!rc) {
       ga.grid = grid_for(N);
@@ -689,37 +690,63 @@ static int crt_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int64
     }
     if (!rc) rc = crt_combine_launch(ga, s);
   } else {
-    // panel boundaries on whole 256-column tiles
-    int64_t n0[TC_MAX_PANELS + 1];
-    for (int p = 0; p <= panels; ++p) {
-      const int64_t c = tiles_n * p / panels * 256;
+    // Blocks of C on whole 256 x 256 tiles: `panels` column panels, or 2 x 2 blocks for 4, so
+    // that the first products wait only for half of A's split as well.  Blocks run row by row;
+    // each split of a row panel of A or column panel of B is enqueued on this stream just
+    // before the first block that needs it.
+    const int prow = (panels == 4 && mpad >= 512) ? 2 : 1, pcol = panels / prow;
+    int64_t m0[3], n0[TC_MAX_PANELS + 1];
+    const int64_t tiles_m = mpad / 256;
+    for (int p = 0; p <= prow; ++p) {
+      const int64_t r = tiles_m * p / prow * 256;
+      m0[p] = r < M ? r : M;
+    }
+    for (int p = 0; p <= pcol; ++p) {
+      const int64_t c = tiles_n * p / pcol * 256;
       n0[p] = c < N ? c : N;
     }
-    auto panel_args = [&](int p) {
+    auto block_args = [&](int r, int c) {
       CrtGemmArgs g = ga;
-      g.N = n0[p + 1] - n0[p];
-      g.planes_b = pb + n0[p] * pitch;
-      g.eb = eb + n0[p];
-      g.C = C + n0[p] * ldc;
-      g.res = res + n0[p] * mpad;
-      g.grid = grid_for(g.N);
+      g.M = m0[r + 1] - m0[r];
+      g.N = n0[c + 1] - n0[c];
+      g.planes_a = pa + m0[r] * pitch;
+      g.a_plane_rows = M;
+      g.planes_b = pb + n0[c] * pitch;
+      g.ea = ea + m0[r];
+      g.eb = eb + n0[c];
+      g.C = C + m0[r] + n0[c] * ldc;
+      g.res = res + m0[r] + n0[c] * mpad;
+      const int64_t ctas = 2 * static_cast<int64_t>(tc_pair_tiles(g.M, g.N));
+      const int64_t cap = dev->sms & ~1;
+      g.grid = static_cast<int>(ctas < cap ? ctas : cap);
       return g;
     };
     cudaStream_t hs = lane->stream;
     auto cu = [&](cudaError_t e) {
       if (e != cudaSuccess && !rc) rc = gb_set_cuda_error(e, "ozaki crt panel pipeline");
     };
-    for (int p = 0; p < panels && !rc; ++p) {
-      rc = crt_split(B + n0[p] * b_rs, n0[p + 1] - n0[p], K, b_rs, b_ks, os.b.amax_bits + n0[p], plan_d,
-                     pb + n0[p] * pitch, pitch, N, eb + n0[p], s);
-      if (!rc) cu(cudaEventRecord(lane->ev[2 * p], s));
-      if (!rc) cu(cudaStreamWaitEvent(hs, lane->ev[2 * p], 0));
-      if (!rc) rc = crt_mma_launch(panel_args(p), plan, hs);
-      if (!rc) cu(cudaEventRecord(lane->ev[2 * p + 1], hs));
+    bool a_done[2] = {false, false}, b_done[TC_MAX_PANELS] = {};
+    const int nblocks = prow * pcol;
+    for (int b = 0; b < nblocks && !rc; ++b) {
+      const int r = b / pcol, c = b % pcol;
+      if (!a_done[r]) {
+        rc = crt_split(A + m0[r] * a_rs, m0[r + 1] - m0[r], K, a_rs, a_ks, os.a.amax_bits + m0[r], plan_d,
+                       pa + m0[r] * pitch, pitch, M, ea + m0[r], s);
+        a_done[r] = true;
+      }
+      if (!rc && !b_done[c]) {
+        rc = crt_split(B + n0[c] * b_rs, n0[c + 1] - n0[c], K, b_rs, b_ks, os.b.amax_bits + n0[c], plan_d,
+                       pb + n0[c] * pitch, pitch, N, eb + n0[c], s);
+        b_done[c] = true;
+      }
+      if (!rc) cu(cudaEventRecord(lane->ev[2 * b], s));
+      if (!rc) cu(cudaStreamWaitEvent(hs, lane->ev[2 * b], 0));
+      if (!rc) rc = crt_mma_launch(block_args(r, c), plan, hs);
+      if (!rc) cu(cudaEventRecord(lane->ev[2 * b + 1], hs));
     }
-    for (int p = 0; p < panels && !rc; ++p) {
-      cu(cudaStreamWaitEvent(s, lane->ev[2 * p + 1], 0));
-      if (!rc) rc = crt_combine_launch(panel_args(p), s);
+    for (int b = 0; b < nblocks && !rc; ++b) {
+      cu(cudaStreamWaitEvent(s, lane->ev[2 * b + 1], 0));
+      if (!rc) rc = crt_combine_launch(block_args(b / pcol, b % pcol), s);
     }
     if (rc) {
       // join whatever reached the lane before the error, so the workspace is freed after it

@@ -193,13 +193,14 @@ struct CrtGemmArgs {
   int grid;               // even (CTA pairs)
   const CrtDevicePlan* plan;
   int band;               // pair-tile rows per L2 band of the raster
-  int64_t b_plane_rows;   // rows of the operand whose planes planes_b points into (>= N; a panel
-                          // of columns passes planes_b at its first row)
+  int64_t a_plane_rows;   // rows of the operands whose planes planes_a / planes_b point into
+  int64_t b_plane_rows;   // (>= M, N; a block of C passes both at its first row / column)
 };
 // Residue products on the CTA-pair engine (crt_mma_launch), then the CRT reconstruction into C
 // (crt_combine_launch).  `plan` (host) gives the K chunking and a schedule for up to plan.n
-// moduli; the kernels run the device plan's n <= plan.n.  A panel of C's columns passes
-// planes_b, eb, C and res offset to its first column (a multiple of 256) and N = its width.
+// moduli; the kernels run the device plan's n <= plan.n.  A block of C passes planes_a, ea,
+// planes_b, eb, C and res offset to its first row and column (multiples of 256) and M, N = its
+// size.
 int crt_mma_launch(const CrtGemmArgs& a, const CrtPlan& plan, cudaStream_t s);
 int crt_combine_launch(const CrtGemmArgs& a, cudaStream_t s);
 

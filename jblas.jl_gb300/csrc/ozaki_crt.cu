@@ -938,7 +938,7 @@ __global__ void __launch_bounds__(256) crt_combine_kernel(const uint8_t* __restr
 int crt_mma_launch(const CrtGemmArgs& a, const CrtPlan& plan, cudaStream_t s) {
   CUtensorMap ta, tb;
   // maps and schedule cover plan.n planes; the kernels run the device plan's n of them
-  int rc = make_plane_tmap(&ta, a.planes_a, a.K, a.M, plan.n, a.pitch, 128);
+  int rc = make_plane_tmap(&ta, a.planes_a, a.K, a.M, plan.n, a.pitch, 128, a.a_plane_rows ? a.a_plane_rows : a.M);
   if (rc) return rc;
   rc = make_plane_tmap(&tb, a.planes_b, a.K, a.N, plan.n, a.pitch, 128, a.b_plane_rows ? a.b_plane_rows : a.N);
   if (rc) return rc;
