@@ -103,6 +103,103 @@ def test_crt_panels_with_automatic_plan(restore_tuning):
     assert_bit_equal(got, oracle.ozaki_crt_gemm(A, B, moduli=plan["slices"], bits=plan["bits"]))
 
 
+def test_crt_panels_from_concurrent_threads(restore_tuning):
+    """Two host threads, each on its own stream, make CRT calls in 3 column panels and 2 x 2
+    blocks at once: each call takes its own high-priority lane from the device's pool, and
+    every result equals the single-panel one."""
+    import threading
+    M, K, N = 300, 512, 800
+    cls = tuning.size_class(M, N)
+    ops = []
+    for i in range(4):
+        A = to_dev(workloads.ozaki_matrix(M, K, per="row", stream=810 + 2 * i))
+        B = to_dev(workloads.ozaki_matrix(K, N, per="col", stream=811 + 2 * i))
+        ops.append((A, B))
+    tuning.set_tuning("ozaki_crt", cls, {"engine": 2, "band": 8, "panels": 1})
+    ref = []
+    for A, B in ops:
+        C = torch.empty((N, M), dtype=torch.float64, device="cuda").t()
+        gbblas.gemm_(C, A, B, mode="ozaki_crt", slices=14)
+        ref.append(to_host(C))
+    for panels in (3, 4):
+        tuning.set_tuning("ozaki_crt", cls, {"engine": 2, "band": 8, "panels": panels})
+        results, errors = {}, []
+
+        def worker(t):
+            try:
+                torch.cuda.set_device(0)
+                st = torch.cuda.Stream()
+                with torch.cuda.stream(st):
+                    outs = []
+                    for _ in range(3):
+                        for A, B in ops[2 * t:2 * t + 2]:
+                            C = torch.empty((N, M), dtype=torch.float64, device="cuda").t()
+                            gbblas.gemm_(C, A, B, mode="ozaki_crt", slices=14)
+                            outs.append(C)
+                    st.synchronize()
+                    results[t] = [to_host(o) for o in outs]
+            except Exception as e:   # surfaced in the main thread
+                errors.append(e)
+
+        th = [threading.Thread(target=worker, args=(t,)) for t in (0, 1)]
+        for x in th:
+            x.start()
+        for x in th:
+            x.join()
+        assert not errors, errors
+        gbblas.check_device_status()
+        for t in (0, 1):
+            for i, got in enumerate(results[t]):
+                assert_bit_equal(got, ref[2 * t + i % 2])
+
+
+def test_crt_panels_short_wait_limit(restore_tuning):
+    """A timed-out wait in the residue products of a panel (on the library's lane) is reported
+    by the next status check on the caller's stream, and the next call is right."""
+    from gbblas import _lib
+    g = np.random.default_rng(23)
+    M, K, N = 256, 8192, 768
+    A = np.asfortranarray(g.uniform(-1, 1, (M, K)))
+    B = np.asfortranarray(g.uniform(-1, 1, (K, N)))
+    Ad, Bd = to_dev(A), to_dev(B)
+    C = torch.zeros((N, M), dtype=torch.float64, device="cuda").t()
+    tuning.set_tuning("ozaki_crt", tuning.size_class(M, N), {"engine": 2, "band": 8, "panels": 3})
+    gbblas.check_device_status()
+    gbblas.set_wait_limit_ns(2000)
+    try:
+        gbblas.gemm_(C, Ad, Bd, mode="ozaki_crt", slices=16)
+        torch.cuda.synchronize()
+    finally:
+        gbblas.set_wait_limit_ns(0)
+    with pytest.raises(gbblas.GBError) as e:
+        gbblas.check_device_status()
+    assert e.value.status == _lib.GB_ERR_PIPELINE_TIMEOUT
+    gbblas.gemm_(C, Ad, Bd, mode="ozaki_crt", slices=16)
+    torch.cuda.synchronize()
+    gbblas.check_device_status()
+    assert_bit_equal(to_host(C), oracle.ozaki_crt_gemm(A, B, moduli=16))
+
+
+def test_crt_panels_under_stream_capture(restore_tuning):
+    """Under stream capture a call keeps to one panel on the capturing stream; replays equal
+    the eager call made in 3 panels."""
+    M, K, N = 384, 1024, 900
+    A = to_dev(workloads.ozaki_matrix(M, K, per="row", stream=820))
+    B = to_dev(workloads.ozaki_matrix(K, N, per="col", stream=821))
+    tuning.set_tuning("ozaki_crt", tuning.size_class(M, N), {"engine": 2, "band": 8, "panels": 3})
+    C_eager = torch.empty((N, M), dtype=torch.float64, device="cuda").t()
+    gbblas.gemm_(C_eager, A, B, mode="ozaki_crt")
+    torch.cuda.synchronize()
+    C_graph = torch.empty((N, M), dtype=torch.float64, device="cuda").t()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        gbblas.gemm_(C_graph, A, B, mode="ozaki_crt")
+    graph.replay()
+    torch.cuda.synchronize()
+    gbblas.check_device_status()
+    assert_bit_equal(to_host(C_graph), to_host(C_eager))
+
+
 SHAPES = [(1, 1, 1), (33, 70, 17), (300, 257, 130), (513, 96, 1000), (1024, 512, 768)]
 
 
