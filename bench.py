@@ -164,11 +164,12 @@ def cpu_cores():
         return os.cpu_count() or 1
 
 
-def cpu_sample(A, B, target_s, threads):
+def cpu_sample(A, B, target_s, threads, runs=5):
     """Time jmul!'s register-tiled chain (the tile pick_kernel_size gives for this host's register
-    file) on a column sample of A*B; TFLOP/s, description, columns, seconds.  The sample's
-    result is checked against the scalar chain on 64 entries (the port must compute jmul!'s
-    arithmetic, not only take its time)."""
+    file) on a column sample of A*B: `runs` timed runs of a sample sized to target_s / runs
+    seconds each; TFLOP/s of the median run, description, columns, seconds of the median run.
+    The sample's result is checked against the scalar chain on 64 entries (the port must compute
+    jmul!'s arithmetic, not only take its time)."""
     import oracle
     n = A.shape[0]
     K = A.shape[1]
@@ -177,19 +178,23 @@ def cpu_sample(A, B, target_s, threads):
     t0 = time.perf_counter()
     oracle.jmul_tiled(A, np.asfortranarray(B[:, :cols]), nthreads=threads)
     dt = time.perf_counter() - t0
-    cols = int(min(B.shape[1], max(tc, cols * target_s / max(dt, 1e-6))))
+    cols = int(min(B.shape[1], max(tc, cols * target_s / runs / max(dt, 1e-6))))
     cols -= cols % tc
     Bs = np.asfortranarray(B[:, :cols])
-    t0 = time.perf_counter()
-    out = oracle.jmul_tiled(A, Bs, nthreads=threads)
-    dt = time.perf_counter() - t0
+    times = []
+    for _ in range(runs):
+        t0 = time.perf_counter()
+        out = oracle.jmul_tiled(A, Bs, nthreads=threads)
+        times.append(time.perf_counter() - t0)
+    dt = statistics.median(times)
     g = np.random.default_rng(5)
     ri, ci = g.integers(0, n, 64), g.integers(0, cols, 64)
     if not np.array_equal(out[ri, ci].view(np.uint64), oracle.chain_entries(A, Bs, ri, ci).view(np.uint64)):
         raise RuntimeError("CPU baseline result differs from jmul!'s chain")
     flops = 2.0 * n * K * cols
-    return flops / dt / 1e12, "C[:, :%d] of the %dx%dx%d product (%.3g flop), %.2f s, %dx%d register tile" % (
-        cols, n, K, B.shape[1], flops, dt, tr, tc), cols, dt
+    return flops / dt / 1e12, ("C[:, :%d] of the %dx%dx%d product (%.3g flop), median of %d runs %.2f s "
+                               "(%s s), %dx%d register tile") % (
+        cols, n, K, B.shape[1], flops, runs, dt, ", ".join("%.2f" % x for x in times), tr, tc), cols, dt
 
 
 def reference_shape_timing():
@@ -244,7 +249,7 @@ def reference_arm(args, rank, world):
     B = np.asfortranarray(workloads.ozaki_matrix(n, n, per="col", stream=2))
     threads = cpu_cores()
     per_step_s = 3.0
-    _, _, cols, _ = cpu_sample(A, B, per_step_s, threads)
+    _, _, cols, _ = cpu_sample(A, B, per_step_s, threads, runs=1)
     Bs = np.asfortranarray(B[:, :cols])
     for _ in range(args.warmup):
         oracle.jmul_tiled(A, Bs, nthreads=threads)
