@@ -312,6 +312,30 @@ __global__ void __launch_bounds__(1024) grouped_prefix_kernel(const gb_problem_t
   if (t == 1023) offsets[count] = part[1023];
 }
 
+// The schedule position of tile w: the last pos with offsets[pos] <= w (problems without
+// tiles share their successor's offset).  Each warp searches on its own: its 32 lanes probe 32
+// points of the remaining interval at once, so 4096 problems take 3 rounds of loads instead of
+// the 12 dependent loads of a binary search.  Every warp reaches the same position.
+__device__ __forceinline__ int schedule_pos(const long long* __restrict__ offsets, int count, long long w) {
+  const int lane = threadIdx.x & 31;
+  int lo = 0, hi = count - 1;   // offsets[lo] <= w holds throughout (offsets[0] = 0)
+  while (lo < hi) {
+    const long long span = hi - lo;
+    const int p = lo + static_cast<int>((span * (lane + 1) + 31) / 32);   // in (lo, hi]; lane 31: hi
+    const unsigned ok = __ballot_sync(0xffffffffu, offsets[p] <= w);   // monotone in the lane
+    if (ok == 0u) {
+      hi = __shfl_sync(0xffffffffu, p, 0) - 1;
+    } else {
+      const int L = 31 - __clz(ok);
+      const int pl = __shfl_sync(0xffffffffu, p, L);
+      const int pn = __shfl_sync(0xffffffffu, p, L < 31 ? L + 1 : 31);
+      hi = (L == 31) ? hi : pn - 1;
+      lo = pl;
+    }
+  }
+  return lo;
+}
+
 // Persistent tile loop: CTA b takes tiles b, b + grid, ... of the schedule.
 template <typename T>
 __global__ void __launch_bounds__(GROUPED_THREADS, 2) grouped_gemm_kernel(const gb_problem_t* __restrict__ probs,
@@ -322,12 +346,7 @@ __global__ void __launch_bounds__(GROUPED_THREADS, 2) grouped_gemm_kernel(const 
   const int* order = reinterpret_cast<const int*>(grouped_order_words(ws, count));
   const long long total = offsets[count];
   for (long long w = blockIdx.x; w < total; w += gridDim.x) {
-    // schedule position: last pos with offsets[pos] <= w (problems with no tiles share offsets)
-    int lo = 0, hi = count - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (offsets[mid] <= w) lo = mid; else hi = mid - 1;
-    }
+    const int lo = schedule_pos(offsets, count, w);
     const gb_problem_t p = probs[order[lo]];
     const int cfg = prologue_config(tuning, p, sizeof(T) == 4);
     const TileCfg c = tile_cfg(cfg);
