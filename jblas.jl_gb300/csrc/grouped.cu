@@ -245,8 +245,14 @@ __device__ __forceinline__ int prologue_config(const gb_grouped_tuning_t& tuning
 }
 
 // Workspace of a call over `count` problems (int64 words): the tile prefix sums in schedule
-// order offsets[0..count], then the schedule order (count int32 problem indices).
+// order offsets[0..count], then the schedule order (count int32 entries: the problem index,
+// and for count <= 2^24 its tile configuration in bits 24-30, so the tile loop need not
+// evaluate the per-problem choice again for every tile).
 __host__ __device__ inline long long* grouped_order_words(long long* ws, int count) { return ws + count + 1; }
+constexpr int GROUPED_PACK_LIMIT = 1 << 24;
+__host__ __device__ inline int grouped_order_entry(int i, int cfg, int count) {
+  return count <= GROUPED_PACK_LIMIT ? (i | (cfg << 24)) : i;
+}
 
 // Prologue (one block): the schedule orders the problems by the work of one of their tiles
 // (tile rows x tile columns x k, in 32 power-of-two buckets, heaviest first), so that the CTAs,
@@ -254,7 +260,7 @@ __host__ __device__ inline long long* grouped_order_words(long long* ws, int cou
 // fill the tail; it writes the order and the exclusive prefix sums of the tiles in that order.
 // The order inside a bucket depends on timing, which changes no result (each tile is
 // independent).
-__global__ void __launch_bounds__(1024) grouped_prefix_kernel(const gb_problem_t* __restrict__ probs, int count,
+__global__ void __launch_bounds__(1024, 1) grouped_prefix_kernel(const gb_problem_t* __restrict__ probs, int count,
                                                               gb_grouped_tuning_t tuning, bool f32,
                                                               long long* __restrict__ ws) {
   __shared__ long long part[1024];
@@ -284,14 +290,17 @@ __global__ void __launch_bounds__(1024) grouped_prefix_kernel(const gb_problem_t
   __syncthreads();
   for (int i = t; i < count; i += 1024) {
     const gb_problem_t& p = probs[i];
-    order[atomicAdd(&start[bucket_of(p, tile_cfg(prologue_config(tuning, p, f32)))], 1)] = i;
+    const int cfg = prologue_config(tuning, p, f32);
+    order[atomicAdd(&start[bucket_of(p, tile_cfg(cfg))], 1)] = grouped_order_entry(i, cfg, count);
   }
   __syncthreads();
   const int per = (count + 1023) / 1024;
   const int b = t * per, e = min(count, b + per);
+  const bool packed = count <= GROUPED_PACK_LIMIT;
   auto tiles_of = [&](int pos) -> long long {
-    const gb_problem_t& p = probs[order[pos]];
-    const TileCfg c = tile_cfg(prologue_config(tuning, p, f32));
+    const int e = order[pos];
+    const gb_problem_t& p = probs[packed ? (e & 0xFFFFFF) : e];
+    const TileCfg c = tile_cfg(packed ? (e >> 24) : prologue_config(tuning, p, f32));
     return (p.m <= 0 || p.n <= 0) ? 0 : ((p.m + c.bm - 1) / c.bm) * ((p.n + c.bn - 1) / c.bn);
   };
   long long sum = 0;
@@ -347,12 +356,16 @@ __global__ void __launch_bounds__(GROUPED_THREADS, 2) grouped_gemm_kernel(const 
   const long long total = offsets[count];
   for (long long w = blockIdx.x; w < total; w += gridDim.x) {
     const int lo = schedule_pos(offsets, count, w);
-    const gb_problem_t p = probs[order[lo]];
-    const int cfg = prologue_config(tuning, p, sizeof(T) == 4);
+    const int e = order[lo];
+    const bool packed = count <= GROUPED_PACK_LIMIT;
+    const gb_problem_t p = probs[packed ? (e & 0xFFFFFF) : e];
+    const int cfg = packed ? (e >> 24) : prologue_config(tuning, p, sizeof(T) == 4);
     const TileCfg c = tile_cfg(cfg);
-    const long long local = w - offsets[lo];
+    // tile rows of the problem and the tile's place in it, in 32-bit arithmetic (a problem's
+    // tile count is below 2^31)
+    const int local = static_cast<int>(w - offsets[lo]);
     const int tiles_m = static_cast<int>((p.m + c.bm - 1) / c.bm);
-    const int tm = static_cast<int>(local % tiles_m), tn = static_cast<int>(local / tiles_m);
+    const int tn = local / tiles_m, tm = local - tn * tiles_m;
     if constexpr (sizeof(T) == 8) {
       // FP64 runs at the DFMA rate whatever the tile: the small configurations keep the
       // register count (and so the resident CTAs per SM) low.
