@@ -322,12 +322,14 @@ __global__ void __launch_bounds__(1024, 1) grouped_prefix_kernel(const gb_proble
 }
 
 // The schedule position of tile w: the last pos with offsets[pos] <= w (problems without
-// tiles share their successor's offset).  Each warp searches on its own: its 32 lanes probe 32
-// points of the remaining interval at once, so 4096 problems take 3 rounds of loads instead of
-// the 12 dependent loads of a binary search.  Every warp reaches the same position.
-__device__ __forceinline__ int schedule_pos(const long long* __restrict__ offsets, int count, long long w) {
+// tiles share their successor's offset), searched from `from` (a position with
+// offsets[from] <= w: a CTA's tiles come in increasing order, so its previous tile's position).
+// Each warp searches on its own: its 32 lanes probe 32 points of the remaining interval at
+// once, so 4096 problems take at most 3 rounds of loads instead of the 12 dependent loads of a
+// binary search.  Every warp reaches the same position.
+__device__ __forceinline__ int schedule_pos(const long long* __restrict__ offsets, int count, long long w, int from) {
   const int lane = threadIdx.x & 31;
-  int lo = 0, hi = count - 1;   // offsets[lo] <= w holds throughout (offsets[0] = 0)
+  int lo = from, hi = count - 1;   // offsets[lo] <= w holds throughout
   while (lo < hi) {
     const long long span = hi - lo;
     const int p = lo + static_cast<int>((span * (lane + 1) + 31) / 32);   // in (lo, hi]; lane 31: hi
@@ -354,8 +356,9 @@ __global__ void __launch_bounds__(GROUPED_THREADS, 2) grouped_gemm_kernel(const 
   const long long* offsets = ws;
   const int* order = reinterpret_cast<const int*>(grouped_order_words(ws, count));
   const long long total = offsets[count];
+  int lo = 0;   // offsets[0] = 0 <= w
   for (long long w = blockIdx.x; w < total; w += gridDim.x) {
-    const int lo = schedule_pos(offsets, count, w);
+    lo = schedule_pos(offsets, count, w, lo);
     const int e = order[lo];
     const bool packed = count <= GROUPED_PACK_LIMIT;
     const gb_problem_t p = probs[packed ? (e & 0xFFFFFF) : e];
