@@ -94,7 +94,8 @@ def test_autotune_and_cache(cuda, tmp_path):
     before = [to_host(C) for C in Cs]
     cache = str(tmp_path / "tune.json")
     tuning, ms = grouped.autotune(plan, reps=2, cache=cache)
-    assert all(0 <= c < 6 for c in tuning.as_list())
+    # FP32: any of the tile configurations or the per-problem choice
+    assert all(0 <= c < grouped.CONFIGS or c == grouped.AUTO for c in tuning.as_list())
     for C, b in zip(Cs, before):                 # tuning leaves the caller's C untouched
         assert np.array_equal(to_host(C), b)
     again, _ = grouped.autotune(plan, reps=2, cache=cache)
