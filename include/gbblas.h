@@ -116,7 +116,7 @@ GB_API int gb_get_tc_tuning(int kind, int size_class, gb_tc_tuning_t* out);
  * combination gives GB_ERR_INVALID_VALUE. */
 GB_API int gb_set_tc_tuning(int kind, int size_class, const gb_tc_tuning_t* tuning);
 /* Times every candidate (engines, bands 2..32 pair tiles / 4..64 single tiles, TMA stores where
- * they apply) on seeded synthetic M x N x K operands of the kind (slices: 8 digit slices; CRT:
+ * they apply, 1..4 CRT blocks) on seeded synthetic M x N x K operands of the kind (slices: 8 digit slices; CRT:
  * 15 moduli; FP32: BF16X3) with `reps` timed calls after a warm-up, and returns the fastest in
  * `out` (best_ms: its time per call; may be NULL).  The installed tuning is left as it was; the
  * caller installs the result with gb_set_tc_tuning.  Allocates its operands, synchronises

@@ -21,6 +21,7 @@ layer over the C ABI in `include/gbblas.h`:
     semiring_mul!(C, A, B, semiring; accumulate)   C = [C ⊕] A ⊗ B over (min,+), (max,+),
                                          (max,min), (min,max) or (max,*) (Float64/Float32/Int32)
     ChainRulesCore.rrule(::typeof(gemm), A, B)   pullback through gemm_adjoint!
+    tc_tuning, set_tc_tuning!, reset_tc_tuning!, autotune_tc!   the tensor-core tuning table
 
 Matrices are device arrays (anything with `pointer` to CUDA device memory and a column-
 major layout, e.g. CUDA.jl's `CuArray`); `stream` defaults to the task-local stream of
@@ -338,6 +339,59 @@ Allocating product for use with automatic differentiation: the `rrule` below ret
 the pullback computed by `gemm_adjoint!` (Float32) or two Ozaki products (Float64).
 """
 gemm(A::AbstractMatrix, B::AbstractMatrix) = jmul!(similar(A, size(A, 1), size(B, 2)), A, B)
+
+# ------------------------------------------------------------------ tensor-core tuning
+"""
+    TcTuning(engine, band, tma_store, panels)
+
+`gb_tc_tuning_t`: the launch configuration of the tensor-core engine for one kind of product
+and output-size class (engine 1 = one CTA per 128 x 256 tile, 2 = a CTA pair per 256 x 256
+tile; band = tile rows per L2 band; tma_store = TMA stores of FP32 outputs; panels = CRT
+blocks of C) — the measured counterpart of jBLAS's `pick_kernel_size` and `BLASOptions`
+(src/kernel_structure.jl:76-99, src/blas_options.jl:2-7).
+"""
+struct TcTuning
+    engine::Int32
+    band::Int32
+    tma_store::Int32
+    panels::Int32
+end
+
+const TC_KIND = Dict(:ozaki_slices => Cint(0), :ozaki_crt => Cint(1), :f32 => Cint(2), :adjoint => Cint(3))
+
+"Size class of an M x N output for the tuning table (by max(M, N): 0 up to 2048, 1 up to 8192, 2 beyond)."
+tc_size_class(M::Integer, N::Integer) = Int(ccall((:gb_tc_size_class, libgbblas), Cint, (Int64, Int64), M, N))
+
+"The tuning that calls of `kind` (:ozaki_slices, :ozaki_crt, :f32, :adjoint) in `size_class` use."
+function tc_tuning(kind::Symbol, size_class::Integer)
+    r = Ref{TcTuning}()
+    check(ccall((:gb_get_tc_tuning, libgbblas), Cint, (Cint, Cint, Ptr{TcTuning}), TC_KIND[kind], size_class, r))
+    r[]
+end
+
+"Installs `t` for later calls of `kind` in `size_class`; `reset_tc_tuning!` restores the default."
+set_tc_tuning!(kind::Symbol, size_class::Integer, t::TcTuning) =
+    check(ccall((:gb_set_tc_tuning, libgbblas), Cint, (Cint, Cint, Ref{TcTuning}), TC_KIND[kind], size_class, t))
+reset_tc_tuning!(kind::Symbol, size_class::Integer) =
+    check(ccall((:gb_set_tc_tuning, libgbblas), Cint, (Cint, Cint, Ptr{TcTuning}), TC_KIND[kind], size_class, C_NULL))
+
+"""
+    autotune_tc!(kind, M, N, K; reps = 3, install = true) -> (TcTuning, ms)
+
+Times the candidate configurations of `kind` on seeded M x N x K operands on the device
+(`gb_autotune_tc`) and, with `install`, sets the fastest for that size class.  Persist the
+result with the standard library's `Serialization` (or any format) and install it in a later
+session with `set_tc_tuning!`.
+"""
+function autotune_tc!(kind::Symbol, M::Integer, N::Integer, K::Integer; reps::Integer = 3, install::Bool = true)
+    t = Ref{TcTuning}()
+    ms = Ref{Cfloat}(0)
+    check(ccall((:gb_autotune_tc, libgbblas), Cint,
+                (Cint, Int64, Int64, Int64, Cint, Ptr{TcTuning}, Ptr{Cfloat}, Ptr{Cvoid}),
+                TC_KIND[kind], M, N, K, reps, t, ms, current_stream()))
+    install && set_tc_tuning!(kind, tc_size_class(M, N), t[])
+    t[], Float64(ms[])
+end
 
 # ChainRulesCore is optional: the rrule is defined when the package is available.
 if Base.find_package("ChainRulesCore") !== nothing

@@ -45,6 +45,18 @@ def test_julia_front_end_binds_only_declared_symbols():
     assert bound <= set(declared_functions()), sorted(bound - set(declared_functions()))
 
 
+def test_julia_tuning_struct_matches_header():
+    """GBBLAS.TcTuning is passed by pointer to gb_get/set_tc_tuning and gb_autotune_tc: its
+    fields are the header's gb_tc_tuning_t fields, in order, all 32-bit."""
+    hdr = open(os.path.join(ROOT, "include", "gbblas.h")).read()
+    body = re.search(r"typedef struct \{([^}]*)\} gb_tc_tuning_t;", hdr).group(1)
+    c_fields = re.findall(r"int32_t\s+(\w+);", body)
+    src = open(os.path.join(ROOT, "jblas.jl_gb300", "julia", "GBBLAS.jl")).read()
+    jl = re.search(r"struct TcTuning\n(.*?)\nend", src, re.S).group(1)
+    jl_fields = re.findall(r"(\w+)::Int32", jl)
+    assert c_fields == jl_fields == ["engine", "band", "tma_store", "panels"]
+
+
 def test_status_strings():
     L = gbblas.lib()
     for code in range(0, -7, -1):
