@@ -940,6 +940,27 @@ def main():
     d2h_gbs = C_pin.numel() * 8 / (c1.elapsed_time(c2) * 1e-3) / 1e9
 
     plan = gbblas.last_ozaki_plan()   # the plan the automatic choice used
+    # The residue products alone: the same calls in one column panel, so that nothing runs
+    # beside the tensor-core kernel (in the timed steps the split of the next panel and the
+    # reconstruction of the previous one share its SMs).
+    mma_alone = None
+    if rank == 0 and args.method == "crt" and not args.mnk:
+        from gbblas import tuning
+        cls = tuning.size_class(M, N)
+        saved = tuning.get_tuning("ozaki_crt", cls)
+        tuning.set_tuning("ozaki_crt", cls, dict(saved.as_dict(), panels=1))
+        try:
+            for _ in range(2):
+                gbblas.gemm_(C_d, A_d, B_d, mode=mode, slices=args.slices)
+            torch.cuda.synchronize()
+            with gbblas.profile() as prof_alone:
+                for _ in range(5):
+                    gbblas.gemm_(C_d, A_d, B_d, mode=mode, slices=args.slices)
+                torch.cuda.synchronize()
+        finally:
+            tuning.set_tuning("ozaki_crt", cls, saved)
+        mma_alone = prof_alone.ms.get("ozaki_slice_mma", float("nan")) / max(1, prof_alone.launches.get(
+            "ozaki_slice_mma", 1))
     crt_tuned = None
     if rank == 0 and args.method == "crt" and not args.mnk:
         from gbblas import tuning
@@ -1046,6 +1067,12 @@ def main():
                                            "bound at 8192^3)",
                          "kernel": "ozaki_slice_mma", "ms_per_launch": mma_ms,
                          "launches_per_call": launches_per_call,
+                         "alone": None if mma_alone is None else {
+                             "ms_per_launch": mma_alone,
+                             "achieved": plan["flops_tensor"] / (mma_alone * 1e-3) / 1e12,
+                             "frac": plan["flops_tensor"] / (mma_alone * 1e-3) / 1e12 / peaks[peak_key],
+                             "note": "the same calls in one column panel (5 calls after the timed steps): "
+                                     "the residue products with nothing running beside them"},
                          "peak_source": "%s %s" % (peak_src, peak_key),
                          "work": "BF16 tensor flops per launch = %s * 2*M*N*ceil(K/64)*64 / launches_per_call"
                                  % ("moduli" if args.method == "crt" else "slice_products")},
