@@ -107,12 +107,17 @@ template <typename T>
 struct GroupedChainOp {
   static constexpr bool kInitFromC = false;
   static constexpr bool kPairs = false;
+  static constexpr bool kVecStore = true;   // short K loops: the epilogue's stores matter
   T alpha, beta;
   static __device__ __forceinline__ T init() { return T(-0.0); }
   static __device__ __forceinline__ T step(T acc, T a, T b) { return fma_t<T>(a, b, acc); }
   __device__ __forceinline__ void store(T* c, T acc) const {
     *c = (beta == T(0)) ? alpha * acc : fma_t<T>(alpha, acc, beta * *c);
   }
+  __device__ __forceinline__ T value(T c, T acc) const {
+    return (beta == T(0)) ? alpha * acc : fma_t<T>(alpha, acc, beta * c);
+  }
+  __device__ __forceinline__ bool reads_c() const { return beta != T(0); }
 };
 
 // One BM x BN tile of problem `p` (column-major, no transposes).  Per element the FMA chain

@@ -17,6 +17,7 @@ namespace gb {
 template <typename T>
 struct FmaChainOp {
   static constexpr bool kInitFromC = false;
+  static constexpr bool kVecStore = false;
   static constexpr bool kPairs = false;   // the chain's order is part of its result
   T alpha, beta;
   static __device__ __forceinline__ T init() { return T(-0.0); }
@@ -31,6 +32,7 @@ struct FmaChainOp {
 template <typename T>
 struct FmaOntoCOp {
   static constexpr bool kInitFromC = true;
+  static constexpr bool kVecStore = false;
   static constexpr bool kPairs = false;
   int unused;
   static __device__ __forceinline__ T init() { return T(0); }

@@ -89,6 +89,7 @@ struct SemiringOp {
   using Ar = SrArith<T>;
   static constexpr bool kMinPlus = SR == GB_SEMIRING_MIN_PLUS || SR == GB_SEMIRING_MIN_MAX;
   static constexpr bool kInitFromC = false;   // C is folded in by the epilogue instead
+  static constexpr bool kVecStore = false;
   static constexpr bool kPairs =
       Ar::kHas3 && (std::is_floating_point<T>::value || SR == GB_SEMIRING_MAX_MIN || SR == GB_SEMIRING_MIN_MAX);
   int accumulate;

@@ -11,6 +11,9 @@
 //   Op::init()            the accumulator before k = 1
 //   Op::step(acc, a, b)   one contraction step, applied for k = 1..K in order
 //   op.store(c, acc)      the epilogue writing one element of C
+//   Op::kVecStore         when true (with op.value(c, acc), the value store writes, and
+//                         op.reads_c(), whether it reads C's old value) C is written with vector
+//                         stores or, when C is not aligned for them, through shared memory
 //   Op::kInitFromC        when true the accumulator starts from C's element instead of init()
 //                         (jBLAS's kernel!, which folds A*X onto D's value)
 //   Op::kPairs, Op::step2(acc, a0, b0, a1, b1)
@@ -216,15 +219,75 @@ __device__ __forceinline__ void simt_tile(int64_t M, int64_t N, int64_t K, const
     }
   }
 
+  if constexpr (Op::kVecStore) {
+    // Epilogue for policies with kVecStore (and op.value / op.reads_c), where short K loops
+    // make the stores of C a large part of a tile.  The per-element stores of the general path
+    // write one element in each of 16 columns per warp instruction; instead:
+    //  - beta = 0 and C and ldc multiples of VM elements: a thread's VM consecutive rows of a
+    //    column go out as one vector store (whole 32-byte sectors);
+    //  - otherwise the tile goes through shared memory, half of its rows at a time, and a warp
+    //    writes 32 consecutive rows of one column per instruction.  The panels' shared memory
+    //    is reused: every warp has finished reading it first.
+    const bool rc = op.reads_c();
+    const bool vec_ok = VM > 1 && !rc && (reinterpret_cast<uintptr_t>(C) % (VM * sizeof(T))) == 0 &&
+                        (ldc % VM) == 0;   // the same for the whole CTA
+    if (vec_ok) {
 #pragma unroll
-  for (int i = 0; i < TM; ++i) {
-    const int64_t m = m0 + (i < VM ? ty * VM + i : BM / 2 + ty * VM + (i - VM));
-    if (m >= M) continue;
+      for (int h = 0; h < 2; ++h) {
+        const int64_t mb = m0 + h * (BM / 2) + ty * VM;   // first of this half's VM rows
 #pragma unroll
-    for (int j = 0; j < TN; ++j) {
-      const int64_t n = n0 + (j < VN ? tx * VN + j : BN / 2 + tx * VN + (j - VN));
-      if (n >= N) continue;
-      op.store(&C[m + n * ldc], acc[i][j]);
+        for (int j = 0; j < TN; ++j) {
+          const int64_t n = n0 + (j < VN ? tx * VN + j : BN / 2 + tx * VN + (j - VN));
+          if (n >= N) continue;
+          T* __restrict__ c = &C[mb + n * ldc];
+          if (mb + VM <= M) {
+            VecT<T, VM> v;
+#pragma unroll
+            for (int i = 0; i < VM; ++i) v.v[i] = op.value(T(0), acc[h * VM + i][j]);
+            *reinterpret_cast<VecT<T, VM>*>(c) = v;
+          } else {
+#pragma unroll
+            for (int i = 0; i < VM; ++i)
+              if (mb + i < M) c[i] = op.value(T(0), acc[h * VM + i][j]);
+          }
+        }
+      }
+    } else {
+      constexpr int HR = BM / 2;    // rows per half
+      constexpr int LDS = HR + 1;   // column stride: consecutive rows in consecutive banks
+      static_assert(BN * LDS <= SimtSmem<T, BM, BN, BK>::ELEMS, "staged epilogue does not fit");
+      __syncthreads();
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+#pragma unroll
+        for (int j = 0; j < TN; ++j) {
+          const int col = (j < VN ? tx * VN + j : BN / 2 + tx * VN + (j - VN));
+#pragma unroll
+          for (int i = 0; i < VM; ++i) smem[col * LDS + ty * VM + i] = acc[h * VM + i][j];
+        }
+        __syncthreads();
+        for (int e = tid; e < HR * BN; e += NT) {
+          const int r = e % HR, col = e / HR;
+          const int64_t m = m0 + h * HR + r, n = n0 + col;
+          if (m < M && n < N) {
+            T* c = &C[m + n * ldc];
+            *c = op.value(rc ? *c : T(0), smem[col * LDS + r]);
+          }
+        }
+        __syncthreads();
+      }
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < TM; ++i) {
+      const int64_t m = m0 + (i < VM ? ty * VM + i : BM / 2 + ty * VM + (i - VM));
+      if (m >= M) continue;
+#pragma unroll
+      for (int j = 0; j < TN; ++j) {
+        const int64_t n = n0 + (j < VN ? tx * VN + j : BN / 2 + tx * VN + (j - VN));
+        if (n >= N) continue;
+        op.store(&C[m + n * ldc], acc[i][j]);
+      }
     }
   }
 }
