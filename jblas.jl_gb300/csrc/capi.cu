@@ -56,7 +56,9 @@ static std::atomic<int> g_ozaki_min_chunks{1};
 // a CRT call runs its residue products there while its own stream splits the next column panel
 // and reconstructs the previous one.  One call holds a lane at a time.
 struct Lane {
-  static constexpr int EVENTS = 2 * TC_MAX_PANELS + 1;   // fork and join per panel, one for errors
+  // fork and join per block of C; the statistics' fork and join; the plan; one for errors
+  static constexpr int STATS_FORK = 2 * TC_MAX_PANELS, STATS_JOIN = STATS_FORK + 1, PLAN = STATS_FORK + 2,
+                       ERROR_JOIN = STATS_FORK + 3, EVENTS = STATS_FORK + 4;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[EVENTS] = {};
 };
@@ -344,9 +346,11 @@ struct OperandStats {
   OzRowStats a{}, b{};
 };
 
+// With a lane (and no host copies), B's statistics run on the lane beside A's on `s`, and `s`
+// waits for them before it returns.
 static int run_stats(DeviceInfo* dev, const double* A, int64_t M, int64_t a_rs, int64_t a_ks, const double* B,
                      int64_t N, int64_t b_rs, int64_t b_ks, int64_t K, bool sums, bool host, OperandStats* os,
-                     HostStats* h, cudaStream_t s) {
+                     HostStats* h, cudaStream_t s, Lane* lane = nullptr) {
   const int Sa = oz_stats_kslices(M, K, a_ks, dev->sms), Sb = oz_stats_kslices(N, K, b_ks, dev->sms);
   const int64_t pa = Sa * M, pb = Sb * N;
   const size_t amax_bytes = align256((M + N) * sizeof(unsigned long long));
@@ -362,6 +366,18 @@ static int run_stats(DeviceInfo* dev, const double* A, int64_t M, int64_t a_rs, 
   os->b.part_sq = os->a.part_sq + pa;
   os->a.kslices = Sa;
   os->b.kslices = Sb;
+  if (lane && !host) {
+    cudaError_t e = cudaEventRecord(lane->ev[Lane::STATS_FORK], s);   // after the workspace allocation
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(lane->stream, lane->ev[Lane::STATS_FORK], 0);
+    if (e != cudaSuccess) return gb_set_cuda_error(e, "ozaki statistics fork");
+    int rc = oz_row_stats(A, M, K, a_rs, a_ks, os->a, sums, s);
+    const int rcb = oz_row_stats(B, N, K, b_rs, b_ks, os->b, sums, lane->stream);
+    e = cudaEventRecord(lane->ev[Lane::STATS_JOIN], lane->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, lane->ev[Lane::STATS_JOIN], 0);
+    if (!rc) rc = rcb;
+    if (!rc && e != cudaSuccess) rc = gb_set_cuda_error(e, "ozaki statistics join");
+    return rc;
+  }
   int rc = oz_row_stats(A, M, K, a_rs, a_ks, os->a, sums || host, s);
   if (!rc) rc = oz_row_stats(B, N, K, b_rs, b_ks, os->b, sums || host, s);
   if (rc || !host) return rc;
@@ -577,9 +593,29 @@ static int crt_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int64
   if (rc) return rc;
 
   const bool sums = (moduli == 0 || err_bound_out);
+  // Blocks of C: the residue products of block b run on a high-priority lane while this stream
+  // splits the operand panels of block b + 1 and reconstructs block b - 1, on the SMs' spare
+  // registers and issue slots beside the tensor-core kernel; before the first products, B's
+  // statistics and first panel split run on the lane beside A's.  One block (the plain
+  // sequence on this stream) when the tuning asks for one and under stream capture; at most
+  // one block column per 256 columns.
+  const TcTuning tune = tc_tuning_for(TC_KIND_CRT, M, N);
+  const int64_t tiles_n = (N + 255) / 256;
+  int panels = tune.panels < 1 ? 1 : tune.panels;
+  if (panels > TC_MAX_PANELS) panels = TC_MAX_PANELS;
+  if (panels > tiles_n) panels = static_cast<int>(tiles_n);
+  cudaStreamCaptureStatus cap_status = cudaStreamCaptureStatusNone;
+  Lane* lane = nullptr;
+  if (panels > 1 && cudaStreamIsCapturing(s, &cap_status) == cudaSuccess && cap_status == cudaStreamCaptureStatusNone)
+    lane = take_lane(dev);
+  struct LaneReturn {   // the lane goes back to the pool when the call has enqueued its work
+    DeviceInfo* d;
+    Lane* l;
+    ~LaneReturn() { give_lane(d, l); }
+  } lane_return{dev, lane};
   OperandStats os;
   HostStats h;
-  rc = run_stats(dev, A, M, a_rs, a_ks, B, N, b_rs, b_ks, K, sums, false, &os, &h, s);
+  rc = run_stats(dev, A, M, a_rs, a_ks, B, N, b_rs, b_ks, K, sums, false, &os, &h, s, lane);
   if (rc) {
     if (os.ws) cudaFreeAsync(os.ws, s);
     return rc;
@@ -623,6 +659,10 @@ static int crt_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int64
   }
   rc = crt_plan_device(os.a, os.b, pp, plan_d, record, seq, scratch, s);
   cudaFreeAsync(scratch, s);
+  if (!rc && lane) {   // the lane's first split reads the plan
+    const cudaError_t e = cudaEventRecord(lane->ev[Lane::PLAN], s);
+    if (e != cudaSuccess) rc = gb_set_cuda_error(e, "ozaki crt plan event");
+  }
   if (!rc && err_bound_out) {
     CrtDevicePlan hp;
     e = cudaMemcpyAsync(&hp, plan_d, sizeof(hp), cudaMemcpyDeviceToHost, s);
@@ -659,7 +699,6 @@ static int crt_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int64
   ga.status = dev->status;
   ga.wait_limit_ns = g_wait_limit_ns.load();
   ga.plan = plan_d;
-  const TcTuning tune = tc_tuning_for(TC_KIND_CRT, M, N);
   ga.band = tune.band;
   ga.a_plane_rows = M;
   ga.b_plane_rows = N;
@@ -668,19 +707,6 @@ static int crt_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int64
     const int64_t cap = dev->sms & ~1;
     return static_cast<int>(ctas < cap ? ctas : cap);
   };
-  // Column panels: the residue products of panel p run on a high-priority lane while this
-  // stream splits panel p + 1 of B and reconstructs panel p - 1 of C, on the SMs' spare
-  // registers and issue slots beside the tensor-core kernel.  One panel (the plain sequence
-  // on this stream) when the tuning asks for one and under stream capture; at most one panel
-  // per 256 columns.
-  const int64_t tiles_n = (N + 255) / 256;
-  int panels = tune.panels < 1 ? 1 : tune.panels;
-  if (panels > TC_MAX_PANELS) panels = TC_MAX_PANELS;
-  if (panels > tiles_n) panels = static_cast<int>(tiles_n);
-  cudaStreamCaptureStatus cap_status = cudaStreamCaptureStatusNone;
-  Lane* lane = nullptr;
-  if (panels > 1 && cudaStreamIsCapturing(s, &cap_status) == cudaSuccess && cap_status == cudaStreamCaptureStatusNone)
-    lane = take_lane(dev);
   if (!lane) {
     rc = crt_split(A, M, K, a_rs, a_ks, os.a.amax_bits, plan_d, pa, pitch, M, ea, s);
     if (!rc) rc = crt_split(B, N, K, b_rs, b_ks, os.b.amax_bits, plan_d, pb, pitch, N, eb, s);
@@ -729,15 +755,18 @@ static int crt_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int64
     const int nblocks = prow * pcol;
     for (int b = 0; b < nblocks && !rc; ++b) {
       const int r = b / pcol, c = b % pcol;
-      if (!a_done[r]) {
+      if (!rc && !b_done[c]) {   // the first block's B panel on the lane, beside A's split here
+        cudaStream_t bs = (b == 0) ? hs : s;
+        if (b == 0) cu(cudaStreamWaitEvent(hs, lane->ev[Lane::PLAN], 0));
+        if (!rc)
+          rc = crt_split(B + n0[c] * b_rs, n0[c + 1] - n0[c], K, b_rs, b_ks, os.b.amax_bits + n0[c], plan_d,
+                         pb + n0[c] * pitch, pitch, N, eb + n0[c], bs);
+        b_done[c] = true;
+      }
+      if (!rc && !a_done[r]) {
         rc = crt_split(A + m0[r] * a_rs, m0[r + 1] - m0[r], K, a_rs, a_ks, os.a.amax_bits + m0[r], plan_d,
                        pa + m0[r] * pitch, pitch, M, ea + m0[r], s);
         a_done[r] = true;
-      }
-      if (!rc && !b_done[c]) {
-        rc = crt_split(B + n0[c] * b_rs, n0[c + 1] - n0[c], K, b_rs, b_ks, os.b.amax_bits + n0[c], plan_d,
-                       pb + n0[c] * pitch, pitch, N, eb + n0[c], s);
-        b_done[c] = true;
       }
       if (!rc) cu(cudaEventRecord(lane->ev[2 * b], s));
       if (!rc) cu(cudaStreamWaitEvent(hs, lane->ev[2 * b], 0));
@@ -750,10 +779,9 @@ static int crt_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int64
     }
     if (rc) {
       // join whatever reached the lane before the error, so the workspace is freed after it
-      if (cudaEventRecord(lane->ev[Lane::EVENTS - 1], hs) == cudaSuccess)
-        cudaStreamWaitEvent(s, lane->ev[Lane::EVENTS - 1], 0);
+      if (cudaEventRecord(lane->ev[Lane::ERROR_JOIN], hs) == cudaSuccess)
+        cudaStreamWaitEvent(s, lane->ev[Lane::ERROR_JOIN], 0);
     }
-    give_lane(dev, lane);
   }
   if (!rc) {
     PendingCrtPlan& pd = g_pending_crt;
