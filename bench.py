@@ -56,6 +56,8 @@ def parse_args():
     p.add_argument("--no-alt", action="store_true", help="skip timing the other emulation method")
     p.add_argument("--no-native", action="store_true", help="skip the native FP64 comparison")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    p.add_argument("--ring", type=int, default=8,
+                   help="depth of the end-to-end pipeline's ring of device input / output buffers")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU sample")
     p.add_argument("--workload", choices=["ozaki", "ozaki_sweep", "native", "f32_tc", "grouped", "adjoint",
                                           "semiring"],
@@ -307,10 +309,15 @@ def pipeline_timeline(e0, up_ev, comp_ev, down_ev, nbuf, host_enqueue_ms):
         for c0, c1 in comp:
             overlap += max(0.0, min(z, c1) - max(a, c0))
     up_total = sum(z - a for a, z in up)
+    # every step after the first whose compute waited more than 0.5 ms, with its upload's length
+    stalls = [{"step": r["step"], "idle_ms": r["compute_idle_before_ms"], "waited_on": r["waited_on"],
+               "upload_ms": round(up[r["step"]][1] - up[r["step"]][0], 3)}
+              for r in rows[1:] if r["compute_idle_before_ms"] > 0.5]
     return {"compute_idle_ms_median": statistics.median(idle) if idle else 0.0,
             "compute_idle_ms_total": sum(idle), "waited_on": waited,
             "upload_overlapped_with_compute_frac": overlap / up_total if up_total else 0.0,
-            "steps": rows[:8]}
+            "upload_ms_max": round(max(z - a for a, z in up), 3) if up else 0.0,
+            "stalls": stalls, "steps": rows[:8]}
 
 
 def _event_ms(fn, steps, stream):
@@ -817,8 +824,10 @@ def main():
     # Uploads and downloads run on their own streams (the two copy directions overlap) into a
     # ring of NBUF device input/output buffers: uploads run up to NBUF - 1 steps ahead of the
     # compute and downloads trail it, so the host link's jitter (it is shared with the node's
-    # other GPUs) does not stall the compute (a serving pipeline with a queue of NBUF).
-    NBUF = 4
+    # other GPUs) does not stall the compute (a serving pipeline with a queue of NBUF).  An
+    # upload may end up to about (NBUF - 1) compute steps minus its own length late before the
+    # compute waits for it: 27 ms with 4 buffers at 8192^3, 70 ms with 8 (12 GiB of buffers).
+    NBUF = max(2, args.ring)
     barrier()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     up_stream, down_stream = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
@@ -1086,8 +1095,8 @@ def main():
                                "residue products, so the kinds can sum to more than ms_per_step"),
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "TFLOP/s", "ms_per_step": ms_e2e,
-                    "pipeline": "4-deep ring: uploads run up to 3 steps ahead, the download of step i overlaps step "
-                                "i+1; the timed steps start with an empty pipeline (the first upload and the last "
+                    "pipeline": f"{NBUF}-deep ring: uploads run up to {NBUF - 1} steps ahead, the download of step i "
+                                "overlaps step i+1; the timed steps start with an empty pipeline (the first upload and the last "
                                 "download are not overlapped), after an untimed warm-up pass of the same pipeline",
                     "h2d_GBps": h2d_gbs, "d2h_GBps": d2h_gbs,
                     "compute_ms_in_pipeline": comp_in_pipeline,

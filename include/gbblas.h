@@ -97,7 +97,9 @@ GB_API int gb_set_tc_engine(int engine);
  *              panels; 4: 2 x 2 blocks (column panels when M <= 256); at most one per 256
  *              columns.  The residue products of block b run on a high-priority stream of the
  *              library while the caller's stream splits the operand panels of block b + 1 and
- *              reconstructs block b - 1.  Under stream capture a call uses one block.
+ *              reconstructs block b - 1 (and, before the first products, B's statistics and
+ *              first panel split run there beside A's).  Under stream capture a call uses one
+ *              block.
  *              Results do not depend on it.
  * Size classes by max(M, N): 0 up to 2048, 1 up to 8192, 2 beyond.  gb_set_tc_engine, when set,
  * overrides the engine of every kind. */
