@@ -93,9 +93,12 @@ GB_API int gb_set_tc_engine(int engine);
  *              A rows in L2)
  *   tma_store  FP32 outputs (GB_TC_F32, GB_TC_ADJOINT) on the pair engine: 1 = C staged in
  *              shared memory and written by TMA stores (beta = 0), 0 = direct stores
- *   panels     GB_TC_OZAKI_CRT only (0 elsewhere): C in blocks — 0 or 1: one; 2, 3: column
- *              panels; 4: 2 x 2 blocks (column panels when M <= 256); at most one per 256
- *              columns.  The residue products of block b run on a high-priority stream of the
+ *   panels     GB_TC_OZAKI_CRT only (0 elsewhere): C in blocks — 0 or 1: one; 2: two equal
+ *              column panels; 3: three column panels, a narrow first one, a wide middle one and
+ *              a last one twice the first's width where that adds no round of 256 x 256 tiles
+ *              over the SM pairs to one launch's, else three equal panels where those add
+ *              none, else two; 4: 2 x 2 blocks (column panels when M <= 256); at most one per
+ *              256 columns.  The residue products of block b run on a high-priority stream of the
  *              library while the caller's stream splits the operand panels of block b + 1 and
  *              reconstructs block b - 1 (and, before the first products, B's statistics and
  *              first panel split run there beside A's).  Under stream capture a call uses one

@@ -565,6 +565,36 @@ static int ozaki_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int
 }
 
 // ------------------------------------------------------------------ CRT driver
+// Column panels of a CRT call, in 256-column tiles: widths w[0..pcol) summing to tiles_n.
+// The residue-product kernel runs one pair tile per CTA pair at a time, so a launch of t tiles
+// takes ceil(t / pairs) rounds; panels may split C only where that adds no round over one launch.
+// Three panels are a narrow first panel (the first products wait for a sliver of B's split),
+// a wide middle one and a last one twice as wide as the first (its products run beside the
+// middle panel's reconstruction, and a sliver of C is reconstructed after them): widths
+// (e, tiles_n - 3e, 2e) for the smallest e that adds no round (8192 x 8192: 2, 26 and 4 tiles
+// = 1 + 11 + 2 rounds, as one launch of 1024 tiles on 76 pairs); otherwise, and for other
+// panel counts, equal panels, and two when three equal ones would add rounds.
+// Returns the panel count used.
+static int crt_panel_widths(int64_t tiles_m, int64_t tiles_n, int64_t pairs, int pcol, int64_t* w) {
+  auto rounds = [&](int64_t cols) { return (tiles_m * cols + pairs - 1) / pairs; };
+  const int64_t best = rounds(tiles_n);
+  if (pcol == 3) {
+    for (int64_t e = 1; 5 * e <= tiles_n; ++e) {
+      if (rounds(e) + rounds(tiles_n - 3 * e) + rounds(2 * e) == best) {
+        w[0] = e;
+        w[1] = tiles_n - 3 * e;
+        w[2] = 2 * e;
+        return 3;
+      }
+    }
+    int64_t eq = 0;
+    for (int p = 0; p < 3; ++p) eq += rounds(tiles_n * (p + 1) / 3 - tiles_n * p / 3);
+    if (eq > best) pcol = 2;
+  }
+  for (int p = 0; p < pcol; ++p) w[p] = tiles_n * (p + 1) / pcol - tiles_n * p / pcol;
+  return pcol;
+}
+
 // The plan (moduli n and integer bits t) is chosen on the device from the statistics
 // (crt_plan_device), so an automatic call has no host round trip; the workspace is sized for
 // the largest n the call may take.  The host only learns the plan when asked for it
@@ -716,20 +746,22 @@ static int crt_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int64
     }
     if (!rc) rc = crt_combine_launch(ga, s);
   } else {
-    // Blocks of C on whole 256 x 256 tiles: `panels` column panels, or 2 x 2 blocks for 4, so
-    // that the first products wait only for half of A's split as well.  Blocks run row by row;
-    // each split of a row panel of A or column panel of B is enqueued on this stream just
-    // before the first block that needs it.
-    const int prow = (panels == 4 && mpad >= 512) ? 2 : 1, pcol = panels / prow;
-    int64_t m0[3], n0[TC_MAX_PANELS + 1];
+    // Blocks of C on whole 256 x 256 tiles: `panels` column panels (crt_panel_widths), or
+    // 2 x 2 blocks for 4, so that the first products wait only for half of A's split as well.
+    // Blocks run row by row; each split of a row panel of A or column panel of B is enqueued
+    // on this stream just before the first block that needs it.
+    const int prow = (panels == 4 && mpad >= 512) ? 2 : 1;
+    int64_t m0[3], n0[TC_MAX_PANELS + 1], wcol[TC_MAX_PANELS];
     const int64_t tiles_m = mpad / 256;
     for (int p = 0; p <= prow; ++p) {
       const int64_t r = tiles_m * p / prow * 256;
       m0[p] = r < M ? r : M;
     }
-    for (int p = 0; p <= pcol; ++p) {
-      const int64_t c = tiles_n * p / pcol * 256;
-      n0[p] = c < N ? c : N;
+    const int pcol = crt_panel_widths(tiles_m / prow, tiles_n, dev->sms / 2, panels / prow, wcol);
+    n0[0] = 0;
+    for (int p = 0, t = 0; p < pcol; ++p) {
+      t += static_cast<int>(wcol[p]);
+      n0[p + 1] = static_cast<int64_t>(t) * 256 < N ? static_cast<int64_t>(t) * 256 : N;
     }
     auto block_args = [&](int r, int c) {
       CrtGemmArgs g = ga;

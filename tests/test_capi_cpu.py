@@ -140,8 +140,8 @@ def test_tc_tuning_table_roundtrip_and_validation():
     for kind in _lib.TC_KINDS:
         for cls in range(_lib.TC_SIZE_CLASSES):
             d = tuning.default_tuning(kind, cls)
-            # CRT products above 2048 columns default to two column panels
-            panels = 2 if (kind == "ozaki_crt" and cls > 0) else 0
+            # CRT products above 2048 columns default to three column panels
+            panels = 3 if (kind == "ozaki_crt" and cls > 0) else 0
             assert (d.engine, d.band, d.tma_store, d.panels) == (2, 8, 0, panels)
             assert tuning.get_tuning(kind, cls).as_dict() == d.as_dict()
     tuning.set_tuning("f32", 1, {"engine": 2, "band": 16, "tma_store": 1})

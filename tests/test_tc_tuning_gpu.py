@@ -92,6 +92,37 @@ def test_crt_bit_exact_under_every_panel_count(restore_tuning, panels, tb):
     assert_bit_equal(got, oracle.ozaki_crt_gemm(A, Bl, C=C0, alpha=1.5, beta=0.5, moduli=13))
 
 
+@pytest.mark.parametrize("panels", [2, 3, 4])
+def test_crt_wide_panel_partitions_match_one_panel(restore_tuning, panels):
+    """8192 x 8192 outputs (short K): three panels are a narrow first and last panel (512 and
+    1024 columns) around a wide middle one, two panels and 2 x 2 blocks halves; every partition
+    gives the bits of one panel over the whole of C, and a grid of entries across the panel
+    boundaries equals the restatement."""
+    n, K = 8192, 96
+    g = np.random.default_rng(90 + panels)
+    A = np.asfortranarray(g.uniform(-1, 1, (n, K)) * np.ldexp(1.0, g.integers(-6, 7, (n, K))))
+    B = np.asfortranarray(g.uniform(-1, 1, (K, n)) * np.ldexp(1.0, g.integers(-6, 7, (K, n))))
+    C0 = torch.rand((n, n), dtype=torch.float64, device="cuda", generator=torch.Generator("cuda").manual_seed(9)).t()
+    Ad, Bd = to_dev(A), to_dev(B)
+    cls = tuning.size_class(n, n)
+    out = {}
+    for p in (1, panels):
+        tuning.set_tuning("ozaki_crt", cls, {"engine": 2, "band": 8, "panels": p})
+        C = C0.clone(memory_format=torch.preserve_format)
+        gbblas.gemm_(C, Ad, Bd, 1.5, 0.5, mode="ozaki_crt", slices=12)
+        torch.cuda.synchronize()
+        gbblas.check_device_status()
+        out[p] = C
+    assert torch.equal(out[1], out[panels])
+    rows = np.array([0, 1, 255, 256, 4095, 4096, 8190, 8191])
+    cols = np.array([0, 511, 512, 513, 4095, 4096, 7167, 7168, 8191])
+    got = out[panels][torch.as_tensor(rows, device="cuda")][:, torch.as_tensor(cols, device="cuda")].cpu().numpy()
+    c0 = C0[torch.as_tensor(rows, device="cuda")][:, torch.as_tensor(cols, device="cuda")].cpu().numpy()
+    ref = oracle.ozaki_crt_gemm(np.asfortranarray(A[rows]), np.asfortranarray(B[:, cols]), C=np.asfortranarray(c0),
+                                alpha=1.5, beta=0.5, moduli=12)
+    assert_bit_equal(got, ref)
+
+
 def test_crt_panels_with_automatic_plan(restore_tuning):
     """The automatic plan (moduli chosen on the device) read by every panel's kernels."""
     M, K, N = 512, 300, 1024
