@@ -257,6 +257,9 @@ GB_API int gb_gemm_f32_ex(int transA, int transB, int64_t M, int64_t N, int64_t 
  * unified addressing).  The call uploads op(A), op(B) (and C when beta != 0) into library
  * workspace, runs gb_gemm_* on `stream` with the same mode and arguments, downloads C and
  * returns once `stream` has finished: results are those of the device call, bit for bit.
+ * With a pinned (page-locked) C, a CRT call in column panels copies each panel to C on a
+ * stream of the library as soon as it is reconstructed, beside the later panels' products;
+ * three panels are then two halves and a narrow last panel (the tuning's `panels` = 3).
  * A bounded on-device wait that expired is reported as GB_ERR_PIPELINE_TIMEOUT (the status
  * word is read and cleared).  gb_jmul_*_host: jmul!(D, A, X) on host MMatrix-like buffers
  * (leading dimensions M, N, M). */

@@ -54,13 +54,27 @@ static std::atomic<int> g_ozaki_min_chunks{1};
 
 // A high-priority stream with the events that fork a call's work onto it and join it back:
 // a CRT call runs its residue products there while its own stream splits the next column panel
-// and reconstructs the previous one.  One call holds a lane at a time.
+// and reconstructs the previous one.  A second stream copies the finished blocks of C of a
+// host-buffer call to the host.  One call holds a lane at a time.
 struct Lane {
-  // fork and join per block of C; the statistics' fork and join; the plan; one for errors
+  // fork and join per block of C; the statistics' fork and join; the plan; one for errors;
+  // one per block for its copy to the host and the copies' join
   static constexpr int STATS_FORK = 2 * TC_MAX_PANELS, STATS_JOIN = STATS_FORK + 1, PLAN = STATS_FORK + 2,
-                       ERROR_JOIN = STATS_FORK + 3, EVENTS = STATS_FORK + 4;
+                       ERROR_JOIN = STATS_FORK + 3, COPY = STATS_FORK + 4, COPY_JOIN = COPY + TC_MAX_PANELS,
+                       EVENTS = COPY_JOIN + 1;
   cudaStream_t stream = nullptr;
+  cudaStream_t copy = nullptr;
   cudaEvent_t ev[EVENTS] = {};
+};
+
+// The host C of a host-buffer call (pinned memory): a CRT call in blocks copies each block of C
+// there on its lane's copy stream once the block is reconstructed, beside the products and
+// reconstruction of the later blocks, and sets `done`; otherwise the caller copies C after the
+// call.
+struct HostSink {
+  double* C = nullptr;
+  int64_t ldc = 0;
+  bool done = false;
 };
 
 struct DeviceInfo {
@@ -92,9 +106,14 @@ static Lane* take_lane(DeviceInfo* d) {
   int least = 0, greatest = 0;
   if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) return nullptr;
   if (cudaStreamCreateWithPriority(&l->stream, cudaStreamNonBlocking, greatest) != cudaSuccess) return nullptr;
+  if (cudaStreamCreateWithFlags(&l->copy, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaStreamDestroy(l->stream);
+    return nullptr;
+  }
   for (int i = 0; i < Lane::EVENTS; ++i) {
     if (cudaEventCreateWithFlags(&l->ev[i], cudaEventDisableTiming) != cudaSuccess) {
       for (int j = 0; j < i; ++j) cudaEventDestroy(l->ev[j]);
+      cudaStreamDestroy(l->copy);
       cudaStreamDestroy(l->stream);
       return nullptr;
     }
@@ -574,10 +593,27 @@ static int ozaki_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int
 // (e, tiles_n - 3e, 2e) for the smallest e that adds no round (8192 x 8192: 2, 26 and 4 tiles
 // = 1 + 11 + 2 rounds, as one launch of 1024 tiles on 76 pairs); otherwise, and for other
 // panel counts, equal panels, and two when three equal ones would add rounds.
+// A host-buffer call copies each panel of C to the host once it is reconstructed, so there
+// three panels are two halves and a narrow last panel, (w, w, e) for the smallest e that adds no
+// round (8192 x 8192: 14, 14 and 4 tiles = 6 + 6 + 2 rounds): the first half's copy runs
+// beside the second half's products, the second's beside the last panel's, and only the
+// narrow last panel's copy follows the products.
 // Returns the panel count used.
-static int crt_panel_widths(int64_t tiles_m, int64_t tiles_n, int64_t pairs, int pcol, int64_t* w) {
+static int crt_panel_widths(int64_t tiles_m, int64_t tiles_n, int64_t pairs, int pcol, bool host_copies,
+                            int64_t* w) {
   auto rounds = [&](int64_t cols) { return (tiles_m * cols + pairs - 1) / pairs; };
   const int64_t best = rounds(tiles_n);
+  if (pcol == 3 && host_copies) {
+    for (int64_t e = 1; 5 * e <= tiles_n; ++e) {
+      const int64_t w0 = (tiles_n - e) / 2, w1 = tiles_n - e - w0;
+      if (rounds(w0) + rounds(w1) + rounds(e) == best) {
+        w[0] = w0;
+        w[1] = w1;
+        w[2] = e;
+        return 3;
+      }
+    }
+  }
   if (pcol == 3) {
     for (int64_t e = 1; 5 * e <= tiles_n; ++e) {
       if (rounds(e) + rounds(tiles_n - 3 * e) + rounds(2 * e) == best) {
@@ -602,7 +638,7 @@ static int crt_panel_widths(int64_t tiles_m, int64_t tiles_n, int64_t pairs, int
 
 static int crt_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int64_t K, double alpha, const double* A,
                     int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc, int moduli,
-                    double* err_bound_out, cudaStream_t s) {
+                    double* err_bound_out, cudaStream_t s, HostSink* sink = nullptr) {
   if (moduli < 0 || moduli > TC_MAX_MODULI) return GB_ERR_INVALID_VALUE;
   if ((M + 255) / 256 * ((N + 255) / 256) > 0x7FFFFFFF) return GB_ERR_UNSUPPORTED;
   const int64_t a_rs = ta ? lda : 1, a_ks = ta ? 1 : lda;
@@ -757,7 +793,7 @@ static int crt_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int64
       const int64_t r = tiles_m * p / prow * 256;
       m0[p] = r < M ? r : M;
     }
-    const int pcol = crt_panel_widths(tiles_m / prow, tiles_n, dev->sms / 2, panels / prow, wcol);
+    const int pcol = crt_panel_widths(tiles_m / prow, tiles_n, dev->sms / 2, panels / prow, sink != nullptr, wcol);
     n0[0] = 0;
     for (int p = 0, t = 0; p < pcol; ++p) {
       t += static_cast<int>(wcol[p]);
@@ -805,9 +841,27 @@ static int crt_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int64
       if (!rc) rc = crt_mma_launch(block_args(r, c), plan, hs);
       if (!rc) cu(cudaEventRecord(lane->ev[2 * b + 1], hs));
     }
+    int copies = 0;   // blocks of C on their way to the host C
     for (int b = 0; b < nblocks && !rc; ++b) {
+      const int r = b / pcol, c = b % pcol;
       cu(cudaStreamWaitEvent(s, lane->ev[2 * b + 1], 0));
-      if (!rc) rc = crt_combine_launch(block_args(b / pcol, b % pcol), s);
+      if (!rc) rc = crt_combine_launch(block_args(r, c), s);
+      if (!rc && sink) {
+        cu(cudaEventRecord(lane->ev[Lane::COPY + b], s));
+        cu(cudaStreamWaitEvent(lane->copy, lane->ev[Lane::COPY + b], 0));
+        if (!rc) {
+          const int64_t rows = m0[r + 1] - m0[r], cols = n0[c + 1] - n0[c];
+          cu(cudaMemcpy2DAsync(sink->C + m0[r] + n0[c] * sink->ldc, sink->ldc * sizeof(double),
+                               C + m0[r] + n0[c] * ldc, ldc * sizeof(double), rows * sizeof(double), cols,
+                               cudaMemcpyDeviceToHost, lane->copy));
+          if (!rc) ++copies;
+        }
+      }
+    }
+    if (copies) {   // the caller's stream waits for the copies (its workspace holds C)
+      if (cudaEventRecord(lane->ev[Lane::COPY_JOIN], lane->copy) == cudaSuccess)
+        cudaStreamWaitEvent(s, lane->ev[Lane::COPY_JOIN], 0);
+      if (!rc) sink->done = (copies == nblocks);
     }
     if (rc) {
       // join whatever reached the lane before the error, so the workspace is freed after it
@@ -890,7 +944,9 @@ static int kernel_entry(Onto onto, Init init_fn, T* D, const T* A, const T* X, i
 }
 
 // Host-buffer products: upload the stored operands (packed, leading dimension = rows), run the
-// device call on them, download C, synchronise, read the status word.
+// device call on them, download C, synchronise, read the status word.  With a pinned host C
+// the device call gets it as a sink (HostSink), and a call that already copied C (block by
+// block) leaves nothing to download.
 template <typename T, typename DeviceCall>
 static int gemm_host(DeviceCall call, int ta, int tb, int64_t M, int64_t N, int64_t K, T alpha, const T* A,
                      int64_t lda, const T* B, int64_t ldb, T beta, T* C, int64_t ldc, void* stream) {
@@ -924,8 +980,18 @@ static int gemm_host(DeviceCall call, int ta, int tb, int64_t M, int64_t N, int6
     cudaFreeAsync(ws, s);
     return gb_set_cuda_error(e, "host-buffer upload");
   }
-  rc = call(ta, tb, M, N, K, alpha, need_ab ? dA : nullptr, la, need_ab ? dB : nullptr, lb, beta, dC, lc, stream);
-  if (!rc) {
+  HostSink sink;
+  HostSink* sinkp = nullptr;
+  cudaPointerAttributes attr;
+  if (sizeof(T) == 8 && cudaPointerGetAttributes(&attr, C) == cudaSuccess && attr.type == cudaMemoryTypeHost) {
+    sink.C = reinterpret_cast<double*>(C);
+    sink.ldc = ldc;
+    sinkp = &sink;
+  }
+  cudaGetLastError();   // an unregistered pointer is not an error here
+  rc = call(ta, tb, M, N, K, alpha, need_ab ? dA : nullptr, la, need_ab ? dB : nullptr, lb, beta, dC, lc, stream,
+            sinkp);
+  if (!rc && !sink.done) {
     e = cudaMemcpy2DAsync(C, ldc * sz, dC, lc * sz, M * sz, N, cudaMemcpyDefault, s);
     if (e != cudaSuccess) rc = gb_set_cuda_error(e, "host-buffer download");
   }
@@ -1062,9 +1128,10 @@ int gb_check_status(void* stream) {
   return GB_OK;
 }
 
-int gb_gemm_f64(int transA, int transB, int64_t M, int64_t N, int64_t K, double alpha, const double* A,
-                int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc, int mode,
-                int slices, double* err_bound_out, void* stream) {
+// gb_gemm_f64, with the host C of a host-buffer call (or nullptr).
+static int gemm_f64(int transA, int transB, int64_t M, int64_t N, int64_t K, double alpha, const double* A,
+                    int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc, int mode,
+                    int slices, double* err_bound_out, void* stream, HostSink* sink) {
   if (mode != GB_MODE_NATIVE && mode != GB_MODE_OZAKI_BF16 && mode != GB_MODE_OZAKI_INT8 &&
       mode != GB_MODE_OZAKI_CRT)
     return GB_ERR_INVALID_VALUE;
@@ -1091,9 +1158,17 @@ int gb_gemm_f64(int transA, int transB, int64_t M, int64_t N, int64_t K, double 
     return native_gemm_f64(transA, transB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, dev->sms, s);
   }
   if (mode == GB_MODE_OZAKI_CRT)
-    return crt_gemm(dev, transA, transB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, slices, err_bound_out, s);
+    return crt_gemm(dev, transA, transB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, slices, err_bound_out, s,
+                    sink);
   return ozaki_gemm(dev, transA, transB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, slices,
                     err_bound_out, s);
+}
+
+int gb_gemm_f64(int transA, int transB, int64_t M, int64_t N, int64_t K, double alpha, const double* A,
+                int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc, int mode,
+                int slices, double* err_bound_out, void* stream) {
+  return gemm_f64(transA, transB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, mode, slices, err_bound_out, stream,
+                  nullptr);
 }
 
 int gb_gemm_f32(int transA, int transB, int64_t M, int64_t N, int64_t K, float alpha, const float* A,
@@ -1308,15 +1383,19 @@ int gb_gemm_f64_host(int transA, int transB, int64_t M, int64_t N, int64_t K, do
                      int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc, int mode,
                      int slices, double* err_bound_out, void* stream) {
   auto call = [&](int ta, int tb, int64_t m, int64_t n, int64_t k, double al, const double* a, int64_t la,
-                  const double* b, int64_t lb, double be, double* c, int64_t lc, void* st) {
-    return gb_gemm_f64(ta, tb, m, n, k, al, a, la, b, lb, be, c, lc, mode, slices, err_bound_out, st);
+                  const double* b, int64_t lb, double be, double* c, int64_t lc, void* st, HostSink* sink) {
+    return gemm_f64(ta, tb, m, n, k, al, a, la, b, lb, be, c, lc, mode, slices, err_bound_out, st, sink);
   };
   return gemm_host<double>(call, transA, transB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, stream);
 }
 
 int gb_gemm_f32_host(int transA, int transB, int64_t M, int64_t N, int64_t K, float alpha, const float* A,
                      int64_t lda, const float* B, int64_t ldb, float beta, float* C, int64_t ldc, void* stream) {
-  return gemm_host<float>(gb_gemm_f32, transA, transB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, stream);
+  auto call = [&](int ta, int tb, int64_t m, int64_t n, int64_t k, float al, const float* a, int64_t la,
+                  const float* b, int64_t lb, float be, float* c, int64_t lc, void* st, HostSink*) {
+    return gb_gemm_f32(ta, tb, m, n, k, al, a, la, b, lb, be, c, lc, st);
+  };
+  return gemm_host<float>(call, transA, transB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, stream);
 }
 
 int gb_jmul_f64_host(double* D, const double* A, const double* X, int64_t M, int64_t N, int64_t P, void* stream) {

@@ -78,6 +78,55 @@ def test_crt_host_equals_device_call(cuda):
                                                    bits=gbblas.last_ozaki_plan()["bits"]))
 
 
+@pytest.fixture
+def crt_panels(cuda):
+    from gbblas import tuning
+    yield tuning
+    for cls in range(3):
+        tuning.set_tuning("ozaki_crt", cls, None)
+
+
+@pytest.mark.parametrize("panels", [1, 2, 3, 4])
+def test_crt_host_pinned_block_copies(crt_panels, panels):
+    """Pinned host buffers: a CRT call in blocks copies each block of C to the host C as soon as
+    it is reconstructed (column panels, and the quadrants of 2 x 2 blocks into a C with a
+    larger leading dimension); the result equals the device call, alpha and beta included, and
+    the padding of C is untouched."""
+    tuning = crt_panels
+    M, K, N = 1100, 300, 2400
+    A = np.asfortranarray(workloads.ozaki_matrix(M, K, per="row", stream=83))
+    B = np.asfortranarray(workloads.ozaki_matrix(K, N, per="col", stream=84))
+    C0 = np.asfortranarray(np.random.default_rng(85).uniform(-1, 1, (M, N)))
+    tuning.set_tuning("ozaki_crt", tuning.size_class(M, N), {"engine": 2, "band": 8, "panels": panels})
+    big = torch.full((N, M + 7), 5.0, dtype=torch.float64).pin_memory()   # column-major, ldc = M + 7
+    Ch = big.numpy().T[:M, :]
+    Ch[...] = C0
+    Ap = torch.from_numpy(np.ascontiguousarray(A.T)).pin_memory().numpy().T
+    Bp = torch.from_numpy(np.ascontiguousarray(B.T)).pin_memory().numpy().T
+    gbblas.gemm_host(Ch, Ap, Bp, 1.5, 0.5, mode="ozaki_crt", slices=14)
+    Cd = to_dev(C0)
+    gbblas.gemm_(Cd, to_dev(A), to_dev(B), 1.5, 0.5, mode="ozaki_crt", slices=14)
+    assert_bit_equal(np.asfortranarray(Ch), to_host(Cd))
+    assert np.all(big.numpy().T[M:, :] == 5.0)
+
+
+def test_crt_host_pinned_halves_and_narrow_last_panel(crt_panels):
+    """8192 x 8192 C (short K) from pinned host buffers in the default three panels: a host call
+    cuts them as two halves and a narrow last panel (3584, 3584 and 1024 columns) and copies each
+    to the host as it is reconstructed; C equals the device call's over the whole matrix."""
+    n, K = 8192, 96
+    g = np.random.default_rng(86)
+    A = np.asfortranarray(g.uniform(-1, 1, (n, K)) * np.ldexp(1.0, g.integers(-6, 7, (n, K))))
+    B = np.asfortranarray(g.uniform(-1, 1, (K, n)) * np.ldexp(1.0, g.integers(-6, 7, (K, n))))
+    pin = lambda X: torch.from_numpy(np.ascontiguousarray(X.T)).pin_memory()   # noqa: E731
+    Cp = torch.zeros((n, n), dtype=torch.float64).pin_memory()
+    gbblas.gemm_host(Cp.numpy().T, pin(A).numpy().T, pin(B).numpy().T, mode="ozaki_crt", slices=12)
+    Cd = torch.empty((n, n), dtype=torch.float64, device="cuda").t()
+    gbblas.gemm_(Cd, to_dev(A), to_dev(B), mode="ozaki_crt", slices=12)
+    torch.cuda.synchronize()
+    assert torch.equal(Cp.t().to("cuda"), Cd)
+
+
 def test_host_argument_errors(cuda):
     A = np.zeros((4, 4), order="F")
     with pytest.raises(gbblas.GBError):
