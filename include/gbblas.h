@@ -412,6 +412,14 @@ GB_API int gb_plan_ozaki(int64_t M, int64_t N, int64_t K, int slices, gb_ozaki_p
  * K 2^(2t) <= 2^125), k_chunk, products = groups = moduli, flops_tensor.
  * GB_ERR_UNSUPPORTED when no t >= 1 fits. */
 GB_API int gb_plan_ozaki_crt(int64_t M, int64_t N, int64_t K, int moduli, gb_ozaki_plan_t* out);
+/* Blocks of C of a CRT call on an M x N output (see gb_tc_tuning_t.panels): for the tuning's
+ * `panels` value, a device of `sms` SMs (the residue products run one 256 x 256 tile per SM
+ * pair at a time) and host_copies = 1 for a host-buffer call with a pinned C, the row
+ * boundaries rows[0..*row_blocks] (at most 2 blocks) and column boundaries
+ * cols[0..*col_blocks] (at most 4) of the blocks, multiples of 256 but the last.  A call under
+ * stream capture runs one block whatever this returns. */
+GB_API int gb_crt_blocks(int64_t M, int64_t N, int panels, int sms, int host_copies, int64_t* rows, int* row_blocks,
+                         int64_t* cols, int* col_blocks);
 /* The plan of the most recent OZAKI (BF16 or CRT) gb_gemm_f64 call made by the calling
  * thread (zeroes before the first), e.g. the slice count an automatic call picked. */
 GB_API int gb_last_ozaki_plan(gb_ozaki_plan_t* out);

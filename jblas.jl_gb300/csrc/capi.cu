@@ -631,6 +631,35 @@ static int crt_panel_widths(int64_t tiles_m, int64_t tiles_n, int64_t pairs, int
   return pcol;
 }
 
+// The blocks of C a CRT call cuts an M x N output into, on whole 256 x 256 tiles: for the
+// tuning's `panels` (clamped to 1..TC_MAX_PANELS and to one per 256 columns), `panels` column
+// panels (crt_panel_widths), or 2 x 2 blocks for 4, so that the first products wait only for
+// half of A's split as well (column panels when M <= 256).  Row boundaries m0[0..prow],
+// column boundaries n0[0..pcol].
+struct CrtBlocks {
+  int prow = 1, pcol = 1;
+  int64_t m0[3] = {}, n0[TC_MAX_PANELS + 1] = {};
+};
+static CrtBlocks crt_blocks(int64_t M, int64_t N, int panels, int sms, bool host_copies) {
+  CrtBlocks b;
+  const int64_t tiles_m = (M + 255) / 256, tiles_n = (N + 255) / 256;
+  if (panels < 1) panels = 1;
+  if (panels > TC_MAX_PANELS) panels = TC_MAX_PANELS;
+  if (panels > tiles_n) panels = static_cast<int>(tiles_n > 0 ? tiles_n : 1);
+  b.prow = (panels == 4 && tiles_m >= 2) ? 2 : 1;
+  for (int p = 0; p <= b.prow; ++p) {
+    const int64_t r = tiles_m * p / b.prow * 256;
+    b.m0[p] = r < M ? r : M;
+  }
+  int64_t w[TC_MAX_PANELS];
+  b.pcol = crt_panel_widths(tiles_m / b.prow, tiles_n, sms / 2 > 0 ? sms / 2 : 1, panels / b.prow, host_copies, w);
+  for (int p = 0, t = 0; p < b.pcol; ++p) {
+    t += static_cast<int>(w[p]);
+    b.n0[p + 1] = static_cast<int64_t>(t) * 256 < N ? static_cast<int64_t>(t) * 256 : N;
+  }
+  return b;
+}
+
 // The plan (moduli n and integer bits t) is chosen on the device from the statistics
 // (crt_plan_device), so an automatic call has no host round trip; the workspace is sized for
 // the largest n the call may take.  The host only learns the plan when asked for it
@@ -666,10 +695,8 @@ static int crt_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int64
   // sequence on this stream) when the tuning asks for one and under stream capture; at most
   // one block column per 256 columns.
   const TcTuning tune = tc_tuning_for(TC_KIND_CRT, M, N);
-  const int64_t tiles_n = (N + 255) / 256;
-  int panels = tune.panels < 1 ? 1 : tune.panels;
-  if (panels > TC_MAX_PANELS) panels = TC_MAX_PANELS;
-  if (panels > tiles_n) panels = static_cast<int>(tiles_n);
+  const CrtBlocks blocks = crt_blocks(M, N, tune.panels, dev->sms, sink != nullptr);
+  const int panels = blocks.prow * blocks.pcol;
   cudaStreamCaptureStatus cap_status = cudaStreamCaptureStatusNone;
   Lane* lane = nullptr;
   if (panels > 1 && cudaStreamIsCapturing(s, &cap_status) == cudaSuccess && cap_status == cudaStreamCaptureStatusNone)
@@ -782,23 +809,11 @@ static int crt_gemm(DeviceInfo* dev, int ta, int tb, int64_t M, int64_t N, int64
     }
     if (!rc) rc = crt_combine_launch(ga, s);
   } else {
-    // Blocks of C on whole 256 x 256 tiles: `panels` column panels (crt_panel_widths), or
-    // 2 x 2 blocks for 4, so that the first products wait only for half of A's split as well.
-    // Blocks run row by row; each split of a row panel of A or column panel of B is enqueued
-    // on this stream just before the first block that needs it.
-    const int prow = (panels == 4 && mpad >= 512) ? 2 : 1;
-    int64_t m0[3], n0[TC_MAX_PANELS + 1], wcol[TC_MAX_PANELS];
-    const int64_t tiles_m = mpad / 256;
-    for (int p = 0; p <= prow; ++p) {
-      const int64_t r = tiles_m * p / prow * 256;
-      m0[p] = r < M ? r : M;
-    }
-    const int pcol = crt_panel_widths(tiles_m / prow, tiles_n, dev->sms / 2, panels / prow, sink != nullptr, wcol);
-    n0[0] = 0;
-    for (int p = 0, t = 0; p < pcol; ++p) {
-      t += static_cast<int>(wcol[p]);
-      n0[p + 1] = static_cast<int64_t>(t) * 256 < N ? static_cast<int64_t>(t) * 256 : N;
-    }
+    // Blocks of C (crt_blocks) run row by row; each split of a row panel of A or column panel
+    // of B is enqueued on this stream just before the first block that needs it.
+    const int prow = blocks.prow, pcol = blocks.pcol;
+    const int64_t* m0 = blocks.m0;
+    const int64_t* n0 = blocks.n0;
     auto block_args = [&](int r, int c) {
       CrtGemmArgs g = ga;
       g.M = m0[r + 1] - m0[r];
@@ -1441,6 +1456,20 @@ int gb_plan_ozaki_crt(int64_t M, int64_t N, int64_t K, int moduli, gb_ozaki_plan
   out->products = p.n;
   out->groups = p.n;
   out->flops_tensor = p.flops_tensor;
+  return GB_OK;
+}
+
+int gb_crt_blocks(int64_t M, int64_t N, int panels, int sms, int host_copies, int64_t* rows, int* row_blocks,
+                  int64_t* cols, int* col_blocks) {
+  if (M < 1 || N < 1 || sms < 1 || (host_copies != 0 && host_copies != 1) || !rows || !row_blocks || !cols ||
+      !col_blocks)
+    return GB_ERR_INVALID_VALUE;
+  if ((M + 255) / 256 > 0x7FFFFFFF / ((N + 255) / 256)) return GB_ERR_UNSUPPORTED;
+  const CrtBlocks b = crt_blocks(M, N, panels, sms, host_copies != 0);
+  *row_blocks = b.prow;
+  *col_blocks = b.pcol;
+  for (int p = 0; p <= b.prow; ++p) rows[p] = b.m0[p];
+  for (int p = 0; p <= b.pcol; ++p) cols[p] = b.n0[p];
   return GB_OK;
 }
 

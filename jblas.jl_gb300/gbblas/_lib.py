@@ -110,6 +110,8 @@ SIGNATURES = {
                                c_float, c_vp, c_i64, c_int, c_vp]),
     "gb_plan_ozaki": (c_int, [c_i64, c_i64, c_i64, c_int, ctypes.POINTER(OzakiPlan)]),
     "gb_plan_ozaki_crt": (c_int, [c_i64, c_i64, c_i64, c_int, ctypes.POINTER(OzakiPlan)]),
+    "gb_crt_blocks": (c_int, [c_i64, c_i64, c_int, c_int, c_int, ctypes.POINTER(c_i64), ctypes.POINTER(c_int),
+                              ctypes.POINTER(c_i64), ctypes.POINTER(c_int)]),
     "gb_gemm_adjoint_f32": (c_int, [c_i64, c_i64, c_i64, c_vp, c_i64, c_vp, c_i64, c_vp, c_i64, c_vp, c_i64,
                                     c_vp, c_i64, c_vp]),
     "gb_last_ozaki_plan": (c_int, [ctypes.POINTER(OzakiPlan)]),

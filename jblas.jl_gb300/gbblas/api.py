@@ -342,6 +342,17 @@ def ozaki_crt_plan(M, N, K, moduli):
             "groups": p.groups, "flops_tensor": p.flops_tensor}
 
 
+def crt_blocks(M, N, panels, sms, host_copies=False):
+    """Row and column boundaries of the blocks of C a CRT call on an M x N output cuts, for the
+    tuning's `panels`, a device of `sms` SMs and (host_copies) a host-buffer call with a pinned
+    C (no GPU work): {"rows": [...], "cols": [...]}."""
+    rows, cols = (ctypes.c_int64 * 3)(), (ctypes.c_int64 * 5)()
+    nr, nc = ctypes.c_int(0), ctypes.c_int(0)
+    check(_lib.lib().gb_crt_blocks(M, N, panels, sms, int(bool(host_copies)), rows, ctypes.byref(nr), cols,
+                                   ctypes.byref(nc)), "gb_crt_blocks")
+    return {"rows": list(rows[:nr.value + 1]), "cols": list(cols[:nc.value + 1])}
+
+
 def last_ozaki_plan():
     """Plan of this thread's most recent Ozaki call (the slice count an automatic call chose)."""
     p = _lib.OzakiPlan()

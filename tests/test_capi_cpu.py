@@ -107,6 +107,64 @@ def test_ozaki_crt_plan_matches_restatement(K, moduli):
     assert got["flops_tensor"] == 2.0 * 256 * 128 * kb * 64 * moduli
 
 
+def _crt_blocks_restated(M, N, panels, sms, host):
+    """The block rule restated: 256-tile rounds over sms / 2 SM pairs; three panels cut as
+    (w, w, e) for host copies or (e, tiles - 3e, 2e) when neither adds a round, else three
+    equal panels, else two; four panels as 2 x 2 blocks when there are two tile rows."""
+    tm, tn = -(-M // 256), -(-N // 256)
+    panels = min(max(panels, 1), 4, tn)
+    prow = 2 if panels == 4 and tm >= 2 else 1
+    pcol, rtm, pairs = panels // prow, tm // prow, max(sms // 2, 1)
+    rounds = lambda c: -(-rtm * c // pairs)   # noqa: E731
+    best, w = rounds(tn), None
+    if pcol == 3:
+        for e in range(1, tn // 5 + 1):
+            if host and rounds((tn - e) // 2) + rounds(tn - e - (tn - e) // 2) + rounds(e) == best:
+                w = [(tn - e) // 2, tn - e - (tn - e) // 2, e]
+                break
+        for e in range(1, tn // 5 + 1):
+            if w is None and rounds(e) + rounds(tn - 3 * e) + rounds(2 * e) == best:
+                w = [e, tn - 3 * e, 2 * e]
+                break
+        if w is None and sum(rounds(tn * (p + 1) // 3 - tn * p // 3) for p in range(3)) > best:
+            pcol = 2
+    if w is None:
+        w = [tn * (p + 1) // pcol - tn * p // pcol for p in range(pcol)]
+    cols, t = [0], 0
+    for x in w:
+        t += x
+        cols.append(min(t * 256, N))
+    rows = [min(tm * p // prow * 256, M) for p in range(prow + 1)]
+    return {"rows": rows, "cols": cols}
+
+
+def test_crt_blocks_known_cuts():
+    """8192 x 8192 on 152 SMs: three panels of 2, 26 and 4 tiles (1 + 11 + 2 rounds, as one
+    launch); a host call with a pinned C: halves and a narrow last panel (6 + 6 + 2); four
+    panels: 2 x 2 blocks; 4096 x 4096: three panels fall back to two halves."""
+    assert gbblas.crt_blocks(8192, 8192, 3, 152) == {"rows": [0, 8192], "cols": [0, 512, 7168, 8192]}
+    assert gbblas.crt_blocks(8192, 8192, 3, 152, True) == {"rows": [0, 8192], "cols": [0, 3584, 7168, 8192]}
+    assert gbblas.crt_blocks(8192, 8192, 4, 152) == {"rows": [0, 4096, 8192], "cols": [0, 4096, 8192]}
+    assert gbblas.crt_blocks(8192, 8192, 2, 152) == {"rows": [0, 8192], "cols": [0, 4096, 8192]}
+    assert gbblas.crt_blocks(4096, 4096, 3, 152) == {"rows": [0, 4096], "cols": [0, 2048, 4096]}
+    assert gbblas.crt_blocks(12288, 12288, 3, 152) == {"rows": [0, 12288], "cols": [0, 768, 10752, 12288]}
+    assert gbblas.crt_blocks(300, 1100, 1, 152) == {"rows": [0, 300], "cols": [0, 1100]}
+    with pytest.raises(gbblas.GBError):
+        gbblas.crt_blocks(0, 8, 2, 152)
+
+
+@pytest.mark.parametrize("sms", [2, 16, 132, 152])
+def test_crt_blocks_match_restatement(sms):
+    g = __import__("numpy").random.default_rng(sms)
+    for _ in range(300):
+        M, N = (int(x) for x in g.integers(1, 40000, 2))
+        panels, host = int(g.integers(0, 6)), bool(g.integers(0, 2))
+        got = gbblas.crt_blocks(M, N, panels, sms, host)
+        assert got == _crt_blocks_restated(M, N, panels, sms, host), (M, N, panels, sms, host)
+        assert got["rows"][-1] == M and got["cols"][-1] == N
+        assert all(b % 256 == 0 for b in got["rows"][:-1] + got["cols"][:-1])
+
+
 def test_only_the_c_abi_is_exported():
     """The dynamic symbol table is exactly the header's gb_* functions (internal C++ hidden)."""
     import subprocess
