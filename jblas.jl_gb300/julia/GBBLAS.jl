@@ -393,6 +393,24 @@ function autotune_tc!(kind::Symbol, M::Integer, N::Integer, K::Integer; reps::In
     t[], Float64(ms[])
 end
 
+"""
+    crt_blocks(M, N, panels, sms; host_copies = false) -> (rows, cols)
+
+Row and column boundaries of the blocks of C an Ozaki CRT call cuts an M x N output into
+(`gb_crt_blocks`), for the tuning's `panels`, a device of `sms` SMs and, with `host_copies`, a
+host-buffer call on a pinned C.  No GPU work.
+"""
+function crt_blocks(M::Integer, N::Integer, panels::Integer, sms::Integer; host_copies::Bool = false)
+    rows = zeros(Int64, 3)
+    cols = zeros(Int64, 5)
+    nr = Ref{Cint}(0)
+    nc = Ref{Cint}(0)
+    check(ccall((:gb_crt_blocks, libgbblas), Cint,
+                (Int64, Int64, Cint, Cint, Cint, Ptr{Int64}, Ref{Cint}, Ptr{Int64}, Ref{Cint}),
+                M, N, panels, sms, host_copies ? 1 : 0, rows, nr, cols, nc))
+    rows[1:nr[]+1], cols[1:nc[]+1]
+end
+
 # ChainRulesCore is optional: the rrule is defined when the package is available.
 if Base.find_package("ChainRulesCore") !== nothing
     import ChainRulesCore
